@@ -1,0 +1,388 @@
+"""CPU oracle for the FFT-domain AVO inversion path -- TEST INFRASTRUCTURE ONLY.
+
+This module is the checker: tests, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` leg of ``bench.py`` call it to produce the answer the GPU
+path is compared against, and to time the CPU baseline.  Nothing in the
+product package imports it.
+
+Two native libraries sit behind it:
+
+* ``oracle/_build/libcravaoracle.so`` -- ``cravaoracle.c``, a plain-C
+  restatement of the reference algorithm in FP32 (reference operation order)
+  and FP64 (the FP64 oracle).  Built here and on any test machine.
+* ``oracle/_ref/libcrava_ref.so`` -- the reference's own FFTW 2.1.2,
+  ``lib_matr.c`` and ``RandomGen`` compiled from the reference sources by
+  ``Makefile.ref`` plus ``ref_harness.cpp``.  Only buildable where the
+  reference checkout exists; used to pin the restatement and to generate the
+  golden fixtures in ``tests/golden``.
+
+Array conventions follow ``FFTGrid`` (src/fftgrid.cpp:40-70): a real cube is a
+``(nzp, nyp, rnxp)`` array with ``rnxp = 2*(nxp//2+1)``; its spectrum is the
+same buffer viewed as ``(nzp, nyp, cnxp)`` complex.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+ORACLE_SO = os.path.join(BUILD_DIR, "libcravaoracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_SO = os.path.join(REF_DIR, "libcrava_ref.so")
+REFERENCE_SRC = os.environ.get("CRAVA_REFERENCE_SRC", "/root/reference")
+
+DATA, PARAMETER, COVARIANCE, OPERATOR = 1, 2, 3, 5
+
+_lib = None
+_ref = None
+
+
+def build_oracle(force: bool = False) -> str:
+    """Compile cravaoracle.c (portable C, OpenMP) into oracle/_build."""
+    src = [os.path.join(HERE, "cravaoracle.c"), os.path.join(HERE, "oracle_impl.inc")]
+    if not force and os.path.exists(ORACLE_SO) and all(
+        os.path.getmtime(ORACLE_SO) >= os.path.getmtime(s) for s in src
+    ):
+        return ORACLE_SO
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = ORACLE_SO + f".tmp{os.getpid()}"
+    subprocess.check_call(
+        ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-w",
+         src[0], "-lm", "-o", tmp]
+    )
+    os.replace(tmp, ORACLE_SO)
+    return ORACLE_SO
+
+
+def build_ref() -> str | None:
+    """Build oracle/_ref from the reference sources when they are present."""
+    if not os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft")):
+        return None
+    repo = os.path.dirname(HERE)
+    subprocess.check_call(
+        ["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), f"REF={REFERENCE_SRC}",
+         f"-j{os.cpu_count() or 4}"],
+        cwd=repo,
+    )
+    return REF_SO
+
+
+def _P(dt):
+    return np.ctypeslib.ndpointer(dtype=dt, flags="C_CONTIGUOUS")
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build_oracle()
+        L = ct.CDLL(ORACLE_SO)
+        for sfx, R in (("_f", ct.c_float), ("_d", ct.c_double)):
+            PR = ct.POINTER(R)
+            PPR = ct.POINTER(PR)
+            getattr(L, "or_fft3d_r2c" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+            getattr(L, "or_fft3d_c2r" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+            getattr(L, "or_fft1d_c2c" + sfx).argtypes = [PR, ct.c_int, ct.c_int]
+            getattr(L, "or_invert_bins" + sfx).argtypes = [
+                ct.c_int, ct.c_int, ct.c_int, ct.c_int, PPR, PPR, PPR, PR, PR, PR, PR, PR,
+                ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_int, ct.POINTER(ct.c_int), ct.c_int]
+            getattr(L, "or_simulate_bins" + sfx).argtypes = [ct.c_size_t, PPR, PPR, ct.c_int]
+            getattr(L, "or_state4d_merge" + sfx).argtypes = [ct.c_size_t, PPR, PPR, PPR, PPR, PPR, PPR, PPR, ct.c_int]
+            getattr(L, "or_state4d_split" + sfx).argtypes = [ct.c_size_t, PPR, PPR, PPR, PPR, PPR, PPR, PPR,
+                                                             ct.POINTER(ct.c_int), ct.c_int]
+            getattr(L, "or_fill_param_corr" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, PR, PR,
+                                                               ct.c_float, ct.c_float, R]
+            getattr(L, "or_fill_err_corr" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, PR,
+                                                             ct.c_float, ct.c_float]
+            getattr(L, "or_k_tables" + sfx).argtypes = [
+                ct.c_int, ct.c_int, ct.c_int, PR, ct.c_void_p, ct.c_float, ct.c_float, ct.c_float, ct.c_float,
+                ct.c_float, PR, PR, PR, PR, ct.c_void_p]
+            getattr(L, "or_circ_corr_t" + sfx).argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, PR]
+            getattr(L, "or_circ_corr_t" + sfx).restype = ct.c_int
+        L.or_fill_complex_noise.argtypes = [ct.POINTER(ct.c_float), ct.c_int, ct.c_int, ct.c_int,
+                                            ct.POINTER(ct.c_uint)]
+        L.or_rnorm01.argtypes = [ct.POINTER(ct.c_uint)]
+        L.or_rnorm01.restype = ct.c_double
+        L.or_find_closest_factorable.argtypes = [ct.c_int]
+        L.or_find_closest_factorable.restype = ct.c_int
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft"))
+
+
+def ref():
+    """The reference build (FFTW 2.1.2 + lib_matr + RandomGen).  x86 host only."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            build_ref()
+        L = ct.CDLL(REF_SO)
+        PF = ct.POINTER(ct.c_float)
+        PPF = ct.POINTER(PF)
+        L.ref_fft3d_r2c.argtypes = [PF, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+        L.ref_fft3d_c2r.argtypes = [PF, ct.c_int, ct.c_int, ct.c_int, ct.c_int]
+        L.ref_fft1d_r2c.argtypes = [PF, ct.c_int]
+        L.ref_chol_cpx.argtypes = [ct.c_int, PF]
+        L.ref_chol_cpx.restype = ct.c_int
+        L.ref_invert_bins.argtypes = [ct.c_int, ct.c_int, ct.c_int, ct.c_int, PPF, PPF, PPF, PF, PF, PF, PF, PF,
+                                      ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_int, ct.c_int]
+        L.ref_invert_bins.restype = ct.c_int
+        L.ref_simulate_bins.argtypes = [ct.c_long, PPF, PPF]
+        L.ref_rnorm01_seq.argtypes = [ct.c_uint, ct.c_int, ct.POINTER(ct.c_double)]
+        L.ref_fill_complex_noise.argtypes = [PF, ct.c_int, ct.c_int, ct.c_int, ct.c_uint, ct.c_int]
+        _ref = L
+    return _ref
+
+
+# ----------------------------------------------------------------------------
+# helpers
+# ----------------------------------------------------------------------------
+
+def dims(nxp):
+    cnxp = nxp // 2 + 1
+    return cnxp, 2 * cnxp
+
+
+def _rdt(prec):
+    return np.float32 if prec == "f" else np.float64
+
+
+def _ptr(a, R):
+    return a.ctypes.data_as(ct.POINTER(R))
+
+
+def _pp(arrs, R):
+    P = ct.POINTER(R)
+    return (P * len(arrs))(*[a.ctypes.data_as(P) for a in arrs])
+
+
+def _real_view(c):
+    """complex (.., cnxp) -> float view of the same memory"""
+    return c.view(np.float32 if c.dtype == np.complex64 else np.float64)
+
+
+def pad_real(cube, nxp):
+    """(nzp, nyp, nxp) real -> (nzp, nyp, rnxp) padded FFTGrid layout (pad = 0)."""
+    nzp, nyp, _ = cube.shape
+    _, rnxp = dims(nxp)
+    out = np.zeros((nzp, nyp, rnxp), dtype=cube.dtype)
+    out[:, :, :nxp] = cube
+    return out
+
+
+def fft3d_r2c(real_padded, nxp, cubetype, prec="f", nthreads=1):
+    """FFTGrid::fftInPlace on a copy; returns the (nzp, nyp, cnxp) spectrum."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    a = np.ascontiguousarray(real_padded, dtype=_rdt(prec)).copy()
+    nzp, nyp, _ = a.shape
+    getattr(lib(), "or_fft3d_r2c_" + prec)(_ptr(a, R), nxp, nyp, nzp, cubetype, nthreads)
+    return a.view(np.complex64 if prec == "f" else np.complex128)
+
+
+def fft3d_c2r(spec, nxp, cubetype, prec="f", nthreads=1):
+    """FFTGrid::invFFTInPlace on a copy; returns the (nzp, nyp, rnxp) real cube."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    a = np.ascontiguousarray(spec, dtype=np.complex64 if prec == "f" else np.complex128).copy()
+    nzp, nyp, _ = a.shape
+    r = _real_view(a)
+    getattr(lib(), "or_fft3d_c2r_" + prec)(_ptr(r, R), nxp, nyp, nzp, cubetype, nthreads)
+    return r
+
+
+def invert_bins(data, mean, cov, errcorr, tables, errThetaCov, sigma0, wnc, is4d=False, prec="f",
+                nthreads=1):
+    """Bin loop of Crava::computePostMeanResidAndFFTCov on copies.
+
+    data: list of n spectra; mean: 3; cov: 6 (00,11,22,01,02,12); errcorr: 1.
+    tables: dict with K (nzp,n,3), em1/em2/em3 (nzp,n) complex and band (nzp,) uint8.
+    Returns (residuals, post_mean, post_cov, n_failed_cholesky).
+    """
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    d = [np.ascontiguousarray(x, dtype=cdt).copy() for x in data]
+    m = [np.ascontiguousarray(x, dtype=cdt).copy() for x in mean]
+    c = [np.ascontiguousarray(x, dtype=cdt).copy() for x in cov]
+    e = np.ascontiguousarray(errcorr, dtype=cdt)
+    nzp, nyp, cnxp = d[0].shape
+    nxp = tables["nxp"]
+    n = len(d)
+    K = np.ascontiguousarray(tables["K"], dtype=cdt)
+    e1 = np.ascontiguousarray(tables["em1"], dtype=cdt)
+    e2 = np.ascontiguousarray(tables["em2"], dtype=cdt)
+    e3 = np.ascontiguousarray(tables["em3"], dtype=cdt)
+    band = np.ascontiguousarray(tables["band"], dtype=np.uint8)
+    etc = np.ascontiguousarray(errThetaCov, dtype=np.float64)
+    s0 = np.ascontiguousarray(sigma0, dtype=np.float64)
+    nf = ct.c_int(0)
+    rv = lambda a: _ptr(_real_view(a), R)  # noqa: E731
+    getattr(lib(), "or_invert_bins_" + prec)(
+        nxp, nyp, nzp, n, _pp([_real_view(x) for x in d], R), _pp([_real_view(x) for x in m], R),
+        _pp([_real_view(x) for x in c], R), rv(e), rv(K), rv(e1), rv(e2), rv(e3),
+        band.ctypes.data, etc.ctypes.data, s0.ctypes.data, float(wnc), int(is4d), ct.byref(nf), nthreads)
+    return d, m, c, nf.value
+
+
+def ref_invert_bins(data, mean, cov, errcorr, tables, errThetaCov, sigma0, wnc, is4d=False, nthreads=1):
+    """Same contract as invert_bins, computed with the reference's lib_matr (FP32)."""
+    R = ct.c_float
+    d = [np.ascontiguousarray(x, dtype=np.complex64).copy() for x in data]
+    m = [np.ascontiguousarray(x, dtype=np.complex64).copy() for x in mean]
+    c = [np.ascontiguousarray(x, dtype=np.complex64).copy() for x in cov]
+    e = np.ascontiguousarray(errcorr, dtype=np.complex64)
+    nzp, nyp, cnxp = d[0].shape
+    n = len(d)
+    K = np.ascontiguousarray(tables["K"], dtype=np.complex64)
+    e1 = np.ascontiguousarray(tables["em1"], dtype=np.complex64)
+    e2 = np.ascontiguousarray(tables["em2"], dtype=np.complex64)
+    e3 = np.ascontiguousarray(tables["em3"], dtype=np.complex64)
+    band = np.ascontiguousarray(tables["band"], dtype=np.uint8)
+    etc = np.ascontiguousarray(errThetaCov, dtype=np.float64)
+    s0 = np.ascontiguousarray(sigma0, dtype=np.float64)
+    rv = lambda a: _ptr(_real_view(a), R)  # noqa: E731
+    nf = ref().ref_invert_bins(
+        tables["nxp"], nyp, nzp, n, _pp([_real_view(x) for x in d], R), _pp([_real_view(x) for x in m], R),
+        _pp([_real_view(x) for x in c], R), rv(e), rv(K), rv(e1), rv(e2), rv(e3),
+        band.ctypes.data, etc.ctypes.data, s0.ctypes.data, float(wnc), int(is4d), nthreads)
+    return d, m, c, nf
+
+
+def ref_fft3d_r2c(real_padded, nxp, cubetype):
+    a = np.ascontiguousarray(real_padded, dtype=np.float32).copy()
+    nzp, nyp, _ = a.shape
+    ref().ref_fft3d_r2c(_ptr(a, ct.c_float), nxp, nyp, nzp, cubetype)
+    return a.view(np.complex64)
+
+
+def ref_fft3d_c2r(spec, nxp, cubetype):
+    a = np.ascontiguousarray(spec, dtype=np.complex64).copy()
+    nzp, nyp, _ = a.shape
+    r = a.view(np.float32)
+    ref().ref_fft3d_c2r(_ptr(r, ct.c_float), nxp, nyp, nzp, cubetype)
+    return r
+
+
+def simulate_bins(cov6, seeds3, prec="f", nthreads=1):
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    c = [np.ascontiguousarray(x, dtype=cdt) for x in cov6]
+    s = [np.ascontiguousarray(x, dtype=cdt).copy() for x in seeds3]
+    getattr(lib(), "or_simulate_bins_" + prec)(c[0].size, _pp([_real_view(x) for x in c], R),
+                                               _pp([_real_view(x) for x in s], R), nthreads)
+    return s
+
+
+def ref_simulate_bins(cov6, seeds3):
+    R = ct.c_float
+    c = [np.ascontiguousarray(x, dtype=np.complex64) for x in cov6]
+    s = [np.ascontiguousarray(x, dtype=np.complex64).copy() for x in seeds3]
+    ref().ref_simulate_bins(c[0].size, _pp([_real_view(x) for x in c], R), _pp([_real_view(x) for x in s], R))
+    return s
+
+
+def state4d_merge(mu_s, mu_d, ss, sd, dd, prec="f", nthreads=1):
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    args = [[np.ascontiguousarray(x, dtype=cdt) for x in grp] for grp in (mu_s, mu_d, ss, sd, dd)]
+    mu_cur = [np.zeros_like(args[0][0]) for _ in range(3)]
+    cov_cur = [np.zeros_like(args[0][0]) for _ in range(6)]
+    pp = [_pp([_real_view(x) for x in grp], R) for grp in args + [mu_cur, cov_cur]]
+    getattr(lib(), "or_state4d_merge_" + prec)(args[0][0].size, *pp, nthreads)
+    return mu_cur, cov_cur
+
+
+def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post6, prec="f", nthreads=1):
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    st = [[np.ascontiguousarray(x, dtype=cdt).copy() for x in grp] for grp in (mu_s, mu_d, ss, sd, dd)]
+    post = [[np.ascontiguousarray(x, dtype=cdt) for x in grp] for grp in (mu_post, cov_post6)]
+    nf = ct.c_int(0)
+    pp = [_pp([_real_view(x) for x in grp], R) for grp in st + post]
+    getattr(lib(), "or_state4d_split_" + prec)(st[0][0].size, *pp, ct.byref(nf), nthreads)
+    return st, nf.value
+
+
+def fill_param_corr(nxp, nyp, nzp, corrXY, circCorrT, gradI=0.0, gradJ=0.0, scalar=1.0, prec="f"):
+    R = ct.c_float if prec == "f" else ct.c_double
+    _, rnxp = dims(nxp)
+    buf = np.zeros((nzp, nyp, rnxp), dtype=_rdt(prec))
+    cxy = np.ascontiguousarray(corrXY, dtype=_rdt(prec))
+    ct_ = np.ascontiguousarray(circCorrT, dtype=_rdt(prec))
+    getattr(lib(), "or_fill_param_corr_" + prec)(_ptr(buf, R), nxp, nyp, nzp, _ptr(cxy, R), _ptr(ct_, R),
+                                                 gradI, gradJ, scalar)
+    return buf
+
+
+def fill_err_corr(nxp, nyp, nzp, corrXY, gradI=0.0, gradJ=0.0, prec="f"):
+    R = ct.c_float if prec == "f" else ct.c_double
+    _, rnxp = dims(nxp)
+    buf = np.zeros((nzp, nyp, rnxp), dtype=_rdt(prec))
+    cxy = np.ascontiguousarray(corrXY, dtype=_rdt(prec))
+    getattr(lib(), "or_fill_err_corr_" + prec)(_ptr(buf, R), nxp, nyp, nzp, _ptr(cxy, R), gradI, gradJ)
+    return buf
+
+
+def k_tables(nxp, wavelets, A, nz, nzp, dt_ms, lowCut, highCut, minRelThick=1.0, prec="f"):
+    """fillErrMultVectors for every k (constant-thickness branch)."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    w = np.ascontiguousarray(wavelets, dtype=_rdt(prec))
+    n = w.shape[0]
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    K = np.zeros((nzp, n, 3), dtype=cdt)
+    e1 = np.zeros((nzp, n), dtype=cdt)
+    e2 = np.zeros((nzp, n), dtype=cdt)
+    e3 = np.zeros((nzp, n), dtype=cdt)
+    band = np.zeros(nzp, dtype=np.uint8)
+    lz = nz * dt_ms
+    getattr(lib(), "or_k_tables_" + prec)(n, nz, nzp, _ptr(w, R), A32.ctypes.data, dt_ms, lz, minRelThick,
+                                          lowCut, highCut, _ptr(_real_view(K), R), _ptr(_real_view(e1), R),
+                                          _ptr(_real_view(e2), R), _ptr(_real_view(e3), R), band.ctypes.data)
+    return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band, "nxp": nxp}
+
+
+def circ_corr_t(priorCorrT, minIntFq, nzp, prec="f"):
+    R = ct.c_float if prec == "f" else ct.c_double
+    pc = np.ascontiguousarray(priorCorrT, dtype=np.float32)
+    out = np.zeros(nzp, dtype=_rdt(prec))
+    rc = getattr(lib(), "or_circ_corr_t_" + prec)(pc.ctypes.data, pc.size, minIntFq, nzp, _ptr(out, R))
+    if rc:
+        raise ValueError("circular temporal correlation undefined (CircCorrT[0] <= 1e-5)")
+    return out
+
+
+def fill_complex_noise(nxp, nyp, nzp, seed, ncubes=1):
+    """FFTGrid::fillInComplexNoise x ncubes with a RandomGen seeded by `seed`."""
+    cnxp, _ = dims(nxp)
+    out = np.zeros((ncubes, nzp, nyp, cnxp), dtype=np.complex64)
+    st = ct.c_uint(seed)
+    for c in range(ncubes):
+        lib().or_fill_complex_noise(_ptr(out[c].view(np.float32), ct.c_float), nxp, nyp, nzp, ct.byref(st))
+    return out
+
+
+def ref_fill_complex_noise(nxp, nyp, nzp, seed, ncubes=1):
+    cnxp, _ = dims(nxp)
+    out = np.zeros((ncubes, nzp, nyp, cnxp), dtype=np.complex64)
+    ref().ref_fill_complex_noise(_ptr(out.view(np.float32), ct.c_float), nxp, nyp, nzp, seed, ncubes)
+    return out
+
+
+def rnorm01_seq(seed, n):
+    st = ct.c_uint(seed)
+    return np.array([lib().or_rnorm01(ct.byref(st)) for _ in range(n)])
+
+
+def ref_rnorm01_seq(seed, n):
+    out = np.zeros(n, dtype=np.float64)
+    ref().ref_rnorm01_seq(seed, n, out.ctypes.data_as(ct.POINTER(ct.c_double)))
+    return out
+
+
+def find_closest_factorable(n):
+    return lib().or_find_closest_factorable(int(n))
