@@ -1,0 +1,413 @@
+"""Benchmark: 256^3 FFT-domain AVO inversion on one GB300 (per GPU replica).
+
+Workload: a 256x256x256 padded cube, 5 angle stacks at 0/10/20/30/40 deg, a
+25 Hz Ricker wavelet notched at 2 and 80 Hz, S/N 3, inversion band 1-100 Hz
+(seeded synthetic data, generated on the host).  One step = one complete
+inversion (forward transforms of the 5 data and 3 prior-mean cubes, the
+prior/error spectra, the per-bin posterior, inverse transforms of the 3
+posterior means), inputs resident in HBM.
+
+Forms timed: "plain" (the reference dataflow on the GPU, all FP32), "fp32"
+(fused, all FP32), "mixed" (fused, FP32 bulk + FP64-guarded bins; the
+headline).  "fp64" runs once as the accuracy reference.
+
+Metric: Mbins/s = (cnxp*nyp*nzp bins) / (ms per inversion).  With --gpus N
+under torchrun each rank runs an independent replica (the path does not shard
+a cube; cubes are independent), value = total bins / max time.
+
+--impl reference times the reference algorithm on the host cores (the C
+oracle port: its FFTs and its lib_matr-order bin loop, OpenMP over k like the
+reference) on a bounded sample scaled to a full inversion.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "256^3 AVO inversion ms, Mbins/s: mixed vs plain FP32 GPU at <=1e-5 err vs FP64"
+WORKLOAD = ("256^3 padded cube, 5 stacks 0-40 deg, 25 Hz Ricker notched at 2/80 Hz, S/N 3, "
+            "band 1-100 Hz, seeded synthetic inputs")
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(REPO, "profiles", "ncu_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rel(a, b):
+    import numpy as np
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (oracle port) timing
+# ---------------------------------------------------------------------------
+def cpu_reference_sample(sc, tables, kplanes=8, threads=None):
+    """Time the reference algorithm on the host on a bounded sample.
+
+    Sample: one forward and one inverse 3D transform of a full cube, plus the
+    bin loop over `kplanes` in-band k-planes.  Scaled to one inversion of the
+    reference dataflow: (n + 3 + 6 + 1) forward transforms, 3 inverse
+    transforms, all bins.
+    """
+    import numpy as np
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    nxp, nyp, nzp, n = sc.nxp, sc.nyp, sc.nzp, sc.ntheta
+    t0 = time.perf_counter()
+    spec = O.fft3d_r2c(sc.data[0], nxp, O.DATA, "f", threads)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.fft3d_c2r(spec, nxp, O.PARAMETER, "f", threads)
+    t_inv = time.perf_counter() - t0
+    # bin loop on a slab of in-band k-planes (inputs: random spectra of the right shape)
+    ks = [k for k in range(nzp) if tables["band"][k]][:kplanes]
+    rng = np.random.default_rng(1)
+    cnxp = nxp // 2 + 1
+    shp = (len(ks), nyp, cnxp)
+
+    def rc():
+        return (rng.standard_normal(shp) + 1j * rng.standard_normal(shp)).astype(np.complex64)
+    data = [rc() for _ in range(n)]
+    mean = [rc() for _ in range(3)]
+    # prior spectra of the planes from the separable model (so every Cholesky does its full work)
+    cxy = np.fft.rfft2(sc.corr_xy.astype(np.float64))            # (nyp, cnxp)
+    ctk = np.fft.fft(sc.circ_corr_t.astype(np.float64))[ks]      # (len(ks),)
+    c = (ctk[:, None, None] * cxy[None, :, :]).real.astype(np.float32)
+    s0 = sc.sigma0.astype(np.float32)
+    cov = [(c * s0[p, q]).astype(np.complex64) for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]]
+    ec = np.broadcast_to(cxy.real.astype(np.float32), shp).astype(np.complex64)
+    sub = {"K": tables["K"][ks], "em1": tables["em1"][ks], "em2": tables["em2"][ks], "em3": tables["em3"][ks],
+           "band": np.ones(len(ks), np.uint8), "nxp": nxp}
+    t0 = time.perf_counter()
+    O.invert_bins(data, mean, cov, ec, sub, sc.err_theta_cov, sc.sigma0, sc.wnc, prec="f", nthreads=threads)
+    t_bins = time.perf_counter() - t0
+    inband = int(np.asarray(tables["band"]).sum())
+    t_full = (n + 3 + 6 + 1) * t_fwd + 3 * t_inv + t_bins * inband / max(1, len(ks))
+    sample = (f"1 forward + 1 inverse 256^3 transform and the bin loop over {len(ks)} of {inband} in-band "
+              f"k-planes, scaled to {n + 10} forward + 3 inverse transforms and all bins")
+    return t_full, threads, sample, {"t_fwd_s": t_fwd, "t_inv_s": t_inv, "t_bins_sample_s": t_bins}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import numpy as np
+    from crava_gb300 import synthetic as S
+    from crava_gb300 import api
+    sc = S.config1()
+    tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut)
+    bins = sc.nbins
+    for _ in range(args.warmup):
+        cpu_reference_sample(sc, tables, kplanes=2)
+    times = []
+    info = None
+    for _ in range(args.steps):
+        t, cores, sample, info = cpu_reference_sample(sc, tables)
+        times.append(t)
+    ms = 1e3 * statistics.mean(times)
+    value = bins / (ms * 1e-3) / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": "Mbins/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "nxp": sc.nxp, "nyp": sc.nyp, "nzp": sc.nzp, "ntheta": sc.ntheta,
+                   "bins": bins, "form": "reference dataflow on the host (C oracle port, OpenMP)"},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mbins/s", "cores": cores, "kind": "port",
+                         "sample": sample, **{k: round(v, 4) for k, v in info.items()}},
+        "e2e": {"value": round(value, 4), "unit": "Mbins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU
+# ---------------------------------------------------------------------------
+def run_ours(args, world, rank, local):
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    import crava_gb300
+    from crava_gb300 import _native, api
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+
+    crava_gb300.lib()
+    t0 = time.perf_counter()
+    sc = S.config1(seed=20261204 + rank)
+    t_gen = time.perf_counter() - t0
+    inv = Inversion(sc, forms=("plain", "fp32", "mixed", "fp64"))
+    bins = sc.nbins
+    stream = torch.cuda.current_stream()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # 256 MB > L2
+
+    def timed(form, k):
+        evs = []
+        for _ in range(k):
+            inv.restore(form)          # real-domain inputs back in place (not timed)
+            flush.fill_(1.0)           # evict L2 between steps
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            inv.run(form)
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    results = {}
+    forms = ["plain", "fp32", "mixed"]
+    clocks = ClockSampler(local)
+    for form in forms:
+        timed(form, args.warmup)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    for form in forms:
+        barrier(world)
+        torch.cuda.synchronize()
+        ms = timed(form, args.steps)
+        barrier(world)
+        torch.cuda.synchronize()
+        results[form] = statistics.mean(ms)
+    clk = clocks.stop()
+
+    # accuracy against the FP64 run on the same inputs
+    inv.restore("fp64")
+    inv.run("fp64")
+    torch.cuda.synchronize()
+    pm64, res64, cov64 = inv.results("fp64")
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    acc = {}
+    for form in forms:
+        inv.restore(form)
+        inv.ws.reset_stats()
+        inv.run(form)
+        torch.cuda.synchronize()
+        pm, res, cov = inv.results(form)
+        st = inv.ws.stats()
+        acc[form] = {"mean_rel_err": rel(pm, pm64), "update_rel_err": rel(pm - prior, pm64 - prior),
+                     "resid_rel_err": rel(res, res64), "cov_rel_err": rel(cov, cov64),
+                     "fp64_bins": st["flagged"] if form == "mixed" else 0, "chol_fail": st["failed"]}
+        del pm, res, cov
+
+    # per-kernel launch times and algorithmic bytes, one traced mixed step
+    inv.restore("mixed")
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    inv.run("mixed")
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    launches_per_step = sum(v[0] for v in tr.values())
+    dom = max(tr.items(), key=lambda kv: kv[1][1])
+    dname, (dl, dms, dbytes) = dom
+    peak, peak_kind = load_peaks()
+    achieved = (dbytes / dl) / (dms / dl * 1e-3) / 1e9 if dms > 0 else 0.0
+    traffic = load_traffic().get(dname)
+
+    # end to end: pinned host inputs -> device, inversion, results -> host
+    h_data = torch.from_numpy(np.stack(sc.data)).pin_memory()
+    h_mean = torch.from_numpy(np.stack(sc.mean)).pin_memory()
+    shape = tuple(h_data.shape[1:])
+    h_out_mean = torch.empty((3,) + shape, dtype=torch.float32).pin_memory()
+    h_out_res = torch.empty((sc.ntheta,) + shape, dtype=torch.float32).pin_memory()
+    h_out_cov = torch.empty((6,) + shape, dtype=torch.float32).pin_memory()
+    h2d = (h_data.numel() + h_mean.numel()) * 4
+    d2h = (h_out_mean.numel() + h_out_res.numel() + h_out_cov.numel()) * 4
+
+    def e2e_step():
+        for l in range(sc.ntheta):
+            inv.data[l].copy_(h_data[l], non_blocking=True)
+        for p in range(3):
+            inv.mean[p].copy_(h_mean[p], non_blocking=True)
+        inv.run("mixed")
+        for p in range(3):
+            h_out_mean[p].copy_(inv.mean[p], non_blocking=True)
+        for l in range(sc.ntheta):
+            h_out_res[l].copy_(inv.data[l], non_blocking=True)
+        for t in range(6):
+            h_out_cov[t].copy_(inv.cov[t], non_blocking=True)
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(world)
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    b.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = a.elapsed_time(b) / args.steps
+
+    ms_mixed = max_over_ranks(results["mixed"], world)
+    ms_plain = max_over_ranks(results["plain"], world)
+    ms_fp32 = max_over_ranks(results["fp32"], world)
+    e2e_ms = max_over_ranks(e2e_ms, world)
+    total_bins = bins * world
+    value = total_bins / (ms_mixed * 1e-3) / 1e6
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        t_full, cores, sample, info = cpu_reference_sample(sc, inv.tables)
+        cpu = {"value": round(bins / t_full / 1e6, 4), "unit": "Mbins/s", "cores": cores, "kind": "port",
+               "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mbins/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_mixed, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (FP64-guarded bins)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "nxp": sc.nxp, "nyp": sc.nyp, "nzp": sc.nzp, "ntheta": sc.ntheta,
+                       "bins": bins, "inband_bins": int(inv.tables["band"].sum()) * sc.cnxp * sc.nyp,
+                       "form": "mixed (fused, FP64-guarded)", "parallelism": f"replicas x{world}",
+                       "l2": "256 MB flush + ~1.3 GB input restore between timed steps; working set 1.4 GB > L2"},
+            "forms_ms": {"plain": round(ms_plain, 4), "fp32": round(ms_fp32, 4), "mixed": round(ms_mixed, 4)},
+            "speedup_mixed_vs_plain": round(ms_plain / ms_mixed, 3),
+            "accuracy_vs_fp64": {f: {k: (float(f"{v:.3e}") if isinstance(v, float) else v) for k, v in d.items()}
+                                 for f, d in acc.items()},
+            "roofline": {"bound": "hbm", "kernel": dname, "achieved": round(achieved, 1), "peak": peak,
+                         "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                         "traffic": traffic, "launches_per_step": dl,
+                         "algorithmic_bytes_per_launch": dbytes / dl,
+                         "pipeline_algorithmic_GBps": round(inv.algorithmic_bytes("mixed") / (ms_mixed * 1e-3) / 1e9, 1)},
+            "kernels_per_step": {k: {"launches": v[0], "ms": round(v[1], 4), "GBps": round(v[2] / max(v[1], 1e-9) / 1e6, 1)}
+                                 for k, v in sorted(tr.items(), key=lambda kv: -kv[1][1])},
+            "e2e": {"value": round(total_bins / (e2e_ms * 1e-3) / 1e6, 3), "unit": "Mbins/s",
+                    "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches_per_step * args.steps,
+            "clocks": clk,
+            "cpu_baseline": cpu,
+            "setup_s": {"synthetic_generation": round(t_gen, 1)},
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 0)
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,194 @@
+"""Python mirror of the reference's FFTGrid / Crava surface over the C-ABI.
+
+torch provides device memory and streams; every transform and every per-bin
+solve runs in libcravagpu.so.  Names follow the reference:
+
+* ``fft_in_place`` / ``inv_fft_in_place``  -- FFTGrid::fftInPlace / invFFTInPlace
+  (src/fftgrid.cpp:1783-1842) on a padded cube tensor of shape
+  ``(nzp, nyp, rnxp)`` (float32 or float64), in place.
+* ``Workspace``  -- per-model device state; ``invert_plain`` / ``invert_fused``
+  run the bin loop of Crava::computePostMeanResidAndFFTCov
+  (src/crava.cpp:1084-1247).
+* ``operator_tables`` -- the per-k tables of Crava::fillErrMultVectors
+  (src/crava.cpp:1337-1386) built on the host in C++.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+import torch
+
+from ._native import check, lib
+
+DATA, PARAMETER, COVARIANCE, VELOCITY, OPERATOR = 1, 2, 3, 4, 5
+PREC_FP32, PREC_MIXED, PREC_FP64 = 0, 1, 2
+
+
+def dims(nxp: int):
+    cnxp = nxp // 2 + 1
+    return cnxp, 2 * cnxp
+
+
+def _stream(stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ct.c_void_p(s.cuda_stream)
+
+
+def _vp(t: torch.Tensor):
+    return ct.c_void_p(t.data_ptr())
+
+
+def _pp(ts):
+    arr = (ct.c_void_p * len(ts))(*[t.data_ptr() for t in ts])
+    return ct.cast(arr, ct.POINTER(ct.c_void_p)), arr
+
+
+def check_call(name, *args):
+    """Call a C-ABI entry point by name; tensors and streams become pointers."""
+    conv = []
+    for a in args:
+        if isinstance(a, torch.Tensor):
+            conv.append(ct.c_void_p(a.data_ptr()))
+        elif isinstance(a, torch.cuda.Stream):
+            conv.append(ct.c_void_p(a.cuda_stream))
+        else:
+            conv.append(a)
+    check(getattr(lib(), name)(*conv), name)
+
+
+def new_cube(nxp, nyp, nzp, dtype=torch.float32, device="cuda"):
+    """Zeroed padded cube (nzp, nyp, rnxp) in the FFTGrid in-place layout."""
+    _, rnxp = dims(nxp)
+    return torch.zeros((nzp, nyp, rnxp), dtype=dtype, device=device)
+
+
+def as_spectrum(cube: torch.Tensor) -> torch.Tensor:
+    """Complex view (nzp, nyp, cnxp) of a transformed cube."""
+    nzp, nyp, rnxp = cube.shape
+    return torch.view_as_complex(cube.view(nzp, nyp, rnxp // 2, 2))
+
+
+def _check_cube(t: torch.Tensor, nxp: int):
+    if not t.is_cuda or not t.is_contiguous():
+        raise ValueError("cube must be a contiguous CUDA tensor")
+    _, rnxp = dims(nxp)
+    if t.dim() != 3 or t.shape[2] != rnxp:
+        raise ValueError(f"cube shape {tuple(t.shape)} does not match nxp={nxp} (rnxp={rnxp})")
+
+
+def fft_in_place(cube: torch.Tensor, nxp: int, cubetype: int, stream=None):
+    _check_cube(cube, nxp)
+    nzp, nyp, _ = cube.shape
+    if cube.dtype == torch.float32:
+        check(lib().cg_fft3d_r2c(_vp(cube), nxp, nyp, nzp, cubetype, _stream(stream)), "cg_fft3d_r2c")
+    elif cube.dtype == torch.float64:
+        check(lib().cg_fft3d_r2c_f64(_vp(cube), nxp, nyp, nzp, cubetype, _stream(stream)), "cg_fft3d_r2c_f64")
+    else:
+        raise TypeError(cube.dtype)
+    return cube
+
+
+def inv_fft_in_place(cube: torch.Tensor, nxp: int, cubetype: int, stream=None):
+    _check_cube(cube, nxp)
+    nzp, nyp, _ = cube.shape
+    if cube.dtype == torch.float32:
+        check(lib().cg_fft3d_c2r(_vp(cube), nxp, nyp, nzp, cubetype, _stream(stream)), "cg_fft3d_c2r")
+    elif cube.dtype == torch.float64:
+        check(lib().cg_fft3d_c2r_f64(_vp(cube), nxp, nyp, nzp, cubetype, _stream(stream)), "cg_fft3d_c2r_f64")
+    else:
+        raise TypeError(cube.dtype)
+    return cube
+
+
+def fft_in_place_batch(cubes, nxp: int, cubetype: int, inverse=False, stream=None):
+    for c in cubes:
+        _check_cube(c, nxp)
+        if c.dtype != torch.float32:
+            raise TypeError("batched transforms take float32 cubes")
+    nzp, nyp, _ = cubes[0].shape
+    pp, keep = _pp(cubes)
+    fn = lib().cg_fft3d_c2r_batch if inverse else lib().cg_fft3d_r2c_batch
+    check(fn(pp, len(cubes), nxp, nyp, nzp, cubetype, _stream(stream)), "cg_fft3d batch")
+    del keep
+    return cubes
+
+
+def operator_tables(wavelets, A, nz, nzp, dt_ms, low_cut, high_cut, min_rel_thick=1.0):
+    """Per-k forward operator and error multipliers (host, C++)."""
+    w = np.ascontiguousarray(wavelets, dtype=np.float32)
+    n = w.shape[0]
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    K = np.zeros((nzp, n, 3), dtype=np.complex64)
+    e1 = np.zeros((nzp, n), dtype=np.complex64)
+    e2 = np.zeros((nzp, n), dtype=np.complex64)
+    e3 = np.zeros((nzp, n), dtype=np.complex64)
+    band = np.zeros(nzp, dtype=np.uint8)
+    L = lib()
+    check(L.cg_operator_tables(n, nz, nzp, w.ctypes.data, A32.ctypes.data, dt_ms, min_rel_thick, low_cut, high_cut,
+                               K.ctypes.data, e1.ctypes.data, e2.ctypes.data, e3.ctypes.data, band.ctypes.data),
+          "cg_operator_tables")
+    return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band}
+
+
+class _Model(ct.Structure):
+    _fields_ = [("ntheta", ct.c_int), ("wnc", ct.c_float), ("is4d", ct.c_int), ("K", ct.c_void_p),
+                ("em1", ct.c_void_p), ("em2", ct.c_void_p), ("em3", ct.c_void_p), ("band", ct.c_void_p),
+                ("err_theta_cov", ct.c_void_p), ("sigma0", ct.c_void_p), ("cond_threshold", ct.c_double)]
+
+
+class Workspace:
+    """Device state of one inversion model (cg_workspace)."""
+
+    def __init__(self, nxp, nyp, nzp, ntheta):
+        self.nxp, self.nyp, self.nzp, self.ntheta = nxp, nyp, nzp, ntheta
+        h = ct.c_void_p()
+        check(lib().cg_workspace_create(ct.byref(h), nxp, nyp, nzp, ntheta), "cg_workspace_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cg_workspace_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_model(self, tables, err_theta_cov, sigma0, wnc, is4d=False, cond_threshold=0.0):
+        self._keep = [np.ascontiguousarray(tables[k], dtype=np.complex64) for k in ("K", "em1", "em2", "em3")]
+        band = np.ascontiguousarray(tables["band"], dtype=np.uint8)
+        etc = np.ascontiguousarray(err_theta_cov, dtype=np.float64)
+        s0 = np.ascontiguousarray(sigma0, dtype=np.float64).reshape(9)
+        m = _Model(self.ntheta, float(wnc), int(is4d), *[a.ctypes.data for a in self._keep], band.ctypes.data,
+                   etc.ctypes.data, s0.ctypes.data, float(cond_threshold))
+        check(lib().cg_workspace_set_model(self.h, ct.byref(m)), "cg_workspace_set_model")
+
+    def reset_stats(self, stream=None):
+        check(lib().cg_workspace_reset_stats(self.h, _stream(stream)), "cg_workspace_reset_stats")
+
+    def stats(self):
+        a, b, c = ct.c_int(), ct.c_int(), ct.c_int()
+        check(lib().cg_workspace_stats(self.h, ct.byref(a), ct.byref(b), ct.byref(c)), "cg_workspace_stats")
+        return {"flagged": a.value, "failed": b.value, "overflow": c.value}
+
+    def invert_plain(self, data, mean, cov, errcorr, stream=None):
+        pd, k1 = _pp(data)
+        pm, k2 = _pp(mean)
+        pc, k3 = _pp(cov)
+        check(lib().cg_invert_bins_plain(self.h, pd, pm, pc, _vp(errcorr), _stream(stream)), "cg_invert_bins_plain")
+
+    def prior_spectra(self, corr_xy, circ_corr_t, precision=PREC_MIXED, stream=None):
+        check(lib().cg_prior_spectra(self.h, _vp(corr_xy), _vp(circ_corr_t), precision, _stream(stream)),
+              "cg_prior_spectra")
+
+    def invert_fused(self, data, mean, cov, precision=PREC_MIXED, stream=None):
+        pd, k1 = _pp(data)
+        pm, k2 = _pp(mean)
+        pc, k3 = _pp(cov)
+        if data[0].dtype == torch.float64:
+            check(lib().cg_invert_bins_fused_f64(self.h, pd, pm, pc, _stream(stream)), "cg_invert_bins_fused_f64")
+        else:
+            check(lib().cg_invert_bins_fused(self.h, pd, pm, pc, precision, _stream(stream)), "cg_invert_bins_fused")

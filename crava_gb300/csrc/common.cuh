@@ -1,0 +1,60 @@
+// Shared device/host helpers for the GB300 AVO inversion library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "cravagpu.h"
+
+namespace cg {
+
+// ---------------------------------------------------------------------------
+// complex arithmetic on float2 / double2
+// ---------------------------------------------------------------------------
+template <typename T> struct cplx;
+template <> struct cplx<float> { typedef float2 type; };
+template <> struct cplx<double> { typedef double2 type; };
+
+template <typename T> using C2 = typename cplx<T>::type;
+
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> mk(T re, T im) { C2<T> r; r.x = re; r.y = im; return r; }
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> cadd(C2<T> a, C2<T> b) { return mk<T>(a.x + b.x, a.y + b.y); }
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> csub(C2<T> a, C2<T> b) { return mk<T>(a.x - b.x, a.y - b.y); }
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> cmul(C2<T> a, C2<T> b) {
+  return mk<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> cmulc(C2<T> a, C2<T> b) {
+  return mk<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> cconj(C2<T> a) { return mk<T>(a.x, -a.y); }
+template <typename T>
+__host__ __device__ __forceinline__ C2<T> cscale(C2<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
+
+// ---------------------------------------------------------------------------
+// error plumbing for the C-ABI
+// ---------------------------------------------------------------------------
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *where);
+
+#define CG_CUDA(call)                                           \
+  do {                                                          \
+    cudaError_t e_ = (call);                                    \
+    if (e_ != cudaSuccess) return ::cg::cuda_status(e_, #call); \
+  } while (0)
+
+#define CG_CHECK_LAUNCH(where)                                  \
+  do {                                                          \
+    cudaError_t e_ = cudaGetLastError();                        \
+    if (e_ != cudaSuccess) return ::cg::cuda_status(e_, where); \
+  } while (0)
+
+inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
+
+}  // namespace cg

@@ -1,0 +1,171 @@
+// Shared-memory Stockham FFT building blocks (device) and FFT plan types.
+#pragma once
+
+#include "common.cuh"
+
+namespace cg {
+
+constexpr int kMaxStages = 16;
+constexpr int kMaxFFT = 8192;  // longest axis handled by one shared-memory tile
+constexpr int kFFTThreads = 256;
+constexpr int kRows = 16;      // x rows per CTA in the row passes
+constexpr int kMaxBatch = 16;  // cubes per launch
+constexpr size_t kMaxSmem = 227 * 1024;  // dynamic shared memory per CTA on sm_103a
+
+struct AxisPlan {
+  int n;
+  int nstages;
+  int radix[kMaxStages];
+};
+
+struct CubeSet {
+  void *ptr[kMaxBatch];
+};
+
+bool make_axis_plan(int n, AxisPlan *p);
+template <typename T> const C2<T> *twiddle_table(int n);
+template <typename T>
+int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st);
+
+// twiddle W (forward table entry) applied with the transform's sign
+template <typename T>
+__device__ __forceinline__ C2<T> tw_at(const C2<T> *tw, int idx, int sign)
+{
+  C2<T> w = tw[idx];
+  if (sign > 0) w.y = -w.y;
+  return w;
+}
+
+// multiply by sign*i
+template <typename T>
+__device__ __forceinline__ C2<T> mul_si(C2<T> a, int sign)
+{
+  return sign > 0 ? mk<T>(-a.y, a.x) : mk<T>(a.y, -a.x);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft2(C2<T> *v)
+{
+  C2<T> a = v[0], b = v[1];
+  v[0] = cadd<T>(a, b);
+  v[1] = csub<T>(a, b);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft4(C2<T> *v, int sign)
+{
+  C2<T> s02 = cadd<T>(v[0], v[2]), d02 = csub<T>(v[0], v[2]);
+  C2<T> s13 = cadd<T>(v[1], v[3]), d13 = mul_si<T>(csub<T>(v[1], v[3]), sign);
+  v[0] = cadd<T>(s02, s13);
+  v[2] = csub<T>(s02, s13);
+  v[1] = cadd<T>(d02, d13);
+  v[3] = csub<T>(d02, d13);
+}
+
+template <typename T>
+__device__ __forceinline__ void dft8(C2<T> *v, int sign)
+{
+  C2<T> e[4] = {v[0], v[2], v[4], v[6]};
+  C2<T> o[4] = {v[1], v[3], v[5], v[7]};
+  dft4<T>(e, sign);
+  dft4<T>(o, sign);
+  const T h = (T)0.70710678118654752440;
+  // W8^1 = (1 + s i)/sqrt2, W8^2 = s i, W8^3 = (-1 + s i)/sqrt2
+  C2<T> o1 = o[1], o3 = o[3];
+  C2<T> t1 = mk<T>((o1.x - sign * o1.y) * h, (o1.y + sign * o1.x) * h);
+  C2<T> t2 = mul_si<T>(o[2], sign);
+  C2<T> t3 = mk<T>((-o3.x - sign * o3.y) * h, (-o3.y + sign * o3.x) * h);
+  v[0] = cadd<T>(e[0], o[0]);
+  v[4] = csub<T>(e[0], o[0]);
+  v[1] = cadd<T>(e[1], t1);
+  v[5] = csub<T>(e[1], t1);
+  v[2] = cadd<T>(e[2], t2);
+  v[6] = csub<T>(e[2], t2);
+  v[3] = cadd<T>(e[3], t3);
+  v[7] = csub<T>(e[3], t3);
+}
+
+// odd prime radix: direct DFT with the R-th roots taken from the twiddle
+// table (W_R^e = W_n^{e n / R})
+template <typename T, int R>
+__device__ __forceinline__ void dft_odd(C2<T> *v, int sign, const C2<T> *tw, int rstride)
+{
+  C2<T> w[R];
+#pragma unroll
+  for (int e = 1; e < R; e++) w[e] = tw_at<T>(tw, e * rstride, sign);
+  C2<T> out[R];
+#pragma unroll
+  for (int u = 0; u < R; u++) {
+    C2<T> acc = v[0];
+#pragma unroll
+    for (int q = 1; q < R; q++) {
+      int e = (q * u) % R;
+      if (e == 0) acc = cadd<T>(acc, v[q]);
+      else acc = cadd<T>(acc, cmul<T>(v[q], w[e]));
+    }
+    out[u] = acc;
+  }
+#pragma unroll
+  for (int u = 0; u < R; u++) v[u] = out[u];
+}
+
+// One Stockham stage for the butterfly j of column c:
+// reads src[(j + r*nb)], twiddles by W_{Ns R}^{(j mod Ns) r}, radix-R DFT,
+// writes dst[(j div Ns)*Ns*R + (j mod Ns) + r*Ns].
+template <typename T, int R>
+__device__ __forceinline__ void stockham_bfly(const C2<T> *src, C2<T> *dst, int j, int c, int nb, int Ns, int span,
+                                              int ldw, const C2<T> *tw, int twstride, int sign)
+{
+  C2<T> v[R];
+#pragma unroll
+  for (int r = 0; r < R; r++) v[r] = src[(j + r * nb) * ldw + c];
+  const int jm = j % Ns;
+  if (jm) {
+#pragma unroll
+    for (int r = 1; r < R; r++) v[r] = cmul<T>(v[r], tw_at<T>(tw, jm * r * span * twstride, sign));
+  }
+  if (R == 2) dft2<T>(v);
+  else if (R == 4) dft4<T>(v, sign);
+  else if (R == 8) dft8<T>(v, sign);
+  else dft_odd<T, R>(v, sign, tw, nb * twstride);
+  const int d = (j - jm) * R + jm;
+#pragma unroll
+  for (int r = 0; r < R; r++) dst[(d + r * Ns) * ldw + c] = v[r];
+}
+
+// Transform `width` columns of length p.n held in shared memory at a[e*ldw+c].
+// tw holds W_N^t for a table length N = p.n*twstride.  All threads of the CTA
+// must call it; returns the buffer that holds the result.
+template <typename T>
+__device__ C2<T> *smem_fft(C2<T> *a, C2<T> *b, const AxisPlan &p, int width, int ldw, const C2<T> *tw, int twstride,
+                           int sign)
+{
+  const int n = p.n;
+  int Ns = 1;
+  for (int s = 0; s < p.nstages; s++) {
+    const int R = p.radix[s];
+    const int nb = n / R;
+    const int span = n / (Ns * R);
+    const int total = nb * width;
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+      const int j = t / width;
+      const int c = t - j * width;
+      switch (R) {
+        case 8: stockham_bfly<T, 8>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+        case 4: stockham_bfly<T, 4>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+        case 2: stockham_bfly<T, 2>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+        case 3: stockham_bfly<T, 3>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+        case 5: stockham_bfly<T, 5>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+        default: stockham_bfly<T, 7>(a, b, j, c, nb, Ns, span, ldw, tw, twstride, sign); break;
+      }
+    }
+    __syncthreads();
+    C2<T> *t = a;
+    a = b;
+    b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+}  // namespace cg

@@ -1,0 +1,99 @@
+// Real-domain correlation cubes for the plain (reference-dataflow) form:
+// FFTGrid::fillInParamCorr (src/fftgrid.cpp:1072-1119, times the
+// multiplyByScalar of SeismicParametersHolder::initializeCorrelations,
+// src/seismicparametersholder.cpp:198-223) and FFTGrid::fillInErrCorr
+// (src/fftgrid.cpp:1018-1070), one thread per padded cell, same float
+// arithmetic as the reference.
+#include "common.cuh"
+#include "trace.cuh"
+
+namespace cg {
+
+#define CG_RMISSING (-99999.000f)
+
+__global__ void k_fill_param_corr(float *buf, int nxp, int nyp, int nzp, const float *__restrict__ corr_xy,
+                                  const float *__restrict__ circ_t, float gradI, float gradJ, float scalar)
+{
+  const int rnxp = 2 * (nxp / 2 + 1);
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long n = (long)rnxp * nyp * nzp;
+  if (idx >= n) return;
+  const int i = (int)(idx % rnxp);
+  const int j = (int)((idx / rnxp) % nyp);
+  const int k = (int)(idx / ((long)rnxp * nyp));
+  float value;
+  if (i < nxp) {
+    int cycleI = i - nxp; if (i < -cycleI) cycleI = i;
+    int cycleJ = j - nyp; if (j < -cycleJ) cycleJ = j;
+    float subK = k + cycleI * gradI + cycleJ * gradJ;
+    int baseK = (int)floorf(subK);
+    subK -= baseK;
+    baseK %= nzp;
+    if (baseK < 0) baseK += nzp;
+    value = (1 - subK) * circ_t[baseK];
+    value += subK * circ_t[baseK != nzp - 1 ? baseK + 1 : 0];
+    value *= corr_xy[i + nxp * j];
+  } else {
+    value = CG_RMISSING;
+  }
+  buf[idx] = value * scalar;
+}
+
+__global__ void k_fill_err_corr(float *buf, int nxp, int nyp, int nzp, const float *__restrict__ corr_xy,
+                                float gradI, float gradJ)
+{
+  const int rnxp = 2 * (nxp / 2 + 1);
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long n = (long)rnxp * nyp * nzp;
+  if (idx >= n) return;
+  const int i = (int)(idx % rnxp);
+  const int j = (int)((idx / rnxp) % nyp);
+  const int k = (int)(idx / ((long)rnxp * nyp));
+  const int range = 1;
+  int cycleI = i - nxp; if (i < -cycleI) cycleI = i;
+  int cycleJ = j - nyp; if (j < -cycleJ) cycleJ = j;
+  float subK = k + cycleI * gradI + cycleJ * gradJ;
+  float value;
+  if (i < nxp) {
+    if (fabsf(subK) < range * 1.0f || fabsf(subK - nzp) < range * 1.0f) {
+      int baseK = (int)subK;
+      subK -= baseK;
+      if (baseK < -range) baseK += nzp * ((-range - baseK + nzp - 1) / nzp);
+      if (baseK >= range) baseK -= nzp * ((baseK - range) / nzp + 1);
+      if (baseK < 0) { baseK = -1 - baseK; subK = 1 - subK; }
+      value = (1 - subK) * corr_xy[i + nxp * j];
+    } else {
+      value = 0.0f;
+    }
+  } else {
+    value = CG_RMISSING;
+  }
+  buf[idx] = value;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" int cg_fill_param_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_xy,
+                                  const float *circ_corr_t, float grad_i, float grad_j, float scalar, void *stream)
+{
+  if (!buf || !corr_xy || !circ_corr_t || nxp < 1 || nyp < 1 || nzp < 1) { set_error("cg_fill_param_corr: bad argument"); return CG_ERR_ARG; }
+  const long n = 2L * (nxp / 2 + 1) * nyp * nzp;
+  TraceScope ts("k_fill_param_corr", (cudaStream_t)stream, 4.0 * n);
+  k_fill_param_corr<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(buf, nxp, nyp, nzp, corr_xy, circ_corr_t,
+                                                                        grad_i, grad_j, scalar);
+  CG_CHECK_LAUNCH("k_fill_param_corr");
+  return CG_OK;
+}
+
+extern "C" int cg_fill_err_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_xy, float grad_i,
+                                float grad_j, void *stream)
+{
+  if (!buf || !corr_xy || nxp < 1 || nyp < 1 || nzp < 1) { set_error("cg_fill_err_corr: bad argument"); return CG_ERR_ARG; }
+  const long n = 2L * (nxp / 2 + 1) * nyp * nzp;
+  TraceScope ts("k_fill_err_corr", (cudaStream_t)stream, 4.0 * n);
+  k_fill_err_corr<<<ceil_div(n, 256), 256, 0, (cudaStream_t)stream>>>(buf, nxp, nyp, nzp, corr_xy, grad_i, grad_j);
+  CG_CHECK_LAUNCH("k_fill_err_corr");
+  return CG_OK;
+}

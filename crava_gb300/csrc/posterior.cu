@@ -1,0 +1,955 @@
+// Per-frequency-bin Gaussian posterior of Crava::computePostMeanResidAndFFTCov
+// (src/crava.cpp:1084-1247).
+//
+// Two GPU forms:
+//   plain  -- the reference dataflow: the prior comes from six covariance
+//             spectra and the error correlation from a seventh, all read from
+//             HBM per bin; arithmetic in the reference's order
+//             (invertSeismicData, src/crava.cpp:1389-1438, lib_matr.c), FP32.
+//   fused  -- the prior and error covariances are regenerated per bin from the
+//             separable spectra c(i,j,k) = Cxy(i,j) Ct(k) (fillInParamCorr /
+//             fillInErrCorr with zero correlation gradients), the per-k
+//             matrices K S0 K^H and the error-term matrix are precomputed once
+//             per model, and the posterior is formed from one Cholesky factor:
+//               Sd = s M + lam E + D,  Y = L^-1 K S0,  v = L^-1 (d - K mu)
+//               mu+ = mu + s Y^H v,  S+ = s S0 - s^2 Y^H Y,  res = d - K mu+
+//             FP32, or MIXED (bins whose Cholesky condition estimate exceeds a
+//             threshold are queued and redone in FP64 with one step of
+//             iterative refinement), or FP64 throughout.
+// Bins outside the inversion band keep prior mean, data and covariance, as in
+// the reference; with the in-place buffers only the covariance is written.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "fft.cuh"
+#include "posterior.cuh"
+#include "trace.cuh"
+
+namespace cg {
+
+// ---------------------------------------------------------------------------
+// plain (reference-order) kernel
+// ---------------------------------------------------------------------------
+struct PlainArgs {
+  float2 *data[kMaxTheta];
+  float2 *mean[3];
+  float2 *cov[6];
+  const float2 *errcorr;
+  const float2 *K;
+  const float2 *em1, *em2, *em3;
+  const unsigned char *band;
+  float c0[kMaxTheta * kMaxTheta];  // float(0.5*(1-wnc)*errThetaCov[l][m])
+  float cw[kMaxTheta];              // float(wnc*errThetaCov[l][l])
+  float sig0[6];                    // float(priorVar0): 00 11 22 01 02 12
+  int plane;
+  long csize;
+  int is4d;
+  int *counters;
+};
+
+// SeismicParametersHolder::getParameterCovariance (src/seismicparametersholder.cpp:409-428)
+__device__ __forceinline__ float2 param_cov_entry(float2 v, float s)
+{
+  if (s != 0.0f) v.x = v.x / s;
+  return make_float2(sqrtf(v.x * v.x) * s, 0.0f);
+}
+
+// lib_matrCholCpx (libs/lib/lib_matr.c:78-168) on a packed lower triangle
+template <typename T, int N>
+__device__ __forceinline__ bool chol_ref(C2<T> *L)
+{
+  const T factor = L[0].x;
+  if (!(factor > (T)0)) return false;
+#pragma unroll
+  for (int t = 0; t < N * (N + 1) / 2; t++) { L[t].x = L[t].x / factor; L[t].y = L[t].y / factor; }
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    if (L[tri(i, i)].x <= (T)kCholTol) return false;
+#pragma unroll
+    for (int j = 0; j < i; j++) {
+      T lr = 0, li = 0;
+#pragma unroll
+      for (int k = 0; k < j; k++) {
+        lr += (L[tri(i, k)].x * L[tri(j, k)].x) + (L[tri(i, k)].y * L[tri(j, k)].y);
+        li += -(L[tri(i, k)].x * L[tri(j, k)].y) + (L[tri(i, k)].y * L[tri(j, k)].x);
+      }
+      const C2<T> ljj = L[tri(j, j)];
+      const T help = ljj.x * ljj.x + ljj.y * ljj.y;
+      const C2<T> lij = L[tri(i, j)];
+      L[tri(i, j)].x = ((lij.x - lr) * ljj.x + (lij.y - li) * ljj.y) / help;
+      L[tri(i, j)].y = ((lij.y - li) * ljj.x - (lij.x - lr) * ljj.y) / help;
+    }
+    T lr = 0;
+#pragma unroll
+    for (int k = 0; k < i; k++) lr += (L[tri(i, k)].x * L[tri(i, k)].x) + (L[tri(i, k)].y * L[tri(i, k)].y);
+    lr = L[tri(i, i)].x - lr;
+    if (lr <= (T)kCholTol) return false;
+    L[tri(i, i)] = mk<T>(sqrt(lr), (T)0);
+  }
+  const T sf = sqrt(factor);
+#pragma unroll
+  for (int t = 0; t < N * (N + 1) / 2; t++) { L[t].x *= sf; L[t].y *= sf; }
+  return true;
+}
+
+template <int NT>
+__global__ void __launch_bounds__(128) k_invert_plain(PlainArgs a)
+{
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.csize) return;
+  const int k = (int)(b / a.plane);
+
+  // findParameterVariances (src/seismicparametersholder.cpp:357-407)
+  float2 c6[6];
+#pragma unroll
+  for (int t = 0; t < 6; t++) c6[t] = a.cov[t][b];
+  if (a.is4d) {
+#pragma unroll
+    for (int t = 0; t < 3; t++) c6[t] = make_float2(sqrtf(c6[t].x * c6[t].x + c6[t].y * c6[t].y), 0.0f);
+  } else {
+#pragma unroll
+    for (int t = 0; t < 6; t++) c6[t] = param_cov_entry(c6[t], a.sig0[t]);
+  }
+  float2 S[3][3];
+  S[0][0] = c6[0]; S[1][1] = c6[1]; S[2][2] = c6[2];
+  S[0][1] = c6[3]; S[1][0] = make_float2(c6[3].x, -c6[3].y);
+  S[0][2] = c6[4]; S[2][0] = make_float2(c6[4].x, -c6[4].y);
+  S[1][2] = c6[5]; S[2][1] = make_float2(c6[5].x, -c6[5].y);
+
+  if (a.band[k]) {
+    float2 d[NT], res[NT], mu[3], K[NT][3], KS[NT][3], KScc[3][NT], Sd[NT * (NT + 1) / 2];
+#pragma unroll
+    for (int l = 0; l < NT; l++) { d[l] = a.data[l][b]; res[l] = d[l]; }
+#pragma unroll
+    for (int p = 0; p < 3; p++) mu[p] = a.mean[p][b];
+    const float2 ec = a.errcorr[b];
+    const float lam = sqrtf(ec.x * ec.x);
+#pragma unroll
+    for (int l = 0; l < NT; l++)
+#pragma unroll
+      for (int p = 0; p < 3; p++) K[l][p] = __ldg(&a.K[((long)k * NT + l) * 3 + p]);
+    // KS = K S (lib_matrProdCpx)
+#pragma unroll
+    for (int l = 0; l < NT; l++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          xr += K[l][q].x * S[q][j].x - K[l][q].y * S[q][j].y;
+          xi += K[l][q].y * S[q][j].x + K[l][q].x * S[q][j].y;
+        }
+        KS[l][j] = make_float2(xr, xi);
+      }
+    // Sd = KS K^H + errVar (lower triangle; lib_matrProdAdjointCpx + getNextErrorVariance)
+#pragma unroll
+    for (int l = 0; l < NT; l++) {
+      const float2 e1l = __ldg(&a.em1[(long)k * NT + l]);
+      const float2 e2l = __ldg(&a.em2[(long)k * NT + l]);
+#pragma unroll
+      for (int m = 0; m <= l; m++) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          xr += KS[l][q].x * K[m][q].x + KS[l][q].y * K[m][q].y;
+          xi += KS[l][q].y * K[m][q].x - KS[l][q].x * K[m][q].y;
+        }
+        const float2 e1m = __ldg(&a.em1[(long)k * NT + m]);
+        const float2 e2m = __ldg(&a.em2[(long)k * NT + m]);
+        const float c0 = a.c0[l * NT + m] * lam;
+        float er = c0 * (e1l.x * e1m.x + e1l.y * e1m.y);
+        er += c0 * (e2l.x * e2m.x + e2l.y * e2m.y);
+        float ei;
+        if (l == m) {
+          const float2 e3 = __ldg(&a.em3[(long)k * NT + l]);
+          er += a.cw[l] * e3.x * e3.x;
+          ei = 0.0f;
+        } else {
+          ei = c0 * (-e1l.x * e1m.y + e1l.y * e1m.x);
+          ei += c0 * (-e2l.x * e2m.y + e2l.y * e2m.x);
+        }
+        Sd[tri(l, m)] = make_float2(xr + er, xi + ei);
+      }
+    }
+    if (chol_ref<float, NT>(Sd)) {
+#pragma unroll
+      for (int l = 0; l < NT; l++)
+#pragma unroll
+        for (int p = 0; p < 3; p++) KScc[p][l] = make_float2(KS[l][p].x, -KS[l][p].y);
+      // lib_matrAXeqBMatCpx: KS <- Sd^-1 KS
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+#pragma unroll
+        for (int i = 0; i < NT; i++) {
+          float xr = KS[i][c].x, xi = KS[i][c].y;
+#pragma unroll
+          for (int j = 0; j < i; j++) {
+            xr -= (KS[j][c].x * Sd[tri(i, j)].x - KS[j][c].y * Sd[tri(i, j)].y);
+            xi -= (KS[j][c].y * Sd[tri(i, j)].x + KS[j][c].x * Sd[tri(i, j)].y);
+          }
+          const float2 lii = Sd[tri(i, i)];
+          const float help = lii.x * lii.x + lii.y * lii.y;
+          KS[i][c] = make_float2((xr * lii.x + xi * lii.y) / help, (xi * lii.x - xr * lii.y) / help);
+        }
+#pragma unroll
+        for (int i = NT - 1; i >= 0; i--) {
+          float xr = KS[i][c].x, xi = KS[i][c].y;
+#pragma unroll
+          for (int j = NT - 1; j > i; j--) {
+            xr = xr - (KS[j][c].x * Sd[tri(j, i)].x + KS[j][c].y * Sd[tri(j, i)].y);
+            xi = xi - (-KS[j][c].x * Sd[tri(j, i)].y + KS[j][c].y * Sd[tri(j, i)].x);
+          }
+          const float2 lii = Sd[tri(i, i)];
+          const float help = lii.x * lii.x + lii.y * lii.y;
+          KS[i][c] = make_float2((xr * lii.x - xi * lii.y) / help, (xi * lii.x + xr * lii.y) / help);
+        }
+      }
+      // S -= KScc KS
+#pragma unroll
+      for (int p = 0; p < 3; p++)
+#pragma unroll
+        for (int q = 0; q < 3; q++) {
+          float xr = 0, xi = 0;
+#pragma unroll
+          for (int l = 0; l < NT; l++) {
+            xr += KScc[p][l].x * KS[l][q].x - KScc[p][l].y * KS[l][q].y;
+            xi += KScc[p][l].y * KS[l][q].x + KScc[p][l].x * KS[l][q].y;
+          }
+          S[p][q].x -= xr;
+          S[p][q].y -= xi;
+        }
+      // d -= K mu; ans = KS^H d; mu += ans; res -= K mu
+#pragma unroll
+      for (int l = 0; l < NT; l++) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+          xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
+          xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
+        }
+        d[l].x -= xr;
+        d[l].y -= xi;
+      }
+#pragma unroll
+      for (int p = 0; p < 3; p++) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int l = 0; l < NT; l++) {
+          xr += KS[l][p].x * d[l].x + KS[l][p].y * d[l].y;
+          xi += -KS[l][p].y * d[l].x + KS[l][p].x * d[l].y;
+        }
+        mu[p].x += xr;
+        mu[p].y += xi;
+      }
+#pragma unroll
+      for (int l = 0; l < NT; l++) {
+        float xr = 0, xi = 0;
+#pragma unroll
+        for (int p = 0; p < 3; p++) {
+          xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
+          xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
+        }
+        res[l].x -= xr;
+        res[l].y -= xi;
+      }
+#pragma unroll
+      for (int l = 0; l < NT; l++) a.data[l][b] = res[l];
+#pragma unroll
+      for (int p = 0; p < 3; p++) a.mean[p][b] = mu[p];
+    } else if (a.counters) {
+      atomicAdd(&a.counters[1], 1);
+    }
+  }
+  a.cov[0][b] = S[0][0];
+  a.cov[1][b] = S[1][1];
+  a.cov[2][b] = S[2][2];
+  a.cov[3][b] = S[0][1];
+  a.cov[4][b] = S[0][2];
+  a.cov[5][b] = S[1][2];
+}
+
+// ---------------------------------------------------------------------------
+// fused kernels
+// ---------------------------------------------------------------------------
+template <typename T>
+struct FusedArgs {
+  C2<T> *data[kMaxTheta];
+  C2<T> *mean[3];
+  C2<T> *cov[6];
+  const float2 *cxy;      // cnxp*nyp  (FP32 tables)
+  const float2 *ct;       // nzp/2+1
+  const double2 *cxy_d;   // FP64 tables (FP64 mode)
+  const double2 *ct_d;
+  const KTab<T> *ktab;
+  T sig0[6];
+  int cnxp, nyp, nzp, plane;
+  float cond_thr;
+  int *queue;
+  int queue_cap;
+  int *counters;
+};
+
+// prior scale s = |Re(Cxy Ct)| and error eigenvalue lam = |Re Cxy| of one bin
+template <typename T>
+__device__ __forceinline__ void bin_scales(const FusedArgs<T> &a, int ij, int k, T &s, T &lam)
+{
+  const int cnzp = a.nzp / 2 + 1;
+  if (sizeof(T) == 8) {
+    const double2 cx = a.cxy_d[ij];
+    double2 t = k < cnzp ? a.ct_d[k] : make_double2(a.ct_d[a.nzp - k].x, -a.ct_d[a.nzp - k].y);
+    s = (T)fabs(cx.x * t.x - cx.y * t.y);
+    lam = (T)fabs(cx.x);
+  } else {
+    const float2 cx = __ldg(&a.cxy[ij]);
+    float2 t = k < cnzp ? __ldg(&a.ct[k]) : make_float2(a.ct[a.nzp - k].x, -a.ct[a.nzp - k].y);
+    s = (T)fabsf(cx.x * t.x - cx.y * t.y);
+    lam = (T)fabsf(cx.x);
+  }
+}
+
+// Plain lower Cholesky (no pre-scaling) with the reference's failure rule:
+// fail when A00 <= 0 or any pivot <= 1e-20 * A00 (lib_matr.c:78-168 scales by
+// A00 first).  Returns the squared ratio of the largest to the smallest
+// diagonal of L as a cheap lower bound on the condition number.
+template <typename T, int N>
+__device__ __forceinline__ bool chol_std(C2<T> *L, T &cond)
+{
+  const T a00 = L[0].x;
+  if (!(a00 > (T)0)) return false;
+  const T tol = (T)kCholTol * a00;
+  T dmax = 0, dmin = 0;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+#pragma unroll
+    for (int j = 0; j < i; j++) {
+      C2<T> acc = L[tri(i, j)];
+#pragma unroll
+      for (int k = 0; k < j; k++) acc = csub<T>(acc, cmulc<T>(L[tri(i, k)], L[tri(j, k)]));
+      const T inv = (T)1 / L[tri(j, j)].x;
+      L[tri(i, j)] = mk<T>(acc.x * inv, acc.y * inv);
+    }
+    T piv = L[tri(i, i)].x;
+#pragma unroll
+    for (int k = 0; k < i; k++) piv -= L[tri(i, k)].x * L[tri(i, k)].x + L[tri(i, k)].y * L[tri(i, k)].y;
+    if (!(piv > tol)) return false;
+    const T di = sqrt(piv);
+    L[tri(i, i)] = mk<T>(di, (T)0);
+    dmax = i == 0 ? di : (di > dmax ? di : dmax);
+    dmin = i == 0 ? di : (di < dmin ? di : dmin);
+  }
+  const T r = dmax / dmin;
+  cond = r * r;
+  return true;
+}
+
+// forward substitution L x = b in place
+template <typename T, int N>
+__device__ __forceinline__ void lsolve(const C2<T> *L, C2<T> *x)
+{
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    C2<T> acc = x[i];
+#pragma unroll
+    for (int j = 0; j < i; j++) acc = csub<T>(acc, cmul<T>(L[tri(i, j)], x[j]));
+    const T inv = (T)1 / L[tri(i, i)].x;
+    x[i] = mk<T>(acc.x * inv, acc.y * inv);
+  }
+}
+
+// backward substitution L^H x = b in place
+template <typename T, int N>
+__device__ __forceinline__ void lhsolve(const C2<T> *L, C2<T> *x)
+{
+#pragma unroll
+  for (int i = N - 1; i >= 0; i--) {
+    C2<T> acc = x[i];
+#pragma unroll
+    for (int j = i + 1; j < N; j++) acc = csub<T>(acc, cmulc<T>(x[j], L[tri(j, i)]));
+    const T inv = (T)1 / L[tri(i, i)].x;
+    x[i] = mk<T>(acc.x * inv, acc.y * inv);
+  }
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void build_sd(const KTab<T> &kt, T s, T lam, C2<T> *Sd)
+{
+#pragma unroll
+  for (int l = 0; l < N; l++)
+#pragma unroll
+    for (int m = 0; m <= l; m++) {
+      const int t = tri(l, m);
+      C2<T> v = mk<T>(s * kt.M[t].x + lam * kt.E[t].x, s * kt.M[t].y + lam * kt.E[t].y);
+      if (l == m) v = mk<T>(v.x + kt.D[l], (T)0);
+      Sd[t] = v;
+    }
+}
+
+// Posterior of one in-band bin from the Cholesky factor L of Sd.  d[] holds
+// the data on entry and the residual on exit; mu the prior/posterior mean.
+// refine: solve Sd u = r with one step of iterative refinement (FP64 paths).
+template <typename T, int N>
+__device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *sig0, T s, T lam, const C2<T> *L,
+                                                    C2<T> *d, C2<T> *mu, C2<T> *cov, bool refine)
+{
+  C2<T> r[N];
+#pragma unroll
+  for (int l = 0; l < N; l++) {
+    C2<T> km = mk<T>(0, 0);
+#pragma unroll
+    for (int p = 0; p < 3; p++) km = cadd<T>(km, cmul<T>(kt.K[l][p], mu[p]));
+    r[l] = csub<T>(d[l], km);
+  }
+  // covariance: S+ = s S0 - s^2 Y^H Y with Y = L^-1 K S0
+  C2<T> Y[3][N];
+#pragma unroll
+  for (int p = 0; p < 3; p++) {
+#pragma unroll
+    for (int l = 0; l < N; l++) Y[p][l] = kt.KS0[l][p];
+    lsolve<T, N>(L, Y[p]);
+  }
+  const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+#pragma unroll
+  for (int t = 0; t < 6; t++) {
+    C2<T> acc = mk<T>(0, 0);
+#pragma unroll
+    for (int l = 0; l < N; l++) acc = cadd<T>(acc, cmulc<T>(Y[pq[t][1]][l], Y[pq[t][0]][l]));
+    cov[t] = mk<T>(s * sig0[t] - s * s * acc.x, t < 3 ? (T)0 : -s * s * acc.y);
+  }
+  C2<T> up[3];
+  if (!refine) {
+    // mean: mu+ = mu + s Y^H v, v = L^-1 r
+    C2<T> v[N];
+#pragma unroll
+    for (int l = 0; l < N; l++) v[l] = r[l];
+    lsolve<T, N>(L, v);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      C2<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int l = 0; l < N; l++) acc = cadd<T>(acc, cmulc<T>(v[l], Y[p][l]));
+      up[p] = acc;
+    }
+  } else {
+    // u = Sd^-1 r, one refinement step u += Sd^-1 (r - Sd u), mu+ = mu + s (K S0)^H u
+    C2<T> u[N], rho[N], Sd[N * (N + 1) / 2];
+#pragma unroll
+    for (int l = 0; l < N; l++) u[l] = r[l];
+    lsolve<T, N>(L, u);
+    lhsolve<T, N>(L, u);
+    build_sd<T, N>(kt, s, lam, Sd);
+#pragma unroll
+    for (int l = 0; l < N; l++) {
+      C2<T> acc = r[l];
+#pragma unroll
+      for (int m = 0; m < N; m++) {
+        C2<T> a = l >= m ? Sd[tri(l, m)] : cconj<T>(Sd[tri(m, l)]);
+        acc = csub<T>(acc, cmul<T>(a, u[m]));
+      }
+      rho[l] = acc;
+    }
+    lsolve<T, N>(L, rho);
+    lhsolve<T, N>(L, rho);
+#pragma unroll
+    for (int l = 0; l < N; l++) u[l] = cadd<T>(u[l], rho[l]);
+#pragma unroll
+    for (int p = 0; p < 3; p++) {
+      C2<T> acc = mk<T>(0, 0);
+#pragma unroll
+      for (int l = 0; l < N; l++) acc = cadd<T>(acc, cmulc<T>(u[l], kt.KS0[l][p]));
+      up[p] = acc;
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < 3; p++) mu[p] = mk<T>(mu[p].x + s * up[p].x, mu[p].y + s * up[p].y);
+#pragma unroll
+  for (int l = 0; l < N; l++) {
+    C2<T> km = mk<T>(0, 0);
+#pragma unroll
+    for (int p = 0; p < 3; p++) km = cadd<T>(km, cmul<T>(kt.K[l][p], mu[p]));
+    d[l] = csub<T>(d[l], km);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void write_prior_cov(const FusedArgs<T> &a, long b, T s)
+{
+#pragma unroll
+  for (int t = 0; t < 6; t++) a.cov[t][b] = mk<T>(s * a.sig0[t], (T)0);
+}
+
+// MODE 0: FP32, 1: MIXED (FP32 + queue), 2: FP64 (T = double)
+template <typename T, int NT, int MODE>
+__global__ void __launch_bounds__(128) k_invert_fused(FusedArgs<T> a)
+{
+  __shared__ KTab<T> kt;
+  const int k = blockIdx.y;
+  {
+    const int *src = (const int *)&a.ktab[k];
+    int *dst = (int *)&kt;
+    for (int t = threadIdx.x; t < (int)(sizeof(KTab<T>) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+  const int ij = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ij >= a.plane) return;
+  const long b = (long)k * a.plane + ij;
+  T s, lam;
+  bin_scales<T>(a, ij, k, s, lam);
+  if (!kt.band) {
+    write_prior_cov<T>(a, b, s);
+    return;
+  }
+  C2<T> d[NT], mu[3], cov[6], L[NT * (NT + 1) / 2];
+#pragma unroll
+  for (int l = 0; l < NT; l++) d[l] = a.data[l][b];
+#pragma unroll
+  for (int p = 0; p < 3; p++) mu[p] = a.mean[p][b];
+  build_sd<T, NT>(kt, s, lam, L);
+  T cond = 0;
+  const bool ok = chol_std<T, NT>(L, cond);
+  if (MODE == 1) {
+    const bool flag = !ok || cond > (T)a.cond_thr;
+    const unsigned m = __ballot_sync(__activemask(), flag);
+    if (flag) {
+      const int lane = threadIdx.x & 31;
+      const int leader = __ffs(m) - 1;
+      int base = 0;
+      if (lane == leader) base = atomicAdd(&a.counters[0], __popc(m));
+      base = __shfl_sync(m, base, leader);
+      const int pos = base + __popc(m & ((1u << lane) - 1u));
+      if (pos < a.queue_cap) {
+        a.queue[pos] = (int)b;
+        return;  // the FP64 pass writes this bin
+      }
+      atomicAdd(&a.counters[2], 1);  // queue full: keep the FP32 answer
+    }
+  }
+  if (!ok) {
+    if (a.counters) atomicAdd(&a.counters[1], 1);
+    write_prior_cov<T>(a, b, s);
+    return;
+  }
+  posterior_from_chol<T, NT>(kt, a.sig0, s, lam, L, d, mu, cov, MODE == 2);
+#pragma unroll
+  for (int l = 0; l < NT; l++) a.data[l][b] = d[l];
+#pragma unroll
+  for (int p = 0; p < 3; p++) a.mean[p][b] = mu[p];
+#pragma unroll
+  for (int t = 0; t < 6; t++) a.cov[t][b] = cov[t];
+}
+
+struct S0Args {
+  double v[9];
+};
+
+// FP64 redo of the bins the MIXED pass queued.
+template <int NT>
+__global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, const KTab<double> *__restrict__ ktd,
+                                                        S0Args s0)
+{
+  const double *sig0d = s0.v;
+  const int nq = min(*((volatile int *)&a.counters[0]), a.queue_cap);
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    const long b = a.queue[q];
+    const int k = (int)(b / a.plane);
+    const int ij = (int)(b - (long)k * a.plane);
+    const KTab<double> &kt = ktd[k];
+    float sf, lamf;
+    bin_scales<float>(a, ij, k, sf, lamf);
+    const double s = sf, lam = lamf;
+    double2 d[NT], mu[3], cov[6], L[NT * (NT + 1) / 2];
+#pragma unroll
+    for (int l = 0; l < NT; l++) { float2 v = a.data[l][b]; d[l] = make_double2(v.x, v.y); }
+#pragma unroll
+    for (int p = 0; p < 3; p++) { float2 v = a.mean[p][b]; mu[p] = make_double2(v.x, v.y); }
+    build_sd<double, NT>(kt, s, lam, L);
+    double cond;
+    if (!chol_std<double, NT>(L, cond)) {
+      atomicAdd(&a.counters[1], 1);
+#pragma unroll
+      for (int t = 0; t < 6; t++) a.cov[t][b] = make_float2((float)(s * sig0d[t]), 0.0f);
+      continue;
+    }
+    posterior_from_chol<double, NT>(kt, sig0d, s, lam, L, d, mu, cov, true);
+#pragma unroll
+    for (int l = 0; l < NT; l++) a.data[l][b] = make_float2((float)d[l].x, (float)d[l].y);
+#pragma unroll
+    for (int p = 0; p < 3; p++) a.mean[p][b] = make_float2((float)mu[p].x, (float)mu[p].y);
+#pragma unroll
+    for (int t = 0; t < 6; t++) a.cov[t][b] = make_float2((float)cov[t].x, (float)cov[t].y);
+  }
+}
+
+// per-k tables (double), one thread per k
+__global__ void k_prep_tables(int nzp, int nt, const float2 *K, const float2 *em1, const float2 *em2,
+                              const float2 *em3, const unsigned char *band, const double *etc, S0Args s0, float wnc,
+                              KTab<float> *tf, KTab<double> *td)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nzp) return;
+  KTab<double> t;
+  memset(&t, 0, sizeof(t));
+  for (int l = 0; l < nt; l++)
+    for (int p = 0; p < 3; p++) {
+      float2 v = K[((long)k * nt + l) * 3 + p];
+      t.K[l][p] = make_double2(v.x, v.y);
+    }
+  for (int l = 0; l < nt; l++)
+    for (int p = 0; p < 3; p++) {
+      double2 acc = make_double2(0, 0);
+      for (int q = 0; q < 3; q++) {
+        acc.x += t.K[l][q].x * s0.v[q * 3 + p];
+        acc.y += t.K[l][q].y * s0.v[q * 3 + p];
+      }
+      t.KS0[l][p] = acc;
+    }
+  const double c0 = 0.5 * (1.0 - (double)wnc);
+  for (int l = 0; l < nt; l++) {
+    float2 e1l = em1[(long)k * nt + l], e2l = em2[(long)k * nt + l];
+    for (int m = 0; m <= l; m++) {
+      double2 acc = make_double2(0, 0);
+      for (int p = 0; p < 3; p++) acc = cadd<double>(acc, cmulc<double>(t.KS0[l][p], t.K[m][p]));
+      t.M[tri(l, m)] = acc;
+      float2 e1m = em1[(long)k * nt + m], e2m = em2[(long)k * nt + m];
+      double re = (double)e1l.x * e1m.x + (double)e1l.y * e1m.y + (double)e2l.x * e2m.x + (double)e2l.y * e2m.y;
+      double im = (-(double)e1l.x * e1m.y + (double)e1l.y * e1m.x) + (-(double)e2l.x * e2m.y + (double)e2l.y * e2m.x);
+      double f = c0 * etc[l * nt + m];
+      t.E[tri(l, m)] = l == m ? make_double2(f * re, 0.0) : make_double2(f * re, f * im);
+    }
+    float2 e3 = em3[(long)k * nt + l];
+    t.D[l] = (double)wnc * etc[l * nt + l] * (double)e3.x * (double)e3.x;
+  }
+  t.band = band[k];
+  td[k] = t;
+  KTab<float> f;
+  memset(&f, 0, sizeof(f));
+  for (int l = 0; l < kMaxTheta; l++)
+    for (int p = 0; p < 3; p++) {
+      f.K[l][p] = make_float2((float)t.K[l][p].x, (float)t.K[l][p].y);
+      f.KS0[l][p] = make_float2((float)t.KS0[l][p].x, (float)t.KS0[l][p].y);
+    }
+  for (int q = 0; q < kTri; q++) {
+    f.M[q] = make_float2((float)t.M[q].x, (float)t.M[q].y);
+    f.E[q] = make_float2((float)t.E[q].x, (float)t.E[q].y);
+  }
+  for (int l = 0; l < kMaxTheta; l++) f.D[l] = (float)t.D[l];
+  f.band = t.band;
+  tf[k] = f;
+}
+
+__global__ void k_f2d(const float *in, double *out, long n)
+{
+  long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = in[i];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename F>
+int dispatch_nt(int nt, F &&f)
+{
+  switch (nt) {
+    case 1: return f(std::integral_constant<int, 1>());
+    case 2: return f(std::integral_constant<int, 2>());
+    case 3: return f(std::integral_constant<int, 3>());
+    case 4: return f(std::integral_constant<int, 4>());
+    case 5: return f(std::integral_constant<int, 5>());
+    case 6: return f(std::integral_constant<int, 6>());
+    case 7: return f(std::integral_constant<int, 7>());
+    case 8: return f(std::integral_constant<int, 8>());
+    default: set_error("ntheta %d outside 1..%d", nt, kMaxTheta); return CG_ERR_ARG;
+  }
+}
+
+int check_ws(Workspace *w)
+{
+  if (!w) { set_error("null workspace"); return CG_ERR_ARG; }
+  if (!w->model_set) { set_error("cg_workspace_set_model has not been called"); return CG_ERR_STATE; }
+  int dev = -1;
+  CG_CUDA(cudaGetDevice(&dev));
+  if (dev != w->device) { set_error("workspace belongs to device %d, current device is %d", w->device, dev); return CG_ERR_STATE; }
+  return CG_OK;
+}
+
+}  // namespace
+
+}  // namespace cg
+
+using namespace cg;
+
+struct cg_workspace_s : public Workspace {};
+
+extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp, int ntheta)
+{
+  if (!out) { set_error("null output handle"); return CG_ERR_ARG; }
+  *out = nullptr;
+  if (nxp < 1 || nyp < 1 || nzp < 1 || nxp > kMaxFFT || nyp > kMaxFFT || nzp > kMaxFFT) {
+    set_error("bad dimensions %d x %d x %d", nxp, nyp, nzp);
+    return CG_ERR_ARG;
+  }
+  if (ntheta < 1 || ntheta > kMaxTheta) { set_error("ntheta %d outside 1..%d", ntheta, kMaxTheta); return CG_ERR_ARG; }
+  cg_workspace_s *w = new cg_workspace_s();
+  memset((Workspace *)w, 0, sizeof(Workspace));
+  CG_CUDA(cudaGetDevice(&w->device));
+  w->nxp = nxp; w->nyp = nyp; w->nzp = nzp; w->ntheta = ntheta;
+  const int cnxp = nxp / 2 + 1, cnzp = nzp / 2 + 1;
+  const long csize = (long)cnxp * nyp * nzp;
+  w->queue_cap = (int)std::min<long>(csize, std::max<long>(1 << 16, csize / 8));
+  cudaError_t e = cudaSuccess;
+#define WS_ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (bytes))
+  WS_ALLOC(w->ktab_f, sizeof(KTab<float>) * nzp);
+  WS_ALLOC(w->ktab_d, sizeof(KTab<double>) * nzp);
+  WS_ALLOC(w->K, sizeof(float2) * (size_t)nzp * ntheta * 3);
+  WS_ALLOC(w->em1, sizeof(float2) * (size_t)nzp * ntheta);
+  WS_ALLOC(w->em2, sizeof(float2) * (size_t)nzp * ntheta);
+  WS_ALLOC(w->em3, sizeof(float2) * (size_t)nzp * ntheta);
+  WS_ALLOC(w->band, (size_t)nzp);
+  WS_ALLOC(w->etc, sizeof(double) * ntheta * ntheta);
+  WS_ALLOC(w->cxy_f, sizeof(float) * 2 * (size_t)cnxp * nyp);
+  WS_ALLOC(w->ct_f, sizeof(float) * 2 * (size_t)cnzp);
+  WS_ALLOC(w->cxy_d, sizeof(double) * 2 * (size_t)cnxp * nyp);
+  WS_ALLOC(w->ct_d, sizeof(double) * 2 * (size_t)cnzp);
+  WS_ALLOC(w->queue, sizeof(int) * (size_t)w->queue_cap);
+  WS_ALLOC(w->counters, sizeof(int) * 4);
+#undef WS_ALLOC
+  if (e == cudaSuccess) e = cudaMemset(w->counters, 0, sizeof(int) * 4);
+  if (e != cudaSuccess) {
+    cg_workspace_destroy(w);
+    return cuda_status(e, "cg_workspace_create");
+  }
+  *out = w;
+  return CG_OK;
+}
+
+extern "C" void cg_workspace_destroy(cg_workspace w)
+{
+  if (!w) return;
+  void *ptrs[] = {w->ktab_f, w->ktab_d, w->K, w->em1, w->em2, w->em3, w->band, w->etc,
+                  w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  delete w;
+}
+
+extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
+{
+  if (!w || !m) { set_error("null argument"); return CG_ERR_ARG; }
+  if (m->ntheta != w->ntheta) { set_error("model ntheta %d != workspace ntheta %d", m->ntheta, w->ntheta); return CG_ERR_ARG; }
+  if (!m->K || !m->em1 || !m->em2 || !m->em3 || !m->band || !m->err_theta_cov || !m->sigma0) {
+    set_error("model table pointer is null");
+    return CG_ERR_ARG;
+  }
+  const int nt = w->ntheta, nzp = w->nzp;
+  w->wnc = m->wnc;
+  w->is4d = m->is4d;
+  w->cond_threshold = m->cond_threshold > 0 ? m->cond_threshold : 1.0e3;
+  for (int t = 0; t < 9; t++) { w->sigma0[t] = m->sigma0[t]; w->sigma0f[t] = (float)m->sigma0[t]; }
+  CG_CUDA(cudaMemcpy(w->K, m->K, sizeof(float2) * (size_t)nzp * nt * 3, cudaMemcpyHostToDevice));
+  CG_CUDA(cudaMemcpy(w->em1, m->em1, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
+  CG_CUDA(cudaMemcpy(w->em2, m->em2, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
+  CG_CUDA(cudaMemcpy(w->em3, m->em3, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
+  CG_CUDA(cudaMemcpy(w->band, m->band, (size_t)nzp, cudaMemcpyHostToDevice));
+  long nb = 0;
+  for (int k = 0; k < nzp; k++) nb += m->band[k] ? 1 : 0;
+  w->inband_bins = nb * (long)(w->nxp / 2 + 1) * w->nyp;
+  CG_CUDA(cudaMemcpy(w->etc, m->err_theta_cov, sizeof(double) * nt * nt, cudaMemcpyHostToDevice));
+  S0Args s0;
+  // the prior the reference multiplies into the covariance cubes is float(priorVar0)
+  for (int t = 0; t < 9; t++) s0.v[t] = (double)(float)m->sigma0[t];
+  k_prep_tables<<<ceil_div(nzp, 64), 64>>>(nzp, nt, w->K, w->em1, w->em2, w->em3, w->band, w->etc, s0, w->wnc,
+                                           w->ktab_f, w->ktab_d);
+  CG_CHECK_LAUNCH("k_prep_tables");
+  CG_CUDA(cudaDeviceSynchronize());
+  w->model_set = true;
+  return CG_OK;
+}
+
+extern "C" int cg_workspace_reset_stats(cg_workspace w, void *stream)
+{
+  if (!w) { set_error("null workspace"); return CG_ERR_ARG; }
+  CG_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(int) * 4, (cudaStream_t)stream));
+  return CG_OK;
+}
+
+extern "C" int cg_workspace_stats(cg_workspace w, int *flagged, int *failed, int *overflow)
+{
+  if (!w) { set_error("null workspace"); return CG_ERR_ARG; }
+  int h[4];
+  CG_CUDA(cudaDeviceSynchronize());
+  CG_CUDA(cudaMemcpy(h, w->counters, sizeof(h), cudaMemcpyDeviceToHost));
+  if (flagged) *flagged = h[0];
+  if (failed) *failed = h[1];
+  if (overflow) *overflow = h[2];
+  return CG_OK;
+}
+
+extern "C" int cg_invert_bins_plain(cg_workspace w, float *const *data, float *const *mean, float *const *cov,
+                                    const float *errcorr, void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!data || !mean || !cov || !errcorr) { set_error("null buffer argument"); return CG_ERR_ARG; }
+  const int nt = w->ntheta;
+  PlainArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int l = 0; l < nt; l++) { if (!data[l]) { set_error("null data[%d]", l); return CG_ERR_ARG; } a.data[l] = (float2 *)data[l]; }
+  for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } a.mean[p] = (float2 *)mean[p]; }
+  for (int t = 0; t < 6; t++) { if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; } a.cov[t] = (float2 *)cov[t]; }
+  a.errcorr = (const float2 *)errcorr;
+  a.K = w->K; a.em1 = w->em1; a.em2 = w->em2; a.em3 = w->em3; a.band = w->band;
+  std::vector<double> etc(nt * nt);
+  // errThetaCov is needed on the host for the per-launch constants
+  CG_CUDA(cudaMemcpy(etc.data(), w->etc, sizeof(double) * nt * nt, cudaMemcpyDeviceToHost));
+  for (int l = 0; l < nt; l++) {
+    for (int m = 0; m < nt; m++) a.c0[l * nt + m] = (float)(0.5 * (1.0 - w->wnc) * etc[l * nt + m]);
+    a.cw[l] = (float)(w->wnc * etc[l * nt + l]);
+  }
+  const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int t = 0; t < 6; t++) a.sig0[t] = w->sigma0f[pq[t][0] * 3 + pq[t][1]];
+  const int cnxp = w->nxp / 2 + 1;
+  a.plane = cnxp * w->nyp;
+  a.csize = (long)a.plane * w->nzp;
+  a.is4d = w->is4d;
+  a.counters = w->counters;
+  const int threads = 128;
+  const long blocks = (a.csize + threads - 1) / threads;
+  const long outband = a.csize - w->inband_bins;
+  TraceScope ts("k_invert_plain", (cudaStream_t)stream,
+                8.0 * w->inband_bins * ((nt + 3 + 7) + (nt + 3 + 6)) + 8.0 * outband * 12);
+  return dispatch_nt(nt, [&](auto NTc) -> int {
+    constexpr int NT = decltype(NTc)::value;
+    k_invert_plain<NT><<<(unsigned)blocks, threads, 0, (cudaStream_t)stream>>>(a);
+    CG_CHECK_LAUNCH("k_invert_plain");
+    return CG_OK;
+  });
+}
+
+// pad a real nxp x nyp surface into the FFTGrid layout and transform it
+template <typename T>
+static int prior_tables(Workspace *w, const float *corr_xy, const float *circ_corr_t, T *cxy, T *ct, cudaStream_t st)
+{
+  const int nxp = w->nxp, nyp = w->nyp, nzp = w->nzp;
+  const int rnxp = 2 * (nxp / 2 + 1), rnzp = 2 * (nzp / 2 + 1);
+  if (sizeof(T) == 4) {
+    CG_CUDA(cudaMemsetAsync(cxy, 0, sizeof(T) * (size_t)rnxp * nyp, st));
+    CG_CUDA(cudaMemcpy2DAsync(cxy, sizeof(T) * rnxp, corr_xy, sizeof(float) * nxp, sizeof(float) * nxp, nyp,
+                              cudaMemcpyDeviceToDevice, st));
+    CG_CUDA(cudaMemsetAsync(ct, 0, sizeof(T) * (size_t)rnzp, st));
+    CG_CUDA(cudaMemcpyAsync(ct, circ_corr_t, sizeof(float) * nzp, cudaMemcpyDeviceToDevice, st));
+  } else {
+    // float -> double into the padded layout, row by row through the float staging buffers
+    CG_CUDA(cudaMemsetAsync(w->cxy_f, 0, sizeof(float) * (size_t)rnxp * nyp, st));
+    CG_CUDA(cudaMemcpy2DAsync(w->cxy_f, sizeof(float) * rnxp, corr_xy, sizeof(float) * nxp, sizeof(float) * nxp,
+                              nyp, cudaMemcpyDeviceToDevice, st));
+    CG_CUDA(cudaMemsetAsync(w->ct_f, 0, sizeof(float) * (size_t)rnzp, st));
+    CG_CUDA(cudaMemcpyAsync(w->ct_f, circ_corr_t, sizeof(float) * nzp, cudaMemcpyDeviceToDevice, st));
+    long n1 = (long)rnxp * nyp, n2 = rnzp;
+    k_f2d<<<ceil_div(n1, 256), 256, 0, st>>>(w->cxy_f, (double *)cxy, n1);
+    k_f2d<<<ceil_div(n2, 256), 256, 0, st>>>(w->ct_f, (double *)ct, n2);
+    CG_CHECK_LAUNCH("k_f2d");
+  }
+  void *b1[1] = {cxy};
+  int rc = fft3d<T>(b1, 1, nxp, nyp, 1, CG_COVARIANCE, true, st);
+  if (rc) return rc;
+  void *b2[1] = {ct};
+  return fft3d<T>(b2, 1, nzp, 1, 1, CG_COVARIANCE, true, st);
+}
+
+extern "C" int cg_prior_spectra(cg_workspace w, const float *corr_xy, const float *circ_corr_t, int precision,
+                                void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!corr_xy || !circ_corr_t) { set_error("null correlation input"); return CG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (precision == CG_PREC_FP64) {
+    rc = prior_tables<double>(w, corr_xy, circ_corr_t, w->cxy_d, w->ct_d, st);
+    if (rc) return rc;
+  }
+  return prior_tables<float>(w, corr_xy, circ_corr_t, w->cxy_f, w->ct_f, st);
+}
+
+template <typename T>
+static int fused_launch(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision,
+                        cudaStream_t st)
+{
+  const int nt = w->ntheta;
+  FusedArgs<T> a;
+  memset(&a, 0, sizeof(a));
+  for (int l = 0; l < nt; l++) { if (!data[l]) { set_error("null data[%d]", l); return CG_ERR_ARG; } a.data[l] = (C2<T> *)data[l]; }
+  for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } a.mean[p] = (C2<T> *)mean[p]; }
+  for (int t = 0; t < 6; t++) { if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; } a.cov[t] = (C2<T> *)cov[t]; }
+  a.cxy = (const float2 *)w->cxy_f;
+  a.ct = (const float2 *)w->ct_f;
+  a.cxy_d = (const double2 *)w->cxy_d;
+  a.ct_d = (const double2 *)w->ct_d;
+  a.ktab = (const KTab<T> *)(sizeof(T) == 8 ? (const void *)w->ktab_d : (const void *)w->ktab_f);
+  const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int t = 0; t < 6; t++) a.sig0[t] = (T)w->sigma0f[pq[t][0] * 3 + pq[t][1]];
+  a.cnxp = w->nxp / 2 + 1;
+  a.nyp = w->nyp;
+  a.nzp = w->nzp;
+  a.plane = a.cnxp * w->nyp;
+  a.cond_thr = (float)w->cond_threshold;
+  a.queue = w->queue;
+  a.queue_cap = w->queue_cap;
+  a.counters = w->counters;
+  const int threads = 128;
+  dim3 grid(ceil_div(a.plane, threads), w->nzp);
+  const long outband = (long)a.plane * w->nzp - w->inband_bins;
+  const double fbytes = (double)sizeof(C2<T>) * (w->inband_bins * (double)((nt + 3) + (nt + 3 + 6)) + outband * 6.0);
+  return dispatch_nt(nt, [&](auto NTc) -> int {
+    constexpr int NT = decltype(NTc)::value;
+    if constexpr (sizeof(T) == 8) {
+      TraceScope ts("k_invert_fused_fp64", st, fbytes);
+      k_invert_fused<T, NT, 2><<<grid, threads, 0, st>>>(a);
+    } else if (precision == CG_PREC_MIXED) {
+      {
+        TraceScope ts("k_invert_fused_mixed", st, fbytes);
+        k_invert_fused<T, NT, 1><<<grid, threads, 0, st>>>(a);
+      }
+      CG_CHECK_LAUNCH("k_invert_fused");
+      S0Args sd;
+      for (int t = 0; t < 6; t++) sd.v[t] = (double)w->sigma0f[pq[t][0] * 3 + pq[t][1]];
+      FusedArgs<float> af;
+      memcpy(&af, &a, sizeof(af));
+      int nsm = 0;
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
+      TraceScope ts("k_invert_fixup64", st, 0.0);
+      k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
+    } else {
+      TraceScope ts("k_invert_fused_fp32", st, fbytes);
+      k_invert_fused<T, NT, 0><<<grid, threads, 0, st>>>(a);
+    }
+    CG_CHECK_LAUNCH("k_invert_fused");
+    return CG_OK;
+  });
+}
+
+extern "C" int cg_invert_bins_fused(cg_workspace w, float *const *data, float *const *mean, float *const *cov,
+                                    int precision, void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!data || !mean || !cov) { set_error("null buffer argument"); return CG_ERR_ARG; }
+  if (w->is4d) { set_error("the fused form needs a separable 3-parameter prior; use cg_invert_bins_plain for 4D"); return CG_ERR_UNSUPPORTED; }
+  if (precision != CG_PREC_FP32 && precision != CG_PREC_MIXED) { set_error("precision %d not valid for FP32 buffers", precision); return CG_ERR_ARG; }
+  return fused_launch<float>(w, (void *const *)data, (void *const *)mean, (void *const *)cov, precision,
+                             (cudaStream_t)stream);
+}
+
+extern "C" int cg_invert_bins_fused_f64(cg_workspace w, double *const *data, double *const *mean,
+                                        double *const *cov, void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!data || !mean || !cov) { set_error("null buffer argument"); return CG_ERR_ARG; }
+  if (w->is4d) { set_error("the fused form needs a separable 3-parameter prior"); return CG_ERR_UNSUPPORTED; }
+  return fused_launch<double>(w, (void *const *)data, (void *const *)mean, (void *const *)cov, CG_PREC_FP64,
+                              (cudaStream_t)stream);
+}

@@ -1,0 +1,65 @@
+// Per-frequency-bin posterior: tables and device math shared by the kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace cg {
+
+constexpr int kMaxTheta = 8;
+constexpr int kTri = kMaxTheta * (kMaxTheta + 1) / 2;
+constexpr double kCholTol = 1e-20;  // lib_matr.c:19, applied to the pivots scaled by A00
+
+__host__ __device__ constexpr int tri(int l, int m) { return l * (l + 1) / 2 + m; }  // l >= m
+
+// Per temporal-frequency tables.  For one k (constant-thickness branch of
+// Crava::fillErrMultVectors, src/crava.cpp:1337-1361, and getNextErrorVariance,
+// src/crava.cpp:1442-1469), with S0 the 3x3 prior and lam the per-(i,j)
+// error-correlation eigenvalue:
+//   K      forward operator kD(k) conj(W_l(k)) A_l            (ntheta x 3)
+//   KS0    K S0                                               (ntheta x 3)
+//   M      K S0 K^H                                           (lower, packed)
+//   E      0.5 (1-wnc) errThetaCov (e1 e1^H + e2 e2^H)        (lower, packed)
+//   D      wnc errThetaCov_ll |Re e3_l|^2                     (diagonal)
+// so that for a bin with prior scale s and error eigenvalue lam the data
+// covariance is  Sd = s M + lam E + diag(D).
+template <typename T>
+struct KTab {
+  C2<T> K[kMaxTheta][3];
+  C2<T> KS0[kMaxTheta][3];
+  C2<T> M[kTri];
+  C2<T> E[kTri];
+  T D[kMaxTheta];
+  int band;
+  int pad_[3];
+};
+
+// Opaque workspace behind cg_workspace (device buffers of one model).
+struct Workspace {
+  int device;
+  int nxp, nyp, nzp, ntheta;
+  float wnc;
+  int is4d;
+  double sigma0[9];
+  float sigma0f[9];
+  double cond_threshold;
+  // per-model tables (device)
+  KTab<float> *ktab_f;
+  KTab<double> *ktab_d;
+  float2 *K;        // nzp*ntheta*3 (reference-order tables for the plain path)
+  float2 *em1, *em2, *em3;
+  unsigned char *band;
+  double *etc;      // ntheta*ntheta
+  // separable prior spectra (device), rebuilt by every fused inversion
+  float *cxy_f;     // real staging rnxp*nyp -> complex cnxp*nyp
+  float *ct_f;      // real staging 2*(nzp/2+1) -> complex nzp/2+1
+  double *cxy_d;
+  double *ct_d;
+  // mixed-precision fix-up queue and counters (device)
+  int *queue;
+  int queue_cap;
+  int *counters;    // [0] flagged, [1] failed cholesky, [2] queue overflow
+  long inband_bins;  // bins whose k is inside the inversion band
+  bool model_set;
+};
+
+}  // namespace cg

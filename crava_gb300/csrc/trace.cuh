@@ -1,0 +1,23 @@
+// RAII launch tracer (see trace.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace cg {
+
+bool trace_on();
+
+class TraceScope {
+ public:
+  TraceScope(const char *name, cudaStream_t st, double bytes);
+  ~TraceScope();
+
+ private:
+  const char *name_;
+  cudaStream_t st_;
+  double bytes_;
+  void *a_ = nullptr;
+  void *b_ = nullptr;
+};
+
+}  // namespace cg

@@ -1,0 +1,198 @@
+/*
+ * cravagpu.h -- C-ABI of the GB300 (sm_103a) FFT-domain Bayesian AVO
+ * inversion library (libcravagpu.so).
+ *
+ * Every entry point takes plain pointers and sizes, returns CG_OK (0) or a
+ * negative status (cg_last_error() gives the text) and never exits the
+ * process.  Buffers follow the reference FFTGrid in-place layout
+ * (src/fftgrid.cpp:40-70): a padded cube of nxp*nyp*nzp cells is stored as
+ * rnxp*nyp*nzp floats with rnxp = 2*(nxp/2+1), x fastest; after a forward
+ * transform the same memory holds cnxp*nyp*nzp interleaved complex floats
+ * (cnxp = nxp/2+1), bin (i,j,k) at i + cnxp*j + cnxp*nyp*k.
+ *
+ * Unless an entry point's name ends in _host, pointers are device pointers
+ * and work is queued on `stream` (a cudaStream_t, NULL = legacy default
+ * stream) without synchronising.  _host variants take host memory, copy it to
+ * the device, run, copy the results back and synchronise.
+ *
+ * Paths in comments are relative to the CRAVA source tree.
+ */
+#ifndef CRAVAGPU_H
+#define CRAVAGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define CG_OK 0
+#define CG_ERR_ARG (-1)         /* bad argument (size, pointer, type) */
+#define CG_ERR_CUDA (-2)        /* CUDA runtime error */
+#define CG_ERR_UNSUPPORTED (-3) /* valid input this build does not handle */
+#define CG_ERR_STATE (-4)       /* call out of order (e.g. handle not set up) */
+
+/* ---- cube types: the values of FFTGrid::gridTypes (src/fftgrid.h:199) -- */
+#define CG_CTMISSING 0
+#define CG_DATA 1
+#define CG_PARAMETER 2
+#define CG_COVARIANCE 3
+#define CG_VELOCITY 4
+#define CG_OPERATOR 5
+
+/* ---- precision modes of the fused per-bin posterior ------------------- */
+#define CG_PREC_FP32 0  /* all FP32 */
+#define CG_PREC_MIXED 1 /* FP32 bulk, FP64 Cholesky/solves + 1 refinement step on flagged bins */
+#define CG_PREC_FP64 2  /* all FP64 (accuracy reference on the GPU) */
+
+/* Text of the last error raised on the calling thread. */
+const char *cg_last_error(void);
+/* Library version, e.g. 100 = 0.1.0. */
+int cg_version(void);
+/* Largest transform length supported along one axis. */
+int cg_fft_max_length(void);
+
+/* Launch tracing (the GPU counterpart of the reference's Timings phase timers,
+ * src/timings.h:11-30).  When enabled, every library launch records CUDA
+ * events on its own stream and its algorithmic HBM bytes (the bytes the
+ * kernel must move at minimum).  cg_trace_collect synchronises and returns
+ * the number of distinct kernels; cg_trace_entry reads one aggregate. */
+int cg_trace_enable(int on);
+int cg_trace_collect(void);
+int cg_trace_entry(int index, char *name, int name_len, long *launches, double *ms_total, double *bytes_total);
+
+/* ========================================================================
+ * 3D real<->complex transforms of padded cubes.
+ * ======================================================================== */
+
+/* Replaces FFTGrid::fftInPlace (src/fftgrid.cpp:1783-1809): scale by
+ * 1/sqrt(nxp*nyp*nzp) unless cubetype is CG_COVARIANCE or CG_OPERATOR, then an
+ * unnormalised forward (sign -1) R2C transform in place, as
+ * rfftwnd_one_real_to_complex (libs/fft/rfftw/rfftwnd.c:558). */
+int cg_fft3d_r2c(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
+/* Replaces FFTGrid::invFFTInPlace (src/fftgrid.cpp:1811-1842): unnormalised
+ * backward (sign +1) C2R transform in place -- complex dimensions first, then
+ * x, keeping only the real part of the x=0 and (even nxp) x=nxp/2 bins as
+ * rfftwnd_one_complex_to_real does (libs/fft/rfftw/rfftwnd.c:564) -- then
+ * scale by 1/N (CG_COVARIANCE, CG_OPERATOR) or 1/sqrt(N) (others). */
+int cg_fft3d_c2r(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
+/* The same two transforms on `count` equally sized cubes in one launch per
+ * pass (bufs: host array of device pointers). */
+int cg_fft3d_r2c_batch(float *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, void *stream);
+int cg_fft3d_c2r_batch(float *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
+/* FP64 variants (double buffers, same layout); the GPU accuracy reference. */
+int cg_fft3d_r2c_f64(double *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+int cg_fft3d_c2r_f64(double *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
+/* Host-memory variants of cg_fft3d_r2c / cg_fft3d_c2r (synchronous). */
+int cg_fft3d_r2c_host(float *hbuf, int nxp, int nyp, int nzp, int cubetype);
+int cg_fft3d_c2r_host(float *hbuf, int nxp, int nyp, int nzp, int cubetype);
+
+/* ========================================================================
+ * Model set-up helpers.
+ * ======================================================================== */
+
+/* Per-k operator tables of Crava::fillErrMultVectors (src/crava.cpp:1337-1361,
+ * constant-thickness branch) from the resampled wavelets (HOST arrays):
+ * wavelets [ntheta][nzp] real samples in FFT order (Wavelet::resample,
+ * src/wavelet.cpp:416-463), A [ntheta][3] reflection coefficients.  Outputs
+ * (HOST): K [nzp][ntheta][3], em1/em2/em3 [nzp][ntheta] interleaved complex,
+ * band [nzp] (lowCut*minRelThick < f_k < highCut, src/crava.cpp:1104-1105). */
+int cg_operator_tables(int ntheta, int nz, int nzp, const float *wavelets, const float *A, float dt_ms,
+                       float min_rel_thick, float low_cut, float high_cut, float *K, float *em1, float *em2,
+                       float *em3, unsigned char *band);
+
+/* FFTGrid::findClosestFactorableNumber (src/fftgrid.cpp:2857-2885). */
+int cg_find_closest_factorable(int n);
+
+/* FFTGrid::fillInParamCorr (src/fftgrid.cpp:1072-1119) times `scalar` into a
+ * padded real cube (device): corr_xy [nyp][nxp], circ_corr_t [nzp]. */
+int cg_fill_param_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_xy, const float *circ_corr_t,
+                       float grad_i, float grad_j, float scalar, void *stream);
+
+/* FFTGrid::fillInErrCorr (src/fftgrid.cpp:1018-1070) into a padded real cube
+ * (device). */
+int cg_fill_err_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_xy, float grad_i, float grad_j,
+                     void *stream);
+
+/* ========================================================================
+ * Per-frequency-bin posterior (Crava::computePostMeanResidAndFFTCov bin loop,
+ * src/crava.cpp:1084-1247).
+ * ======================================================================== */
+
+/* Device-side state of one inversion model: per-k operator tables, the
+ * separable prior spectra, and the mixed-precision fix-up queue. */
+typedef struct cg_workspace_s *cg_workspace;
+
+/* Model description; every pointer is HOST memory, read during
+ * cg_workspace_set_model only.  Complex arrays are interleaved (re, im) float
+ * pairs in the reference's per-k loop order. */
+typedef struct cg_model {
+  int ntheta;                  /* angle stacks, 1..8 */
+  float wnc;                   /* white-noise component (Crava::wnc_) */
+  int is4d;                    /* 4D branch of findParameterVariances
+                                  (src/seismicparametersholder.cpp:366-373) */
+  const float *K;              /* [nzp][ntheta][3] complex: kD(k) conj(W_l(k)) A[l][p]
+                                  (Crava::fillErrMultVectors, src/crava.cpp:1337-1361) */
+  const float *em1;            /* [nzp][ntheta] complex errMult1 */
+  const float *em2;            /* [nzp][ntheta] complex errMult2 */
+  const float *em3;            /* [nzp][ntheta] complex errMult3 */
+  const unsigned char *band;   /* [nzp] 1 = invert this k (src/crava.cpp:1104-1105) */
+  const double *err_theta_cov; /* [ntheta][ntheta] Crava::errThetaCov_ */
+  const double *sigma0;        /* [3][3] prior covariance (priorVar0) */
+  double cond_threshold;       /* CG_PREC_MIXED: redo a bin in FP64 when the squared
+                                  ratio of largest to smallest Cholesky pivot exceeds
+                                  this; <= 0 selects 1e3 */
+} cg_model;
+
+/* Allocate the device workspace for nxp x nyp x nzp cubes and ntheta stacks
+ * (on the current device).  Allocation happens here only. */
+int cg_workspace_create(cg_workspace *ws, int nxp, int nyp, int nzp, int ntheta);
+void cg_workspace_destroy(cg_workspace ws);
+
+/* Upload the model and build the per-k tables (synchronous). */
+int cg_workspace_set_model(cg_workspace ws, const cg_model *model);
+
+/* Counters since the last reset: bins queued for FP64, bins whose Cholesky
+ * failed (they keep the prior, like lib_matrCholCpx failures in the
+ * reference, src/crava.cpp:1421-1423), queue overflows.  Synchronises. */
+int cg_workspace_stats(cg_workspace ws, int *flagged, int *failed, int *overflow);
+int cg_workspace_reset_stats(cg_workspace ws, void *stream);
+
+/* Reference dataflow, FP32.  data[ntheta]: data spectra in, residual spectra
+ * out; mean[3]: prior-mean spectra in, posterior-mean spectra out; cov[6]
+ * (order covAlpha, covBeta, covRho, crCovAlphaBeta, crCovAlphaRho,
+ * crCovBetaRho): prior covariance spectra (unnormalised COVARIANCE transforms
+ * of fillInParamCorr cubes) in, posterior covariance spectra out; errcorr: the
+ * error-correlation spectrum (fillInErrCorr + COVARIANCE transform). */
+int cg_invert_bins_plain(cg_workspace ws, float *const *data, float *const *mean, float *const *cov,
+                         const float *errcorr, void *stream);
+
+/* Rebuild the separable prior spectra from the lateral correlation surface
+ * corr_xy (device, nyp rows of nxp floats, ModelGeneral::findCorrXYGrid) and
+ * the cyclic temporal correlation circ_corr_t (device, nzp floats,
+ * SeismicParametersHolder::computeCircCorrT).  Replaces FFTCovGrids and the
+ * errCorr transform of the reference when the correlation gradients are 0.
+ * precision CG_PREC_FP64 also builds the FP64 tables. */
+int cg_prior_spectra(cg_workspace ws, const float *corr_xy, const float *circ_corr_t, int precision,
+                     void *stream);
+
+/* Fused posterior: same data/mean in-out convention as the plain form; cov[6]
+ * is output only.  precision CG_PREC_FP32 or CG_PREC_MIXED.  Needs
+ * cg_prior_spectra first. */
+int cg_invert_bins_fused(cg_workspace ws, float *const *data, float *const *mean, float *const *cov,
+                         int precision, void *stream);
+
+/* Fused posterior on FP64 spectra (needs cg_prior_spectra with CG_PREC_FP64). */
+int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,
+                             void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CRAVAGPU_H */

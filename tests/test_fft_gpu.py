@@ -1,0 +1,131 @@
+"""GPU 3D transforms against the reference's FFTW 2.1.2 vectors and the oracle."""
+import ctypes as ct
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import from_cube, golden, rel
+
+pytestmark = pytest.mark.gpu
+
+FFT_TOL = 2e-6  # FP32, relative L2 over the cube
+
+
+@pytest.mark.parametrize("case", ["fft_even.npz", "fft_odd.npz", "fft_mixed.npz"])
+def test_fft_matches_reference_fftw(cuda, case):
+    from crava_gb300 import api
+    g = golden(case)
+    nxp = int(g["nxp"])
+    for ctype, key in ((api.DATA, "r2c_data"), (api.COVARIANCE, "r2c_cov")):
+        x = torch.from_numpy(g["real_in"].copy()).cuda()
+        api.fft_in_place(x, nxp, ctype)
+        assert rel(from_cube(x), g[key]) < FFT_TOL, key
+    for ctype, key in ((api.PARAMETER, "c2r_param"), (api.COVARIANCE, "c2r_cov")):
+        x = torch.from_numpy(g["spec_in"].view(np.float32).copy()).cuda()
+        api.inv_fft_in_place(x, nxp, ctype)
+        assert rel(x.cpu().numpy()[..., :nxp], g[key][..., :nxp]) < FFT_TOL, key
+
+
+SIZES = [(80, 80, 160), (16, 12, 20), (15, 9, 7), (21, 15, 35), (49, 27, 25), (128, 1, 1), (1, 64, 1),
+         (2, 2, 2), (200, 100, 8), (98, 54, 45), (256, 16, 24), (7, 5, 3), (64, 343, 10)]
+
+
+@pytest.mark.parametrize("dims", SIZES)
+def test_fft_matches_oracle(cuda, oracle, dims):
+    from crava_gb300 import api
+    nxp, nyp, nzp = dims
+    cnxp, rnxp = oracle.dims(nxp)
+    rng = np.random.default_rng(nxp * 1000 + nyp * 10 + nzp)
+    x = np.zeros((nzp, nyp, rnxp), np.float32)
+    x[..., :nxp] = rng.standard_normal((nzp, nyp, nxp))
+    ref = oracle.fft3d_r2c(x, nxp, oracle.DATA, "d")
+    t = torch.from_numpy(x.copy()).cuda()
+    api.fft_in_place(t, nxp, api.DATA)
+    assert rel(from_cube(t), ref) < FFT_TOL
+    spec = (rng.standard_normal((nzp, nyp, cnxp)) + 1j * rng.standard_normal((nzp, nyp, cnxp))).astype(np.complex64)
+    ref = oracle.fft3d_c2r(spec, nxp, oracle.PARAMETER, "d")[..., :nxp]
+    t = torch.from_numpy(spec.view(np.float32).copy()).cuda()
+    api.inv_fft_in_place(t, nxp, api.PARAMETER)
+    assert rel(t.cpu().numpy()[..., :nxp], ref) < FFT_TOL
+
+
+@pytest.mark.parametrize("dims", [(80, 80, 160), (21, 15, 35), (64, 48, 40)])
+def test_fft_fp64_matches_fp64_oracle(cuda, oracle, dims):
+    from crava_gb300 import api
+    nxp, nyp, nzp = dims
+    cnxp, rnxp = oracle.dims(nxp)
+    rng = np.random.default_rng(5)
+    x = np.zeros((nzp, nyp, rnxp), np.float64)
+    x[..., :nxp] = rng.standard_normal((nzp, nyp, nxp))
+    ref = oracle.fft3d_r2c(x, nxp, oracle.COVARIANCE, "d")
+    t = torch.from_numpy(x.copy()).cuda()
+    api.fft_in_place(t, nxp, api.COVARIANCE)
+    assert rel(from_cube(t), ref) < 1e-13
+    api.inv_fft_in_place(t, nxp, api.COVARIANCE)
+    assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < 1e-13
+
+
+def test_batch_equals_single(cuda):
+    from crava_gb300 import api
+    nxp, nyp, nzp = 40, 30, 24
+    g = torch.Generator(device="cuda").manual_seed(3)
+    cubes = [torch.randn((nzp, nyp, 42), device="cuda", generator=g) for _ in range(19)]
+    singles = [c.clone() for c in cubes]
+    api.fft_in_place_batch(cubes, nxp, api.DATA)
+    for s in singles:
+        api.fft_in_place(s, nxp, api.DATA)
+    for a, b in zip(cubes, singles):
+        assert torch.equal(a, b)
+    api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
+
+
+def test_round_trip_full_size(cuda):
+    """256^3 DATA transform and back is the identity (1/sqrt(N) both ways)."""
+    from crava_gb300 import api
+    n = 256
+    g = torch.Generator(device="cuda").manual_seed(11)
+    x = torch.randn((n, n, n + 2), device="cuda", generator=g)
+    x[..., n:] = 0
+    y = x.clone()
+    api.fft_in_place(y, n, api.DATA)
+    # Parseval for the norm-preserving transform: sum |x|^2 = sum over the full spectrum
+    s = api.as_spectrum(y)
+    w = torch.full((n // 2 + 1,), 2.0, device="cuda", dtype=torch.float64)
+    w[0] = 1
+    w[-1] = 1
+    e_spec = (s.abs().double() ** 2 * w).sum()
+    e_x = (x[..., :n].double() ** 2).sum()
+    assert abs(float(e_spec / e_x) - 1) < 1e-5
+    api.inv_fft_in_place(y, n, api.DATA)
+    err = float((y[..., :n] - x[..., :n]).norm() / x[..., :n].norm())
+    assert err < 2e-6
+
+
+def test_host_variant_matches_device(cuda, native):
+    from crava_gb300 import api
+    nxp, nyp, nzp = 30, 20, 18
+    rng = np.random.default_rng(9)
+    x = np.zeros((nzp, nyp, 32), np.float32)
+    x[..., :nxp] = rng.standard_normal((nzp, nyp, nxp))
+    h = x.copy()
+    assert native.cg_fft3d_r2c_host(h.ctypes.data, nxp, nyp, nzp, api.DATA) == 0
+    t = torch.from_numpy(x.copy()).cuda()
+    api.fft_in_place(t, nxp, api.DATA)
+    np.testing.assert_array_equal(h, t.cpu().numpy())
+    assert native.cg_fft3d_c2r_host(h.ctypes.data, nxp, nyp, nzp, api.DATA) == 0
+    assert rel(h[..., :nxp], x[..., :nxp]) < FFT_TOL
+
+
+def test_bad_arguments_return_status(cuda, native):
+    from crava_gb300 import api
+    t = torch.zeros((8, 8, 12), device="cuda")
+    s = ct.c_void_p(0)
+    assert native.cg_fft3d_r2c(ct.c_void_p(t.data_ptr()), 0, 8, 8, api.DATA, s) == -1
+    assert native.cg_fft3d_r2c(ct.c_void_p(t.data_ptr()), 10, 8, 8, 0, s) == -1
+    assert native.cg_fft3d_r2c(None, 10, 8, 8, api.DATA, s) == -1
+    # 11 and 13 are not factors the reference pads to; refused, not mis-transformed
+    t2 = torch.zeros((8, 8, 12), device="cuda")
+    assert native.cg_fft3d_r2c(ct.c_void_p(t2.data_ptr()), 11, 8, 8, api.DATA, s) == -3
+    assert b"prime factor" in native.cg_last_error()
+    torch.cuda.synchronize()

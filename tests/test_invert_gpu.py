@@ -1,0 +1,101 @@
+"""GPU per-bin posterior against the reference's own FP32 outputs and the FP64 oracle."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import from_cube, golden, oracle_pipeline, rel, to_cube
+
+pytestmark = pytest.mark.gpu
+
+
+def _ws_from_golden(g, cond_threshold=0.0):
+    from crava_gb300 import api
+    n = len(g["theta_deg"])
+    ws = api.Workspace(int(g["nxp"]), int(g["nyp"]), int(g["nzp"]), n)
+    tab = {k: g[k] for k in ("K", "em1", "em2", "em3", "band")}
+    ws.set_model(tab, g["err_theta_cov"], g["sigma0"], float(g["wnc"]), cond_threshold=cond_threshold)
+    return ws
+
+
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+def test_plain_matches_reference_lib_matr(cuda, case):
+    """Same input spectra as the reference run -> same posterior (FP32 vs FP32)."""
+    g = golden(case)
+    ws = _ws_from_golden(g)
+    data = [to_cube(x) for x in g["data_spec"]]
+    mean = [to_cube(x) for x in g["mean_spec"]]
+    cov = [to_cube(x) for x in g["cov_spec"]]
+    ec = to_cube(g["errcorr_spec"])
+    ws.reset_stats()
+    ws.invert_plain(data, mean, cov, ec)
+    torch.cuda.synchronize()
+    res = np.stack([from_cube(x) for x in data])
+    mu = np.stack([from_cube(x) for x in mean])
+    cv = np.stack([from_cube(x) for x in cov])
+    upd, upd_ref = mu - g["mean_spec"], g["out_mean"] - g["mean_spec"]
+    e_upd, e_res, e_cov = rel(upd, upd_ref), rel(res, g["out_resid"]), rel(cv, g["out_cov"])
+    print(case, "plain vs reference: update", e_upd, "resid", e_res, "cov", e_cov)
+    assert e_upd < 1e-4 and e_res < 1e-5 and e_cov < 1e-5
+    assert ws.stats()["failed"] == int(g["nfail"])
+
+
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+@pytest.mark.parametrize("form", ["fp32", "mixed"])
+def test_fused_matches_fp64_oracle_on_reference_inputs(cuda, oracle, case, form):
+    """Fused kernel (prior regenerated from the separable spectra) vs the FP64 restatement."""
+    from crava_gb300 import api
+    g = golden(case)
+    ws = _ws_from_golden(g)
+    nxp, nyp, nzp = int(g["nxp"]), int(g["nyp"]), int(g["nzp"])
+    corr_xy = torch.from_numpy(g["corr_xy"].astype(np.float32)).cuda()
+    circ = torch.from_numpy(g["circ_corr_t"].astype(np.float32)).cuda()
+    ws.prior_spectra(corr_xy, circ, api.PREC_FP32)
+    data = [to_cube(x) for x in g["data_spec"]]
+    mean = [to_cube(x) for x in g["mean_spec"]]
+    cov = [to_cube(np.zeros_like(x)) for x in g["cov_spec"]]
+    ws.reset_stats()
+    ws.invert_fused(data, mean, cov, api.PREC_MIXED if form == "mixed" else api.PREC_FP32)
+    torch.cuda.synchronize()
+    # FP64 oracle on the same input spectra, prior spectra from FP64 transforms of the filled cubes
+    covs = []
+    s0f = g["sigma0"].astype(np.float32).astype(np.float64)
+    for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]:
+        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], 0, 0, float(s0f[p, q]), prec="d")
+        covs.append(oracle.fft3d_r2c(c, nxp, oracle.COVARIANCE, "d"))
+    ec = oracle.fft3d_r2c(oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"], prec="d"), nxp, oracle.COVARIANCE, "d")
+    tab = {k: g[k].astype(np.complex128) if g[k].dtype == np.complex64 else g[k] for k in ("K", "em1", "em2", "em3", "band")}
+    tab["nxp"] = nxp
+    r64, m64, c64, _ = oracle.invert_bins(list(g["data_spec"].astype(np.complex128)),
+                                          list(g["mean_spec"].astype(np.complex128)), covs, ec, tab,
+                                          g["err_theta_cov"], s0f, float(g["wnc"]), prec="d")
+    mu = np.stack([from_cube(x) for x in mean])
+    res = np.stack([from_cube(x) for x in data])
+    cv = np.stack([from_cube(x) for x in cov])
+    e_upd = rel(mu - g["mean_spec"], np.stack(m64) - g["mean_spec"])
+    e_res = rel(res, np.stack(r64))
+    e_cov = rel(cv, np.stack(c64))
+    print(case, form, "vs FP64 oracle: update", e_upd, "resid", e_res, "cov", e_cov, ws.stats())
+    assert e_upd < 1e-4 and e_res < 1e-5 and e_cov < 1e-4
+
+
+@pytest.mark.parametrize("form", ["plain", "fp32", "mixed", "fp64"])
+def test_pipeline_matches_fp64_oracle(cuda, oracle, form):
+    """Whole inversion from real-domain cubes (config-1 physics on a 40x36x48 cube)."""
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.scaled_config1(40, 36, 48, seed=21)
+    inv = Inversion(sc, forms=(form,))
+    inv.restore(form)
+    inv.run(form)
+    torch.cuda.synchronize()
+    pm, res, cov = inv.results(form)
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d")
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    e_mean = rel(pm, post64)
+    e_upd = rel(pm - prior, post64 - prior)
+    e_res = rel(res, res64)
+    e_cov = rel(cov, cov64)
+    print(form, "pipeline vs FP64 oracle: mean", e_mean, "update", e_upd, "resid", e_res, "cov", e_cov)
+    tol = 1e-10 if form == "fp64" else 1e-4
+    assert e_mean < (1e-12 if form == "fp64" else 1e-6)
+    assert e_upd < tol and e_res < tol and e_cov < tol
