@@ -133,6 +133,10 @@ def _declare(L):
         "cg_find_closest_factorable": ([I], I),
         "cg_fill_param_corr": ([V, I, I, I, V, V, F, F, F, V], I),
         "cg_fill_err_corr": ([V, I, I, I, V, F, F, V], I),
+        "cg_posterior_cholesky": ([PP, V, I, I, I, V, V], I),
+        "cg_simulate_fields": ([V, PP, PP, I, I, ct.c_uint64, I, I, I, PP, V], I),
+        "cg_state4d_merge": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V], I),
+        "cg_state4d_split": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V, V], I),
         "cg_trace_enable": ([I], I),
         "cg_trace_collect": ([], I),
         "cg_trace_entry": ([I, ct.c_char_p, I, ct.POINTER(ct.c_long), ct.POINTER(D), ct.POINTER(D)], I),

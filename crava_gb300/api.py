@@ -192,3 +192,42 @@ class Workspace:
             check(lib().cg_invert_bins_fused_f64(self.h, pd, pm, pc, _stream(stream)), "cg_invert_bins_fused_f64")
         else:
             check(lib().cg_invert_bins_fused(self.h, pd, pm, pc, precision, _stream(stream)), "cg_invert_bins_fused")
+
+
+def posterior_cholesky(post_cov, nxp, stream=None):
+    """Per-bin Cholesky factor of the posterior covariance spectra (9 float planes)."""
+    nzp, nyp, _ = post_cov[0].shape
+    cnxp, _ = dims(nxp)
+    chol = torch.empty((9, nzp, nyp, cnxp), dtype=torch.float32, device=post_cov[0].device)
+    nfail = torch.zeros(1, dtype=torch.int32, device=post_cov[0].device)
+    pc, k = _pp(post_cov)
+    check(lib().cg_posterior_cholesky(pc, _vp(chol), nxp, nyp, nzp, _vp(nfail), _stream(stream)),
+          "cg_posterior_cholesky")
+    return chol, nfail
+
+
+def simulate_fields(chol, fields, nxp, seed=0, real0=0, noise=None, post_mean=None, stream=None):
+    """Fill fields (3 per realisation) with posterior realisations (see cg_simulate_fields)."""
+    nzp, nyp, _ = fields[0].shape
+    pf, k1 = _pp(fields)
+    pn, k2 = _pp(noise) if noise is not None else (None, None)
+    pm, k3 = _pp(post_mean) if post_mean is not None else (None, None)
+    check(lib().cg_simulate_fields(_vp(chol), pn, pf, len(fields) // 3, real0, seed, nxp, nyp, nzp, pm,
+                                   _stream(stream)), "cg_simulate_fields")
+
+
+def state4d_merge(mu_s, mu_d, ss, sd, dd, mu_cur, cov_cur, nxp, stream=None):
+    """State4D::merge/mergeCov into mu_cur[3], cov_cur[6] (order 00 01 02 11 12 22)."""
+    nzp, nyp, _ = mu_s[0].shape
+    keep = [_pp(x) for x in (mu_s, mu_d, ss, sd, dd, mu_cur, cov_cur)]
+    check(lib().cg_state4d_merge(*[k[0] for k in keep], nxp, nyp, nzp, _stream(stream)), "cg_state4d_merge")
+
+
+def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, nxp, stream=None):
+    """State4D::split in place; returns a device counter of bins that kept the prior."""
+    nzp, nyp, _ = mu_s[0].shape
+    nfail = torch.zeros(1, dtype=torch.int32, device=mu_s[0].device)
+    keep = [_pp(x) for x in (mu_s, mu_d, ss, sd, dd, mu_post, cov_post)]
+    check(lib().cg_state4d_split(*[k[0] for k in keep], nxp, nyp, nzp, _vp(nfail), _stream(stream)),
+          "cg_state4d_split")
+    return nfail

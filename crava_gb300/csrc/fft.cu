@@ -174,8 +174,9 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p
 
 // x rows, half spectrum -> real, postscale fused into the store.
 template <typename T>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, AxisPlan p, const C2<T> *__restrict__ twg,
-                                                          int nxp, int nrows, T postscale)
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet addend, AxisPlan p,
+                                                          const C2<T> *__restrict__ twg, int nxp, int nrows,
+                                                          T postscale)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = p.n;
@@ -217,18 +218,28 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, AxisPlan p
   }
   __syncthreads();
   C2<T> *res = smem_fft<T>(bufA, bufB, p, kRows, ldw, tw, even ? 2 : 1, +1);
+  // optional fused FFTGrid::add of a real cube (src/fftgrid.cpp:1870-1891)
+  const T *add = addend.ptr[blockIdx.z] ? (const T *)addend.ptr[blockIdx.z] + (long)r0 * rnxp : nullptr;
   if (even) {
     const int tot2 = nr * (m + 1);
     for (int t = threadIdx.x; t < tot2; t += blockDim.x) {
       int row = t / (m + 1), e = t - row * (m + 1);
       C2<T> z = (e < m) ? res[e * ldw + row] : mk<T>(0, 0);
-      ((C2<T> *)(base + (long)row * rnxp))[e] = mk<T>(z.x * postscale, z.y * postscale);
+      z = mk<T>(z.x * postscale, z.y * postscale);
+      if (add) {
+        const C2<T> a = ((const C2<T> *)(add + (long)row * rnxp))[e];
+        z.x += a.x;
+        z.y += a.y;
+      }
+      ((C2<T> *)(base + (long)row * rnxp))[e] = z;
     }
   } else {
     const int tot2 = nr * rnxp;
     for (int t = threadIdx.x; t < tot2; t += blockDim.x) {
       int row = t / rnxp, e = t - row * rnxp;
-      base[(long)row * rnxp + e] = (e < nxp) ? res[e * ldw + row].x * postscale : (T)0;
+      T v = (e < nxp) ? res[e * ldw + row].x * postscale : (T)0;
+      if (add) v += add[(long)row * rnxp + e];
+      base[(long)row * rnxp + e] = v;
     }
   }
 }
@@ -239,7 +250,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, AxisPlan p
 namespace {
 
 template <typename T>
-int launch_rows(bool forward, const CubeSet &cs, int ncubes, int nxp, int nyp, int nzp, T scale, cudaStream_t st)
+int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nyp, int nzp,
+                T scale, cudaStream_t st)
 {
   const bool even = (nxp % 2) == 0;
   const int m = even ? nxp / 2 : nxp;
@@ -266,7 +278,7 @@ int launch_rows(bool forward, const CubeSet &cs, int ncubes, int nxp, int nyp, i
     k_r2c_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, nxp, nrows, scale);
   } else {
     CG_CUDA(cudaFuncSetAttribute(k_c2r_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_c2r_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, nxp, nrows, scale);
+    k_c2r_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, addend, p, tw, nxp, nrows, scale);
   }
   CG_CHECK_LAUNCH(forward ? "k_r2c_rows" : "k_c2r_rows");
   return CG_OK;
@@ -333,6 +345,20 @@ int check_dims(int nxp, int nyp, int nzp, int count)
 template <typename T>
 int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st)
 {
+  return fft3d_add<T>(bufs, nullptr, count, nxp, nyp, nzp, cubetype, forward, st);
+}
+
+template <typename T>
+int fft3d_c2r_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
+                  cudaStream_t st)
+{
+  return fft3d_add<T>(bufs, addends, count, nxp, nyp, nzp, cubetype, false, st);
+}
+
+template <typename T>
+int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
+              bool forward, cudaStream_t st)
+{
   int rc = check_dims(nxp, nyp, nzp, count);
   if (rc) return rc;
   if (cubetype < CG_CTMISSING || cubetype > CG_OPERATOR || cubetype == CG_CTMISSING) {
@@ -344,30 +370,33 @@ int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype,
   const bool covlike = (cubetype == CG_COVARIANCE || cubetype == CG_OPERATOR);
   for (int b0 = 0; b0 < count; b0 += kMaxBatch) {
     int nb = count - b0 < kMaxBatch ? count - b0 : kMaxBatch;
-    CubeSet cs;
+    CubeSet cs, ad;
+    for (int i = 0; i < kMaxBatch; i++) { cs.ptr[i] = nullptr; ad.ptr[i] = nullptr; }
     for (int i = 0; i < nb; i++) {
       if (!bufs[b0 + i]) {
         set_error("null buffer %d", b0 + i);
         return CG_ERR_ARG;
       }
       cs.ptr[i] = bufs[b0 + i];
+      if (addends) ad.ptr[i] = (void *)addends[b0 + i];
     }
     if (forward) {
       T pre = covlike ? (T)1 : (T)(1.0 / sqrt(N));
-      if ((rc = launch_rows<T>(true, cs, nb, nxp, nyp, nzp, pre, st))) return rc;
+      if ((rc = launch_rows<T>(true, cs, ad, nb, nxp, nyp, nzp, pre, st))) return rc;
       if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, -1, st))) return rc;
       if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, -1, st))) return rc;
     } else {
       T post = covlike ? (T)(1.0 / N) : (T)(1.0 / sqrt(N));
       if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, +1, st))) return rc;
       if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, +1, st))) return rc;
-      if ((rc = launch_rows<T>(false, cs, nb, nxp, nyp, nzp, post, st))) return rc;
+      if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st))) return rc;
     }
   }
   return CG_OK;
 }
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);
+template int fft3d_c2r_add<float>(void *const *, const void *const *, int, int, int, int, int, cudaStream_t);
 
 }  // namespace cg
 

@@ -26,6 +26,13 @@ bool make_axis_plan(int n, AxisPlan *p);
 template <typename T> const C2<T> *twiddle_table(int n);
 template <typename T>
 int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st);
+template <typename T>
+int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
+              bool forward, cudaStream_t st);
+// inverse transform with a real cube added to each result (FFTGrid::add fused)
+template <typename T>
+int fft3d_c2r_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
+                  cudaStream_t st);
 
 // twiddle W (forward table entry) applied with the transform's sign
 template <typename T>

@@ -26,6 +26,7 @@
 #include "common.cuh"
 #include "fft.cuh"
 #include "posterior.cuh"
+#include "linalg.cuh"
 #include "trace.cuh"
 
 namespace cg {
@@ -55,44 +56,6 @@ __device__ __forceinline__ float2 param_cov_entry(float2 v, float s)
 {
   if (s != 0.0f) v.x = v.x / s;
   return make_float2(sqrtf(v.x * v.x) * s, 0.0f);
-}
-
-// lib_matrCholCpx (libs/lib/lib_matr.c:78-168) on a packed lower triangle
-template <typename T, int N>
-__device__ __forceinline__ bool chol_ref(C2<T> *L)
-{
-  const T factor = L[0].x;
-  if (!(factor > (T)0)) return false;
-#pragma unroll
-  for (int t = 0; t < N * (N + 1) / 2; t++) { L[t].x = L[t].x / factor; L[t].y = L[t].y / factor; }
-#pragma unroll
-  for (int i = 0; i < N; i++) {
-    if (L[tri(i, i)].x <= (T)kCholTol) return false;
-#pragma unroll
-    for (int j = 0; j < i; j++) {
-      T lr = 0, li = 0;
-#pragma unroll
-      for (int k = 0; k < j; k++) {
-        lr += (L[tri(i, k)].x * L[tri(j, k)].x) + (L[tri(i, k)].y * L[tri(j, k)].y);
-        li += -(L[tri(i, k)].x * L[tri(j, k)].y) + (L[tri(i, k)].y * L[tri(j, k)].x);
-      }
-      const C2<T> ljj = L[tri(j, j)];
-      const T help = ljj.x * ljj.x + ljj.y * ljj.y;
-      const C2<T> lij = L[tri(i, j)];
-      L[tri(i, j)].x = ((lij.x - lr) * ljj.x + (lij.y - li) * ljj.y) / help;
-      L[tri(i, j)].y = ((lij.y - li) * ljj.x - (lij.x - lr) * ljj.y) / help;
-    }
-    T lr = 0;
-#pragma unroll
-    for (int k = 0; k < i; k++) lr += (L[tri(i, k)].x * L[tri(i, k)].x) + (L[tri(i, k)].y * L[tri(i, k)].y);
-    lr = L[tri(i, i)].x - lr;
-    if (lr <= (T)kCholTol) return false;
-    L[tri(i, i)] = mk<T>(sqrt(lr), (T)0);
-  }
-  const T sf = sqrt(factor);
-#pragma unroll
-  for (int t = 0; t < N * (N + 1) / 2; t++) { L[t].x *= sf; L[t].y *= sf; }
-  return true;
 }
 
 template <int NT>

@@ -192,6 +192,53 @@ int cg_invert_bins_fused(cg_workspace ws, float *const *data, float *const *mean
 int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,
                              void *stream);
 
+/* ========================================================================
+ * Posterior simulation (Crava::simulate, src/crava.cpp:1551-1734).
+ * ======================================================================== */
+
+/* Cholesky factor (lib_matrCholCpx semantics, libs/lib/lib_matr.c:78-168) of
+ * every bin's 3x3 posterior covariance post_cov[6] (device spectra, order as
+ * cg_invert_bins_plain's cov) into `chol`: 9 planes of cnxp*nyp*nzp floats
+ * (L00 L11 L22 Re L10 Im L10 Re L20 Im L20 Re L21 Im L21).  A bin whose
+ * factorisation fails gets a zero factor, i.e. zero noise, as in the
+ * reference (src/crava.cpp:1644-1651); nfail_dev (device int, may be NULL)
+ * counts them.  Compute once per posterior, reuse for every realisation. */
+int cg_posterior_cholesky(float *const *post_cov, float *chol, int nxp, int nyp, int nzp, int *nfail_dev,
+                          void *stream);
+
+/* Realisations real0 .. real0+nreal-1 of the posterior: fields[3*r + p] (r <
+ * nreal, p = Vp, Vs, rho) are padded cubes that receive
+ *   C2R(L xi) (PARAMETER scaling) + post_mean[p]
+ * where xi is the injected noise[3] (complex spectra, nreal must be 1), or, if
+ * noise is NULL, complex Gaussian noise drawn in the kernel from a
+ * Philox4x32-10 stream keyed by (seed, realisation) with the Hermitian
+ * structure of FFTGrid::fillInComplexNoise (src/fftgrid.cpp:1191-1241).
+ * post_mean[3] are real posterior-mean cubes (device), or NULL to skip the
+ * add. */
+int cg_simulate_fields(const float *chol, const float *const *noise, float *const *fields, int nreal, int real0,
+                       uint64_t seed, int nxp, int nyp, int nzp, const float *const *post_mean, void *stream);
+
+/* ========================================================================
+ * 4D time-lapse state (State4D, src/state4d.cpp:140-580).  All grids are
+ * device spectra.  6x6 prior layout: ss[6] static-static (0,0)(0,1)(0,2)
+ * (1,1)(1,2)(2,2); sd[9] static-dynamic (0,3)(0,4)(0,5)(1,3)(1,4)(1,5)(2,3)
+ * (2,4)(2,5); dd[6] dynamic-dynamic (3,3)(3,4)(3,5)(4,4)(4,5)(5,5).
+ * Current-state covariance order cov_cur[6]: 00 01 02 11 12 22.
+ * ======================================================================== */
+
+/* State4D::merge / mergeCov (src/state4d.cpp:140-299): mu_cur = mu_s + mu_d,
+ * cov_cur = S_ss + S_dd + S_sd + S_ds folded to 3x3. */
+int cg_state4d_merge(float *const *mu_s, float *const *mu_d, float *const *ss, float *const *sd, float *const *dd,
+                     float *const *mu_cur, float *const *cov_cur, int nxp, int nyp, int nzp, void *stream);
+
+/* State4D::split (src/state4d.cpp:301-580): conditional update of the
+ * 6-parameter state (updated in place) from the current-state posterior
+ * mu_post[3] / cov_post[6].  Bins whose 3x3 prior factorisation fails keep
+ * their prior (counted in nfail_dev, may be NULL). */
+int cg_state4d_split(float *const *mu_s, float *const *mu_d, float *const *ss, float *const *sd, float *const *dd,
+                     float *const *mu_post, float *const *cov_post, int nxp, int nyp, int nzp, int *nfail_dev,
+                     void *stream);
+
 #ifdef __cplusplus
 }
 #endif

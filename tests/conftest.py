@@ -68,8 +68,11 @@ def oracle_pipeline(O, sc, prec="d", nthreads=None):
     import os
     import numpy as np
     nt = nthreads or os.cpu_count()
-    tables = O.k_tables(sc.nxp, sc.wavelets if prec == "f" else sc.wavelets.astype(np.float64), sc.A, sc.nz,
-                        sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut, prec=prec)
+    # the operator tables are FP32 inputs on every path (fillErrMultVectors is float in the reference)
+    tables = O.k_tables(sc.nxp, sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut, prec="f")
+    if prec == "d":
+        tables = {k: (v.astype(np.complex128) if hasattr(v, "dtype") and v.dtype == np.complex64 else v)
+                  for k, v in tables.items()}
     data = [O.fft3d_r2c(d, sc.nxp, O.DATA, prec, nt) for d in sc.data]
     mean = [O.fft3d_r2c(m, sc.nxp, O.PARAMETER, prec, nt) for m in sc.mean]
     covs = []
