@@ -137,6 +137,14 @@ def _declare(L):
         "cg_simulate_fields": ([V, PP, PP, I, I, ct.c_uint64, I, I, I, PP, V], I),
         "cg_state4d_merge": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V], I),
         "cg_state4d_split": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V, V], I),
+        "cg_scale": ([V, ct.c_long, F, V], I),
+        "cg_add": ([V, V, ct.c_long, V], I),
+        "cg_host_register": ([V, ct.c_size_t], I),
+        "cg_host_unregister": ([V], I),
+        "cg_inversion_create": ([ct.POINTER(V), I, I, I, I, I, I, V], I),
+        "cg_inversion_destroy": ([V], None),
+        "cg_inversion_run_host": ([V, PP, PP, PP, PP, V, I], I),
+        "cg_inversion_stats": ([V, ct.POINTER(I), ct.POINTER(I), ct.POINTER(I)], I),
         "cg_trace_enable": ([I], I),
         "cg_trace_collect": ([], I),
         "cg_trace_entry": ([I, ct.c_char_p, I, ct.POINTER(ct.c_long), ct.POINTER(D), ct.POINTER(D)], I),

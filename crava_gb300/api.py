@@ -231,3 +231,58 @@ def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, nxp, stream=None):
     check(lib().cg_state4d_split(*[k[0] for k in keep], nxp, nyp, nzp, _vp(nfail), _stream(stream)),
           "cg_state4d_split")
     return nfail
+
+
+class _InvModel(ct.Structure):
+    _fields_ = [("ntheta", ct.c_int), ("wavelets", ct.c_void_p), ("A", ct.c_void_p), ("err_theta_cov", ct.c_void_p),
+                ("sigma0", ct.c_void_p), ("corr_xy", ct.c_void_p), ("circ_corr_t", ct.c_void_p),
+                ("wnc", ct.c_float), ("low_cut", ct.c_float), ("high_cut", ct.c_float), ("dt_ms", ct.c_float),
+                ("min_rel_thick", ct.c_float), ("cond_threshold", ct.c_double)]
+
+
+class HostInversion:
+    """The C++ host layer's inversion context (cg_inversion_*): host buffers in and out."""
+
+    FORMS = {"plain": 0, "fp32": 1, "mixed": 2}
+
+    def __init__(self, sc, cond_threshold=0.0):
+        self.sc = sc
+        self._arrs = [np.ascontiguousarray(sc.wavelets, dtype=np.float32), np.ascontiguousarray(sc.A, np.float32),
+                      np.ascontiguousarray(sc.err_theta_cov, np.float64),
+                      np.ascontiguousarray(sc.sigma0, np.float64).reshape(9),
+                      np.ascontiguousarray(sc.corr_xy, np.float32), np.ascontiguousarray(sc.circ_corr_t, np.float32)]
+        m = _InvModel(sc.ntheta, *[a.ctypes.data for a in self._arrs], sc.wnc, sc.low_cut, sc.high_cut, sc.dt_ms,
+                      sc.min_rel_thick, cond_threshold)
+        h = ct.c_void_p()
+        check(lib().cg_inversion_create(ct.byref(h), sc.nx, sc.ny, sc.nz, sc.nxp, sc.nyp, sc.nzp, ct.byref(m)),
+              "cg_inversion_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cg_inversion_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, data, mean, cov_out, form="mixed", prior_cov_real=None, err_corr_real=None):
+        """data/mean/cov_out: lists of float32 host arrays (numpy or pinned torch) of rsize floats each."""
+        def ptrs(xs):
+            arr = (ct.c_void_p * len(xs))(*[(x.data_ptr() if isinstance(x, torch.Tensor) else x.ctypes.data)
+                                            for x in xs])
+            return ct.cast(arr, ct.POINTER(ct.c_void_p)), arr
+        pd, k1 = ptrs(data)
+        pm, k2 = ptrs(mean)
+        pc, k3 = ptrs(cov_out)
+        pp, k4 = ptrs(prior_cov_real) if prior_cov_real is not None else (None, None)
+        pe = ct.c_void_p(err_corr_real.ctypes.data) if err_corr_real is not None else None
+        check(lib().cg_inversion_run_host(self.h, pd, pm, pc, pp, pe, self.FORMS[form]), "cg_inversion_run_host")
+
+    def stats(self):
+        a, b, c = ct.c_int(), ct.c_int(), ct.c_int()
+        check(lib().cg_inversion_stats(self.h, ct.byref(a), ct.byref(b), ct.byref(c)), "cg_inversion_stats")
+        return {"flagged": a.value, "failed": b.value, "overflow": c.value}

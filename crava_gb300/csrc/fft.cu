@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "fft.cuh"
+#include "fft_fast.cuh"
 #include "trace.cuh"
 
 namespace cg {
@@ -91,8 +92,8 @@ __host__ __device__ inline size_t c2r_bufb_elems(int m, int cnxp)
 
 template <typename T>
 __global__ void __launch_bounds__(kFFTThreads) k_fft_cols(CubeSet cs, AxisPlan p, const C2<T> *__restrict__ twg,
-                                                          int ncols, int wfull, int ntiles, long axis_stride,
-                                                          long batch_stride, int sign)
+                                                          int col0, int ncols, int wfull, int ntiles,
+                                                          long axis_stride, long batch_stride, int sign)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int n = p.n;
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_fft_cols(CubeSet cs, AxisPlan p
   const int tile = blockIdx.x;
   const int c0 = tile * wfull;
   const int width = (tile == ntiles - 1) ? (ncols - c0) : wfull;
-  C2<T> *base = (C2<T> *)cs.ptr[blockIdx.z] + (long)blockIdx.y * batch_stride + c0;
+  C2<T> *base = (C2<T> *)cs.ptr[blockIdx.z] + (long)blockIdx.y * batch_stride + col0 + c0;
 
   for (int t = threadIdx.x; t < n; t += blockDim.x) tw[t] = twg[t];
   const int tot = n * width;
@@ -263,6 +264,11 @@ int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncub
   const C2<T> *tw = twiddle_table<T>(nxp);
   if (!tw) return cuda_status(cudaGetLastError(), "twiddle table");
   const int nrows = nyp * nzp;
+  if constexpr (sizeof(T) == 4) {
+    const int rc = fast_rows(forward, cs, addend, ncubes, nxp, nrows, (float)scale, (const float2 *)tw, st);
+    if (rc < 0) return rc;
+    if (rc == 1) return CG_OK;
+  }
   const size_t bufb = forward ? (size_t)m * (kRows + 1) : c2r_bufb_elems(m, nxp / 2 + 1);
   size_t smem = ((size_t)m * (kRows + 1) + bufb + (size_t)nxp) * sizeof(C2<T>);
   if (smem > kMaxSmem) {
@@ -296,6 +302,16 @@ int launch_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_strid
   }
   const C2<T> *tw = twiddle_table<T>(n);
   if (!tw) return cuda_status(cudaGetLastError(), "twiddle table");
+  int col0 = 0;
+  if constexpr (sizeof(T) == 4) {
+    int done = 0;
+    const int rc = fast_cols(cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, (const float2 *)tw, st,
+                             &done);
+    if (rc < 0) return rc;
+    col0 = done;
+    ncols -= done;
+    if (ncols == 0) return CG_OK;
+  }
   // tile width: 16 columns (128 B rows for float) when shared memory allows
   const size_t budget = 200 * 1024;
   int wfull = 16 / (int)(sizeof(T) / sizeof(float));
@@ -318,7 +334,8 @@ int launch_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_strid
   CG_CUDA(cudaFuncSetAttribute(k_fft_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid(ntiles, nbatch, ncubes);
   TraceScope ts("k_fft_cols", st, 2.0 * ncubes * nbatch * (double)ncols * n * sizeof(C2<T>));
-  k_fft_cols<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, ncols, wfull, ntiles, axis_stride, batch_stride, sign);
+  k_fft_cols<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, col0, ncols, wfull, ntiles, axis_stride, batch_stride,
+                                                 sign);
   CG_CHECK_LAUNCH("k_fft_cols");
   return CG_OK;
 }

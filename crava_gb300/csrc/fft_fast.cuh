@@ -1,0 +1,249 @@
+// Compile-time specialised FFT passes for the common padded lengths.
+//
+// Same transforms as the generic kernels in fft.cu, but with the length N
+// and tile width W known at compile time:
+//   * the Stockham plan (radices 8, 4, 2, 3, 5, 7 in that order, exactly as
+//     make_axis_plan) and every index of every stage fold to constants;
+//   * one shared buffer: each stage reads all of a thread's butterflies into
+//     registers, synchronises, then writes them back in place (Stockham
+//     stages are permutations, so this is race free), halving shared memory
+//     and raising resident CTAs per SM;
+//   * the tile is staged with cp.async, so every load of the tile is in
+//     flight at once instead of one dependent load per thread.
+#pragma once
+
+#include "fft.cuh"
+
+namespace cg {
+
+__host__ __device__ constexpr int radix_order(int q) { return q == 0 ? 8 : q == 1 ? 4 : q == 2 ? 2 : q == 3 ? 3 : q == 4 ? 5 : 7; }
+
+__host__ __device__ constexpr int plan_nstages(int n)
+{
+  int m = n, s = 0;
+  for (int q = 0; q < 6; q++)
+    while (m % radix_order(q) == 0) { m /= radix_order(q); s++; }
+  return m == 1 ? s : -1;
+}
+
+__host__ __device__ constexpr int plan_radix(int n, int stage)
+{
+  int m = n, s = 0;
+  for (int q = 0; q < 6; q++)
+    while (m % radix_order(q) == 0) {
+      if (s == stage) return radix_order(q);
+      m /= radix_order(q);
+      s++;
+    }
+  return 1;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+// 8-byte global -> shared asynchronous copy (LDGSTS through L1)
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gsrc)
+{
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem_dst)), "l"(gsrc) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+  asm volatile("cp.async.commit_group;\ncp.async.wait_group 0;\n" ::: "memory");
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void dft_any(C2<T> *v, int sign, const C2<T> *tw, int rstride)
+{
+  if constexpr (R == 2) dft2<T>(v);
+  else if constexpr (R == 4) dft4<T>(v, sign);
+  else if constexpr (R == 8) dft8<T>(v, sign);
+  else dft_odd<T, R>(v, sign, tw, rstride);
+}
+
+// All Stockham stages of a length-N transform on W columns held in place at
+// buf[e*LDW + c]; the twiddle table has N*TWS entries.
+template <typename T, int N, int W, int LDW, int TWS, int S = 0, int NS = 1>
+__device__ __forceinline__ void cstages(C2<T> *buf, const C2<T> *tw, int sign)
+{
+  if constexpr (S < plan_nstages(N)) {
+    constexpr int R = plan_radix(N, S);
+    constexpr int NB = N / R;
+    constexpr int SPAN = N / (NS * R);
+    constexpr int TOT = NB * W;
+    constexpr int BPT = (TOT + kFFTThreads - 1) / kFFTThreads;
+    C2<T> v[BPT][R];
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[q][r] = buf[(j + r * NB) * LDW + c];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+        const int jm = j % NS;
+        if (NS > 1) {
+#pragma unroll
+          for (int r = 1; r < R; r++) v[q][r] = cmul<T>(v[q][r], tw_at<T>(tw, jm * r * SPAN * TWS, sign));
+        }
+        dft_any<T, R>(v[q], sign, tw, NB * TWS);
+        const int d = (j - jm) * R + jm;
+#pragma unroll
+        for (int r = 0; r < R; r++) buf[(d + r * NS) * LDW + c] = v[q][r];
+      }
+    }
+    __syncthreads();
+    cstages<T, N, W, LDW, TWS, S + 1, NS * R>(buf, tw, sign);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// strided column pass: full tiles of W columns
+// ---------------------------------------------------------------------------
+template <int N, int W, int MINB>
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs, const float2 *__restrict__ twg, int col0,
+                                                               long axis_stride, long batch_stride, int sign)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + N * W;
+  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)blockIdx.y * batch_stride + col0 + (long)blockIdx.x * W;
+  for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
+#pragma unroll
+  for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
+    const int t = t0 + threadIdx.x;
+    if ((N * W) % kFFTThreads == 0 || t < N * W) {
+      const int e = t / W, c = t % W;
+      cp_async8(&buf[e * W + c], &base[(long)e * axis_stride + c]);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  cstages<float, N, W, W, 1>(buf, tw, sign);
+#pragma unroll
+  for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
+    const int t = t0 + threadIdx.x;
+    if ((N * W) % kFFTThreads == 0 || t < N * W) {
+      const int e = t / W, c = t % W;
+      base[(long)e * axis_stride + c] = buf[e * W + c];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x rows, real -> half spectrum (even nxp = 2M), prescale applied to X
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_fast(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+                                                               float prescale)
+{
+  constexpr int LDW = kRows + 1;
+  constexpr int NX = 2 * M, CN = M + 1, RN = 2 * CN;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + M * LDW;
+  const int r0 = blockIdx.x * kRows;
+  const int nr = min(kRows, nrows - r0);
+  float *base = (float *)cs.ptr[blockIdx.z] + (long)r0 * RN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+#pragma unroll
+  for (int t0 = 0; t0 < kRows * M; t0 += kFFTThreads) {
+    const int t = t0 + threadIdx.x;
+    if ((kRows * M) % kFFTThreads == 0 || t < kRows * M) {
+      const int row = t / M, e = t % M;
+      if (row < nr) cp_async8(&buf[e * LDW + row], base + (long)row * RN + 2 * e);
+      else buf[e * LDW + row] = make_float2(0.f, 0.f);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  cstages<float, M, kRows, LDW, 2>(buf, tw, -1);
+  for (int t = threadIdx.x; t < nr * CN; t += kFFTThreads) {
+    const int row = t / CN, k = t - row * CN;
+    const float2 A = buf[(k == M ? 0 : k) * LDW + row];
+    const float2 Bc = buf[(k == 0 ? 0 : M - k) * LDW + row];
+    const float2 B = make_float2(Bc.x, -Bc.y);
+    const float2 E = make_float2((A.x + B.x) * 0.5f, (A.y + B.y) * 0.5f);
+    const float2 O = make_float2((A.y - B.y) * 0.5f, -(A.x - B.x) * 0.5f);
+    float2 X = cadd<float>(E, cmul<float>(tw[k], O));
+    X.x *= prescale;
+    X.y *= prescale;
+    ((float2 *)(base + (long)row * RN))[k] = X;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x rows, half spectrum -> real (even nxp = 2M), postscale and optional add
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeSet addend,
+                                                               const float2 *__restrict__ twg, int nrows,
+                                                               float postscale)
+{
+  constexpr int LDW = kRows + 1;
+  constexpr int NX = 2 * M, CN = M + 1, RN = 2 * CN;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *S = buf + M * LDW;      // kRows x CN staged spectra
+  float2 *tw = S + kRows * CN;
+  const int r0 = blockIdx.x * kRows;
+  const int nr = min(kRows, nrows - r0);
+  float *base = (float *)cs.ptr[blockIdx.z] + (long)r0 * RN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  for (int t = threadIdx.x; t < nr * CN; t += kFFTThreads) {
+    const int row = t / CN, k = t - row * CN;
+    cp_async8(&S[row * CN + k], base + (long)row * RN + 2 * k);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+#pragma unroll
+  for (int t0 = 0; t0 < kRows * M; t0 += kFFTThreads) {
+    const int t = t0 + threadIdx.x;
+    if ((kRows * M) % kFFTThreads == 0 || t < kRows * M) {
+      const int row = t / M, k = t % M;
+      float2 Z = make_float2(0.f, 0.f);
+      if (row < nr) {
+        float2 Xk = S[row * CN + k];
+        float2 Xm = S[row * CN + (M - k)];
+        if (k == 0) { Xk.y = 0.f; Xm.y = 0.f; }  // rfftw_c2hc keeps only Re of DC and Nyquist
+        Xm.y = -Xm.y;
+        const float2 E = cadd<float>(Xk, Xm);
+        const float2 O = cmulc<float>(csub<float>(Xk, Xm), tw[k]);
+        Z = make_float2(E.x - O.y, E.y + O.x);
+      }
+      buf[k * LDW + row] = Z;
+    }
+  }
+  __syncthreads();
+  cstages<float, M, kRows, LDW, 2>(buf, tw, +1);
+  const float *add = addend.ptr[blockIdx.z] ? (const float *)addend.ptr[blockIdx.z] + (long)r0 * RN : nullptr;
+  for (int t = threadIdx.x; t < nr * CN; t += kFFTThreads) {
+    const int row = t / CN, e = t - row * CN;
+    float2 z = (e < M) ? buf[e * LDW + row] : make_float2(0.f, 0.f);
+    z.x *= postscale;
+    z.y *= postscale;
+    if (add) {
+      const float2 a = ((const float2 *)(add + (long)row * RN))[e];
+      z.x += a.x;
+      z.y += a.y;
+    }
+    ((float2 *)(base + (long)row * RN))[e] = z;
+  }
+}
+
+// host-side dispatch (fft_fast_*.cu): return 1 if a specialisation ran the pass
+int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
+              int sign, const float2 *tw, cudaStream_t st, int *done_cols);
+int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
+              const float2 *tw, cudaStream_t st);
+
+}  // namespace cg

@@ -1,0 +1,70 @@
+// Specialised strided-column FFT passes (see fft_fast.cuh).
+#include <cstdlib>
+
+#include "fft_fast.cuh"
+#include "trace.cuh"
+
+namespace cg {
+
+namespace {
+constexpr int kW = 16;
+
+// Resident-CTA target per length: 3 keeps lengths up to 160 spill free at the
+// 85-register cap; longer lengths default to 2.  CRAVA_COLS_MINB=2|3 forces
+// one variant (used by the tuning sweep in crava_gb300.microbench).
+int minb_for(int n)
+{
+  static int forced = -1;
+  if (forced < 0) {
+    const char *e = getenv("CRAVA_COLS_MINB");
+    forced = (e && (e[0] == '2' || e[0] == '3')) ? e[0] - '0' : 0;
+  }
+  if (forced) return forced;
+  return n <= 160 ? 3 : 2;
+}
+
+template <int N, int MINB>
+int launch_v(const CubeSet &cs, int ncubes, int nfull, long axis_stride, long batch_stride, int nbatch, int sign,
+             const float2 *tw, cudaStream_t st)
+{
+  const size_t smem = ((size_t)N * kW + N) * sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(k_fft_cols_fast<N, kW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem);
+  if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_fast attribute");
+  dim3 grid(nfull, nbatch, ncubes);
+  TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)nfull * kW * N * sizeof(float2));
+  k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, 0, axis_stride, batch_stride, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_fast");
+  return 1;
+}
+
+template <int N>
+int launch(const CubeSet &cs, int ncubes, int nfull, long axis_stride, long batch_stride, int nbatch, int sign,
+           const float2 *tw, cudaStream_t st)
+{
+  if (minb_for(N) == 3) return launch_v<N, 3>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st);
+  return launch_v<N, 2>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st);
+}
+}  // namespace
+
+// Runs the full W-column tiles of a column pass when the length has a
+// specialisation; *done_cols receives how many leading columns were handled.
+int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
+              int sign, const float2 *tw, cudaStream_t st, int *done_cols)
+{
+  *done_cols = 0;
+  const int nfull = ncols / kW;
+  if (nfull == 0) return 0;
+  int rc = 0;
+  switch (n) {
+#define CG_COLS(NN) case NN: rc = launch<NN>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st); break;
+    CG_COLS(64) CG_COLS(80) CG_COLS(96) CG_COLS(100) CG_COLS(120) CG_COLS(128) CG_COLS(160) CG_COLS(192)
+    CG_COLS(200) CG_COLS(240) CG_COLS(256) CG_COLS(320) CG_COLS(384) CG_COLS(400) CG_COLS(480) CG_COLS(512)
+#undef CG_COLS
+    default: return 0;
+  }
+  if (rc == 1) *done_cols = nfull * kW;
+  return rc;
+}
+
+}  // namespace cg

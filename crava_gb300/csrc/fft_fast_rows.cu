@@ -1,0 +1,48 @@
+// Specialised x-row R2C / C2R passes (see fft_fast.cuh).
+#include "fft_fast.cuh"
+#include "trace.cuh"
+
+namespace cg {
+
+namespace {
+template <int M>
+int launch(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nrows, float scale,
+           const float2 *tw, cudaStream_t st)
+{
+  constexpr int LDW = kRows + 1;
+  const size_t smem = forward ? ((size_t)M * LDW + 2 * M) * sizeof(float2)
+                              : ((size_t)M * LDW + (size_t)kRows * (M + 1) + 2 * M) * sizeof(float2);
+  dim3 grid(ceil_div(nrows, kRows), 1, ncubes);
+  const double bytes = (double)ncubes * nrows * (2.0 * M * sizeof(float) + (M + 1.0) * sizeof(float2));
+  cudaError_t e;
+  if (forward) {
+    e = cudaFuncSetAttribute(k_r2c_rows_fast<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "k_r2c_rows_fast attribute");
+    TraceScope ts("k_r2c_rows_fast", st, bytes);
+    k_r2c_rows_fast<M><<<grid, kFFTThreads, smem, st>>>(cs, tw, nrows, scale);
+  } else {
+    e = cudaFuncSetAttribute(k_c2r_rows_fast<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_fast attribute");
+    TraceScope ts("k_c2r_rows_fast", st, bytes);
+    k_c2r_rows_fast<M><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale);
+  }
+  CG_CHECK_LAUNCH(forward ? "k_r2c_rows_fast" : "k_c2r_rows_fast");
+  return 1;
+}
+}  // namespace
+
+// Runs the x-row pass when nxp is even and nxp/2 has a specialisation.
+int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
+              const float2 *tw, cudaStream_t st)
+{
+  if (nxp % 2) return 0;
+  switch (nxp / 2) {
+#define CG_ROWS(MM) case MM: return launch<MM>(forward, cs, addend, ncubes, nrows, scale, tw, st);
+    CG_ROWS(32) CG_ROWS(40) CG_ROWS(48) CG_ROWS(50) CG_ROWS(60) CG_ROWS(64) CG_ROWS(80) CG_ROWS(96)
+    CG_ROWS(100) CG_ROWS(120) CG_ROWS(128) CG_ROWS(160) CG_ROWS(192) CG_ROWS(200) CG_ROWS(240) CG_ROWS(256)
+#undef CG_ROWS
+    default: return 0;
+  }
+}
+
+}  // namespace cg

@@ -97,3 +97,50 @@ extern "C" int cg_fill_err_corr(float *buf, int nxp, int nyp, int nzp, const flo
   CG_CHECK_LAUNCH("k_fill_err_corr");
   return CG_OK;
 }
+
+// FFTGrid::multiplyByScalar / add (src/fftgrid.cpp:1985-1996, :1870-1891)
+// over the whole padded buffer, vectorised by float4 where aligned.
+__global__ void k_scale(float *buf, long n, float s)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long n4 = n / 4;
+  if (i < n4) {
+    float4 v = reinterpret_cast<float4 *>(buf)[i];
+    v.x *= s; v.y *= s; v.z *= s; v.w *= s;
+    reinterpret_cast<float4 *>(buf)[i] = v;
+  }
+  if (i < n - 4 * n4) buf[4 * n4 + i] *= s;
+}
+
+__global__ void k_add(float *y, const float *x, long n)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long n4 = n / 4;
+  if (i < n4) {
+    float4 a = reinterpret_cast<float4 *>(y)[i];
+    const float4 b = reinterpret_cast<const float4 *>(x)[i];
+    a.x += b.x; a.y += b.y; a.z += b.z; a.w += b.w;
+    reinterpret_cast<float4 *>(y)[i] = a;
+  }
+  if (i < n - 4 * n4) y[4 * n4 + i] += x[4 * n4 + i];
+}
+
+extern "C" int cg_scale(float *buf, long n, float s, void *stream)
+{
+  if (!buf || n < 0 || ((uintptr_t)buf & 15)) { cg::set_error("cg_scale: bad argument (buffer must be 16-byte aligned)"); return CG_ERR_ARG; }
+  if (n == 0) return CG_OK;
+  cg::TraceScope ts("k_scale", (cudaStream_t)stream, 8.0 * n);
+  k_scale<<<cg::ceil_div(n / 4 + 4, 256), 256, 0, (cudaStream_t)stream>>>(buf, n, s);
+  CG_CHECK_LAUNCH("k_scale");
+  return CG_OK;
+}
+
+extern "C" int cg_add(float *y, const float *x, long n, void *stream)
+{
+  if (!y || !x || n < 0 || ((uintptr_t)y & 15) || ((uintptr_t)x & 15)) { cg::set_error("cg_add: bad argument (buffers must be 16-byte aligned)"); return CG_ERR_ARG; }
+  if (n == 0) return CG_OK;
+  cg::TraceScope ts("k_add", (cudaStream_t)stream, 12.0 * n);
+  k_add<<<cg::ceil_div(n / 4 + 4, 256), 256, 0, (cudaStream_t)stream>>>(y, x, n);
+  CG_CHECK_LAUNCH("k_add");
+  return CG_OK;
+}

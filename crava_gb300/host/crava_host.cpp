@@ -1,0 +1,385 @@
+// C++ host layer: FFTGrid / Crava mirror over the C-ABI, plus the
+// host-buffer inversion entry point (cg_inversion_*) that a drop-in
+// replacement of Crava::computePostMeanResidAndFFTCov calls.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "cravagpu.h"
+#include "cravagpu_host.hpp"
+
+namespace cg {
+void set_error(const char *fmt, ...);
+}
+
+namespace cravagpu {
+
+void check(int status, const char *what)
+{
+  if (status != CG_OK) throw Error(status, std::string(what) + ": " + cg_last_error());
+}
+
+static void cuda_check(cudaError_t e, const char *what)
+{
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    throw Error(CG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FFTGrid
+// ---------------------------------------------------------------------------
+FFTGrid::FFTGrid(int nx, int ny, int nz, int nxp, int nyp, int nzp)
+    : nx_(nx), ny_(ny), nz_(nz), nxp_(nxp), nyp_(nyp), nzp_(nzp)
+{
+  if (nxp < 1 || nyp < 1 || nzp < 1) throw Error(CG_ERR_ARG, "FFTGrid: bad padded size");
+  cuda_check(cudaMalloc((void **)&d_, sizeof(float) * (size_t)getrsize()), "FFTGrid allocation");
+  cuda_check(cudaMemset(d_, 0, sizeof(float) * (size_t)getrsize()), "FFTGrid clear");
+}
+
+FFTGrid::~FFTGrid()
+{
+  if (d_) cudaFree(d_);
+}
+
+void FFTGrid::fftInPlace(void *stream)
+{
+  if (istransformed_) throw Error(CG_ERR_STATE, "fftInPlace on a transformed grid");
+  if (cubetype_ == CTMISSING) throw Error(CG_ERR_STATE, "fftInPlace on a grid without a cube type");
+  check(cg_fft3d_r2c(d_, nxp_, nyp_, nzp_, cubetype_, stream), "fftInPlace");
+  istransformed_ = true;
+}
+
+void FFTGrid::invFFTInPlace(void *stream)
+{
+  if (!istransformed_) throw Error(CG_ERR_STATE, "invFFTInPlace on a real grid");
+  if (cubetype_ == CTMISSING) throw Error(CG_ERR_STATE, "invFFTInPlace on a grid without a cube type");
+  check(cg_fft3d_c2r(d_, nxp_, nyp_, nzp_, cubetype_, stream), "invFFTInPlace");
+  istransformed_ = false;
+}
+
+void FFTGrid::fillInFromArray(const float *host)
+{
+  cuda_check(cudaMemcpy(d_, host, sizeof(float) * (size_t)getrsize(), cudaMemcpyHostToDevice), "fillInFromArray");
+}
+
+void FFTGrid::copyToArray(float *host) const
+{
+  cuda_check(cudaMemcpy(host, d_, sizeof(float) * (size_t)getrsize(), cudaMemcpyDeviceToHost), "copyToArray");
+}
+
+// FFTGrid::getComplexValue / setComplexValue (src/fftgrid.cpp:1526-1556,
+// :1667-1684): outside the (extended) simbox the getter returns RMISSING and
+// the setter returns 1.
+static const float kRMissing = -99999.0f;
+
+Complex FFTGrid::getComplexValue(int i, int j, int k, bool ext) const
+{
+  if (!istransformed_) throw Error(CG_ERR_STATE, "getComplexValue on a real grid");
+  const bool in = ext ? (i < getCNxp() && j < nyp_ && k < nzp_) : (i < nx_ && j < ny_ && k < nz_);
+  if (!in || i < 0 || j < 0 || k < 0) return Complex{kRMissing, kRMissing};
+  Complex v;
+  const long idx = i + (long)j * getCNxp() + (long)k * getCNxp() * nyp_;
+  cuda_check(cudaMemcpy(&v, d_ + 2 * idx, sizeof(v), cudaMemcpyDeviceToHost), "getComplexValue");
+  return v;
+}
+
+int FFTGrid::setComplexValue(int i, int j, int k, Complex value, bool ext)
+{
+  if (!istransformed_) throw Error(CG_ERR_STATE, "setComplexValue on a real grid");
+  const bool in = ext ? (i < getCNxp() && j < nyp_ && k < nzp_) : (i < nx_ && j < ny_ && k < nz_);
+  if (!in || i < 0 || j < 0 || k < 0) return 1;
+  const long idx = i + (long)j * getCNxp() + (long)k * getCNxp() * nyp_;
+  cuda_check(cudaMemcpy(d_ + 2 * idx, &value, sizeof(value), cudaMemcpyHostToDevice), "setComplexValue");
+  return 0;
+}
+
+float FFTGrid::getRealValue(int i, int j, int k, bool ext) const
+{
+  if (istransformed_) throw Error(CG_ERR_STATE, "getRealValue on a transformed grid");
+  const bool in = ext ? (i < nxp_ && j < nyp_ && k < nzp_) : (i < nx_ && j < ny_ && k < nz_);
+  if (!in || i < 0 || j < 0 || k < 0) return kRMissing;
+  float v;
+  const long idx = i + (long)j * getRNxp() + (long)k * getRNxp() * nyp_;
+  cuda_check(cudaMemcpy(&v, d_ + idx, sizeof(v), cudaMemcpyDeviceToHost), "getRealValue");
+  return v;
+}
+
+int FFTGrid::setRealValue(int i, int j, int k, float value, bool ext)
+{
+  if (istransformed_) throw Error(CG_ERR_STATE, "setRealValue on a transformed grid");
+  const bool in = ext ? (i < nxp_ && j < nyp_ && k < nzp_) : (i < nx_ && j < ny_ && k < nz_);
+  if (!in || i < 0 || j < 0 || k < 0) return 1;
+  const long idx = i + (long)j * getRNxp() + (long)k * getRNxp() * nyp_;
+  cuda_check(cudaMemcpy(d_ + idx, &value, sizeof(value), cudaMemcpyHostToDevice), "setRealValue");
+  return 0;
+}
+
+void FFTGrid::multiplyByScalar(float s, void *stream)
+{
+  check(cg_scale(d_, getrsize(), s, stream), "multiplyByScalar");
+}
+
+void FFTGrid::add(const FFTGrid *o, void *stream)
+{
+  if (!o || o->nxp_ != nxp_ || o->nyp_ != nyp_ || o->nzp_ != nzp_) throw Error(CG_ERR_ARG, "add: size mismatch");
+  check(cg_add(d_, o->d_, getrsize(), stream), "add");
+}
+
+void FFTGrid::fillInParamCorr(const float *corr_xy, const float *circ_t, float gradI, float gradJ, void *stream)
+{
+  if (istransformed_) throw Error(CG_ERR_STATE, "fillInParamCorr on a transformed grid");
+  check(cg_fill_param_corr(d_, nxp_, nyp_, nzp_, corr_xy, circ_t, gradI, gradJ, 1.0f, stream), "fillInParamCorr");
+}
+
+void FFTGrid::fillInErrCorr(const float *corr_xy, float gradI, float gradJ, void *stream)
+{
+  if (istransformed_) throw Error(CG_ERR_STATE, "fillInErrCorr on a transformed grid");
+  check(cg_fill_err_corr(d_, nxp_, nyp_, nzp_, corr_xy, gradI, gradJ, stream), "fillInErrCorr");
+}
+
+// ---------------------------------------------------------------------------
+// Crava
+// ---------------------------------------------------------------------------
+Crava::Crava(int nx, int ny, int nz, int nxp, int nyp, int nzp, const InversionModel &model)
+    : nx_(nx), ny_(ny), nz_(nz), nxp_(nxp), nyp_(nyp), nzp_(nzp), m_(model)
+{
+  const int n = m_.ntheta;
+  if (n < 1 || (int)m_.wavelets.size() != n * nzp || (int)m_.A.size() != 3 * n ||
+      (int)m_.errThetaCov.size() != n * n || m_.sigma0.size() != 9 || (long)m_.corrXY.size() != (long)nxp * nyp ||
+      (int)m_.circCorrT.size() != nzp)
+    throw Error(CG_ERR_ARG, "Crava: model arrays do not match the grid sizes");
+  std::vector<float> K((size_t)nzp * n * 6), e1((size_t)nzp * n * 2), e2((size_t)nzp * n * 2), e3((size_t)nzp * n * 2);
+  band_.assign(nzp, 0);
+  check(cg_operator_tables(n, nz, nzp, m_.wavelets.data(), m_.A.data(), m_.dt_ms, m_.minRelThick, m_.lowCut,
+                           m_.highCut, K.data(), e1.data(), e2.data(), e3.data(), band_.data()),
+        "operator tables");
+  check(cg_workspace_create(&ws_, nxp, nyp, nzp, n), "workspace");
+  cg_model cm;
+  memset(&cm, 0, sizeof(cm));
+  cm.ntheta = n;
+  cm.wnc = m_.wnc;
+  cm.is4d = 0;
+  cm.K = K.data();
+  cm.em1 = e1.data();
+  cm.em2 = e2.data();
+  cm.em3 = e3.data();
+  cm.band = band_.data();
+  cm.err_theta_cov = m_.errThetaCov.data();
+  cm.sigma0 = m_.sigma0.data();
+  cm.cond_threshold = m_.condThreshold;
+  check(cg_workspace_set_model(ws_, &cm), "set model");
+  cuda_check(cudaMalloc((void **)&d_corr_xy_, sizeof(float) * m_.corrXY.size()), "corrXY");
+  cuda_check(cudaMalloc((void **)&d_circ_t_, sizeof(float) * m_.circCorrT.size()), "circCorrT");
+  cuda_check(cudaMemcpy(d_corr_xy_, m_.corrXY.data(), sizeof(float) * m_.corrXY.size(), cudaMemcpyHostToDevice),
+             "corrXY upload");
+  cuda_check(cudaMemcpy(d_circ_t_, m_.circCorrT.data(), sizeof(float) * m_.circCorrT.size(), cudaMemcpyHostToDevice),
+             "circCorrT upload");
+}
+
+Crava::~Crava()
+{
+  if (ws_) cg_workspace_destroy(ws_);
+  if (d_corr_xy_) cudaFree(d_corr_xy_);
+  if (d_circ_t_) cudaFree(d_circ_t_);
+  if (d_chol_) cudaFree(d_chol_);
+}
+
+int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha, FFTGrid *&postBeta,
+                                         FFTGrid *&postRho, FFTGrid **postCov, FFTGrid *errCorr, Form form,
+                                         void *stream)
+{
+  const int n = m_.ntheta;
+  FFTGrid *mean[3] = {postAlpha, postBeta, postRho};
+  std::vector<float *> fwd;
+  for (int l = 0; l < n; l++) {
+    if (seisData[l]->getIsTransformed()) throw Error(CG_ERR_STATE, "seismic data already transformed");
+    fwd.push_back(seisData[l]->devicePtr());
+  }
+  for (int p = 0; p < 3; p++) {
+    if (mean[p]->getIsTransformed()) throw Error(CG_ERR_STATE, "prior mean already transformed");
+    fwd.push_back(mean[p]->devicePtr());
+  }
+  // DATA and PARAMETER share the 1/sqrt(N) scaling: one batched transform
+  check(cg_fft3d_r2c_batch(fwd.data(), (int)fwd.size(), nxp_, nyp_, nzp_, CG_DATA, stream), "forward transforms");
+  float *d[8], *mu[3], *cv[6];
+  for (int l = 0; l < n; l++) { d[l] = seisData[l]->devicePtr(); seisData[l]->setTransformedStatus(true); }
+  for (int p = 0; p < 3; p++) { mu[p] = mean[p]->devicePtr(); mean[p]->setTransformedStatus(true); }
+  for (int t = 0; t < 6; t++) cv[t] = postCov[t]->devicePtr();
+  if (form == PLAIN) {
+    if (!errCorr) throw Error(CG_ERR_ARG, "the plain form needs the error-correlation cube");
+    std::vector<float *> covs(cv, cv + 6);
+    covs.push_back(errCorr->devicePtr());
+    check(cg_fft3d_r2c_batch(covs.data(), 7, nxp_, nyp_, nzp_, CG_COVARIANCE, stream), "FFTCovGrids");
+    errCorr->setTransformedStatus(true);
+    check(cg_invert_bins_plain(ws_, d, mu, cv, errCorr->devicePtr(), stream), "bin loop (plain)");
+  } else {
+    if (m_.corrGradI != 0.0f || m_.corrGradJ != 0.0f)
+      throw Error(CG_ERR_UNSUPPORTED, "the fused form needs zero correlation gradients; use the plain form");
+    check(cg_prior_spectra(ws_, d_corr_xy_, d_circ_t_, CG_PREC_FP32, stream), "prior spectra");
+    check(cg_invert_bins_fused(ws_, d, mu, cv, form == FUSED_MIXED ? CG_PREC_MIXED : CG_PREC_FP32, stream),
+          "bin loop (fused)");
+  }
+  for (int t = 0; t < 6; t++) { postCov[t]->setType(FFTGrid::COVARIANCE); postCov[t]->setTransformedStatus(true); }
+  check(cg_fft3d_c2r_batch(mu, 3, nxp_, nyp_, nzp_, CG_PARAMETER, stream), "posterior-mean inverse transforms");
+  for (int p = 0; p < 3; p++) mean[p]->setTransformedStatus(false);
+  return 0;
+}
+
+int Crava::simulate(FFTGrid **postCov, FFTGrid *const *postMean, int nSim, unsigned long long seed, FFTGrid **fields,
+                    void *stream)
+{
+  if (nSim < 1) return 0;
+  if (!d_chol_)
+    cuda_check(cudaMalloc((void **)&d_chol_, sizeof(float) * 9 * (size_t)postCov[0]->getcsize()), "factor planes");
+  float *cv[6];
+  for (int t = 0; t < 6; t++) cv[t] = postCov[t]->devicePtr();
+  check(cg_posterior_cholesky(cv, d_chol_, nxp_, nyp_, nzp_, nullptr, stream), "posterior factor");
+  const float *mean[3] = {postMean[0]->devicePtr(), postMean[1]->devicePtr(), postMean[2]->devicePtr()};
+  std::vector<float *> f(3 * (size_t)nSim);
+  for (int t = 0; t < 3 * nSim; t++) { f[t] = fields[t]->devicePtr(); fields[t]->setType(FFTGrid::PARAMETER); }
+  check(cg_simulate_fields(d_chol_, nullptr, f.data(), nSim, 0, seed, nxp_, nyp_, nzp_, mean, stream), "simulate");
+  for (int t = 0; t < 3 * nSim; t++) fields[t]->setTransformedStatus(false);
+  return 0;
+}
+
+}  // namespace cravagpu
+
+// ---------------------------------------------------------------------------
+// host-buffer inversion context (C-ABI)
+// ---------------------------------------------------------------------------
+using namespace cravagpu;
+
+struct cg_inversion_s {
+  int nx, ny, nz, nxp, nyp, nzp, ntheta;
+  Crava *crava = nullptr;
+  std::vector<FFTGrid *> data, mean, cov;
+  FFTGrid *errcorr = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+#define CG_TRY(...)                                    \
+  try {                                                \
+    __VA_ARGS__                                        \
+  } catch (const Error &e) {                           \
+    cg::set_error("%s", e.what());                     \
+    return e.status;                                   \
+  } catch (const std::exception &e) {                  \
+    cg::set_error("%s", e.what());                     \
+    return CG_ERR_STATE;                               \
+  }
+
+extern "C" int cg_inversion_create(cg_inversion *out, int nx, int ny, int nz, int nxp, int nyp, int nzp,
+                                   const cg_inversion_model *m)
+{
+  if (!out || !m) { cg::set_error("null argument"); return CG_ERR_ARG; }
+  *out = nullptr;
+  CG_TRY({
+    InversionModel im;
+    im.ntheta = m->ntheta;
+    if (m->ntheta < 1 || m->ntheta > 8) throw Error(CG_ERR_ARG, "ntheta outside 1..8");
+    if (!m->wavelets || !m->A || !m->err_theta_cov || !m->sigma0 || !m->corr_xy || !m->circ_corr_t)
+      throw Error(CG_ERR_ARG, "null model array");
+    im.wavelets.assign(m->wavelets, m->wavelets + (size_t)m->ntheta * nzp);
+    im.A.assign(m->A, m->A + 3 * m->ntheta);
+    im.errThetaCov.assign(m->err_theta_cov, m->err_theta_cov + m->ntheta * m->ntheta);
+    im.sigma0.assign(m->sigma0, m->sigma0 + 9);
+    im.corrXY.assign(m->corr_xy, m->corr_xy + (size_t)nxp * nyp);
+    im.circCorrT.assign(m->circ_corr_t, m->circ_corr_t + nzp);
+    im.wnc = m->wnc;
+    im.lowCut = m->low_cut;
+    im.highCut = m->high_cut;
+    im.dt_ms = m->dt_ms;
+    im.minRelThick = m->min_rel_thick > 0 ? m->min_rel_thick : 1.0f;
+    im.condThreshold = m->cond_threshold;
+    cg_inversion_s *h = new cg_inversion_s();
+    h->nx = nx; h->ny = ny; h->nz = nz; h->nxp = nxp; h->nyp = nyp; h->nzp = nzp; h->ntheta = m->ntheta;
+    try {
+      h->crava = new Crava(nx, ny, nz, nxp, nyp, nzp, im);
+      for (int l = 0; l < m->ntheta; l++) { h->data.push_back(new FFTGrid(nx, ny, nz, nxp, nyp, nzp)); h->data.back()->setType(FFTGrid::DATA); }
+      for (int p = 0; p < 3; p++) { h->mean.push_back(new FFTGrid(nx, ny, nz, nxp, nyp, nzp)); h->mean.back()->setType(FFTGrid::PARAMETER); }
+      for (int t = 0; t < 6; t++) { h->cov.push_back(new FFTGrid(nx, ny, nz, nxp, nyp, nzp)); h->cov.back()->setType(FFTGrid::COVARIANCE); }
+      cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+    } catch (...) {
+      cg_inversion_destroy(h);
+      throw;
+    }
+    *out = h;
+    return CG_OK;
+  })
+}
+
+extern "C" void cg_inversion_destroy(cg_inversion h)
+{
+  if (!h) return;
+  for (auto *g : h->data) delete g;
+  for (auto *g : h->mean) delete g;
+  for (auto *g : h->cov) delete g;
+  delete h->errcorr;
+  delete h->crava;
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+extern "C" int cg_inversion_run_host(cg_inversion h, float *const *seis_data, float *const *mean, float *const *post_cov,
+                                     const float *const *prior_cov_real, const float *err_corr_real, int form)
+{
+  if (!h || !seis_data || !mean || !post_cov) { cg::set_error("null argument"); return CG_ERR_ARG; }
+  CG_TRY({
+    const size_t bytes = sizeof(float) * (size_t)h->data[0]->getrsize();
+    cudaStream_t st = h->stream;
+    for (int l = 0; l < h->ntheta; l++) {
+      cuda_check(cudaMemcpyAsync(h->data[l]->devicePtr(), seis_data[l], bytes, cudaMemcpyHostToDevice, st), "H2D data");
+      h->data[l]->setTransformedStatus(false);
+    }
+    for (int p = 0; p < 3; p++) {
+      cuda_check(cudaMemcpyAsync(h->mean[p]->devicePtr(), mean[p], bytes, cudaMemcpyHostToDevice, st), "H2D mean");
+      h->mean[p]->setTransformedStatus(false);
+    }
+    Crava::Form f = form == 0 ? Crava::PLAIN : form == 1 ? Crava::FUSED_FP32 : Crava::FUSED_MIXED;
+    if (f == Crava::PLAIN) {
+      if (!prior_cov_real || !err_corr_real) throw Error(CG_ERR_ARG, "the plain form needs the real prior covariance cubes");
+      if (!h->errcorr) { h->errcorr = new FFTGrid(h->nx, h->ny, h->nz, h->nxp, h->nyp, h->nzp); h->errcorr->setType(FFTGrid::COVARIANCE); }
+      for (int t = 0; t < 6; t++) {
+        cuda_check(cudaMemcpyAsync(h->cov[t]->devicePtr(), prior_cov_real[t], bytes, cudaMemcpyHostToDevice, st), "H2D cov");
+        h->cov[t]->setTransformedStatus(false);
+      }
+      cuda_check(cudaMemcpyAsync(h->errcorr->devicePtr(), err_corr_real, bytes, cudaMemcpyHostToDevice, st), "H2D errCorr");
+      h->errcorr->setTransformedStatus(false);
+    }
+    FFTGrid *a = h->mean[0], *b = h->mean[1], *c = h->mean[2];
+    h->crava->computePostMeanResidAndFFTCov(h->data.data(), a, b, c, h->cov.data(), h->errcorr, f, st);
+    for (int l = 0; l < h->ntheta; l++)
+      cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H residual");
+    for (int t = 0; t < 6; t++)
+      cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H cov");
+    for (int p = 0; p < 3; p++)
+      cuda_check(cudaMemcpyAsync(mean[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
+    cuda_check(cudaStreamSynchronize(st), "inversion");
+    return CG_OK;
+  })
+}
+
+extern "C" int cg_inversion_stats(cg_inversion h, int *flagged, int *failed, int *overflow)
+{
+  if (!h) { cg::set_error("null argument"); return CG_ERR_ARG; }
+  return cg_workspace_stats(h->crava->workspace(), flagged, failed, overflow);
+}
+
+extern "C" int cg_host_register(void *ptr, size_t bytes)
+{
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) { (void)cudaGetLastError(); cg::set_error("cudaHostRegister: %s", cudaGetErrorString(e)); return CG_ERR_CUDA; }
+  return CG_OK;
+}
+
+extern "C" int cg_host_unregister(void *ptr)
+{
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) { (void)cudaGetLastError(); cg::set_error("cudaHostUnregister: %s", cudaGetErrorString(e)); return CG_ERR_CUDA; }
+  return CG_OK;
+}

@@ -120,6 +120,20 @@ int cg_fill_param_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_
 int cg_fill_err_corr(float *buf, int nxp, int nyp, int nzp, const float *corr_xy, float grad_i, float grad_j,
                      void *stream);
 
+/* FFTGrid::multiplyByScalar (src/fftgrid.cpp:1985-1996) over n floats
+ * (device, 16-byte aligned). */
+int cg_scale(float *buf, long n, float scalar, void *stream);
+
+/* FFTGrid::add (src/fftgrid.cpp:1870-1891): y += x over n floats (device,
+ * 16-byte aligned). */
+int cg_add(float *y, const float *x, long n, void *stream);
+
+/* Page-lock a caller's host buffer (e.g. an FFTGrid's fftw_malloc block) so
+ * the _host entry points copy it at full link speed; undo with
+ * cg_host_unregister. */
+int cg_host_register(void *ptr, size_t bytes);
+int cg_host_unregister(void *ptr);
+
 /* ========================================================================
  * Per-frequency-bin posterior (Crava::computePostMeanResidAndFFTCov bin loop,
  * src/crava.cpp:1084-1247).
@@ -191,6 +205,42 @@ int cg_invert_bins_fused(cg_workspace ws, float *const *data, float *const *mean
 /* Fused posterior on FP64 spectra (needs cg_prior_spectra with CG_PREC_FP64). */
 int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,
                              void *stream);
+
+/* ========================================================================
+ * Whole inversion from host buffers: the entry point a replacement of
+ * Crava::computePostMeanResidAndFFTCov (src/crava.cpp:975-1285) calls with
+ * its FFTGrids' host memory.  The context owns the device cubes, the model
+ * tables and a stream.
+ * ======================================================================== */
+typedef struct cg_inversion_s *cg_inversion;
+
+typedef struct cg_inversion_model {
+  int ntheta;
+  const float *wavelets;        /* [ntheta][nzp] resampled wavelets, FFT order */
+  const float *A;               /* [ntheta][3] reflection coefficients */
+  const double *err_theta_cov;  /* [ntheta][ntheta] */
+  const double *sigma0;         /* [3][3] priorVar0 */
+  const float *corr_xy;         /* [nyp][nxp] lateral correlation (findCorrXYGrid) */
+  const float *circ_corr_t;     /* [nzp] cyclic temporal correlation (computeCircCorrT) */
+  float wnc, low_cut, high_cut, dt_ms, min_rel_thick;
+  double cond_threshold;        /* CG_PREC_MIXED guard, <= 0 for the default */
+} cg_inversion_model;
+
+int cg_inversion_create(cg_inversion *inv, int nx, int ny, int nz, int nxp, int nyp, int nzp,
+                        const cg_inversion_model *model);
+void cg_inversion_destroy(cg_inversion inv);
+
+/* One inversion.  seis_data[ntheta]: host rsize-float buffers, real data in,
+ * residual spectra out; mean[3]: prior-mean real cubes in, posterior-mean real
+ * cubes out; post_cov[6]: posterior covariance spectra out.  form 0 = plain
+ * (then prior_cov_real[6] and err_corr_real are the real-domain
+ * fillInParamCorr / fillInErrCorr cubes), 1 = fused FP32, 2 = fused mixed.
+ * Synchronous. */
+int cg_inversion_run_host(cg_inversion inv, float *const *seis_data, float *const *mean, float *const *post_cov,
+                          const float *const *prior_cov_real, const float *err_corr_real, int form);
+
+/* Counters of the last runs (see cg_workspace_stats). */
+int cg_inversion_stats(cg_inversion inv, int *flagged, int *failed, int *overflow);
 
 /* ========================================================================
  * Posterior simulation (Crava::simulate, src/crava.cpp:1551-1734).

@@ -63,13 +63,19 @@ def from_cube(cube):
     return a.view(np.complex64 if a.dtype == np.float32 else np.complex128)
 
 
-def oracle_pipeline(O, sc, prec="d", nthreads=None):
-    """The whole inversion on the CPU oracle, from real-domain inputs."""
+def oracle_pipeline(O, sc, prec="d", nthreads=None, tables=None):
+    """The whole inversion on the CPU oracle, from real-domain inputs.
+
+    tables: the FP32 per-k operator tables to use (default: the oracle's own);
+    pass the GPU path's tables to compare arithmetic on identical inputs."""
     import os
     import numpy as np
     nt = nthreads or os.cpu_count()
     # the operator tables are FP32 inputs on every path (fillErrMultVectors is float in the reference)
-    tables = O.k_tables(sc.nxp, sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut, prec="f")
+    if tables is None:
+        tables = O.k_tables(sc.nxp, sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut, prec="f")
+    tables = dict(tables)
+    tables["nxp"] = sc.nxp
     if prec == "d":
         tables = {k: (v.astype(np.complex128) if hasattr(v, "dtype") and v.dtype == np.complex64 else v)
                   for k, v in tables.items()}

@@ -89,7 +89,7 @@ def test_pipeline_matches_fp64_oracle(cuda, oracle, form):
     inv.run(form)
     torch.cuda.synchronize()
     pm, res, cov = inv.results(form)
-    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d")
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
     prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
     e_mean = rel(pm, post64)
     e_upd = rel(pm - prior, post64 - prior)
