@@ -107,23 +107,31 @@ __device__ __forceinline__ void cstages(C2<T> *buf, const C2<T> *tw, int sign)
 }
 
 // ---------------------------------------------------------------------------
-// strided column pass: full tiles of W columns
+// strided column pass on tiles of W columns.  Element (e, c) of the tile of
+// CTA (x, y, z) is cube z at  y*by + x*bx + c*cs + e*axis_stride, and only
+// columns with x*W + c < climit exist.  Full tiles of adjacent columns use
+// (by, bx, cs) = (batch stride, W, 1); the columns left over after the full
+// tiles (the Nyquist column of an odd cnxp) are gathered across the batch
+// with (by, bx, cs) = (1, W*batch stride, batch stride).
 // ---------------------------------------------------------------------------
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs, const float2 *__restrict__ twg, int col0,
-                                                               long axis_stride, long batch_stride, int sign)
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs, const float2 *__restrict__ twg,
+                                                                     long by, long bx, long cstride, int climit,
+                                                                     long axis_stride, int sign)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + N * W;
-  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)blockIdx.y * batch_stride + col0 + (long)blockIdx.x * W;
+  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)blockIdx.y * by + (long)blockIdx.x * bx;
+  const int cvalid = climit - (int)blockIdx.x * W;  // columns of this tile that exist
   for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
 #pragma unroll
   for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
     const int t = t0 + threadIdx.x;
     if ((N * W) % kFFTThreads == 0 || t < N * W) {
       const int e = t / W, c = t % W;
-      cp_async8(&buf[e * W + c], &base[(long)e * axis_stride + c]);
+      if (c < cvalid) cp_async8(&buf[e * W + c], &base[(long)e * axis_stride + (long)c * cstride]);
+      else buf[e * W + c] = make_float2(0.f, 0.f);
     }
   }
   cp_async_wait_all();
@@ -134,7 +142,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs,
     const int t = t0 + threadIdx.x;
     if ((N * W) % kFFTThreads == 0 || t < N * W) {
       const int e = t / W, c = t % W;
-      base[(long)e * axis_stride + c] = buf[e * W + c];
+      if (c < cvalid) base[(long)e * axis_stride + (long)c * cstride] = buf[e * W + c];
     }
   }
 }

@@ -9,8 +9,8 @@ namespace cg {
 namespace {
 constexpr int kW = 16;
 
-// Resident-CTA target per length: 3 keeps lengths up to 160 spill free at the
-// 85-register cap; longer lengths default to 2.  CRAVA_COLS_MINB=2|3 forces
+// Resident-CTA target per length: 3 for lengths up to 256 (measured faster
+// at 256 despite a small spill), 2 above.  CRAVA_COLS_MINB=2|3 forces
 // one variant (used by the tuning sweep in crava_gb300.microbench).
 int minb_for(int n)
 {
@@ -20,50 +20,64 @@ int minb_for(int n)
     forced = (e && (e[0] == '2' || e[0] == '3')) ? e[0] - '0' : 0;
   }
   if (forced) return forced;
-  return n <= 160 ? 3 : 2;
+  return n <= 256 ? 3 : 2;
 }
 
 template <int N, int MINB>
-int launch_v(const CubeSet &cs, int ncubes, int nfull, long axis_stride, long batch_stride, int nbatch, int sign,
+int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
              const float2 *tw, cudaStream_t st)
 {
   const size_t smem = ((size_t)N * kW + N) * sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(k_fft_cols_fast<N, kW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_fast attribute");
-  dim3 grid(nfull, nbatch, ncubes);
-  TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)nfull * kW * N * sizeof(float2));
-  k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, 0, axis_stride, batch_stride, sign);
-  CG_CHECK_LAUNCH("k_fft_cols_fast");
+  const int nfull = ncols / kW;
+  const int ntail = ncols - nfull * kW;
+  if (nfull > 0) {
+    dim3 grid(nfull, nbatch, ncubes);
+    TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)nfull * kW * N * sizeof(float2));
+    k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, batch_stride, kW, 1, nfull * kW,
+                                                                  axis_stride, sign);
+    CG_CHECK_LAUNCH("k_fft_cols_fast");
+  }
+  if (ntail > 0) {
+    // leftover columns: tile across the batch index instead
+    CubeSet tc = cs;
+    for (int z = 0; z < ncubes; z++) tc.ptr[z] = (float2 *)cs.ptr[z] + nfull * kW;
+    dim3 grid(ceil_div(nbatch, kW), ntail, ncubes);
+    TraceScope ts("k_fft_cols_fast_tail", st, 2.0 * ncubes * nbatch * (double)ntail * N * sizeof(float2));
+    k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(tc, tw, 1, (long)kW * batch_stride, batch_stride,
+                                                                  nbatch, axis_stride, sign);
+    CG_CHECK_LAUNCH("k_fft_cols_fast tail");
+  }
   return 1;
 }
 
 template <int N>
-int launch(const CubeSet &cs, int ncubes, int nfull, long axis_stride, long batch_stride, int nbatch, int sign,
+int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
-  if (minb_for(N) == 3) return launch_v<N, 3>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st);
-  return launch_v<N, 2>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st);
+  if (minb_for(N) == 3) return launch_v<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  return launch_v<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
 }
 }  // namespace
 
-// Runs the full W-column tiles of a column pass when the length has a
-// specialisation; *done_cols receives how many leading columns were handled.
+// Runs a whole column pass when the length has a specialisation; *done_cols
+// receives how many columns were handled (all of them, or 0).
 int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
               int sign, const float2 *tw, cudaStream_t st, int *done_cols)
 {
   *done_cols = 0;
-  const int nfull = ncols / kW;
-  if (nfull == 0) return 0;
+  if (ncols < 1) return 0;
   int rc = 0;
   switch (n) {
-#define CG_COLS(NN) case NN: rc = launch<NN>(cs, ncubes, nfull, axis_stride, batch_stride, nbatch, sign, tw, st); break;
+#define CG_COLS(NN) case NN: rc = launch<NN>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st); break;
     CG_COLS(64) CG_COLS(80) CG_COLS(96) CG_COLS(100) CG_COLS(120) CG_COLS(128) CG_COLS(160) CG_COLS(192)
     CG_COLS(200) CG_COLS(240) CG_COLS(256) CG_COLS(320) CG_COLS(384) CG_COLS(400) CG_COLS(480) CG_COLS(512)
 #undef CG_COLS
     default: return 0;
   }
-  if (rc == 1) *done_cols = nfull * kW;
+  if (rc == 1) *done_cols = ncols;
   return rc;
 }
 

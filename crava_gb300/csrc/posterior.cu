@@ -275,10 +275,18 @@ __device__ __forceinline__ void bin_scales(const FusedArgs<T> &a, int ij, int k,
 
 // Plain lower Cholesky (no pre-scaling) with the reference's failure rule:
 // fail when A00 <= 0 or any pivot <= 1e-20 * A00 (lib_matr.c:78-168 scales by
-// A00 first).  Returns the squared ratio of the largest to the smallest
-// diagonal of L as a cheap lower bound on the condition number.
+// A00 first).  inv[i] receives 1/L_ii (FP32: from one rsqrt per pivot), and
+// cond the squared ratio of the largest to the smallest pivot of L, a cheap
+// lower bound on the condition number.
+template <typename T>
+__device__ __forceinline__ T inv_sqrt(T x)
+{
+  if constexpr (sizeof(T) == 4) return rsqrtf(x);
+  else return 1.0 / sqrt(x);
+}
+
 template <typename T, int N>
-__device__ __forceinline__ bool chol_std(C2<T> *L, T &cond)
+__device__ __forceinline__ bool chol_std(C2<T> *L, T *inv, T &cond)
 {
   const T a00 = L[0].x;
   if (!(a00 > (T)0)) return false;
@@ -291,48 +299,47 @@ __device__ __forceinline__ bool chol_std(C2<T> *L, T &cond)
       C2<T> acc = L[tri(i, j)];
 #pragma unroll
       for (int k = 0; k < j; k++) acc = csub<T>(acc, cmulc<T>(L[tri(i, k)], L[tri(j, k)]));
-      const T inv = (T)1 / L[tri(j, j)].x;
-      L[tri(i, j)] = mk<T>(acc.x * inv, acc.y * inv);
+      L[tri(i, j)] = mk<T>(acc.x * inv[j], acc.y * inv[j]);
     }
     T piv = L[tri(i, i)].x;
 #pragma unroll
     for (int k = 0; k < i; k++) piv -= L[tri(i, k)].x * L[tri(i, k)].x + L[tri(i, k)].y * L[tri(i, k)].y;
     if (!(piv > tol)) return false;
-    const T di = sqrt(piv);
+    const T r = inv_sqrt<T>(piv);
+    const T di = piv * r;
+    inv[i] = r;
     L[tri(i, i)] = mk<T>(di, (T)0);
     dmax = i == 0 ? di : (di > dmax ? di : dmax);
     dmin = i == 0 ? di : (di < dmin ? di : dmin);
   }
-  const T r = dmax / dmin;
-  cond = r * r;
+  const T q = dmax / dmin;
+  cond = q * q;
   return true;
 }
 
 // forward substitution L x = b in place
 template <typename T, int N>
-__device__ __forceinline__ void lsolve(const C2<T> *L, C2<T> *x)
+__device__ __forceinline__ void lsolve(const C2<T> *L, const T *inv, C2<T> *x)
 {
 #pragma unroll
   for (int i = 0; i < N; i++) {
     C2<T> acc = x[i];
 #pragma unroll
     for (int j = 0; j < i; j++) acc = csub<T>(acc, cmul<T>(L[tri(i, j)], x[j]));
-    const T inv = (T)1 / L[tri(i, i)].x;
-    x[i] = mk<T>(acc.x * inv, acc.y * inv);
+    x[i] = mk<T>(acc.x * inv[i], acc.y * inv[i]);
   }
 }
 
 // backward substitution L^H x = b in place
 template <typename T, int N>
-__device__ __forceinline__ void lhsolve(const C2<T> *L, C2<T> *x)
+__device__ __forceinline__ void lhsolve(const C2<T> *L, const T *inv, C2<T> *x)
 {
 #pragma unroll
   for (int i = N - 1; i >= 0; i--) {
     C2<T> acc = x[i];
 #pragma unroll
     for (int j = i + 1; j < N; j++) acc = csub<T>(acc, cmulc<T>(x[j], L[tri(j, i)]));
-    const T inv = (T)1 / L[tri(i, i)].x;
-    x[i] = mk<T>(acc.x * inv, acc.y * inv);
+    x[i] = mk<T>(acc.x * inv[i], acc.y * inv[i]);
   }
 }
 
@@ -355,7 +362,7 @@ __device__ __forceinline__ void build_sd(const KTab<T> &kt, T s, T lam, C2<T> *S
 // refine: solve Sd u = r with one step of iterative refinement (FP64 paths).
 template <typename T, int N>
 __device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *sig0, T s, T lam, const C2<T> *L,
-                                                    C2<T> *d, C2<T> *mu, C2<T> *cov, bool refine)
+                                                    const T *inv, C2<T> *d, C2<T> *mu, C2<T> *cov, bool refine)
 {
   C2<T> r[N];
 #pragma unroll
@@ -371,7 +378,7 @@ __device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *
   for (int p = 0; p < 3; p++) {
 #pragma unroll
     for (int l = 0; l < N; l++) Y[p][l] = kt.KS0[l][p];
-    lsolve<T, N>(L, Y[p]);
+    lsolve<T, N>(L, inv, Y[p]);
   }
   const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
 #pragma unroll
@@ -387,7 +394,7 @@ __device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *
     C2<T> v[N];
 #pragma unroll
     for (int l = 0; l < N; l++) v[l] = r[l];
-    lsolve<T, N>(L, v);
+    lsolve<T, N>(L, inv, v);
 #pragma unroll
     for (int p = 0; p < 3; p++) {
       C2<T> acc = mk<T>(0, 0);
@@ -400,8 +407,8 @@ __device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *
     C2<T> u[N], rho[N], Sd[N * (N + 1) / 2];
 #pragma unroll
     for (int l = 0; l < N; l++) u[l] = r[l];
-    lsolve<T, N>(L, u);
-    lhsolve<T, N>(L, u);
+    lsolve<T, N>(L, inv, u);
+    lhsolve<T, N>(L, inv, u);
     build_sd<T, N>(kt, s, lam, Sd);
 #pragma unroll
     for (int l = 0; l < N; l++) {
@@ -413,8 +420,8 @@ __device__ __forceinline__ void posterior_from_chol(const KTab<T> &kt, const T *
       }
       rho[l] = acc;
     }
-    lsolve<T, N>(L, rho);
-    lhsolve<T, N>(L, rho);
+    lsolve<T, N>(L, inv, rho);
+    lhsolve<T, N>(L, inv, rho);
 #pragma unroll
     for (int l = 0; l < N; l++) u[l] = cadd<T>(u[l], rho[l]);
 #pragma unroll
@@ -470,8 +477,8 @@ __global__ void __launch_bounds__(128) k_invert_fused(FusedArgs<T> a)
 #pragma unroll
   for (int p = 0; p < 3; p++) mu[p] = a.mean[p][b];
   build_sd<T, NT>(kt, s, lam, L);
-  T cond = 0;
-  const bool ok = chol_std<T, NT>(L, cond);
+  T cond = 0, inv[NT];
+  const bool ok = chol_std<T, NT>(L, inv, cond);
   if (MODE == 1) {
     const bool flag = !ok || cond > (T)a.cond_thr;
     const unsigned m = __ballot_sync(__activemask(), flag);
@@ -494,7 +501,7 @@ __global__ void __launch_bounds__(128) k_invert_fused(FusedArgs<T> a)
     write_prior_cov<T>(a, b, s);
     return;
   }
-  posterior_from_chol<T, NT>(kt, a.sig0, s, lam, L, d, mu, cov, MODE == 2);
+  posterior_from_chol<T, NT>(kt, a.sig0, s, lam, L, inv, d, mu, cov, MODE == 2);
 #pragma unroll
   for (int l = 0; l < NT; l++) a.data[l][b] = d[l];
 #pragma unroll
@@ -528,14 +535,14 @@ __global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, cons
 #pragma unroll
     for (int p = 0; p < 3; p++) { float2 v = a.mean[p][b]; mu[p] = make_double2(v.x, v.y); }
     build_sd<double, NT>(kt, s, lam, L);
-    double cond;
-    if (!chol_std<double, NT>(L, cond)) {
+    double cond, inv[NT];
+    if (!chol_std<double, NT>(L, inv, cond)) {
       atomicAdd(&a.counters[1], 1);
 #pragma unroll
       for (int t = 0; t < 6; t++) a.cov[t][b] = make_float2((float)(s * sig0d[t]), 0.0f);
       continue;
     }
-    posterior_from_chol<double, NT>(kt, sig0d, s, lam, L, d, mu, cov, true);
+    posterior_from_chol<double, NT>(kt, sig0d, s, lam, L, inv, d, mu, cov, true);
 #pragma unroll
     for (int l = 0; l < NT; l++) a.data[l][b] = make_float2((float)d[l].x, (float)d[l].y);
 #pragma unroll
