@@ -115,26 +115,18 @@ class ClockSampler:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from crava_gb300 import replicas
+    return replicas.world()
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as dist
-        dist.barrier()
+    from crava_gb300 import replicas
+    replicas.barrier(world)
 
 
 def max_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from crava_gb300 import replicas
+    return replicas.max_over_ranks(x, world, device="cuda")
 
 
 def rel(a, b):
@@ -351,8 +343,9 @@ def run_ours(args, world, rank, local):
     ms_plain = max_over_ranks(results["plain"], world)
     ms_fp32 = max_over_ranks(results["fp32"], world)
     e2e_ms = max_over_ranks(e2e_ms, world)
+    from crava_gb300 import replicas
     total_bins = bins * world
-    value = total_bins / (ms_mixed * 1e-3) / 1e6
+    value = replicas.whole_job_rate(bins, ms_mixed, world)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

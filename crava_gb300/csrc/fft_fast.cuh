@@ -114,16 +114,39 @@ __device__ __forceinline__ void cstages(C2<T> *buf, const C2<T> *tw, int sign)
 // tiles (the Nyquist column of an odd cnxp) are gathered across the batch
 // with (by, bx, cs) = (1, W*batch stride, batch stride).
 // ---------------------------------------------------------------------------
+struct ColsGeom {
+  long axis_stride;   // between elements of one column
+  long batch_stride;  // between batch rows (y)
+  int nfull;          // full W-column tiles per batch row (grid.x = nfull + 1 when ntail > 0)
+  int ntail;          // leftover columns after the full tiles
+  int nbatch;
+};
+
 template <int N, int W, int MINB>
 __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs, const float2 *__restrict__ twg,
-                                                                     long by, long bx, long cstride, int climit,
-                                                                     long axis_stride, int sign)
+                                                                     ColsGeom g, int sign)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + N * W;
-  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)blockIdx.y * by + (long)blockIdx.x * bx;
-  const int cvalid = climit - (int)blockIdx.x * W;  // columns of this tile that exist
+  // full tiles: (x < nfull, y = batch row); grid column x == nfull holds the
+  // tail tiles, y = group of W batch rows (CTAs past the last group exit)
+  long by, bx, cstride;
+  int cvalid;
+  float2 *cube = (float2 *)cs.ptr[blockIdx.z];
+  if ((int)blockIdx.x < g.nfull) {
+    by = g.batch_stride; bx = W; cstride = 1; cvalid = W;
+  } else {
+    const int groups = (g.nbatch + W - 1) / W;
+    const int tcol = (int)blockIdx.y / groups, grp = (int)blockIdx.y % groups;
+    if (tcol >= g.ntail) return;
+    cube += (long)g.nfull * W + tcol;
+    by = 0; bx = 0; cstride = g.batch_stride;
+    cube += (long)grp * W * g.batch_stride;
+    cvalid = g.nbatch - grp * W;
+  }
+  const long axis_stride = g.axis_stride;
+  float2 *base = cube + ((int)blockIdx.x < g.nfull ? (long)blockIdx.y * by + (long)blockIdx.x * bx : 0);
   for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
 #pragma unroll
   for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
@@ -201,34 +224,40 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeS
   constexpr int NX = 2 * M, CN = M + 1, RN = 2 * CN;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
-  float2 *S = buf + M * LDW;      // kRows x CN staged spectra
-  float2 *tw = S + kRows * CN;
+  float2 *tw = buf + M * LDW;
   const int r0 = blockIdx.x * kRows;
   const int nr = min(kRows, nrows - r0);
   float *base = (float *)cs.ptr[blockIdx.z] + (long)r0 * RN;
   for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
-  for (int t = threadIdx.x; t < nr * CN; t += kFFTThreads) {
-    const int row = t / CN, k = t - row * CN;
-    cp_async8(&S[row * CN + k], base + (long)row * RN + 2 * k);
-  }
-  cp_async_wait_all();
-  __syncthreads();
+  // pack X[k], conj X[M-k] of every row straight from global memory (the
+  // second read of each row hits L1)
+  constexpr int NIT = (kRows * M + kFFTThreads - 1) / kFFTThreads;
+  float2 xk[NIT], xm[NIT];
 #pragma unroll
-  for (int t0 = 0; t0 < kRows * M; t0 += kFFTThreads) {
-    const int t = t0 + threadIdx.x;
-    if ((kRows * M) % kFFTThreads == 0 || t < kRows * M) {
+  for (int q = 0; q < NIT; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int row = t / M, k = t % M;
+    if ((t < kRows * M) && row < nr) {
+      const float2 *rp = (const float2 *)(base + (long)row * RN);
+      xk[q] = __ldg(rp + k);
+      xm[q] = __ldg(rp + (M - k));
+    } else {
+      xk[q] = make_float2(0.f, 0.f);
+      xm[q] = make_float2(0.f, 0.f);
+    }
+  }
+  __syncthreads();  // twiddles staged
+#pragma unroll
+  for (int q = 0; q < NIT; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (t < kRows * M) {
       const int row = t / M, k = t % M;
-      float2 Z = make_float2(0.f, 0.f);
-      if (row < nr) {
-        float2 Xk = S[row * CN + k];
-        float2 Xm = S[row * CN + (M - k)];
-        if (k == 0) { Xk.y = 0.f; Xm.y = 0.f; }  // rfftw_c2hc keeps only Re of DC and Nyquist
-        Xm.y = -Xm.y;
-        const float2 E = cadd<float>(Xk, Xm);
-        const float2 O = cmulc<float>(csub<float>(Xk, Xm), tw[k]);
-        Z = make_float2(E.x - O.y, E.y + O.x);
-      }
-      buf[k * LDW + row] = Z;
+      float2 Xk = xk[q], Xm = xm[q];
+      if (k == 0) { Xk.y = 0.f; Xm.y = 0.f; }  // rfftw_c2hc keeps only Re of DC and Nyquist
+      Xm.y = -Xm.y;
+      const float2 E = cadd<float>(Xk, Xm);
+      const float2 O = cmulc<float>(csub<float>(Xk, Xm), tw[k]);
+      buf[k * LDW + row] = make_float2(E.x - O.y, E.y + O.x);
     }
   }
   __syncthreads();

@@ -31,25 +31,21 @@ int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long ba
   cudaError_t e = cudaFuncSetAttribute(k_fft_cols_fast<N, kW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_fast attribute");
-  const int nfull = ncols / kW;
-  const int ntail = ncols - nfull * kW;
-  if (nfull > 0) {
-    dim3 grid(nfull, nbatch, ncubes);
-    TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)nfull * kW * N * sizeof(float2));
-    k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, batch_stride, kW, 1, nfull * kW,
-                                                                  axis_stride, sign);
-    CG_CHECK_LAUNCH("k_fft_cols_fast");
+  ColsGeom g;
+  g.axis_stride = axis_stride;
+  g.batch_stride = batch_stride;
+  g.nfull = ncols / kW;
+  g.ntail = ncols - g.nfull * kW;
+  g.nbatch = nbatch;
+  const int groups = ceil_div(nbatch, kW);
+  if (g.ntail > 0 && g.ntail * groups > nbatch) {
+    set_error("column tail does not fit the launch grid");
+    return CG_ERR_STATE;
   }
-  if (ntail > 0) {
-    // leftover columns: tile across the batch index instead
-    CubeSet tc = cs;
-    for (int z = 0; z < ncubes; z++) tc.ptr[z] = (float2 *)cs.ptr[z] + nfull * kW;
-    dim3 grid(ceil_div(nbatch, kW), ntail, ncubes);
-    TraceScope ts("k_fft_cols_fast_tail", st, 2.0 * ncubes * nbatch * (double)ntail * N * sizeof(float2));
-    k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(tc, tw, 1, (long)kW * batch_stride, batch_stride,
-                                                                  nbatch, axis_stride, sign);
-    CG_CHECK_LAUNCH("k_fft_cols_fast tail");
-  }
+  dim3 grid(g.nfull + (g.ntail > 0 ? 1 : 0), nbatch, ncubes);
+  TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
+  k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_fast");
   return 1;
 }
 

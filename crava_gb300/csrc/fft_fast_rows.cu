@@ -10,8 +10,7 @@ int launch(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, i
            const float2 *tw, cudaStream_t st)
 {
   constexpr int LDW = kRows + 1;
-  const size_t smem = forward ? ((size_t)M * LDW + 2 * M) * sizeof(float2)
-                              : ((size_t)M * LDW + (size_t)kRows * (M + 1) + 2 * M) * sizeof(float2);
+  const size_t smem = ((size_t)M * LDW + 2 * M) * sizeof(float2);
   dim3 grid(ceil_div(nrows, kRows), 1, ncubes);
   const double bytes = (double)ncubes * nrows * (2.0 * M * sizeof(float) + (M + 1.0) * sizeof(float2));
   cudaError_t e;

@@ -450,9 +450,11 @@ __device__ __forceinline__ void write_prior_cov(const FusedArgs<T> &a, long b, T
   for (int t = 0; t < 6; t++) a.cov[t][b] = mk<T>(s * a.sig0[t], (T)0);
 }
 
-// MODE 0: FP32, 1: MIXED (FP32 + queue), 2: FP64 (T = double)
-template <typename T, int NT, int MODE>
-__global__ void __launch_bounds__(128) k_invert_fused(FusedArgs<T> a)
+// MODE 0: FP32, 1: MIXED (FP32 + queue), 2: FP64 (T = double).  MINB is the
+// resident-CTA target handed to the register allocator (1 = unconstrained,
+// 6 = at most 85 registers).
+template <typename T, int NT, int MODE, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a)
 {
   __shared__ KTab<T> kt;
   const int k = blockIdx.y;
@@ -844,6 +846,18 @@ extern "C" int cg_prior_spectra(cg_workspace w, const float *corr_xy, const floa
   return prior_tables<float>(w, corr_xy, circ_corr_t, w->cxy_f, w->ct_f, st);
 }
 
+// Occupancy variant of the FP32 fused kernels; CRAVA_BIN_MINB=1|6 forces one
+// (used by the tuning sweep in crava_gb300.microbench).
+static int bin_minb()
+{
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("CRAVA_BIN_MINB");
+    v = (e && e[0] == '6') ? 6 : 1;
+  }
+  return v;
+}
+
 template <typename T>
 static int fused_launch(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision,
                         cudaStream_t st)
@@ -881,7 +895,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
     } else if (precision == CG_PREC_MIXED) {
       {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
-        k_invert_fused<T, NT, 1><<<grid, threads, 0, st>>>(a);
+        if (bin_minb() == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
+        else k_invert_fused<T, NT, 1, 1><<<grid, threads, 0, st>>>(a);
       }
       CG_CHECK_LAUNCH("k_invert_fused");
       S0Args sd;
@@ -894,7 +909,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
     } else {
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
-      k_invert_fused<T, NT, 0><<<grid, threads, 0, st>>>(a);
+      if (bin_minb() == 6) k_invert_fused<T, NT, 0, 6><<<grid, threads, 0, st>>>(a);
+      else k_invert_fused<T, NT, 0, 1><<<grid, threads, 0, st>>>(a);
     }
     CG_CHECK_LAUNCH("k_invert_fused");
     return CG_OK;
