@@ -280,10 +280,12 @@ int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncub
   TraceScope ts(forward ? "k_r2c_rows" : "k_c2r_rows", st,
                 (double)ncubes * nrows * ((double)nxp * sizeof(T) + (double)cnxp * sizeof(C2<T>)));
   if (forward) {
-    CG_CUDA(cudaFuncSetAttribute(k_r2c_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static bool attr[64] = {};
+    CG_CUDA(smem_limit_once(k_r2c_rows<T>, kMaxSmem, attr));
     k_r2c_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, nxp, nrows, scale);
   } else {
-    CG_CUDA(cudaFuncSetAttribute(k_c2r_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static bool attr[64] = {};
+    CG_CUDA(smem_limit_once(k_c2r_rows<T>, kMaxSmem, attr));
     k_c2r_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, addend, p, tw, nxp, nrows, scale);
   }
   CG_CHECK_LAUNCH(forward ? "k_r2c_rows" : "k_c2r_rows");
@@ -331,7 +333,8 @@ int launch_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_strid
     set_error("axis length %d too long for the shared-memory tile", n);
     return CG_ERR_UNSUPPORTED;
   }
-  CG_CUDA(cudaFuncSetAttribute(k_fft_cols<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  static bool attr[64] = {};
+  CG_CUDA(smem_limit_once(k_fft_cols<T>, kMaxSmem, attr));
   dim3 grid(ntiles, nbatch, ncubes);
   TraceScope ts("k_fft_cols", st, 2.0 * ncubes * nbatch * (double)ncols * n * sizeof(C2<T>));
   k_fft_cols<T><<<grid, kFFTThreads, smem, st>>>(cs, p, tw, col0, ncols, wfull, ntiles, axis_stride, batch_stride,

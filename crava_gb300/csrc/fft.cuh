@@ -23,6 +23,22 @@ struct CubeSet {
 };
 
 bool make_axis_plan(int n, AxisPlan *p);
+
+// Raise a kernel's dynamic shared-memory limit once per device (the attribute
+// is per device; setting it on every launch would be wasted work and is not
+// wanted inside a stream capture).
+template <typename K>
+inline cudaError_t smem_limit_once(K kernel, size_t bytes, bool *done_per_device)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (done_per_device[dev]) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) done_per_device[dev] = true;
+  return e;
+}
 template <typename T> const C2<T> *twiddle_table(int n);
 template <typename T>
 int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st);

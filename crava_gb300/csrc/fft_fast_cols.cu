@@ -28,8 +28,8 @@ int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long ba
              const float2 *tw, cudaStream_t st)
 {
   const size_t smem = ((size_t)N * kW + N) * sizeof(float2);
-  cudaError_t e = cudaFuncSetAttribute(k_fft_cols_fast<N, kW, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem);
+  static bool attr_set[64] = {};
+  cudaError_t e = smem_limit_once(k_fft_cols_fast<N, kW, MINB>, smem, attr_set);
   if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_fast attribute");
   ColsGeom g;
   g.axis_stride = axis_stride;

@@ -13,14 +13,15 @@ int launch(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, i
   const size_t smem = ((size_t)M * LDW + 2 * M) * sizeof(float2);
   dim3 grid(ceil_div(nrows, kRows), 1, ncubes);
   const double bytes = (double)ncubes * nrows * (2.0 * M * sizeof(float) + (M + 1.0) * sizeof(float2));
+  static bool attr_fwd[64] = {}, attr_inv[64] = {};
   cudaError_t e;
   if (forward) {
-    e = cudaFuncSetAttribute(k_r2c_rows_fast<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = smem_limit_once(k_r2c_rows_fast<M>, smem, attr_fwd);
     if (e != cudaSuccess) return cuda_status(e, "k_r2c_rows_fast attribute");
     TraceScope ts("k_r2c_rows_fast", st, bytes);
     k_r2c_rows_fast<M><<<grid, kFFTThreads, smem, st>>>(cs, tw, nrows, scale);
   } else {
-    e = cudaFuncSetAttribute(k_c2r_rows_fast<M>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = smem_limit_once(k_c2r_rows_fast<M>, smem, attr_inv);
     if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_fast attribute");
     TraceScope ts("k_c2r_rows_fast", st, bytes);
     k_c2r_rows_fast<M><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale);

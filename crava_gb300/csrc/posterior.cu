@@ -846,16 +846,21 @@ extern "C" int cg_prior_spectra(cg_workspace w, const float *corr_xy, const floa
   return prior_tables<float>(w, corr_xy, circ_corr_t, w->cxy_f, w->ct_f, st);
 }
 
-// Occupancy variant of the FP32 fused kernels; CRAVA_BIN_MINB=1|6 forces one
-// (used by the tuning sweep in crava_gb300.microbench).
-static int bin_minb()
+// Occupancy variant of the FP32 fused kernels.  Measured at 256^3 with five
+// stacks, capping registers for 6 resident CTAs (85 registers) is 1.34x
+// faster than the unconstrained build despite a small spill; with six or more
+// stacks the cap spills heavily, so those keep the unconstrained build.
+// CRAVA_BIN_MINB=1|6 forces one (used by the tuning sweep in
+// crava_gb300.microbench).
+static int bin_minb(int ntheta)
 {
-  static int v = -1;
-  if (v < 0) {
+  static int forced = -1;
+  if (forced < 0) {
     const char *e = getenv("CRAVA_BIN_MINB");
-    v = (e && e[0] == '6') ? 6 : 1;
+    forced = (e && e[0] == '6') ? 6 : (e && e[0] == '1') ? 1 : 0;
   }
-  return v;
+  if (forced) return forced;
+  return ntheta <= 5 ? 6 : 1;
 }
 
 template <typename T>
@@ -895,7 +900,7 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
     } else if (precision == CG_PREC_MIXED) {
       {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
-        if (bin_minb() == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
+        if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
         else k_invert_fused<T, NT, 1, 1><<<grid, threads, 0, st>>>(a);
       }
       CG_CHECK_LAUNCH("k_invert_fused");
@@ -909,7 +914,7 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
     } else {
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
-      if (bin_minb() == 6) k_invert_fused<T, NT, 0, 6><<<grid, threads, 0, st>>>(a);
+      if (bin_minb(NT) == 6) k_invert_fused<T, NT, 0, 6><<<grid, threads, 0, st>>>(a);
       else k_invert_fused<T, NT, 0, 1><<<grid, threads, 0, st>>>(a);
     }
     CG_CHECK_LAUNCH("k_invert_fused");
