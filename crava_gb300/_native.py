@@ -118,6 +118,8 @@ def _declare(L):
         "cg_fft3d_c2r_batch": ([PP, I, I, I, I, I, V], I),
         "cg_fft3d_r2c_f64": ([V, I, I, I, I, V], I),
         "cg_fft3d_c2r_f64": ([V, I, I, I, I, V], I),
+        "cg_fft3d_r2c_noalloc": ([V, I, I, I, I, V], I),
+        "cg_fft3d_c2r_noalloc": ([V, I, I, I, I, V], I),
         "cg_fft3d_r2c_host": ([V, I, I, I, I], I),
         "cg_fft3d_c2r_host": ([V, I, I, I, I], I),
         "cg_workspace_create": ([ct.POINTER(V), I, I, I, I], I),

@@ -89,6 +89,23 @@ int cg_fft3d_c2r_batch(float *const *bufs, int count, int nxp, int nyp, int nzp,
 int cg_fft3d_r2c_f64(double *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
 int cg_fft3d_c2r_f64(double *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
 
+/* The same transforms without any device allocation, for callers that cannot
+ * let a library call cudaMalloc (an application capturing a CUDA graph with
+ * allocation forbidden, or a host whose device memory belongs to its own
+ * allocator).  No counterpart in the reference.  cg_fft3d_r2c/c2r allocate
+ * their twiddle tables the first time a length is used; these keep them in
+ * one 128 KiB array in the library's static device memory instead, which
+ * every GPU that loads the library holds until exit.  Limits: even nxp with
+ * nxp/2 in {32,40,48,50,60,64,80,96,100,120,128,160,192,200,240,256}, nyp
+ * and nzp equal to 1 or in {64,80,96,100,120,128,160,192,200,240,256,320,
+ * 384,400,480,512}, nxp+nyp+nzp <= 16384; anything else is rejected with
+ * CG_ERR_ARG or CG_ERR_UNSUPPORTED before the buffer is touched.  Every call
+ * rewrites the shared array, so calls that overlap on the GPU race.  The
+ * first call on a device looks the array up for that device; make it before
+ * any stream capture. */
+int cg_fft3d_r2c_noalloc(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+int cg_fft3d_c2r_noalloc(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
 /* Host-memory variants of cg_fft3d_r2c / cg_fft3d_c2r (synchronous). */
 int cg_fft3d_r2c_host(float *hbuf, int nxp, int nyp, int nzp, int cubetype);
 int cg_fft3d_c2r_host(float *hbuf, int nxp, int nyp, int nzp, int cubetype);
