@@ -147,6 +147,13 @@ def _declare(L):
         "cg_inversion_destroy": ([V], None),
         "cg_inversion_run_host": ([V, PP, PP, PP, PP, V, I], I),
         "cg_inversion_stats": ([V, ct.POINTER(I), ct.POINTER(I), ct.POINTER(I)], I),
+        "cg_batch_create": ([ct.POINTER(V), V, I, I], I),
+        "cg_batch_destroy": ([V], None),
+        "cg_batch_load": ([V, I, PP, PP], I),
+        "cg_batch_reset": ([V, V], I),
+        "cg_batch_run": ([V, I, I, V], I),
+        "cg_batch_read": ([V, I, PP, PP, PP], I),
+        "cg_batch_bins": ([V], ct.c_long),
         "cg_trace_enable": ([I], I),
         "cg_trace_collect": ([], I),
         "cg_trace_entry": ([I, ct.c_char_p, I, ct.POINTER(ct.c_long), ct.POINTER(D), ct.POINTER(D)], I),

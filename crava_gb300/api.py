@@ -286,3 +286,73 @@ class HostInversion:
         a, b, c = ct.c_int(), ct.c_int(), ct.c_int()
         check(lib().cg_inversion_stats(self.h, ct.byref(a), ct.byref(b), ct.byref(c)), "cg_inversion_stats")
         return {"flagged": a.value, "failed": b.value, "overflow": c.value}
+
+
+class _BatchCube(ct.Structure):
+    _fields_ = [("nx", ct.c_int), ("ny", ct.c_int), ("nz", ct.c_int), ("nxp", ct.c_int), ("nyp", ct.c_int),
+                ("nzp", ct.c_int), ("model", _InvModel)]
+
+
+class Batch:
+    """Many independent inversions of uneven cubes as one unit of GPU work (cg_batch_*)."""
+
+    def __init__(self, scenarios, nstreams=8, cond_threshold=0.0):
+        self.scs = list(scenarios)
+        self._keep = []
+        cubes = (_BatchCube * len(self.scs))()
+        for i, sc in enumerate(self.scs):
+            arrs = [np.ascontiguousarray(sc.wavelets, dtype=np.float32), np.ascontiguousarray(sc.A, np.float32),
+                    np.ascontiguousarray(sc.err_theta_cov, np.float64),
+                    np.ascontiguousarray(sc.sigma0, np.float64).reshape(9),
+                    np.ascontiguousarray(sc.corr_xy, np.float32), np.ascontiguousarray(sc.circ_corr_t, np.float32)]
+            self._keep.append(arrs)
+            m = _InvModel(sc.ntheta, *[a.ctypes.data for a in arrs], sc.wnc, sc.low_cut, sc.high_cut, sc.dt_ms,
+                          sc.min_rel_thick, cond_threshold)
+            cubes[i] = _BatchCube(sc.nx, sc.ny, sc.nz, sc.nxp, sc.nyp, sc.nzp, m)
+        h = ct.c_void_p()
+        check(lib().cg_batch_create(ct.byref(h), ct.cast(cubes, ct.c_void_p), len(self.scs), nstreams),
+              "cg_batch_create")
+        self.h = h
+        for i, sc in enumerate(self.scs):
+            pd, k1 = _pp_np([np.ascontiguousarray(d, np.float32) for d in sc.data])
+            pm, k2 = _pp_np([np.ascontiguousarray(m, np.float32) for m in sc.mean])
+            check(lib().cg_batch_load(self.h, i, pd, pm), "cg_batch_load")
+
+    @property
+    def bins(self):
+        return lib().cg_batch_bins(self.h)
+
+    def reset(self, stream=None):
+        check(lib().cg_batch_reset(self.h, _stream(stream)), "cg_batch_reset")
+
+    def run(self, form="mixed", use_graph=True, stream=None):
+        f = {"fp32": 1, "mixed": 2}[form]
+        check(lib().cg_batch_run(self.h, f, 1 if use_graph else 0, _stream(stream)), "cg_batch_run")
+
+    def read(self, i):
+        sc = self.scs[i]
+        mean = [np.empty_like(sc.mean[0]) for _ in range(3)]
+        res = [np.empty_like(sc.data[0]) for _ in range(sc.ntheta)]
+        cov = [np.empty_like(sc.data[0]) for _ in range(6)]
+        pm, k1 = _pp_np(mean)
+        pr, k2 = _pp_np(res)
+        pc, k3 = _pp_np(cov)
+        check(lib().cg_batch_read(self.h, i, pm, pr, pc), "cg_batch_read")
+        return (np.stack([m[:, :, :sc.nxp] for m in mean]), np.stack([r.view(np.complex64) for r in res]),
+                np.stack([c.view(np.complex64) for c in cov]))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().cg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _pp_np(arrs):
+    arr = (ct.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    return ct.cast(arr, ct.POINTER(ct.c_void_p)), (arr, arrs)

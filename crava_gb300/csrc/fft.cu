@@ -82,6 +82,27 @@ template const C2<double> *twiddle_table<double>(int);
 // ---------------------------------------------------------------------------
 // kernels
 // ---------------------------------------------------------------------------
+// asynchronous global -> shared copy of one complex element (8 or 16 bytes)
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(C2<T> *dst, const C2<T> *src)
+{
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_real(T *dst, const T *src)
+{
+  if constexpr (sizeof(T) == 4) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  } else {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+  }
+}
+
 // the C2R row kernel stages kRows whole rows in bufB, so bufB holds
 // max(m*(kRows+1), kRows*cnxp) elements
 __host__ __device__ inline size_t c2r_bufb_elems(int m, int cnxp)
@@ -110,8 +131,9 @@ __global__ void __launch_bounds__(kFFTThreads) k_fft_cols(CubeSet cs, AxisPlan p
   const int tot = n * width;
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int e = t / width, c = t - e * width;
-    bufA[e * width + c] = base[(long)e * axis_stride + c];
+    cp_async_elem<T>(&bufA[e * width + c], &base[(long)e * axis_stride + c]);
   }
+  cp_async_wait_all();
   __syncthreads();
   C2<T> *res = smem_fft<T>(bufA, bufB, p, width, width, tw, 1, sign);
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
@@ -141,18 +163,18 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p
   const int tot = kRows * m;
   for (int t = threadIdx.x; t < tot; t += blockDim.x) {
     int row = t / m, e = t - row * m;
-    C2<T> z = mk<T>(0, 0);
     if (row < nr) {
       if (even) {
-        z = ((const C2<T> *)(base + (long)row * rnxp))[e];
-        z.x *= prescale;
-        z.y *= prescale;
+        cp_async_elem<T>(&bufA[e * ldw + row], (const C2<T> *)(base + (long)row * rnxp) + e);
       } else {
-        z.x = base[(long)row * rnxp + e] * prescale;
+        bufA[e * ldw + row].y = (T)0;
+        cp_async_real<T>(&bufA[e * ldw + row].x, base + (long)row * rnxp + e);
       }
+    } else {
+      bufA[e * ldw + row] = mk<T>(0, 0);
     }
-    bufA[e * ldw + row] = z;
   }
+  cp_async_wait_all();
   __syncthreads();
   C2<T> *res = smem_fft<T>(bufA, bufB, p, kRows, ldw, tw, even ? 2 : 1, -1);
   const int tot2 = nr * cnxp;
@@ -169,6 +191,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p
     } else {
       X = res[k * ldw + row];
     }
+    X.x *= prescale;  // the transform is linear: scaling the output equals scaling the input
+    X.y *= prescale;
     ((C2<T> *)(base + (long)row * rnxp))[k] = X;
   }
 }
@@ -195,9 +219,14 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet ad
   for (int t = threadIdx.x; t < nxp; t += blockDim.x) tw[t] = twg[t];
   for (int t = threadIdx.x; t < nr * cnxp; t += blockDim.x) {
     int row = t / cnxp, k = t - row * cnxp;
-    C2<T> x = ((const C2<T> *)(base + (long)row * rnxp))[k];
-    if (k == 0 || (even && k == cnxp - 1)) x.y = 0;  // rfftw_c2hc drops these
-    S[row * cnxp + k] = x;
+    cp_async_elem<T>(&S[row * cnxp + k], (const C2<T> *)(base + (long)row * rnxp) + k);
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  // rfftw_c2hc keeps only the real part of the DC and (even nxp) Nyquist bins
+  for (int row = threadIdx.x; row < nr; row += blockDim.x) {
+    S[row * cnxp].y = (T)0;
+    if (even) S[row * cnxp + cnxp - 1].y = (T)0;
   }
   __syncthreads();
   const int tot = kRows * m;

@@ -898,6 +898,9 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       TraceScope ts("k_invert_fused_fp64", st, fbytes);
       k_invert_fused<T, NT, 2><<<grid, threads, 0, st>>>(a);
     } else if (precision == CG_PREC_MIXED) {
+      // the queue position counter starts at zero for every inversion (stream ordered)
+      cudaError_t me = cudaMemsetAsync(w->counters, 0, sizeof(int), st);
+      if (me != cudaSuccess) return cuda_status(me, "queue reset");
       {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
         if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);

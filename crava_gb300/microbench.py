@@ -36,9 +36,20 @@ def invert_case(a):
         inv.run(a.form)
 
 
+def batch_case(a):
+    from . import synthetic as S
+    if not hasattr(a, "_batch"):
+        scs = S.config2(a.ncubes)
+        a._batch = api.Batch(scs, nstreams=a.streams)
+    a._batch.reset()
+    a._batch.run(a.form, use_graph=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["fft", "invert"])
+    ap.add_argument("what", choices=["fft", "invert", "batch"])
+    ap.add_argument("--ncubes", type=int, default=64)
+    ap.add_argument("--streams", type=int, default=8)
     ap.add_argument("--nxp", type=int, default=256)
     ap.add_argument("--nyp", type=int, default=256)
     ap.add_argument("--nzp", type=int, default=64)
@@ -47,8 +58,30 @@ def main():
     ap.add_argument("--form", default="mixed")
     a = ap.parse_args()
     _native.lib()
-    run = fft_case if a.what == "fft" else invert_case
-    run(argparse.Namespace(**{**vars(a), "reps": 1}))  # warm-up (plans, twiddles)
+    if a.what == "batch":
+        # graph replays: time the whole batch with CUDA events
+        batch_case(a)  # warm-up and capture
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(a.reps):
+            a._batch.reset()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            a._batch.run(a.form, use_graph=True)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        bins = a._batch.bins
+        best = min(ms)
+        print(json.dumps({"case": {k: v for k, v in vars(a).items() if not k.startswith("_")}, "bins": bins,
+                          "ms_per_batch": ms, "Mbins_per_s": bins / (best * 1e-3) / 1e6}))
+        return
+    run = {"fft": fft_case, "invert": invert_case, "batch": batch_case}[a.what]
+    if a.what == "batch":
+        run(a)  # warm-up and graph capture on the same batch
+    else:
+        run(argparse.Namespace(**{**vars(a), "reps": 1}))  # warm-up (plans, twiddles)
     torch.cuda.synchronize()
     _native.trace_enable(True)
     run(a)
@@ -56,7 +89,8 @@ def main():
     _native.trace_enable(False)
     out = {k: {"launches": v[0], "ms_per_launch": v[1] / v[0], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
            for k, v in tr.items()}
-    print(json.dumps({"case": vars(a), "kernels": out}))
+    case = {k: v for k, v in vars(a).items() if not k.startswith("_")}
+    print(json.dumps({"case": case, "kernels": out}))
 
 
 if __name__ == "__main__":

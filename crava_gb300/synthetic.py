@@ -32,9 +32,25 @@ matching how CRAVA turns S/N into an error variance, src/crava.cpp:462-465).
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
+
+try:  # multi-threaded transforms for the input generator when scipy is present
+    import scipy.fft as _sfft
+
+    def _fftn(a):
+        return _sfft.fftn(a, norm="ortho", workers=os.cpu_count() or 1)
+
+    def _ifftn(a):
+        return _sfft.ifftn(a, norm="ortho", workers=os.cpu_count() or 1)
+except ImportError:  # pragma: no cover
+    def _fftn(a):
+        return np.fft.fftn(a, norm="ortho")
+
+    def _ifftn(a):
+        return np.fft.ifftn(a, norm="ortho")
 
 LN_VP, LN_VS, LN_RHO = math.log(3000.0), math.log(1500.0), math.log(2.3)
 
@@ -232,8 +248,8 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     z = []
     for _ in range(3):
         w = rng.standard_normal((nzp, nyp, nxp))
-        f = np.fft.fftn(w, norm="ortho") * np.sqrt(c3)
-        z.append(np.real(np.fft.ifftn(f, norm="ortho")))
+        f = _fftn(w) * np.sqrt(c3)
+        z.append(np.real(_ifftn(f)))
     mu = np.array([LN_VP, LN_VS, LN_RHO])
     truth = [mu[p] + sum(L0[p, q] * z[q] for q in range(3)) for p in range(3)]
 
@@ -241,13 +257,13 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     # d^ = kD(k) conj(W(k)) A m^  (src/crava.cpp:1349-1351), white noise on top
     kk = np.arange(nzp)
     kD = -1.0 + np.exp(2j * np.pi * kk / nzp)  # FFT of {-1 at 0, +1 at nzp-1}
-    M = [np.fft.fftn(truth[p] - mu[p], norm="ortho") for p in range(3)]
+    M = [_fftn(truth[p] - mu[p]) for p in range(3)]
     data = []
     snr = sn if np.ndim(sn) else [sn] * n
     for l in range(n):
         W = np.fft.fft(wav[l].astype(np.float64))
         op = (kD * np.conj(W))[:, None, None]
-        s = np.real(np.fft.ifftn(op * sum(float(A[l, q]) * M[q] for q in range(3)), norm="ortho"))
+        s = np.real(_ifftn(op * sum(float(A[l, q]) * M[q] for q in range(3))))
         var_s = float(np.var(s))
         noise_sd = math.sqrt(var_s / max(snr[l] - 1.0, 1e-3))
         d = s + rng.standard_normal(s.shape) * noise_sd
@@ -295,3 +311,19 @@ def scaled_config1(nxp, nyp, nzp, seed=20261204, **kw) -> Scenario:
     return make_scenario(max(2, int(nxp / 1.25)), max(2, int(nyp / 1.25)), max(2, int(nzp / 1.25)),
                          [0.0, 10.0, 20.0, 30.0, 40.0], 25.0, nxp=nxp, nyp=nyp, nzp=nzp, sn=3.0,
                          notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=seed, **kw)
+
+
+def config2(ncubes=64, seed=20261205, **kw):
+    """64 independent cubes of uneven size: nx, ny ~ U{32..192}, nz ~ U{64..160},
+    each padded (25 %) to the next 2/3/5/7-smooth size; 2-8 stacks at 0-40 deg,
+    Ricker peak U(15, 45) Hz, S/N U(2, 6), prior stds scaled by U(0.5, 1.5)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for c in range(ncubes):
+        nx, ny = int(rng.integers(32, 193)), int(rng.integers(32, 193))
+        nz = int(rng.integers(64, 161))
+        nt = int(rng.integers(2, 9))
+        theta = list(np.linspace(0.0, 40.0, nt)) if nt > 1 else [20.0]
+        out.append(make_scenario(nx, ny, nz, theta, float(rng.uniform(15, 45)), sn=float(rng.uniform(2, 6)),
+                                 std_scale=float(rng.uniform(0.5, 1.5)), seed=seed + 1 + c, **kw))
+    return out

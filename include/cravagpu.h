@@ -189,9 +189,10 @@ void cg_workspace_destroy(cg_workspace ws);
 /* Upload the model and build the per-k tables (synchronous). */
 int cg_workspace_set_model(cg_workspace ws, const cg_model *model);
 
-/* Counters since the last reset: bins queued for FP64, bins whose Cholesky
- * failed (they keep the prior, like lib_matrCholCpx failures in the
- * reference, src/crava.cpp:1421-1423), queue overflows.  Synchronises. */
+/* Counters: bins queued for FP64 by the last mixed-precision inversion, and,
+ * since the last reset, bins whose Cholesky failed (they keep the prior, like
+ * lib_matrCholCpx failures in the reference, src/crava.cpp:1421-1423) and
+ * queue overflows.  Synchronises. */
 int cg_workspace_stats(cg_workspace ws, int *flagged, int *failed, int *overflow);
 int cg_workspace_reset_stats(cg_workspace ws, void *stream);
 
@@ -258,6 +259,36 @@ int cg_inversion_run_host(cg_inversion inv, float *const *seis_data, float *cons
 
 /* Counters of the last runs (see cg_workspace_stats). */
 int cg_inversion_stats(cg_inversion inv, int *flagged, int *failed, int *overflow);
+
+/* ========================================================================
+ * Batches of independent inversions of uneven size: each cube's whole
+ * computePostMeanResidAndFFTCov (fused form) queued on one of several streams
+ * forked from the caller's stream, optionally captured once into a CUDA graph
+ * and replayed.  (The reference inverts one cube per run of the program.)
+ * ======================================================================== */
+typedef struct cg_batch_s *cg_batch;
+
+typedef struct cg_batch_cube {
+  int nx, ny, nz, nxp, nyp, nzp;
+  cg_inversion_model model;     /* host arrays, read during cg_batch_create only */
+} cg_batch_cube;
+
+/* Allocates every cube's device grids, pristine input copies and model. */
+int cg_batch_create(cg_batch *batch, const cg_batch_cube *cubes, int ncubes, int nstreams);
+void cg_batch_destroy(cg_batch batch);
+/* Upload cube i's real-domain inputs (host, rsize floats each) as its pristine copy. */
+int cg_batch_load(cg_batch batch, int i, const float *const *seis_data, const float *const *mean);
+/* Working grids <- pristine inputs, queued on `stream`. */
+int cg_batch_reset(cg_batch batch, void *stream);
+/* One inversion of every cube, ordered after earlier work on `stream` and
+ * before later work on it.  form 1 = fused FP32, 2 = fused mixed.  use_graph:
+ * the first call runs once uncaptured (creating transform tables), captures
+ * the batch into a CUDA graph and launches it; later calls launch the graph. */
+int cg_batch_run(cg_batch batch, int form, int use_graph, void *stream);
+/* Copy cube i's results to host buffers (any may be NULL); synchronises. */
+int cg_batch_read(cg_batch batch, int i, float *const *post_mean, float *const *resid, float *const *post_cov);
+/* Total frequency bins of the batch (sum of cnxp*nyp*nzp). */
+long cg_batch_bins(cg_batch batch);
 
 /* ========================================================================
  * Posterior simulation (Crava::simulate, src/crava.cpp:1551-1734).
