@@ -129,16 +129,18 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + N * W;
-  // full tiles: (x < nfull, y = batch row); grid column x == nfull holds the
-  // tail tiles, y = group of W batch rows (CTAs past the last group exit)
+  // full tiles: (x < nfull, y = batch row); grid columns x >= nfull hold the
+  // tail tiles, numbered (x - nfull)*nbatch + y (CTAs past the last one exit)
   long by, bx, cstride;
   int cvalid;
   float2 *cube = (float2 *)cs.ptr[blockIdx.z];
   if ((int)blockIdx.x < g.nfull) {
     by = g.batch_stride; bx = W; cstride = 1; cvalid = W;
   } else {
+    // tail tile tt = (x - nfull)*nbatch + y, tt < ntail*groups
     const int groups = (g.nbatch + W - 1) / W;
-    const int tcol = (int)blockIdx.y / groups, grp = (int)blockIdx.y % groups;
+    const int tt = ((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
+    const int tcol = tt / groups, grp = tt % groups;
     if (tcol >= g.ntail) return;
     cube += (long)g.nfull * W + tcol;
     by = 0; bx = 0; cstride = g.batch_stride;
@@ -168,6 +170,95 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs,
       if (c < cvalid) base[(long)e * axis_stride + (long)c * cstride] = buf[e * W + c];
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// persistent, double-buffered column pass: CTA b handles tiles b, b+G, b+2G...
+// of a linear tile list (per cube: nbatch*nfull full tiles, then ntail*groups
+// gathered tail tiles); the next tile is prefetched with cp.async while the
+// current one is transformed and stored.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int PENDING>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(PENDING) : "memory"); }
+
+struct TileRef {
+  float2 *base;
+  long cstride;
+  int cvalid;
+};
+
+template <int W>
+__device__ __forceinline__ TileRef cols_tile(const CubeSet &cs, const ColsGeom &g, int t)
+{
+  const int groups = (g.nbatch + W - 1) / W;
+  const int per_cube = g.nbatch * g.nfull + g.ntail * groups;
+  const int z = t / per_cube, r = t - z * per_cube;
+  float2 *cube = (float2 *)cs.ptr[z];
+  TileRef ref;
+  if (r < g.nbatch * g.nfull) {
+    const int y = r / g.nfull, x = r - y * g.nfull;
+    ref.base = cube + (long)y * g.batch_stride + (long)x * W;
+    ref.cstride = 1;
+    ref.cvalid = W;
+  } else {
+    const int q = r - g.nbatch * g.nfull;
+    const int tcol = q / groups, grp = q - tcol * groups;
+    ref.base = cube + (long)g.nfull * W + tcol + (long)grp * W * g.batch_stride;
+    ref.cstride = g.batch_stride;
+    ref.cvalid = g.nbatch - grp * W;
+  }
+  return ref;
+}
+
+template <int N, int W>
+__device__ __forceinline__ void cols_prefetch(float2 *buf, const TileRef &ref, long axis_stride)
+{
+#pragma unroll
+  for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
+    const int t = t0 + threadIdx.x;
+    if ((N * W) % kFFTThreads == 0 || t < N * W) {
+      const int e = t / W, c = t % W;
+      if (c < ref.cvalid) cp_async8(&buf[e * W + c], &ref.base[(long)e * axis_stride + (long)c * ref.cstride]);
+      else buf[e * W + c] = make_float2(0.f, 0.f);
+    }
+  }
+}
+
+template <int N, int W, int MINB>
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_pipe(CubeSet cs, const float2 *__restrict__ twg,
+                                                                     ColsGeom g, int ntiles, int sign)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf0 = (float2 *)smem_raw;
+  float2 *buf1 = buf0 + N * W;
+  float2 *tw = buf1 + N * W;
+  for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
+  int tile = blockIdx.x;
+  if (tile < ntiles) cols_prefetch<N, W>(buf0, cols_tile<W>(cs, g, tile), g.axis_stride);
+  cp_async_commit();
+  for (int it = 0; tile < ntiles; it++) {
+    float2 *cur = (it & 1) ? buf1 : buf0;
+    float2 *nxt = (it & 1) ? buf0 : buf1;
+    const int next = tile + gridDim.x;
+    if (next < ntiles) cols_prefetch<N, W>(nxt, cols_tile<W>(cs, g, next), g.axis_stride);
+    cp_async_commit();
+    cp_async_wait<1>();  // the current tile's copies are done; the next tile's may be in flight
+    __syncthreads();
+    cstages<float, N, W, W, 1>(cur, tw, sign);
+    const TileRef ref = cols_tile<W>(cs, g, tile);
+#pragma unroll
+    for (int t0 = 0; t0 < N * W; t0 += kFFTThreads) {
+      const int t = t0 + threadIdx.x;
+      if ((N * W) % kFFTThreads == 0 || t < N * W) {
+        const int e = t / W, c = t % W;
+        if (c < ref.cvalid) ref.base[(long)e * g.axis_stride + (long)c * ref.cstride] = cur[e * W + c];
+      }
+    }
+    __syncthreads();  // cur is refilled by the prefetch two iterations on
+    tile = next;
+  }
+  cp_async_wait<0>();
 }
 
 // ---------------------------------------------------------------------------

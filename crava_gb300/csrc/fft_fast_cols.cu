@@ -38,14 +38,60 @@ int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long ba
   g.ntail = ncols - g.nfull * kW;
   g.nbatch = nbatch;
   const int groups = ceil_div(nbatch, kW);
-  if (g.ntail > 0 && g.ntail * groups > nbatch) {
-    set_error("column tail does not fit the launch grid");
-    return CG_ERR_STATE;
-  }
-  dim3 grid(g.nfull + (g.ntail > 0 ? 1 : 0), nbatch, ncubes);
+  const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
+  dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
   TraceScope ts("k_fft_cols_fast", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
   k_fft_cols_fast<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
   CG_CHECK_LAUNCH("k_fft_cols_fast");
+  return 1;
+}
+
+// persistent double-buffered variant: one CTA per resident slot, each walking
+// the tile list.  CRAVA_COLS_PIPE=0|1 selects it (tuning sweep).
+bool use_pipe()
+{
+  static int v = -1;
+  if (v < 0) {
+    const char *e = getenv("CRAVA_COLS_PIPE");
+    v = (e && e[0] == '0') ? 0 : 1;
+  }
+  return v == 1;
+}
+
+template <int N, int MINB>
+int launch_pipe(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+                const float2 *tw, cudaStream_t st)
+{
+  const size_t smem = (2 * (size_t)N * kW + N) * sizeof(float2);
+  static bool attr_set[64] = {};
+  static int slots[64] = {};
+  cudaError_t e = smem_limit_once(k_fft_cols_pipe<N, kW, MINB>, smem, attr_set);
+  if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_pipe attribute");
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  int &nslots = slots[dev < 64 ? dev : 0];
+  if (nslots == 0) {
+    int per_sm = 0, nsm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_pipe<N, kW, MINB>, kFFTThreads,
+                                                           smem)) != cudaSuccess)
+      return cuda_status(e, "occupancy");
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return cuda_status(e, "SM count");
+    nslots = (per_sm > 0 ? per_sm : 1) * nsm;
+  }
+  ColsGeom g;
+  g.axis_stride = axis_stride;
+  g.batch_stride = batch_stride;
+  g.nfull = ncols / kW;
+  g.ntail = ncols - g.nfull * kW;
+  g.nbatch = nbatch;
+  const long groups = ceil_div(nbatch, kW);
+  const long ntiles = (long)ncubes * ((long)nbatch * g.nfull + (long)g.ntail * groups);
+  if (ntiles > 0x7fffffffL) { set_error("too many column tiles"); return CG_ERR_UNSUPPORTED; }
+  const int grid = (int)(ntiles < nslots ? ntiles : nslots);
+  TraceScope ts("k_fft_cols_pipe", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
+  k_fft_cols_pipe<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, (int)ntiles, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_pipe");
   return 1;
 }
 
@@ -53,6 +99,10 @@ template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
+  if (use_pipe()) {
+    if (minb_for(N) == 3) return launch_pipe<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    return launch_pipe<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  }
   if (minb_for(N) == 3) return launch_v<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   return launch_v<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
 }

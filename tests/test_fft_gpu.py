@@ -28,7 +28,9 @@ def test_fft_matches_reference_fftw(cuda, case):
 
 
 SIZES = [(80, 80, 160), (16, 12, 20), (15, 9, 7), (21, 15, 35), (49, 27, 25), (128, 1, 1), (1, 64, 1),
-         (2, 2, 2), (200, 100, 8), (98, 54, 45), (256, 16, 24), (7, 5, 3), (64, 343, 10)]
+         (2, 2, 2), (200, 100, 8), (98, 54, 45), (256, 16, 24), (7, 5, 3), (64, 343, 10),
+         # specialised axes with one batch row and a column tail (2D / 1D prior-spectrum transforms)
+         (80, 64, 1), (256, 256, 1), (100, 1, 128), (48, 1, 1)]
 
 
 @pytest.mark.parametrize("dims", SIZES)
