@@ -101,8 +101,29 @@ def lib():
             raise RuntimeError(f"{LIB_PATH} is missing: run crava_gb300.build() (needs nvcc)")
         L = ct.CDLL(LIB_PATH)
         _declare(L)
+        _apply_tuning(L)
         _lib = L
     return _lib
+
+
+TUNING_PATH = os.path.join(PKG, "tuning.json")
+
+
+def _apply_tuning(L):
+    """Load the autotuner's choices (crava_gb300/autotune.py) into the library."""
+    if not os.path.exists(TUNING_PATH):
+        return
+    import json
+    try:
+        with open(TUNING_PATH) as f:
+            t = json.load(f)
+        for n, v in t.get("cols", {}).items():
+            L.cg_tune_set(1, int(n), int(v["pipe"]))
+            L.cg_tune_set(0, int(n), int(v["minb"]))
+        for n, v in t.get("bin", {}).items():
+            L.cg_tune_set(2, int(n), int(v["minb"]))
+    except (OSError, ValueError, KeyError):
+        pass  # a damaged table leaves the built-in defaults
 
 
 def _declare(L):
@@ -154,6 +175,9 @@ def _declare(L):
         "cg_batch_run": ([V, I, I, V], I),
         "cg_batch_read": ([V, I, PP, PP, PP], I),
         "cg_batch_bins": ([V], ct.c_long),
+        "cg_tune_set": ([I, I, I], I),
+        "cg_tune_get": ([I, I], I),
+        "cg_tune_clear": ([], I),
         "cg_trace_enable": ([I], I),
         "cg_trace_collect": ([], I),
         "cg_trace_entry": ([I, ct.c_char_p, I, ct.POINTER(ct.c_long), ct.POINTER(D), ct.POINTER(D)], I),

@@ -1,0 +1,108 @@
+"""Measure the launch variants of the hot kernels on this GPU and store the winners.
+
+    python -m crava_gb300.autotune [--out crava_gb300/tuning.json]
+
+Candidates (see cg_tune_set in include/cravagpu.h):
+  * column transform pass, per axis length: resident-CTA target 2 or 3, and
+    the plain or the persistent double-buffered kernel;
+  * fused bin kernel, per stack count: unconstrained or 85-register build.
+Each candidate is timed with the library's launch tracer (CUDA events on the
+launch stream) on cubes larger than L2; the fastest is kept.  The loader
+(crava_gb300._native.lib) applies tuning.json when it is present.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+import torch
+
+from . import _native, api
+
+KEY_COLS_MINB, KEY_COLS_PIPE, KEY_BIN_MINB = 0, 1, 2
+
+
+def _time_kernels(fn, prefix, reps=3):
+    fn()  # warm-up: tables, attributes
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    for _ in range(reps):
+        fn()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    return sum(v[1] for k, v in tr.items() if k.startswith(prefix)) / reps
+
+
+def tune_cols(lengths, L):
+    out = {}
+    for n in lengths:
+        g = torch.Generator(device="cuda").manual_seed(n)
+        nxp = 256
+        cubes = [torch.randn((n, n, nxp + 2), device="cuda", generator=g) for _ in range(3)]
+
+        def run():
+            api.fft_in_place_batch(cubes, nxp, api.DATA)
+            api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
+        best = None
+        for pipe in (0, 1):
+            for minb in (2, 3):
+                L.cg_tune_set(KEY_COLS_PIPE, n, pipe)
+                L.cg_tune_set(KEY_COLS_MINB, n, minb)
+                ms = _time_kernels(run, "k_fft_cols")
+                if best is None or ms < best[0]:
+                    best = (ms, pipe, minb)
+        L.cg_tune_set(KEY_COLS_PIPE, n, best[1])
+        L.cg_tune_set(KEY_COLS_MINB, n, best[2])
+        out[str(n)] = {"pipe": best[1], "minb": best[2], "ms": round(best[0], 4)}
+        del cubes
+        torch.cuda.empty_cache()
+    return out
+
+
+def tune_bin(ntheta_list, L):
+    from . import synthetic as S
+    from .pipeline import Inversion
+    out = {}
+    for nt in ntheta_list:
+        sc = S.make_scenario(160, 160, 160, [40.0 * i / max(nt - 1, 1) for i in range(nt)], 25.0, nxp=200, nyp=200,
+                             nzp=200, sn=3.0, seed=nt)
+        inv = Inversion(sc, forms=("mixed",))
+
+        def run():
+            inv.restore("mixed")
+            inv.run("mixed")
+        best = None
+        for minb in (1, 6):
+            L.cg_tune_set(KEY_BIN_MINB, nt, minb)
+            ms = _time_kernels(run, "k_invert_fused")
+            if best is None or ms < best[0]:
+                best = (ms, minb)
+        L.cg_tune_set(KEY_BIN_MINB, nt, best[1])
+        out[str(nt)] = {"minb": best[1], "ms": round(best[0], 4)}
+        del inv
+        torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json"))
+    ap.add_argument("--lengths", default="128,160,192,200,240,256")
+    ap.add_argument("--ntheta", default="3,5,8")
+    a = ap.parse_args()
+    L = _native.lib()
+    L.cg_tune_clear()
+    t0 = time.time()
+    cols = tune_cols([int(x) for x in a.lengths.split(",")], L)
+    binr = tune_bin([int(x) for x in a.ntheta.split(",")], L)
+    res = {"device": torch.cuda.get_device_name(0), "cols": cols, "bin": binr,
+           "tuning_seconds": round(time.time() - t0, 1)}
+    with open(a.out, "w") as f:
+        json.dump(res, f, indent=1)
+    print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -2,6 +2,7 @@
 #include <cstdlib>
 
 #include "fft_fast.cuh"
+#include "tuning.cuh"
 #include "trace.cuh"
 
 namespace cg {
@@ -9,19 +10,9 @@ namespace cg {
 namespace {
 constexpr int kW = 16;
 
-// Resident-CTA target per length: 3 for lengths up to 256 (measured faster
-// at 256 despite a small spill), 2 above.  CRAVA_COLS_MINB=2|3 forces
-// one variant (used by the tuning sweep in crava_gb300.microbench).
-int minb_for(int n)
-{
-  static int forced = -1;
-  if (forced < 0) {
-    const char *e = getenv("CRAVA_COLS_MINB");
-    forced = (e && (e[0] == '2' || e[0] == '3')) ? e[0] - '0' : 0;
-  }
-  if (forced) return forced;
-  return n <= 256 ? 3 : 2;
-}
+// Resident-CTA target per length (tuning key CG_TUNE_COLS_MINB): 3 for lengths
+// up to 256 (measured faster at 256 despite a small spill), 2 above.
+int minb_for(int n) { return cg_tune_get(CG_TUNE_COLS_MINB, n); }
 
 template <int N, int MINB>
 int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
@@ -47,16 +38,9 @@ int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long ba
 }
 
 // persistent double-buffered variant: one CTA per resident slot, each walking
-// the tile list.  CRAVA_COLS_PIPE=0|1 selects it (tuning sweep).
-bool use_pipe()
-{
-  static int v = -1;
-  if (v < 0) {
-    const char *e = getenv("CRAVA_COLS_PIPE");
-    v = (e && e[0] == '0') ? 0 : 1;
-  }
-  return v == 1;
-}
+// the tile list (tuning key CG_TUNE_COLS_PIPE).  Off by default: on GB300 it
+// measured 25-30 % slower than one CTA per tile at lengths 200 and 256.
+bool use_pipe(int n) { return cg_tune_get(CG_TUNE_COLS_PIPE, n) == 1; }
 
 template <int N, int MINB>
 int launch_pipe(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
@@ -99,7 +83,7 @@ template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
-  if (use_pipe()) {
+  if (use_pipe(N)) {
     if (minb_for(N) == 3) return launch_pipe<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     return launch_pipe<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   }

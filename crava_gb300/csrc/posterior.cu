@@ -846,22 +846,12 @@ extern "C" int cg_prior_spectra(cg_workspace w, const float *corr_xy, const floa
   return prior_tables<float>(w, corr_xy, circ_corr_t, w->cxy_f, w->ct_f, st);
 }
 
-// Occupancy variant of the FP32 fused kernels.  Measured at 256^3 with five
-// stacks, capping registers for 6 resident CTAs (85 registers) is 1.34x
-// faster than the unconstrained build despite a small spill; with six or more
-// stacks the cap spills heavily, so those keep the unconstrained build.
-// CRAVA_BIN_MINB=1|6 forces one (used by the tuning sweep in
-// crava_gb300.microbench).
-static int bin_minb(int ntheta)
-{
-  static int forced = -1;
-  if (forced < 0) {
-    const char *e = getenv("CRAVA_BIN_MINB");
-    forced = (e && e[0] == '6') ? 6 : (e && e[0] == '1') ? 1 : 0;
-  }
-  if (forced) return forced;
-  return ntheta <= 5 ? 6 : 1;
-}
+// Occupancy variant of the FP32 fused kernels (tuning key CG_TUNE_BIN_MINB).
+// Measured at 256^3 with five stacks, capping registers for 6 resident CTAs
+// (85 registers) is 1.34x faster than the unconstrained build despite a small
+// spill; with six or more stacks the cap spills heavily, so those default to
+// the unconstrained build.
+static int bin_minb(int ntheta) { return cg_tune_get(CG_TUNE_BIN_MINB, ntheta); }
 
 template <typename T>
 static int fused_launch(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision,

@@ -1,0 +1,74 @@
+// Tuning table: launch variants chosen per transform length or stack count.
+// Defaults are built in (measured on GB300); cg_tune_set overrides them, and
+// the environment variables CRAVA_COLS_MINB, CRAVA_COLS_PIPE and
+// CRAVA_BIN_MINB override both (used by ad-hoc sweeps).
+#include <cstdlib>
+#include <map>
+#include <mutex>
+
+#include "common.cuh"
+#include "tuning.cuh"
+
+namespace cg {
+
+namespace {
+std::mutex g_mu;
+std::map<long, int> g_table;  // (key << 32) | n  ->  value, n = 0 for "every n"
+const char *env_name(int key)
+{
+  switch (key) {
+    case CG_TUNE_COLS_MINB: return "CRAVA_COLS_MINB";
+    case CG_TUNE_COLS_PIPE: return "CRAVA_COLS_PIPE";
+    case CG_TUNE_BIN_MINB: return "CRAVA_BIN_MINB";
+    default: return nullptr;
+  }
+}
+}  // namespace
+
+int tune_get(int key, int n, int dflt)
+{
+  const char *en = env_name(key);
+  if (en) {
+    const char *e = getenv(en);
+    if (e && *e) return atoi(e);
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  auto it = g_table.find(((long)key << 32) | (unsigned)n);
+  if (it != g_table.end()) return it->second;
+  it = g_table.find((long)key << 32);
+  if (it != g_table.end()) return it->second;
+  return dflt;
+}
+
+}  // namespace cg
+
+using namespace cg;
+
+extern "C" int cg_tune_set(int key, int n, int value)
+{
+  if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_BIN_MINB || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
+  const bool ok = (key == CG_TUNE_COLS_MINB && (value == 2 || value == 3)) ||
+                  (key == CG_TUNE_COLS_PIPE && (value == 0 || value == 1)) ||
+                  (key == CG_TUNE_BIN_MINB && (value == 1 || value == 6));
+  if (!ok) { set_error("cg_tune_set: value %d not valid for key %d", value, key); return CG_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_table[((long)key << 32) | (unsigned)n] = value;
+  return CG_OK;
+}
+
+extern "C" int cg_tune_clear(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_table.clear();
+  return CG_OK;
+}
+
+extern "C" int cg_tune_get(int key, int n)
+{
+  switch (key) {
+    case CG_TUNE_COLS_MINB: return tune_get(key, n, n <= 256 ? 3 : 2);
+    case CG_TUNE_COLS_PIPE: return tune_get(key, n, 0);
+    case CG_TUNE_BIN_MINB: return tune_get(key, n, n <= 5 ? 6 : 1);
+    default: set_error("cg_tune_get: bad key"); return CG_ERR_ARG;
+  }
+}

@@ -50,6 +50,11 @@ struct cg_batch_s {
   std::vector<cudaStream_t> streams;
   std::vector<cudaEvent_t> join;
   cudaEvent_t fork = nullptr;
+  // graphs are captured on and launched from this stream, ordered after and
+  // before the caller's stream by the two events (the caller's stream may be
+  // the legacy default stream, which cannot be captured)
+  cudaStream_t cap = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int graph_form = -1;
@@ -83,6 +88,9 @@ extern "C" void cg_batch_destroy(cg_batch b)
   for (auto s : b->streams) cudaStreamDestroy(s);
   for (auto e : b->join) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->cap) cudaStreamDestroy(b->cap);
+  if (b->ev_in) cudaEventDestroy(b->ev_in);
+  if (b->ev_out) cudaEventDestroy(b->ev_out);
   delete b;
 }
 
@@ -145,6 +153,9 @@ extern "C" int cg_batch_create(cg_batch *out, const cg_batch_cube *cubes, int nc
         b->join.push_back(e);
       }
       cuda_check(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "batch event");
+      cuda_check(cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking), "batch capture stream");
+      cuda_check(cudaEventCreateWithFlags(&b->ev_in, cudaEventDisableTiming), "batch event");
+      cuda_check(cudaEventCreateWithFlags(&b->ev_out, cudaEventDisableTiming), "batch event");
     } catch (...) {
       cg_batch_destroy(b);
       throw;
@@ -228,20 +239,25 @@ extern "C" int cg_batch_run(cg_batch b, int form, int use_graph, void *stream)
       }
       if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
       if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
-      cuda_check(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+      cuda_check(cudaStreamSynchronize(st), "batch pre-capture");
+      cuda_check(cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeThreadLocal), "begin capture");
       try {
-        queue_batch(b, f, st);
+        queue_batch(b, f, b->cap);
       } catch (...) {
         cudaGraph_t g = nullptr;
-        cudaStreamEndCapture(st, &g);
+        cudaStreamEndCapture(b->cap, &g);
         if (g) cudaGraphDestroy(g);
         throw;
       }
-      cuda_check(cudaStreamEndCapture(st, &b->graph), "end capture");
+      cuda_check(cudaStreamEndCapture(b->cap, &b->graph), "end capture");
       cuda_check(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
       b->graph_form = form;
     }
-    cuda_check(cudaGraphLaunch(b->exec, st), "graph launch");
+    cuda_check(cudaEventRecord(b->ev_in, st), "order in");
+    cuda_check(cudaStreamWaitEvent(b->cap, b->ev_in, 0), "order in wait");
+    cuda_check(cudaGraphLaunch(b->exec, b->cap), "graph launch");
+    cuda_check(cudaEventRecord(b->ev_out, b->cap), "order out");
+    cuda_check(cudaStreamWaitEvent(st, b->ev_out, 0), "order out wait");
     return CG_OK;
   })
 }

@@ -68,3 +68,16 @@ def test_circ_corr_t_matches_oracle(oracle):
     a = S.circ_corr_t(corr, 2, 64)
     b = oracle.circ_corr_t(corr, 2, 64, prec="d")
     assert rel(a, b) < 1e-6
+
+
+def test_tuning_table_defaults_overrides_and_validation(native):
+    native.cg_tune_clear()
+    assert native.cg_tune_get(0, 256) == 3 and native.cg_tune_get(0, 512) == 2   # column-pass CTA target
+    assert native.cg_tune_get(2, 5) == 6 and native.cg_tune_get(2, 8) == 1       # bin-kernel register cap
+    assert native.cg_tune_set(0, 256, 2) == 0
+    assert native.cg_tune_get(0, 256) == 2 and native.cg_tune_get(0, 200) == 3   # per-length entry wins
+    assert native.cg_tune_set(1, 0, 0) == 0 and native.cg_tune_get(1, 128) == 0  # n = 0: every length
+    assert native.cg_tune_set(0, 256, 7) == -1                                    # not a built variant
+    assert native.cg_tune_set(9, 1, 1) == -1
+    native.cg_tune_clear()
+    assert native.cg_tune_get(0, 256) == 3
