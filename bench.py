@@ -57,36 +57,68 @@ def load_traffic():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """SM clock and clock-event reasons of the measured GPU, sampled during the timed region.
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    Samples every 10 ms from a separate process (crava_gb300.clocks, NVML by GPU UUID); falls back to
+    nvidia-smi every 200 ms when NVML cannot be opened.  Read-only: no GPU setting is touched."""
+
+    SMI_FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                  "clocks_event_reasons.sw_power_cap")
+    SMI_NAMES = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
 
     def __init__(self, gpu_index):
         self.gpu = gpu_index
         self.proc = None
+        self.kind = None
         self.lines = []
         self.t = None
+        self.ready = threading.Event()
+
+    def _uuid(self):
+        try:
+            import torch
+            u = str(torch.cuda.get_device_properties(self.gpu).uuid)
+            return u if u.startswith("GPU-") else "GPU-" + u
+        except Exception:
+            return None
 
     def start(self):
-        try:
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except Exception:
-            self.proc = None
-            return
-        self.t = threading.Thread(target=self._read, daemon=True)
-        self.t.start()
+        uuid = self._uuid()
+        cmds = []
+        if uuid:
+            cmds.append(("nvml", [sys.executable, "-m", "crava_gb300.clocks", "--uuid", uuid, "--interval-ms", "10"]))
+        cmds.append(("smi", ["nvidia-smi", "-i", uuid or str(self.gpu), f"--query-gpu={self.SMI_FIELDS}",
+                             "--format=csv,noheader,nounits", "-lms", "200"]))
+        for kind, cmd in cmds:
+            try:
+                self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True,
+                                             cwd=REPO)
+            except Exception:
+                self.proc = None
+                continue
+            self.kind = kind
+            self.lines = []
+            self.ready.clear()
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            if self.ready.wait(timeout=20):
+                return
+            self._kill()
+        self.proc = None
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            line = line.strip()
+            if line == "ready":
+                self.ready.set()
+                continue
+            self.lines.append(line)
+            self.ready.set()
 
-    def stop(self):
+    def _kill(self):
         if self.proc is None:
-            return None
+            return
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
@@ -94,24 +126,31 @@ class ClockSampler:
             self.proc.kill()
         if self.t:
             self.t.join(timeout=2)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self._kill()
         sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 9:
-                continue
             try:
-                sm.append(float(parts[1]))
-                mx.append(float(parts[2]))
+                if self.kind == "nvml" and len(parts) == 4:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                    from crava_gb300.clocks import REASONS
+                    bits = int(parts[3])
+                    reasons.update(name for bit, name in REASONS.items() if bits & bit)
+                elif self.kind == "smi" and len(parts) >= 7:
+                    sm.append(float(parts[0]))
+                    mx.append(float(parts[1]))
+                    reasons.update(n for n, v in zip(self.SMI_NAMES, parts[3:7]) if v.lower().startswith("active"))
             except ValueError:
                 continue
-            for name, v in zip(names, parts[5:9]):
-                if v.lower().startswith("active"):
-                    reasons.add(name)
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": "NVML every 10 ms" if self.kind == "nvml" else "nvidia-smi every 200 ms"}
 
 
 def dist_setup():
@@ -268,7 +307,6 @@ def run_ours(args, world, rank, local):
         barrier(world)
         torch.cuda.synchronize()
         results[form] = statistics.mean(ms)
-    clk = clocks.stop()
 
     # accuracy against the FP64 run on the same inputs
     inv.restore("fp64")
@@ -301,43 +339,39 @@ def run_ours(args, world, rank, local):
     dname, (dl, dms, dbytes) = dom
     peak, peak_kind = load_peaks()
     achieved = (dbytes / dl) / (dms / dl * 1e-3) / 1e9 if dms > 0 else 0.0
-    traffic = load_traffic().get(dname)
+    tinfo = load_traffic().get(dname)
+    # DRAM bytes per launch: the ncu read+write / algorithmic ratio of a smaller capture times this launch's
+    # algorithmic bytes (single-pass kernels: traffic scales with the cube size)
+    traffic = None
+    if isinstance(tinfo, dict) and tinfo.get("ratio"):
+        traffic = round(float(tinfo["ratio"]) * dbytes / dl)
 
-    # end to end: pinned host inputs -> device, inversion, results -> host
-    h_data = torch.from_numpy(np.stack(sc.data)).pin_memory()
-    h_mean = torch.from_numpy(np.stack(sc.mean)).pin_memory()
-    shape = tuple(h_data.shape[1:])
-    h_out_mean = torch.empty((3,) + shape, dtype=torch.float32).pin_memory()
-    h_out_res = torch.empty((sc.ntheta,) + shape, dtype=torch.float32).pin_memory()
-    h_out_cov = torch.empty((6,) + shape, dtype=torch.float32).pin_memory()
-    h2d = (h_data.numel() + h_mean.numel()) * 4
-    d2h = (h_out_mean.numel() + h_out_res.numel() + h_out_cov.numel()) * 4
+    # end to end through the C-ABI host entry point (cg_inversion_run_host, the call the reference's
+    # Crava::computePostMeanResidAndFFTCov shim makes): pinned host cubes in, residual, covariance and
+    # posterior-mean cubes out, every host<->device copy inside the timed call.  The call overwrites its
+    # inputs (as the reference loop does), so each step starts from a pristine host copy, restored
+    # outside the timed region.
+    hinv = api.HostInversion(sc)
+    pristine = [torch.from_numpy(np.ascontiguousarray(x)).pin_memory() for x in list(sc.data) + list(sc.mean)]
+    work = [torch.empty_like(x).pin_memory() for x in pristine]
+    h_cov = [torch.empty_like(pristine[0]).pin_memory() for _ in range(6)]
+    h2d = sum(x.numel() for x in pristine) * 4
+    d2h = (len(pristine) + 6) * pristine[0].numel() * 4
 
     def e2e_step():
-        for l in range(sc.ntheta):
-            inv.data[l].copy_(h_data[l], non_blocking=True)
-        for p in range(3):
-            inv.mean[p].copy_(h_mean[p], non_blocking=True)
-        inv.run("mixed")
-        for p in range(3):
-            h_out_mean[p].copy_(inv.mean[p], non_blocking=True)
-        for l in range(sc.ntheta):
-            h_out_res[l].copy_(inv.data[l], non_blocking=True)
-        for t in range(6):
-            h_out_cov[t].copy_(inv.cov[t], non_blocking=True)
+        for w, p0 in zip(work, pristine):
+            w.copy_(p0)
+        t0 = time.perf_counter()
+        hinv.run(work[:sc.ntheta], work[sc.ntheta:], h_cov, "mixed")
+        return (time.perf_counter() - t0) * 1e3
 
     for _ in range(args.warmup):
         e2e_step()
     torch.cuda.synchronize()
     barrier(world)
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    a.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    b.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = a.elapsed_time(b) / args.steps
+    e2e_ms = sum(e2e_step() for _ in range(args.steps)) / args.steps
+    hinv.close()
+    clk = clocks.stop()  # sampled from the first timed form step to the last end-to-end step
 
     ms_mixed = max_over_ranks(results["mixed"], world)
     ms_plain = max_over_ranks(results["plain"], world)

@@ -122,6 +122,8 @@ def _apply_tuning(L):
             L.cg_tune_set(0, int(n), int(v["minb"]))
         for n, v in t.get("bin", {}).items():
             L.cg_tune_set(2, int(n), int(v["minb"]))
+        for n, v in t.get("rows", {}).items():
+            L.cg_tune_set(3, int(n), int(v["kernel"]))
     except (OSError, ValueError, KeyError):
         pass  # a damaged table leaves the built-in defaults
 

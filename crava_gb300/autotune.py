@@ -4,7 +4,9 @@
 
 Candidates (see cg_tune_set in include/cravagpu.h):
   * column transform pass, per axis length: resident-CTA target 2 or 3, and
-    the plain or the persistent double-buffered kernel;
+    the staged (0), persistent double-buffered (1), register-direct (2) or
+    four-step (3) kernel;
+  * x-row pass, per half length nxp/2: staged (0) or four-step (1) kernel;
   * fused bin kernel, per stack count: unconstrained or 85-register build.
 Each candidate is timed with the library's launch tracer (CUDA events on the
 launch stream) on cubes larger than L2; the fastest is kept.  The loader
@@ -21,7 +23,7 @@ import torch
 
 from . import _native, api
 
-KEY_COLS_MINB, KEY_COLS_PIPE, KEY_BIN_MINB = 0, 1, 2
+KEY_COLS_MINB, KEY_COLS_PIPE, KEY_BIN_MINB, KEY_ROWS = 0, 1, 2, 3
 
 
 def _time_kernels(fn, prefix, reps=3):
@@ -46,7 +48,7 @@ def tune_cols(lengths, L):
             api.fft_in_place_batch(cubes, nxp, api.DATA)
             api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
         best = None
-        for pipe in (0, 1):
+        for pipe in (0, 1, 2, 3):
             for minb in (2, 3):
                 L.cg_tune_set(KEY_COLS_PIPE, n, pipe)
                 L.cg_tune_set(KEY_COLS_MINB, n, minb)
@@ -56,6 +58,29 @@ def tune_cols(lengths, L):
         L.cg_tune_set(KEY_COLS_PIPE, n, best[1])
         L.cg_tune_set(KEY_COLS_MINB, n, best[2])
         out[str(n)] = {"pipe": best[1], "minb": best[2], "ms": round(best[0], 4)}
+        del cubes
+        torch.cuda.empty_cache()
+    return out
+
+
+def tune_rows(halves, L):
+    out = {}
+    for m in halves:
+        g = torch.Generator(device="cuda").manual_seed(m)
+        nxp = 2 * m
+        cubes = [torch.randn((128, 256, nxp + 2), device="cuda", generator=g) for _ in range(3)]
+
+        def run():
+            api.fft_in_place_batch(cubes, nxp, api.DATA)
+            api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
+        best = None
+        for kern in (0, 1):
+            L.cg_tune_set(KEY_ROWS, m, kern)
+            ms = _time_kernels(run, ("k_r2c_rows", "k_c2r_rows"))
+            if best is None or ms < best[0]:
+                best = (ms, kern)
+        L.cg_tune_set(KEY_ROWS, m, best[1])
+        out[str(m)] = {"kernel": best[1], "ms": round(best[0], 4)}
         del cubes
         torch.cuda.empty_cache()
     return out
@@ -91,13 +116,15 @@ def main():
     ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json"))
     ap.add_argument("--lengths", default="128,160,192,200,240,256")
     ap.add_argument("--ntheta", default="3,5,8")
+    ap.add_argument("--halves", default="64,100,128,200,256")
     a = ap.parse_args()
     L = _native.lib()
     L.cg_tune_clear()
     t0 = time.time()
     cols = tune_cols([int(x) for x in a.lengths.split(",")], L)
+    rows = tune_rows([int(x) for x in a.halves.split(",")], L)
     binr = tune_bin([int(x) for x in a.ntheta.split(",")], L)
-    res = {"device": torch.cuda.get_device_name(0), "cols": cols, "bin": binr,
+    res = {"device": torch.cuda.get_device_name(0), "cols": cols, "rows": rows, "bin": binr,
            "tuning_seconds": round(time.time() - t0, 1)}
     with open(a.out, "w") as f:
         json.dump(res, f, indent=1)

@@ -1,0 +1,367 @@
+// Four-step FFT passes: a length-N transform split as N = N1 x N2 and done
+// mostly in registers.
+//
+//   x[n], n = N2*n1 + n2        X[k], k = k1 + N1*k2
+//   X[k1 + N1*k2] = sum_n2 W_N2^(n2 k2) * [ W_N^(n2 k1) * sum_n1 x[N2 n1 + n2] W_N1^(n1 k1) ]
+//
+// Pass 1: one thread per (line, n2) loads its N1 inputs straight from global
+// memory, does the N1-point DFT in registers and the W_N^(n2 k1) twiddles, and
+// writes the N1 results to shared memory.  Pass 2: one thread per (line, k1)
+// reads N2 values back, does the N2-point DFT in registers and stores the
+// outputs straight to global memory.  Every element crosses shared memory
+// once (one write, one read) instead of once per Stockham stage, which is what
+// bounds the staged kernels in fft_fast.cuh.
+//
+// The in-register DFTs are fully unrolled Stockham plans (radices 8, 4, 2, 3,
+// 5, 7 as in make_axis_plan): every index is a compile-time constant, so the
+// stage permutations are register renames.  Twiddles come from the same
+// forward table as the other kernels (W_L^t for the table length L), staged
+// in shared memory.
+#pragma once
+
+#include "fft_fast.cuh"
+
+namespace cg {
+
+// all stages of a length-N DFT held in v[]; tw[m*TWS] = W_N^m (forward table)
+template <typename T, int N, int TWS, int S = 0, int NS = 1>
+__device__ __forceinline__ void reg_fft(C2<T> *v, int sign, const C2<T> *tw)
+{
+  if constexpr (S < plan_nstages(N)) {
+    constexpr int R = plan_radix(N, S);
+    constexpr int NB = N / R;
+    constexpr int SPAN = N / (NS * R);
+    C2<T> w[N];
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+      C2<T> a[R];
+#pragma unroll
+      for (int r = 0; r < R; r++) a[r] = v[j + r * NB];
+      const int jm = j % NS;
+      if (NS > 1 && jm > 0) {
+#pragma unroll
+        for (int r = 1; r < R; r++) a[r] = cmul<T>(a[r], tw_at<T>(tw, jm * r * SPAN * TWS, sign));
+      }
+      dft_any<T, R>(a, sign, tw, NB * TWS);
+      const int d = (j - jm) * R + jm;
+#pragma unroll
+      for (int r = 0; r < R; r++) w[d + r * NS] = a[r];
+    }
+#pragma unroll
+    for (int i = 0; i < N; i++) v[i] = w[i];
+    reg_fft<T, N, TWS, S + 1, NS * R>(v, sign, tw);
+  }
+}
+
+// N1: the smallest divisor of N not below sqrt(N) (both factors stay small
+// enough for registers; N1 is even for every specialised length)
+__host__ __device__ constexpr int fs_n1(int n)
+{
+  for (int d = 1; d <= n; d++)
+    if (n % d == 0 && d * d >= n) return d;
+  return n;
+}
+
+// column tile width: 16 columns when both factors are >= 16 (256 items per
+// pass), else 32
+__host__ __device__ constexpr int fs_cols_w(int n)
+{
+  return (fs_n1(n) >= 16 && n / fs_n1(n) >= 16) ? 16 : 32;
+}
+
+// ---------------------------------------------------------------------------
+// strided column pass.  Tiles and the column tail follow ColsGeom exactly as
+// in k_fft_cols_fast: full tiles of W adjacent columns, then the tail columns
+// gathered W batch rows at a time.
+// Shared layout: buf[(k1*N2 + n2)*W + c] (conflict-free for both passes).
+// ---------------------------------------------------------------------------
+template <int N, int W, int MINB>
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, const float2 *__restrict__ twg,
+                                                                   ColsGeom g, int sign)
+{
+  constexpr int N1 = fs_n1(N), N2 = N / N1;
+  constexpr int P1 = W * N2, P2 = W * N1;
+  constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + N * W;
+  float2 *cube = (float2 *)cs.ptr[blockIdx.z];
+  long cstride;
+  int cvalid;
+  float2 *base;
+  if ((int)blockIdx.x < g.nfull) {
+    base = cube + (long)blockIdx.y * g.batch_stride + (long)blockIdx.x * W;
+    cstride = 1;
+    cvalid = W;
+  } else {
+    const int groups = (g.nbatch + W - 1) / W;
+    const int tt = ((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
+    const int tcol = tt / groups, grp = tt % groups;
+    if (tcol >= g.ntail) return;
+    base = cube + (long)g.nfull * W + tcol + (long)grp * W * g.batch_stride;
+    cstride = g.batch_stride;
+    cvalid = g.nbatch - grp * W;
+  }
+  const long as = g.axis_stride;
+  for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
+  // pass 1, one item at a time (registers hold one item); the first item's
+  // loads are issued before the barrier that publishes the twiddle table
+  auto load1 = [&](int q, float2 *v) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int c = t % W, n2 = t / W;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && c < cvalid;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++)
+      v[n1] = ok ? base[(long)(N2 * n1 + n2) * as + (long)c * cstride] : make_float2(0.f, 0.f);
+  };
+  float2 v[N1];
+  load1(0, v);
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < B1; q++) {
+    if (q > 0) load1(q, v);
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P1 % kFFTThreads == 0 || t < P1) {
+      const int c = t % W, n2 = t / W;
+      reg_fft<float, N1, N2>(v, sign, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw_at<float>(tw, n2 * k1, sign));
+#pragma unroll
+      for (int k1 = 0; k1 < N1; k1++) buf[(k1 * N2 + n2) * W + c] = v[k1];
+    }
+  }
+  __syncthreads();
+  // pass 2
+#pragma unroll
+  for (int q = 0; q < B2; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P2 % kFFTThreads == 0 || t < P2) {
+      const int c = t % W, k1 = t / W;
+      float2 u[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[(k1 * N2 + n2) * W + c];
+      reg_fft<float, N2, N1>(u, sign, tw);
+      if (c < cvalid) {
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) base[(long)(k1 + N1 * k2) * as + (long)c * cstride] = u[k2];
+      }
+    }
+  }
+}
+
+// rows per CTA for the row passes: enough (row, n2) items for 256 threads
+__host__ __device__ constexpr int fs_rows_per_cta(int m) { return kFFTThreads / (m / fs_n1(m)) < 1 ? 1 : kFFTThreads / (m / fs_n1(m)); }
+
+// pitch (float2) of one row's exchange block: >= N2*(N1+1), = 8 mod 16 so the
+// two rows a half-warp touches fall in opposite bank halves
+__host__ __device__ constexpr int fs_row_pitch(int m)
+{
+  const int need = (m / fs_n1(m)) * (fs_n1(m) + 1);
+  return need + ((8 - need % 16) + 16) % 16;
+}
+
+// ---------------------------------------------------------------------------
+// x rows, real -> half spectrum (even nxp = 2M), prescale applied.
+// The 2M reals of a row are read as M complex z[n] = x[2n] + i x[2n+1]; the
+// M-point four-step gives Z[k], and the half-length unpack
+//   X[k] = E + W_2M^k O,  E = (Z[k] + conj Z[M-k])/2,  O = -i (Z[k] - conj Z[M-k])/2
+// needs Z[k] and Z[M-k] together: a pass-2 thread transforms the two columns
+// k1 and N1-k1 (k1 = 0 pairs with N1/2), which hold exactly those partners.
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+                                                             float prescale)
+{
+  constexpr int N1 = fs_n1(M), N2 = M / N1;
+  static_assert(N1 % 2 == 0, "the R2C pairing needs an even N1");
+  constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
+  constexpr int NX = 2 * M, CN = M + 1;
+  constexpr int P1 = RPC * N2, P2 = RPC * (N1 / 2);
+  constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + RPC * P;
+  const int r0 = blockIdx.x * RPC;
+  const int nr = min(RPC, nrows - r0);
+  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  auto load1 = [&](int q, float2 *v) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int n2 = t % N2, row = t / N2;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && row < nr;
+    const float2 *rp = base + (long)row * CN;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) v[n1] = ok ? rp[N2 * n1 + n2] : make_float2(0.f, 0.f);
+  };
+  float2 v[N1];
+  load1(0, v);
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < B1; q++) {
+    if (q > 0) load1(q, v);
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P1 % kFFTThreads == 0 || t < P1) {
+      const int n2 = t % N2, row = t / N2;
+      reg_fft<float, N1, 2 * N2>(v, -1, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw[2 * n2 * k1]);
+#pragma unroll
+      for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < B2; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P2 % kFFTThreads == 0 || t < P2) {
+      const int ka = t % (N1 / 2), row = t / (N1 / 2);
+      const int kb = ka == 0 ? N1 / 2 : N1 - ka;
+      float2 a[N2], b[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) {
+        a[n2] = buf[row * P + n2 * Q + ka];
+        b[n2] = buf[row * P + n2 * Q + kb];
+      }
+      reg_fft<float, N2, 2 * N1>(a, -1, tw);
+      reg_fft<float, N2, 2 * N1>(b, -1, tw);
+      if (row < nr) {
+        float2 *op = base + (long)row * CN;
+        // Z[M-k] for k = ka + N1*k2 sits in b[N2-1-k2]; for ka = 0 it is a[(N2-k2) % N2]
+        // and for kb = N1/2 (paired with ka = 0) it is b[N2-1-k2]; for kb = N1-ka it is a[N2-1-k2]
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+          {
+            const int k = ka + N1 * k2;
+            const float2 A = a[k2];
+            const float2 Bc = ka == 0 ? a[(N2 - k2) % N2] : b[N2 - 1 - k2];
+            const float2 B = make_float2(Bc.x, -Bc.y);
+            const float2 E = make_float2((A.x + B.x) * 0.5f, (A.y + B.y) * 0.5f);
+            const float2 O = make_float2((A.y - B.y) * 0.5f, -(A.x - B.x) * 0.5f);
+            float2 X = cadd<float>(E, cmul<float>(tw[k], O));
+            op[k] = make_float2(X.x * prescale, X.y * prescale);
+          }
+          {
+            const int k = kb + N1 * k2;
+            const float2 A = b[k2];
+            const float2 Bc = ka == 0 ? b[N2 - 1 - k2] : a[N2 - 1 - k2];
+            const float2 B = make_float2(Bc.x, -Bc.y);
+            const float2 E = make_float2((A.x + B.x) * 0.5f, (A.y + B.y) * 0.5f);
+            const float2 O = make_float2((A.y - B.y) * 0.5f, -(A.x - B.x) * 0.5f);
+            float2 X = cadd<float>(E, cmul<float>(tw[k], O));
+            op[k] = make_float2(X.x * prescale, X.y * prescale);
+          }
+        }
+        if (ka == 0) {
+          // Nyquist bin k = M: A = Z[0], B = conj Z[0], W_2M^M = -1
+          const float2 A = a[0];
+          op[M] = make_float2((A.x - A.y) * prescale, 0.f);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// x rows, half spectrum -> real (even nxp = 2M), postscale and optional add.
+// Pass 1 packs Z[k] = E + i O from X[k] and conj X[M-k] read straight from
+// global memory (the second read of a row hits L1), so no shared memory is
+// used before the exchange; pass 2 stores z[n] = (x[2n], x[2n+1]).
+// ---------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet addend,
+                                                             const float2 *__restrict__ twg, int nrows,
+                                                             float postscale)
+{
+  constexpr int N1 = fs_n1(M), N2 = M / N1;
+  constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
+  constexpr int NX = 2 * M, CN = M + 1;
+  constexpr int P1 = RPC * N2, P2 = RPC * N1;
+  constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + RPC * P;
+  const int r0 = blockIdx.x * RPC;
+  const int nr = min(RPC, nrows - r0);
+  float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  // X[k] and X[M-k] of the first item are loaded before the twiddle barrier
+  auto load1 = [&](int q, float2 *xk, float2 *xm) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int n2 = t % N2, row = t / N2;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && row < nr;
+    const float2 *rp = base + (long)row * CN;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) {
+      const int k = N2 * n1 + n2;
+      xk[n1] = ok ? __ldg(rp + k) : make_float2(0.f, 0.f);
+      xm[n1] = ok ? __ldg(rp + (M - k)) : make_float2(0.f, 0.f);
+    }
+  };
+  float2 xk[N1], xm[N1];
+  load1(0, xk, xm);
+  __syncthreads();  // twiddles staged
+#pragma unroll
+  for (int q = 0; q < B1; q++) {
+    if (q > 0) load1(q, xk, xm);
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P1 % kFFTThreads == 0 || t < P1) {
+      const int n2 = t % N2, row = t / N2;
+      float2 v[N1];
+#pragma unroll
+      for (int n1 = 0; n1 < N1; n1++) {
+        const int k = N2 * n1 + n2;
+        float2 Xk = xk[n1], Xm = xm[n1];
+        if (k == 0) { Xk.y = 0.f; Xm.y = 0.f; }  // rfftw_c2hc keeps only Re of DC and Nyquist
+        Xm.y = -Xm.y;
+        const float2 E = cadd<float>(Xk, Xm);
+        const float2 O = cmulc<float>(csub<float>(Xk, Xm), tw[k]);
+        v[n1] = make_float2(E.x - O.y, E.y + O.x);
+      }
+      reg_fft<float, N1, 2 * N2>(v, +1, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw_at<float>(tw, 2 * n2 * k1, +1));
+#pragma unroll
+      for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
+    }
+  }
+  __syncthreads();
+  const float2 *add = addend.ptr[blockIdx.z] ? (const float2 *)addend.ptr[blockIdx.z] + (long)r0 * CN : nullptr;
+#pragma unroll
+  for (int q = 0; q < B2; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P2 % kFFTThreads == 0 || t < P2) {
+      const int k1 = t % N1, row = t / N1;
+      float2 u[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[row * P + n2 * Q + k1];
+      reg_fft<float, N2, 2 * N1>(u, +1, tw);
+      if (row < nr) {
+        float2 *op = base + (long)row * CN;
+        const float2 *ap = add ? add + (long)row * CN : nullptr;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+          const int e = k1 + N1 * k2;
+          float2 z = make_float2(u[k2].x * postscale, u[k2].y * postscale);
+          if (ap) {
+            const float2 s = ap[e];
+            z.x += s.x;
+            z.y += s.y;
+          }
+          op[e] = z;
+        }
+        if (k1 == 0) {
+          // the row's padding pair: zero, plus the addend's padding
+          float2 z = make_float2(0.f, 0.f);
+          if (ap) {
+            const float2 s = ap[M];
+            z.x += s.x;
+            z.y += s.y;
+          }
+          op[M] = z;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace cg

@@ -262,6 +262,150 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_pipe(CubeSet cs,
 }
 
 // ---------------------------------------------------------------------------
+// register-direct column pass: the first Stockham stage reads its operands
+// straight from global memory (each butterfly's R operands are R tile rows
+// apart, and a warp covers 16 adjacent columns, so every load is part of a
+// 128-byte row segment) and the last stage writes straight back, halving the
+// shared-memory traffic of the staged kernel.
+// ---------------------------------------------------------------------------
+template <typename T, int N, int W, int LDW, int TWS, int S, int NS, int SEND>
+__device__ __forceinline__ void cstages_range(C2<T> *buf, const C2<T> *tw, int sign)
+{
+  if constexpr (S < SEND) {
+    constexpr int R = plan_radix(N, S);
+    constexpr int NB = N / R;
+    constexpr int SPAN = N / (NS * R);
+    constexpr int TOT = NB * W;
+    constexpr int BPT = (TOT + kFFTThreads - 1) / kFFTThreads;
+    C2<T> v[BPT][R];
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+#pragma unroll
+        for (int r = 0; r < R; r++) v[q][r] = buf[(j + r * NB) * LDW + c];
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+        const int jm = j % NS;
+        if (NS > 1) {
+#pragma unroll
+          for (int r = 1; r < R; r++) v[q][r] = cmul<T>(v[q][r], tw_at<T>(tw, jm * r * SPAN * TWS, sign));
+        }
+        dft_any<T, R>(v[q], sign, tw, NB * TWS);
+        const int d = (j - jm) * R + jm;
+#pragma unroll
+        for (int r = 0; r < R; r++) buf[(d + r * NS) * LDW + c] = v[q][r];
+      }
+    }
+    __syncthreads();
+    cstages_range<T, N, W, LDW, TWS, S + 1, NS * R, SEND>(buf, tw, sign);
+  }
+}
+
+__host__ __device__ constexpr int plan_ns_before(int n, int stage)
+{
+  int ns = 1;
+  for (int s = 0; s < stage; s++) ns *= plan_radix(n, s);
+  return ns;
+}
+
+template <int N, int W, int MINB>
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(CubeSet cs, const float2 *__restrict__ twg,
+                                                                   ColsGeom g, int sign)
+{
+  static_assert(plan_nstages(N) >= 2, "register-direct pass needs two stages or more");
+  constexpr int NST = plan_nstages(N);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + N * W;
+  float2 *cube = (float2 *)cs.ptr[blockIdx.z];
+  long cstride;
+  int cvalid;
+  float2 *base;
+  if ((int)blockIdx.x < g.nfull) {
+    base = cube + (long)blockIdx.y * g.batch_stride + (long)blockIdx.x * W;
+    cstride = 1;
+    cvalid = W;
+  } else {
+    const int groups = (g.nbatch + W - 1) / W;
+    const int tt = ((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
+    const int tcol = tt / groups, grp = tt % groups;
+    if (tcol >= g.ntail) return;
+    base = cube + (long)g.nfull * W + tcol + (long)grp * W * g.batch_stride;
+    cstride = g.batch_stride;
+    cvalid = g.nbatch - grp * W;
+  }
+  const long as = g.axis_stride;
+  for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
+  // first stage (no twiddles): global -> registers -> shared
+  {
+    constexpr int R = plan_radix(N, 0);
+    constexpr int NB = N / R;
+    constexpr int TOT = NB * W;
+    constexpr int BPT = (TOT + kFFTThreads - 1) / kFFTThreads;
+    float2 v[BPT][R];
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      const int j = t / W, c = t % W;
+      const bool ok = (TOT % kFFTThreads == 0 || t < TOT) && c < cvalid;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[q][r] = ok ? base[(long)(j + r * NB) * as + (long)c * cstride] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();  // twiddles staged (odd radices read them inside the DFT)
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+        dft_any<float, R>(v[q], sign, tw, NB);
+#pragma unroll
+        for (int r = 0; r < R; r++) buf[(j * R + r) * W + c] = v[q][r];
+      }
+    }
+    __syncthreads();
+  }
+  // middle stages in shared memory
+  cstages_range<float, N, W, W, 1, 1, plan_radix(N, 0), NST - 1>(buf, tw, sign);
+  // last stage: shared -> registers -> global
+  {
+    constexpr int S = NST - 1;
+    constexpr int R = plan_radix(N, S);
+    constexpr int NS = plan_ns_before(N, S);
+    constexpr int NB = N / R;
+    constexpr int SPAN = N / (NS * R);
+    constexpr int TOT = NB * W;
+    constexpr int BPT = (TOT + kFFTThreads - 1) / kFFTThreads;
+#pragma unroll
+    for (int q = 0; q < BPT; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT % kFFTThreads == 0 || t < TOT) {
+        const int j = t / W, c = t % W;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) v[r] = buf[(j + r * NB) * W + c];
+        const int jm = j % NS;
+#pragma unroll
+        for (int r = 1; r < R; r++) v[r] = cmul<float>(v[r], tw_at<float>(tw, jm * r * SPAN, sign));
+        dft_any<float, R>(v, sign, tw, NB);
+        const int d = (j - jm) * R + jm;
+        if (c < cvalid) {
+#pragma unroll
+          for (int r = 0; r < R; r++) base[(long)(d + r * NS) * as + (long)c * cstride] = v[r];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
 // x rows, real -> half spectrum (even nxp = 2M), prescale applied to X
 // ---------------------------------------------------------------------------
 template <int M>
@@ -373,5 +517,10 @@ int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride,
               int sign, const float2 *tw, cudaStream_t st, int *done_cols);
 int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
               const float2 *tw, cudaStream_t st);
+// four-step kernels (fft_4step_*.cu); chosen by the tuning table
+int four_step_cols(int minb, const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride,
+                   int nbatch, int sign, const float2 *tw, cudaStream_t st);
+int four_step_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
+                   const float2 *tw, cudaStream_t st);
 
 }  // namespace cg

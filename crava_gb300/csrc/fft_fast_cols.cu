@@ -79,10 +79,40 @@ int launch_pipe(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long
   return 1;
 }
 
+// register-direct first and last stages (tuning: CG_TUNE_COLS_PIPE value 2)
+template <int N, int MINB>
+int launch_rd(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+              const float2 *tw, cudaStream_t st)
+{
+  const size_t smem = ((size_t)N * kW + N) * sizeof(float2);
+  static bool attr_set[64] = {};
+  cudaError_t e = smem_limit_once(k_fft_cols_rd<N, kW, MINB>, smem, attr_set);
+  if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_rd attribute");
+  ColsGeom g;
+  g.axis_stride = axis_stride;
+  g.batch_stride = batch_stride;
+  g.nfull = ncols / kW;
+  g.ntail = ncols - g.nfull * kW;
+  g.nbatch = nbatch;
+  const int groups = ceil_div(nbatch, kW);
+  const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
+  dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
+  TraceScope ts("k_fft_cols_rd", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
+  k_fft_cols_rd<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_rd");
+  return 1;
+}
+
 template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
+  const int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
+  if (kind == 3) return four_step_cols(minb_for(N), cs, ncubes, N, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  if (kind == 2) {
+    if (minb_for(N) == 3) return launch_rd<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    return launch_rd<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  }
   if (use_pipe(N)) {
     if (minb_for(N) == 3) return launch_pipe<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     return launch_pipe<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);

@@ -1,6 +1,8 @@
 // Specialised x-row R2C / C2R passes (see fft_fast.cuh).
 #include "fft_fast.cuh"
 #include "trace.cuh"
+#include "tuning.cuh"
+#include "cravagpu.h"
 
 namespace cg {
 
@@ -36,6 +38,8 @@ int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes
               const float2 *tw, cudaStream_t st)
 {
   if (nxp % 2) return 0;
+  if (cg_tune_get(CG_TUNE_ROWS_KERNEL, nxp / 2) == 1)
+    return four_step_rows(forward, cs, addend, ncubes, nxp, nrows, scale, tw, st);
   switch (nxp / 2) {
 #define CG_ROWS(MM) case MM: return launch<MM>(forward, cs, addend, ncubes, nrows, scale, tw, st);
     CG_ROWS(32) CG_ROWS(40) CG_ROWS(48) CG_ROWS(50) CG_ROWS(60) CG_ROWS(64) CG_ROWS(80) CG_ROWS(96)

@@ -191,7 +191,7 @@ Crava::~Crava()
 
 int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha, FFTGrid *&postBeta,
                                          FFTGrid *&postRho, FFTGrid **postCov, FFTGrid *errCorr, Form form,
-                                         void *stream)
+                                         void *stream, void *binsDone)
 {
   const int n = m_.ntheta;
   FFTGrid *mean[3] = {postAlpha, postBeta, postRho};
@@ -225,6 +225,7 @@ int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha
           "bin loop (fused)");
   }
   for (int t = 0; t < 6; t++) { postCov[t]->setType(FFTGrid::COVARIANCE); postCov[t]->setTransformedStatus(true); }
+  if (binsDone) cuda_check(cudaEventRecord((cudaEvent_t)binsDone, (cudaStream_t)stream), "bins-done event");
   check(cg_fft3d_c2r_batch(mu, 3, nxp_, nyp_, nzp_, CG_PARAMETER, stream), "posterior-mean inverse transforms");
   for (int p = 0; p < 3; p++) mean[p]->setTransformedStatus(false);
   return 0;
@@ -260,6 +261,8 @@ struct cg_inversion_s {
   std::vector<FFTGrid *> data, mean, cov;
   FFTGrid *errcorr = nullptr;
   cudaStream_t stream = nullptr;
+  cudaStream_t out_stream = nullptr;  // residual and covariance copies, beside the mean inverse transforms
+  cudaEvent_t bins_done = nullptr;
 };
 
 #define CG_TRY(...)                                    \
@@ -304,6 +307,8 @@ extern "C" int cg_inversion_create(cg_inversion *out, int nx, int ny, int nz, in
       for (int p = 0; p < 3; p++) { h->mean.push_back(new FFTGrid(nx, ny, nz, nxp, nyp, nzp)); h->mean.back()->setType(FFTGrid::PARAMETER); }
       for (int t = 0; t < 6; t++) { h->cov.push_back(new FFTGrid(nx, ny, nz, nxp, nyp, nzp)); h->cov.back()->setType(FFTGrid::COVARIANCE); }
       cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
+      cuda_check(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking), "stream");
+      cuda_check(cudaEventCreateWithFlags(&h->bins_done, cudaEventDisableTiming), "event");
     } catch (...) {
       cg_inversion_destroy(h);
       throw;
@@ -322,6 +327,8 @@ extern "C" void cg_inversion_destroy(cg_inversion h)
   delete h->errcorr;
   delete h->crava;
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->out_stream) cudaStreamDestroy(h->out_stream);
+  if (h->bins_done) cudaEventDestroy(h->bins_done);
   delete h;
 }
 
@@ -352,14 +359,18 @@ extern "C" int cg_inversion_run_host(cg_inversion h, float *const *seis_data, fl
       h->errcorr->setTransformedStatus(false);
     }
     FFTGrid *a = h->mean[0], *b = h->mean[1], *c = h->mean[2];
-    h->crava->computePostMeanResidAndFFTCov(h->data.data(), a, b, c, h->cov.data(), h->errcorr, f, st);
+    h->crava->computePostMeanResidAndFFTCov(h->data.data(), a, b, c, h->cov.data(), h->errcorr, f, st, h->bins_done);
+    // residual and covariance spectra leave while the posterior means are transformed back
+    cudaStream_t os = h->out_stream;
+    cuda_check(cudaStreamWaitEvent(os, h->bins_done, 0), "wait bins");
     for (int l = 0; l < h->ntheta; l++)
-      cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H residual");
+      cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H residual");
     for (int t = 0; t < 6; t++)
-      cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H cov");
+      cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H cov");
     for (int p = 0; p < 3; p++)
       cuda_check(cudaMemcpyAsync(mean[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
-    cuda_check(cudaStreamSynchronize(st), "inversion");
+    const cudaError_t e1 = cudaStreamSynchronize(st), e2 = cudaStreamSynchronize(os);
+    cuda_check(e1 != cudaSuccess ? e1 : e2, "inversion");
     return CG_OK;
   })
 }

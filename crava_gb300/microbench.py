@@ -2,6 +2,7 @@
 
     python -m crava_gb300.microbench fft   --nxp 256 --nyp 256 --nzp 64 --batch 5 --reps 3
     python -m crava_gb300.microbench invert --nxp 256 --nyp 256 --nzp 64 --form mixed --reps 3
+    python -m crava_gb300.microbench copy  --mb 512 --reps 5
 
 Inputs are seeded random cubes (fft) or a scaled config-1 scenario (invert).
 Prints one JSON line with per-kernel launch times and algorithmic bandwidth
@@ -45,9 +46,61 @@ def batch_case(a):
     a._batch.run(a.form, use_graph=True)
 
 
+def copy_case(a):
+    """Pinned host <-> device copy rates: one stream, split over streams, both directions at once."""
+    n = a.mb * (1 << 20) // 4
+    h_in = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_out = torch.empty(n, dtype=torch.float32).pin_memory()
+    d_in = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_out = torch.empty(n, dtype=torch.float32, device="cuda")
+    streams = [torch.cuda.Stream() for _ in range(4)]
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        best = None
+        for _ in range(a.reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for s in streams:
+                s.wait_event(e0)
+            fn()
+            for s in streams:
+                torch.cuda.current_stream().wait_stream(s)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            best = ms if best is None else min(best, ms)
+        return best
+
+    def split(k, src, dst):
+        def fn():
+            c = (n + k - 1) // k
+            for i in range(k):
+                with torch.cuda.stream(streams[i]):
+                    dst[i * c:(i + 1) * c].copy_(src[i * c:(i + 1) * c], non_blocking=True)
+        return fn
+
+    gb = n * 4 / 1e9
+    out = {}
+    for k in (1, 2, 4):
+        out[f"h2d_{k}streams_GBps"] = gb / (timed(split(k, h_in, d_in)) * 1e-3)
+        out[f"d2h_{k}streams_GBps"] = gb / (timed(split(k, d_out, h_out)) * 1e-3)
+
+    def both():
+        with torch.cuda.stream(streams[0]):
+            d_in.copy_(h_in, non_blocking=True)
+        with torch.cuda.stream(streams[1]):
+            h_out.copy_(d_out, non_blocking=True)
+    out["h2d_plus_d2h_concurrent_GBps_total"] = 2 * gb / (timed(both) * 1e-3)
+    print(json.dumps({"case": {"what": "copy", "mb": a.mb, "reps": a.reps}, "rates": out}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["fft", "invert", "batch"])
+    ap.add_argument("what", choices=["fft", "invert", "batch", "copy"])
+    ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
     ap.add_argument("--streams", type=int, default=8)
     ap.add_argument("--nxp", type=int, default=256)
@@ -58,6 +111,9 @@ def main():
     ap.add_argument("--form", default="mixed")
     a = ap.parse_args()
     _native.lib()
+    if a.what == "copy":
+        copy_case(a)
+        return
     if a.what == "batch":
         # graph replays: time the whole batch with CUDA events
         batch_case(a)  # warm-up and capture

@@ -65,14 +65,17 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
 
 /* Launch-variant tuning table.  Keys: CG_TUNE_COLS_MINB (resident CTAs the
  * column-pass build targets, 2 or 3, per axis length n), CG_TUNE_COLS_PIPE
- * (persistent double-buffered column pass, 0 or 1, per n), CG_TUNE_BIN_MINB
- * (fused bin kernel register cap: 1 = none, 6 = 85 registers, per stack
- * count n).  n = 0 sets the value for every n.  Built-in defaults were
+ * (column-pass kernel per n: 0 shared-memory staged, 1 persistent
+ * double-buffered, 2 first and last stages in registers, 3 four-step),
+ * CG_TUNE_BIN_MINB (fused bin kernel register cap: 1 = none, 6 = 85
+ * registers, per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per
+ * half length n = nxp/2: 0 shared-memory staged, 1 four-step).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0
 #define CG_TUNE_COLS_PIPE 1
 #define CG_TUNE_BIN_MINB 2
+#define CG_TUNE_ROWS_KERNEL 3
 int cg_tune_set(int key, int n, int value);
 int cg_tune_get(int key, int n);
 int cg_tune_clear(void);

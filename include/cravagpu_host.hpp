@@ -116,10 +116,13 @@ class Crava {
   // residual spectra, postAlpha/Beta/Rho (real prior-mean cubes) the
   // real-domain posterior means, postCov[6] the posterior covariance spectra.
   // The plain form also needs the 6 prior covariance cubes and errCorr in the
-  // real domain (it transforms them, as FFTCovGrids does).
+  // real domain (it transforms them, as FFTCovGrids does).  binsDone, when
+  // given (a cudaEvent_t), is recorded on the stream once the residual and
+  // covariance spectra are final, before the posterior-mean inverse
+  // transforms: a caller can start copying those cubes out from then on.
   int computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha, FFTGrid *&postBeta,
                                     FFTGrid *&postRho, FFTGrid **postCov, FFTGrid *errCorr, Form form,
-                                    void *stream = nullptr);
+                                    void *stream = nullptr, void *binsDone = nullptr);
 
   // Crava::simulate (src/crava.cpp:1551-1734) for nSim realisations, written
   // to fields[3*r + p]; the posterior covariance spectra are factored once.

@@ -131,3 +131,45 @@ def test_bad_arguments_return_status(cuda, native):
     assert native.cg_fft3d_r2c(ct.c_void_p(t2.data_ptr()), 11, 8, 8, api.DATA, s) == -3
     assert b"prime factor" in native.cg_last_error()
     torch.cuda.synchronize()
+
+
+# every kernel variant of the tuning table -- column pass (CG_TUNE_COLS_PIPE: 0 staged, 1 persistent,
+# 2 register-direct, 3 four-step) with both resident-CTA targets, x-row pass (CG_TUNE_ROWS_KERNEL: 0 staged,
+# 1 four-step) -- on specialised lengths with full tiles, column tails and one-row batches
+VARIANT_SIZES = [(80, 80, 160), (256, 256, 1), (100, 1, 128), (64, 200, 96), (128, 240, 64), (96, 64, 512),
+                 (400, 120, 100), (480, 192, 80), (320, 384, 64), (200, 160, 200), (512, 100, 64), (120, 256, 240)]
+
+
+_VARIANT_REFS = {}
+
+
+def _variant_case(oracle, nxp, nyp, nzp):
+    key = (nxp, nyp, nzp)
+    if key not in _VARIANT_REFS:
+        _, rnxp = oracle.dims(nxp)
+        rng = np.random.default_rng(nxp + nyp + nzp)
+        x = np.zeros((nzp, nyp, rnxp), np.float32)
+        x[..., :nxp] = rng.standard_normal((nzp, nyp, nxp))
+        _VARIANT_REFS[key] = (x, oracle.fft3d_r2c(x, nxp, oracle.DATA, "d"))
+    return _VARIANT_REFS[key]
+
+
+@pytest.mark.parametrize("pipe", [0, 1, 2, 3])
+@pytest.mark.parametrize("minb", [2, 3])
+def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
+    from crava_gb300 import api
+    native.cg_tune_clear()
+    try:
+        assert native.cg_tune_set(1, 0, pipe) == 0 and native.cg_tune_set(0, 0, minb) == 0
+        assert native.cg_tune_set(3, 0, minb - 2) == 0   # staged rows with minb 2, four-step rows with 3
+        for nxp, nyp, nzp in VARIANT_SIZES:
+            x, ref = _variant_case(oracle, nxp, nyp, nzp)
+            t = torch.from_numpy(x.copy()).cuda()
+            api.fft_in_place(t, nxp, api.DATA)
+            assert rel(from_cube(t), ref) < FFT_TOL, (nxp, nyp, nzp)
+            api.inv_fft_in_place(t, nxp, api.DATA)
+            assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL, (nxp, nyp, nzp)
+    finally:
+        from crava_gb300 import _native
+        native.cg_tune_clear()
+        _native._apply_tuning(native)
