@@ -165,6 +165,8 @@ def _declare(L):
         "cg_scale": ([V, ct.c_long, F, V], I),
         "cg_add": ([V, V, ct.c_long, V], I),
         "cg_host_register": ([V, ct.c_size_t], I),
+        "cg_copy": ([V, V, ct.c_size_t, V], I),
+        "cg_host_access": ([], I),
         "cg_host_unregister": ([V], I),
         "cg_inversion_create": ([ct.POINTER(V), I, I, I, I, I, I, V], I),
         "cg_inversion_destroy": ([V], None),

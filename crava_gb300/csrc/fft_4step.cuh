@@ -149,8 +149,13 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
   }
 }
 
-// rows per CTA for the row passes: enough (row, n2) items for 256 threads
-__host__ __device__ constexpr int fs_rows_per_cta(int m) { return kFFTThreads / (m / fs_n1(m)) < 1 ? 1 : kFFTThreads / (m / fs_n1(m)); }
+// rows per CTA for the row passes: enough (row, n2) items and (row, k1 pair)
+// items for the 256 threads of both passes
+__host__ __device__ constexpr int fs_rows_per_cta(int m)
+{
+  const int a = kFFTThreads / (m / fs_n1(m)), b = 2 * kFFTThreads / fs_n1(m);
+  return a > b ? a : b;
+}
 
 // pitch (float2) of one row's exchange block: >= N2*(N1+1), = 8 mod 16 so the
 // two rows a half-warp touches fall in opposite bank halves

@@ -69,9 +69,9 @@ extern "C" int cg_tune_get(int key, int n)
 {
   switch (key) {
     case CG_TUNE_COLS_MINB: return tune_get(key, n, n <= 256 ? 3 : 2);
-    case CG_TUNE_COLS_PIPE: return tune_get(key, n, 0);
+    case CG_TUNE_COLS_PIPE: return tune_get(key, n, n == 256 ? 2 : 3);  // register-direct at 256, four-step elsewhere
     case CG_TUNE_BIN_MINB: return tune_get(key, n, n <= 5 ? 6 : 1);
-    case CG_TUNE_ROWS_KERNEL: return tune_get(key, n, 0);
+    case CG_TUNE_ROWS_KERNEL: return tune_get(key, n, 1);  // four-step
     default: set_error("cg_tune_get: bad key"); return CG_ERR_ARG;
   }
 }

@@ -383,7 +383,7 @@ extern "C" int cg_inversion_stats(cg_inversion h, int *flagged, int *failed, int
 
 extern "C" int cg_host_register(void *ptr, size_t bytes)
 {
-  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterPortable | cudaHostRegisterMapped);
   if (e != cudaSuccess) { (void)cudaGetLastError(); cg::set_error("cudaHostRegister: %s", cudaGetErrorString(e)); return CG_ERR_CUDA; }
   return CG_OK;
 }

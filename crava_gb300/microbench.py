@@ -94,6 +94,26 @@ def copy_case(a):
         with torch.cuda.stream(streams[1]):
             h_out.copy_(d_out, non_blocking=True)
     out["h2d_plus_d2h_concurrent_GBps_total"] = 2 * gb / (timed(both) * 1e-3)
+
+    # the same traffic moved by kernels that load/store host memory directly (cg_copy)
+    L = _native.lib()
+
+    def kcopy(dst, src):
+        def fn():
+            _native.check(L.cg_copy(dst.data_ptr(), src.data_ptr(), n * 4, torch.cuda.current_stream().cuda_stream),
+                          "cg_copy")
+        return fn
+    out["kernel_h2d_GBps"] = gb / (timed(kcopy(d_in, h_in)) * 1e-3)
+    out["kernel_d2h_GBps"] = gb / (timed(kcopy(h_out, d_out)) * 1e-3)
+    out["kernel_d2d_GBps_read_plus_write"] = 2 * gb / (timed(kcopy(d_out, d_in)) * 1e-3)
+
+    def kboth():
+        with torch.cuda.stream(streams[0]):
+            _native.check(L.cg_copy(d_in.data_ptr(), h_in.data_ptr(), n * 4, streams[0].cuda_stream), "cg_copy")
+        with torch.cuda.stream(streams[1]):
+            _native.check(L.cg_copy(h_out.data_ptr(), d_out.data_ptr(), n * 4, streams[1].cuda_stream), "cg_copy")
+    out["kernel_h2d_plus_d2h_GBps_total"] = 2 * gb / (timed(kboth) * 1e-3)
+    out["host_access_bits"] = int(L.cg_host_access())
     print(json.dumps({"case": {"what": "copy", "mb": a.mb, "reps": a.reps}, "rates": out}))
 
 

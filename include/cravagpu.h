@@ -168,6 +168,20 @@ int cg_add(float *y, const float *x, long n, void *stream);
 int cg_host_register(void *ptr, size_t bytes);
 int cg_host_unregister(void *ptr);
 
+/* No reference counterpart (a building block of the host-buffer entry
+ * points).  Copy bytes with a kernel between any two addresses the device
+ * can reach: device memory, page-locked host memory (the GPU reads and writes
+ * it over the coherent NVLink-C2C link), or pageable host memory when the
+ * device reports pageable access (cg_host_access bit 1).  Pointers and size
+ * 16-byte aligned.  CG_ERR_UNSUPPORTED when a pointer is out of the device's
+ * reach. */
+int cg_copy(void *dst, const void *src, size_t bytes, void *stream);
+
+/* How this device reaches host memory, as bits: 1 pageable memory access,
+ * 2 through the host's page tables, 4 registered memory at its host
+ * address. */
+int cg_host_access(void);
+
 /* ========================================================================
  * Per-frequency-bin posterior (Crava::computePostMeanResidAndFFTCov bin loop,
  * src/crava.cpp:1084-1247).

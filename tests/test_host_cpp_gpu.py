@@ -1,6 +1,7 @@
 """The C++ host layer (FFTGrid / Crava mirror behind cg_inversion_*) with host buffers."""
 import numpy as np
 import pytest
+import torch
 
 from conftest import oracle_pipeline, rel
 
@@ -38,3 +39,20 @@ def test_host_buffers_inversion_matches_oracle(cuda, oracle, form):
     mean2 = [m.copy() for m in sc.mean]
     inv.run(data2, mean2, cov, form=form, **kw)
     assert rel(np.stack([m[:, :, :sc.nxp] for m in mean2]), pm) < 1e-6
+
+
+def test_kernel_copy_between_host_and_device(cuda, native):
+    """cg_copy moves page-locked host memory with a kernel (no copy engine), both directions."""
+    from crava_gb300 import _native
+    n = (1 << 20) + 12
+    h = torch.randn(n).pin_memory()
+    d = torch.empty(n, device="cuda")
+    back = torch.zeros(n).pin_memory()
+    _native.check(native.cg_copy(d.data_ptr(), h.data_ptr(), n * 4, None), "h2d")
+    _native.check(native.cg_copy(back.data_ptr(), d.data_ptr(), n * 4, None), "d2h")
+    torch.cuda.synchronize()
+    assert torch.equal(d.cpu(), h) and torch.equal(back, h)
+    assert native.cg_copy(d.data_ptr() + 4, h.data_ptr(), 64, None) == -1      # misaligned
+    assert native.cg_copy(d.data_ptr(), h.data_ptr(), 20, None) == -1          # size not a multiple of 16
+    assert native.cg_copy(None, h.data_ptr(), 16, None) == -1
+    assert native.cg_host_access() >= 0
