@@ -10,6 +10,7 @@
 
 #include "cravagpu.h"
 #include "cravagpu_host.hpp"
+#include "../csrc/trace.cuh"
 
 namespace cg {
 void set_error(const char *fmt, ...);
@@ -339,13 +340,16 @@ extern "C" int cg_inversion_run_host(cg_inversion h, float *const *seis_data, fl
   CG_TRY({
     const size_t bytes = sizeof(float) * (size_t)h->data[0]->getrsize();
     cudaStream_t st = h->stream;
-    for (int l = 0; l < h->ntheta; l++) {
-      cuda_check(cudaMemcpyAsync(h->data[l]->devicePtr(), seis_data[l], bytes, cudaMemcpyHostToDevice, st), "H2D data");
-      h->data[l]->setTransformedStatus(false);
-    }
-    for (int p = 0; p < 3; p++) {
-      cuda_check(cudaMemcpyAsync(h->mean[p]->devicePtr(), mean[p], bytes, cudaMemcpyHostToDevice, st), "H2D mean");
-      h->mean[p]->setTransformedStatus(false);
+    {
+      cg::TraceScope ts("copy_h2d", st, (double)bytes * (h->ntheta + 3));
+      for (int l = 0; l < h->ntheta; l++) {
+        cuda_check(cudaMemcpyAsync(h->data[l]->devicePtr(), seis_data[l], bytes, cudaMemcpyHostToDevice, st), "H2D data");
+        h->data[l]->setTransformedStatus(false);
+      }
+      for (int p = 0; p < 3; p++) {
+        cuda_check(cudaMemcpyAsync(h->mean[p]->devicePtr(), mean[p], bytes, cudaMemcpyHostToDevice, st), "H2D mean");
+        h->mean[p]->setTransformedStatus(false);
+      }
     }
     Crava::Form f = form == 0 ? Crava::PLAIN : form == 1 ? Crava::FUSED_FP32 : Crava::FUSED_MIXED;
     if (f == Crava::PLAIN) {
@@ -363,12 +367,18 @@ extern "C" int cg_inversion_run_host(cg_inversion h, float *const *seis_data, fl
     // residual and covariance spectra leave while the posterior means are transformed back
     cudaStream_t os = h->out_stream;
     cuda_check(cudaStreamWaitEvent(os, h->bins_done, 0), "wait bins");
-    for (int l = 0; l < h->ntheta; l++)
-      cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H residual");
-    for (int t = 0; t < 6; t++)
-      cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H cov");
-    for (int p = 0; p < 3; p++)
-      cuda_check(cudaMemcpyAsync(mean[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
+    {
+      cg::TraceScope ts("copy_d2h_resid_cov", os, (double)bytes * (h->ntheta + 6));
+      for (int l = 0; l < h->ntheta; l++)
+        cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H residual");
+      for (int t = 0; t < 6; t++)
+        cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H cov");
+    }
+    {
+      cg::TraceScope ts("copy_d2h_mean", st, (double)bytes * 3);
+      for (int p = 0; p < 3; p++)
+        cuda_check(cudaMemcpyAsync(mean[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
+    }
     const cudaError_t e1 = cudaStreamSynchronize(st), e2 = cudaStreamSynchronize(os);
     cuda_check(e1 != cudaSuccess ? e1 : e2, "inversion");
     return CG_OK;

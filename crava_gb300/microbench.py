@@ -3,6 +3,8 @@
     python -m crava_gb300.microbench fft   --nxp 256 --nyp 256 --nzp 64 --batch 5 --reps 3
     python -m crava_gb300.microbench invert --nxp 256 --nyp 256 --nzp 64 --form mixed --reps 3
     python -m crava_gb300.microbench copy  --mb 512 --reps 5
+    python -m crava_gb300.microbench simulate --nreal 128 --reps 3
+    python -m crava_gb300.microbench timelapse --reps 3
 
 Inputs are seeded random cubes (fft) or a scaled config-1 scenario (invert).
 Prints one JSON line with per-kernel launch times and algorithmic bandwidth
@@ -117,9 +119,97 @@ def copy_case(a):
     print(json.dumps({"case": {"what": "copy", "mb": a.mb, "reps": a.reps}, "rates": out}))
 
 
+def simulate_case(a):
+    """Posterior simulation on the 200^3 three-stack workload: one mixed inversion, the per-bin posterior
+    factor, then nreal realisations (noise, factor, inverse transform, mean add), timed with CUDA events."""
+    from . import synthetic as S
+    from .pipeline import Inversion
+    sc = S.config3()
+    inv = Inversion(sc, forms=("mixed",))
+    inv.restore("mixed")
+    inv.run("mixed")
+    torch.cuda.synchronize()
+    _, rnxp = api.dims(sc.nxp)
+    fields = [torch.empty((sc.nzp, sc.nyp, rnxp), device="cuda") for _ in range(3 * a.nreal)]
+    chol, nfail = api.posterior_cholesky(inv.cov, sc.nxp)
+
+    def step(rep):
+        c, _ = api.posterior_cholesky(inv.cov, sc.nxp)
+        api.simulate_fields(c, fields, sc.nxp, seed=1000 + rep, post_mean=inv.mean)
+    step(0)
+    torch.cuda.synchronize()
+    ms = []
+    for r in range(a.reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step(r + 1)
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    _native.trace_enable(True)
+    step(99)
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    best = min(ms)
+    bins = sc.nbins
+    # algorithmic bytes per realisation: 3 C2R (8 B/bin + 4 B/cell each) + mean read and field write
+    # (2 x 3 x 4 B/cell); the factor (36 B/bin) is read once per call
+    cells = sc.nxp * sc.nyp * sc.nzp
+    alg = a.nreal * (3 * (8 * bins + 4 * cells) + 24 * cells) + 36 * bins
+    print(json.dumps({"case": {"what": "simulate", "workload": "200^3 padded cube, 3 stacks, config-0 prior",
+                               "nreal": a.nreal, "bins": bins, "chol_fail": int(nfail.item())},
+                      "ms_per_call": ms, "realisations_per_s": a.nreal / (best * 1e-3),
+                      "Mbins_per_s": a.nreal * bins / (best * 1e-3) / 1e6,
+                      "algorithmic_GBps": alg / (best * 1e-3) / 1e9,
+                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
+                                  for k, v in tr.items()}}))
+
+
+def timelapse_case(a):
+    """4D time-lapse on the 256x256x192 workload: two vintages x 4 stacks, each merge -> data transforms
+    -> plain bin loop (4D branch) -> split -> posterior-mean inverse transforms; timed with CUDA events,
+    the state restored between repetitions outside the timed region."""
+    from . import synthetic as S
+    from .pipeline import TimeLapse
+    tl = S.config4()
+    run = TimeLapse(tl)
+    run.restore()
+    run.run()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(a.reps):
+        run.restore()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run.run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    run.restore()
+    _native.trace_enable(True)
+    run.run()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    best = min(ms)
+    bins = tl.nbins
+    fails = [int(x.item()) for x in run.nfail_split]
+    st = [w.stats() for w in run.ws]
+    print(json.dumps({"case": {"what": "timelapse", "workload": "256x256x192 padded cube, 2 vintages x 4 stacks, "
+                                                            "6-parameter state", "bins": bins},
+                      "ms_per_run": ms, "Mbins_per_s": bins / (best * 1e-3) / 1e6,
+                      "joint_algorithmic_GBps": run.algorithmic_bytes() / (best * 1e-3) / 1e9,
+                      "split_fails": fails, "chol_fail": [x["failed"] for x in st],
+                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
+                                  for k, v in tr.items()}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["fft", "invert", "batch", "copy"])
+    ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse"])
+    ap.add_argument("--nreal", type=int, default=128)
     ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
     ap.add_argument("--streams", type=int, default=8)
@@ -133,6 +223,12 @@ def main():
     _native.lib()
     if a.what == "copy":
         copy_case(a)
+        return
+    if a.what == "simulate":
+        simulate_case(a)
+        return
+    if a.what == "timelapse":
+        timelapse_case(a)
         return
     if a.what == "batch":
         # graph replays: time the whole batch with CUDA events

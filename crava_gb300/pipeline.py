@@ -142,3 +142,127 @@ class Inversion:
             nfft = n + 3 + 3
             binb = inband * 2 * word * ((n + 3) + (n + 3 + 6)) + outband * 2 * word * 6
         return nfft * per_fft * (word // 4) + binb
+
+
+# State4D grid orders (src/state4d.cpp): static-static, static-dynamic and dynamic-dynamic blocks of the
+# 6x6 covariance (parameters 0..2 static, 3..5 dynamic)
+SS_PAIRS = [(0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2)]
+SD_PAIRS = [(0, 3), (0, 4), (0, 5), (1, 3), (1, 4), (1, 5), (2, 3), (2, 4), (2, 5)]
+DD_PAIRS = [(3, 3), (3, 4), (3, 5), (4, 4), (4, 5), (5, 5)]
+# merge/split order of the current 3x3 covariance (00 01 02 11 12 22) -> bin-loop order (00 11 22 01 02 12)
+MERGE_TO_BIN = [0, 3, 5, 1, 2, 4]
+
+
+class TimeLapse:
+    """4D time-lapse inversion in the reference's sequential form, per vintage:
+
+        State4D::merge / mergeCov (src/state4d.cpp:140-299) -> current prior spectra;
+        forward transform of the vintage's data cubes (DATA);
+        the bin loop with the 4D branch of findParameterVariances
+        (src/seismicparametersholder.cpp:366-373), plain form (the prior is no longer separable);
+        State4D::split (src/state4d.cpp:301-580) -> updated static and dynamic state;
+        inverse transform of a copy of the current posterior mean (the vintage's output).
+
+    The state is held as spectra (27 cubes: 3 + 3 means, 6 + 9 + 6 covariance blocks), built from the
+    separable prior exactly as the reference builds its 4D grids (fillInParamCorr x Sigma entry, then a
+    COVARIANCE transform).  Between vintages nothing evolves (E = I, c = 0, C = 0).  The reference's
+    inverse-then-forward transform of the posterior means between the bin loop and split
+    (src/crava.cpp:1262-1264, :352-354) is an identity up to rounding and is not repeated here.
+    """
+
+    def __init__(self, tl, device="cuda"):
+        self.tl = tl
+        dev = torch.device(device)
+        f32 = dict(dtype=torch.float32, device=dev)
+        nxp, nyp, nzp, n = tl.nxp, tl.nyp, tl.nzp, tl.ntheta
+        cnxp, rnxp = api.dims(nxp)
+        shape = (nzp, nyp, rnxp)
+        self.shape = shape
+        s = torch.cuda.current_stream()
+        corr_xy = torch.from_numpy(np.ascontiguousarray(tl.corr_xy, dtype=np.float32)).to(**f32)
+        circ_t = torch.from_numpy(np.ascontiguousarray(tl.circ_corr_t, dtype=np.float32)).to(**f32)
+        F = tl.sigma_full
+
+        def cov_spec(i, j):
+            c = torch.empty(shape, **f32)
+            api.check_call("cg_fill_param_corr", c, nxp, nyp, nzp, corr_xy, circ_t, 0.0, 0.0,
+                           float(np.float32(F[i, j])), s)
+            api.fft_in_place(c, nxp, api.COVARIANCE)
+            return c
+
+        self.ss0 = [cov_spec(i, j) for i, j in SS_PAIRS]
+        self.sd0 = [cov_spec(i, j) for i, j in SD_PAIRS]
+        self.dd0 = [cov_spec(i, j) for i, j in DD_PAIRS]
+        self.mu_s0 = []
+        for p in range(3):
+            m = torch.zeros(shape, **f32)
+            m[:, :, :nxp] = float(tl.mu_static[p])
+            api.fft_in_place(m, nxp, api.PARAMETER)
+            self.mu_s0.append(m)
+        self.mu_d0 = [torch.zeros(shape, **f32) for _ in range(3)]
+        # working state (restored from the pristine copies above before a run)
+        self.mu_s = [torch.empty(shape, **f32) for _ in range(3)]
+        self.mu_d = [torch.empty(shape, **f32) for _ in range(3)]
+        self.ss = [torch.empty(shape, **f32) for _ in range(6)]
+        self.sd = [torch.empty(shape, **f32) for _ in range(9)]
+        self.dd = [torch.empty(shape, **f32) for _ in range(6)]
+        self.mu_cur = [torch.empty(shape, **f32) for _ in range(3)]
+        self.cov_cur = [torch.empty(shape, **f32) for _ in range(6)]
+        self.data = [torch.empty(shape, **f32) for _ in range(n)]
+        self.post_mean = [torch.empty(shape, **f32) for _ in range(3)]
+        self.errcorr = torch.empty(shape, **f32)
+        api.check_call("cg_fill_err_corr", self.errcorr, nxp, nyp, nzp, corr_xy, 0.0, 0.0, s)
+        api.fft_in_place(self.errcorr, nxp, api.COVARIANCE)
+        self.tables = api.operator_tables(tl.wavelets, tl.A, tl.nz, nzp, tl.dt_ms, tl.low_cut, tl.high_cut,
+                                          tl.min_rel_thick)
+        self.data_in, self.ws = [], []
+        for v in tl.vintages:
+            self.data_in.append(torch.from_numpy(np.stack(v["data"])).to(**f32))
+            ws = api.Workspace(nxp, nyp, nzp, n)
+            ws.set_model(self.tables, v["err_theta_cov"], tl.sigma_current(), tl.wnc, is4d=True)
+            self.ws.append(ws)
+        self.nfail_split = []
+        torch.cuda.synchronize()
+
+    def restore(self):
+        """Reset the state to the prior (not part of a run)."""
+        for dst, src in ((self.mu_s, self.mu_s0), (self.mu_d, self.mu_d0), (self.ss, self.ss0),
+                         (self.sd, self.sd0), (self.dd, self.dd0)):
+            for a, b in zip(dst, src):
+                a.copy_(b)
+        for ws in self.ws:
+            ws.reset_stats()
+        self.nfail_split = []
+
+    def run_vintage(self, v, stream=None):
+        nxp = self.tl.nxp
+        api.state4d_merge(self.mu_s, self.mu_d, self.ss, self.sd, self.dd, self.mu_cur, self.cov_cur, nxp,
+                          stream=stream)
+        for l, d in enumerate(self.data):
+            d.copy_(self.data_in[v][l])
+        api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
+        self.ws[v].invert_plain(self.data, self.mu_cur, [self.cov_cur[t] for t in MERGE_TO_BIN], self.errcorr,
+                                stream=stream)
+        self.nfail_split.append(api.state4d_split(self.mu_s, self.mu_d, self.ss, self.sd, self.dd, self.mu_cur,
+                                                  self.cov_cur, nxp, stream=stream))
+        for p in range(3):
+            self.post_mean[p].copy_(self.mu_cur[p])
+        api.fft_in_place_batch(self.post_mean, nxp, api.PARAMETER, inverse=True, stream=stream)
+
+    def run(self, stream=None):
+        for v in range(len(self.tl.vintages)):
+            self.run_vintage(v, stream=stream)
+
+    def state(self):
+        """(mu_s, mu_d, ss, sd, dd) spectra as numpy complex arrays."""
+        return [[api.as_spectrum(x).cpu().numpy() for x in grp]
+                for grp in (self.mu_s, self.mu_d, self.ss, self.sd, self.dd)]
+
+    def algorithmic_bytes(self):
+        """Joint 6-state / (vintages x n)-data solve lower bound: per bin, read the data and the 6 prior
+        means, write 6 means, the residuals and the 21 covariance entries (8 B each), plus one DATA
+        transform (4 B/cell + 8 B/bin) per data cube."""
+        tl = self.tl
+        nd = len(tl.vintages) * tl.ntheta
+        cells = tl.nxp * tl.nyp * tl.nzp
+        return tl.nbins * 8 * ((nd + 6) + (6 + nd + 21)) + nd * (4 * cells + 8 * tl.nbins)

@@ -219,6 +219,43 @@ def _pad_x(cube, nxp):
     return out
 
 
+def _forward_data(dm, A, wav, nxp, snr, rng):
+    """Forward model per stack in the norm-preserving spectral domain, d^ = kD(k) conj(W(k)) A m^
+    (src/crava.cpp:1349-1351), white noise on top at the stack's S/N; dm = truth minus prior mean."""
+    n = len(wav)
+    nzp = dm[0].shape[0]
+    kk = np.arange(nzp)
+    kD = -1.0 + np.exp(2j * np.pi * kk / nzp)  # FFT of {-1 at 0, +1 at nzp-1}
+    M = [_fftn(x) for x in dm]
+    data = []
+    for l in range(n):
+        W = np.fft.fft(wav[l].astype(np.float64))
+        op = (kD * np.conj(W))[:, None, None]
+        s = np.real(_ifftn(op * sum(float(A[l, q]) * M[q] for q in range(3))))
+        var_s = float(np.var(s))
+        noise_sd = math.sqrt(var_s / max(snr[l] - 1.0, 1e-3))
+        d = s + rng.standard_normal(s.shape) * noise_sd
+        data.append(_pad_x(d, nxp))
+    return data
+
+
+def _err_theta_cov(data, nx, ny, nz, snr, theta_deg):
+    """Error covariance between stacks (Crava::computeDataVariance + setupErrorCorrelation)."""
+    n = len(data)
+    dvar = []
+    for l in range(n):
+        inner = data[l][:nz, :ny, :nx].astype(np.float32)
+        nzmask = inner != 0.0
+        dvar.append(float(np.sum(inner.astype(np.float64)[nzmask] ** 2) / max(1, int(nzmask.sum()))))
+    ev = np.array([dvar[l] / snr[l] for l in range(n)], dtype=np.float32)
+    ac = angular_corr(theta_deg)
+    etc = np.zeros((n, n), dtype=np.float64)
+    for i in range(n):
+        for j in range(n):
+            etc[i, j] = float(np.float32(math.sqrt(ev[i]) * math.sqrt(ev[j]) * np.float32(ac[i, j])))
+    return etc
+
+
 def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None, pad=0.25, dt_ms=4.0,
                   dx=25.0, dy=25.0, sn=4.0, stds=(0.10, 0.07, 0.05), corr=(0.7, 0.3, 0.3),
                   lateral_range=1000.0, temporal_range_ms=20.0, temporal_power=1.5, low_cut=5.0,
@@ -253,34 +290,9 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     mu = np.array([LN_VP, LN_VS, LN_RHO])
     truth = [mu[p] + sum(L0[p, q] * z[q] for q in range(3)) for p in range(3)]
 
-    # forward model per stack in the norm-preserving spectral domain:
-    # d^ = kD(k) conj(W(k)) A m^  (src/crava.cpp:1349-1351), white noise on top
-    kk = np.arange(nzp)
-    kD = -1.0 + np.exp(2j * np.pi * kk / nzp)  # FFT of {-1 at 0, +1 at nzp-1}
-    M = [_fftn(truth[p] - mu[p]) for p in range(3)]
-    data = []
     snr = sn if np.ndim(sn) else [sn] * n
-    for l in range(n):
-        W = np.fft.fft(wav[l].astype(np.float64))
-        op = (kD * np.conj(W))[:, None, None]
-        s = np.real(_ifftn(op * sum(float(A[l, q]) * M[q] for q in range(3))))
-        var_s = float(np.var(s))
-        noise_sd = math.sqrt(var_s / max(snr[l] - 1.0, 1e-3))
-        d = s + rng.standard_normal(s.shape) * noise_sd
-        data.append(_pad_x(d, nxp))
-
-    # error covariance between stacks (computeDataVariance + setupErrorCorrelation)
-    dvar = []
-    for l in range(n):
-        inner = data[l][:nz, :ny, :nx].astype(np.float32)
-        nzmask = inner != 0.0
-        dvar.append(float(np.sum(inner.astype(np.float64)[nzmask] ** 2) / max(1, int(nzmask.sum()))))
-    ev = np.array([dvar[l] / snr[l] for l in range(n)], dtype=np.float32)
-    ac = angular_corr(theta_deg)
-    etc = np.zeros((n, n), dtype=np.float64)
-    for i in range(n):
-        for j in range(n):
-            etc[i, j] = float(np.float32(math.sqrt(ev[i]) * math.sqrt(ev[j]) * np.float32(ac[i, j])))
+    data = _forward_data([truth[p] - mu[p] for p in range(3)], A, wav, nxp, snr, rng)
+    etc = _err_theta_cov(data, nx, ny, nz, snr, theta_deg)
 
     mean = [_pad_x(np.full((nzp, nyp, nxp), mu[p], dtype=np.float32), nxp) for p in range(3)]
     return Scenario(nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, dt_ms=dt_ms, theta_deg=list(theta_deg),
@@ -313,6 +325,13 @@ def scaled_config1(nxp, nyp, nzp, seed=20261204, **kw) -> Scenario:
                          notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=seed, **kw)
 
 
+def config3(seed=20261206, **kw) -> Scenario:
+    """Posterior simulation workload: 200^3 padded cube, 3 stacks 10/20/30 deg, config-0 prior and
+    wavelet (30 Hz Ricker, S/N 4); the realisations are drawn after the inversion."""
+    return make_scenario(160, 160, 160, [10.0, 20.0, 30.0], 30.0, nxp=200, nyp=200, nzp=200, sn=4.0,
+                         seed=seed, **kw)
+
+
 def config2(ncubes=64, seed=20261205, **kw):
     """64 independent cubes of uneven size: nx, ny ~ U{32..192}, nz ~ U{64..160},
     each padded (25 %) to the next 2/3/5/7-smooth size; 2-8 stacks at 0-40 deg,
@@ -327,3 +346,103 @@ def config2(ncubes=64, seed=20261205, **kw):
         out.append(make_scenario(nx, ny, nz, theta, float(rng.uniform(15, 45)), sn=float(rng.uniform(2, 6)),
                                  std_scale=float(rng.uniform(0.5, 1.5)), seed=seed + 1 + c, **kw))
     return out
+
+
+# ----------------------------------------------------------------------------
+# 4D time-lapse workloads (State4D: static + dynamic parameters, 6x6 prior)
+# ----------------------------------------------------------------------------
+
+@dataclass
+class TimeLapseScenario:
+    """A 6-parameter state (static ln Vp/Vs/rho and their dynamic changes) with a separable prior
+    (6x6 parameter covariance times one spatial correlation), observed by several vintages.  With no
+    evolution between vintages (E = I, c = 0, C = 0) every vintage sees the current state
+    m_s + m_d through the 3-parameter operator, with its own noise."""
+
+    nx: int
+    ny: int
+    nz: int
+    nxp: int
+    nyp: int
+    nzp: int
+    dt_ms: float
+    theta_deg: list
+    A: np.ndarray                 # (n, 3) float32
+    wavelets: np.ndarray          # (n, nzp) float32, FFT order
+    corr_xy: np.ndarray           # (nyp, nxp) float32
+    circ_corr_t: np.ndarray       # (nzp,) float32
+    sigma_full: np.ndarray        # (6, 6) float64: static 0..2, dynamic 3..5
+    mu_static: np.ndarray         # (3,) float64, log domain
+    vintages: list                # per vintage: {"data": n x (nzp, nyp, rnxp) float32, "err_theta_cov": (n, n)}
+    wnc: float = 0.1
+    low_cut: float = 5.0
+    high_cut: float = 55.0
+    min_rel_thick: float = 1.0
+
+    @property
+    def ntheta(self):
+        return len(self.theta_deg)
+
+    @property
+    def cnxp(self):
+        return self.nxp // 2 + 1
+
+    @property
+    def nbins(self):
+        return self.cnxp * self.nyp * self.nzp
+
+    def sigma_current(self):
+        """3x3 prior covariance of the current state m_s + m_d."""
+        F = self.sigma_full
+        return F[:3, :3] + F[3:, 3:] + F[:3, 3:] + F[3:, :3]
+
+
+def make_timelapse(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None, nvintages=2, pad=0.25,
+                   dt_ms=4.0, dx=25.0, dy=25.0, sn=4.0, stds=(0.10, 0.07, 0.05), corr=(0.7, 0.3, 0.3),
+                   dyn_std_range=(0.02, 0.04), static_dynamic_corr=0.3, lateral_range=1000.0,
+                   temporal_range_ms=20.0, temporal_power=1.5, low_cut=5.0, high_cut=55.0, wnc=0.1,
+                   seed=20261207) -> TimeLapseScenario:
+    rng = np.random.default_rng(seed)
+    nxp = nxp or padded_size(nx, pad)
+    nyp = nyp or padded_size(ny, pad)
+    nzp = nzp or padded_size(nz, pad)
+    n = len(theta_deg)
+    A = aki_richards_pp(theta_deg, 1500.0 / 3000.0)
+    wav = np.stack([ricker_fft_order(nzp, dt_ms, f_peak) for _ in range(n)]).astype(np.float32)
+    cxy = genexp_corr_xy(nxp, nyp, dx, dy, lateral_range)
+    corr_t = genexp_corr_t(max(nz, 2), dt_ms, temporal_range_ms, temporal_power)
+    cct = circ_corr_t(corr_t, int(math.floor(low_cut * (nzp * 0.001 * dt_ms))), nzp)
+    # 6x6 parameter covariance D^1/2 (M kron R) D^1/2, M = [[1, c], [c, 1]]: positive definite
+    r01, r02, r12 = corr
+    R = np.array([[1, r01, r02], [r01, 1, r12], [r02, r12, 1]], dtype=np.float64)
+    dyn = rng.uniform(dyn_std_range[0], dyn_std_range[1], 3)
+    sd = np.concatenate([np.asarray(stds, dtype=np.float64), dyn])
+    Mc = np.array([[1.0, static_dynamic_corr], [static_dynamic_corr, 1.0]])
+    F = np.kron(Mc, R) * sd[:, None] * sd[None, :]
+    # one realisation of the current state: (m_s - mu_s) + m_d = L6 z folded by [I I]
+    c3 = np.abs(np.real(np.fft.fft2(cxy.astype(np.float64))))[None, :, :] * \
+        np.abs(np.real(np.fft.fft(cct.astype(np.float64))))[:, None, None]
+    L6 = np.linalg.cholesky(F)
+    z = []
+    for _ in range(6):
+        w = rng.standard_normal((nzp, nyp, nxp))
+        z.append(np.real(_ifftn(_fftn(w) * np.sqrt(c3))))
+    x6 = [sum(L6[p, q] * z[q] for q in range(6)) for p in range(6)]
+    dm = [x6[p] + x6[p + 3] for p in range(3)]
+    snr = [sn] * n
+    vint = []
+    for _ in range(nvintages):
+        data = _forward_data(dm, A, wav, nxp, snr, rng)
+        vint.append({"data": data, "err_theta_cov": _err_theta_cov(data, nx, ny, nz, snr, theta_deg)})
+    return TimeLapseScenario(nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, dt_ms=dt_ms, theta_deg=list(theta_deg),
+                             A=A, wavelets=wav, corr_xy=cxy, circ_corr_t=cct, sigma_full=F,
+                             mu_static=np.array([LN_VP, LN_VS, LN_RHO]), vintages=vint, wnc=wnc, low_cut=low_cut,
+                             high_cut=high_cut)
+
+
+def config4(seed=20261207, **kw) -> TimeLapseScenario:
+    """4D time-lapse workload: 256x256x192 padded cube, two vintages x 4 stacks (0-40 deg, 25 Hz Ricker,
+    S/N 4 each, independent noise), static prior as config 0, dynamic log-std U(0.02, 0.04),
+    static-dynamic correlation 0.3."""
+    return make_timelapse(205, 205, 154, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=256, nyp=256, nzp=192,
+                          seed=seed, **kw)

@@ -62,6 +62,42 @@ def inversion_case(name, sc, is4d=False):
     return out
 
 
+def inversion_4d_case(name, tl, vintage=0):
+    """The 4D branch of the bin loop (findParameterVariances, src/seismicparametersholder.cpp:366-373) on
+    the merged current-state spectra of a time-lapse prior (State4D::merge restated in the oracle)."""
+    from crava_gb300.pipeline import SS_PAIRS, SD_PAIRS, DD_PAIRS, MERGE_TO_BIN
+    F = tl.sigma_full
+
+    def spec(i, j):
+        c = O.fill_param_corr(tl.nxp, tl.nyp, tl.nzp, tl.corr_xy, tl.circ_corr_t, 0, 0, np.float32(F[i, j]))
+        return O.ref_fft3d_r2c(c, tl.nxp, O.COVARIANCE)
+    ss = [spec(i, j) for i, j in SS_PAIRS]
+    sd = [spec(i, j) for i, j in SD_PAIRS]
+    dd = [spec(i, j) for i, j in DD_PAIRS]
+    _, rnxp = O.dims(tl.nxp)
+    mu_s = []
+    for p in range(3):
+        m = np.zeros((tl.nzp, tl.nyp, rnxp), np.float32)
+        m[:, :, :tl.nxp] = np.float32(tl.mu_static[p])
+        mu_s.append(O.ref_fft3d_r2c(m, tl.nxp, O.PARAMETER))
+    mu_d = [np.zeros_like(mu_s[0]) for _ in range(3)]
+    mu_cur, cov_cur = O.state4d_merge(mu_s, mu_d, ss, sd, dd, prec="f")
+    cov_bin = [cov_cur[t] for t in MERGE_TO_BIN]
+    v = tl.vintages[vintage]
+    tab = O.k_tables(tl.nxp, tl.wavelets, tl.A, tl.nz, tl.nzp, tl.dt_ms, tl.low_cut, tl.high_cut)
+    data = [O.ref_fft3d_r2c(d, tl.nxp, O.DATA) for d in v["data"]]
+    ec = O.ref_fft3d_r2c(O.fill_err_corr(tl.nxp, tl.nyp, tl.nzp, tl.corr_xy), tl.nxp, O.COVARIANCE)
+    s0 = tl.sigma_current()
+    res, mu, cov, nfail = O.ref_invert_bins(data, mu_cur, cov_bin, ec, tab, v["err_theta_cov"], s0, tl.wnc,
+                                            is4d=True)
+    out = dict(nxp=tl.nxp, nyp=tl.nyp, nzp=tl.nzp, theta_deg=np.array(tl.theta_deg), sigma0=s0,
+               err_theta_cov=v["err_theta_cov"], wnc=tl.wnc, K=tab["K"], em1=tab["em1"], em2=tab["em2"],
+               em3=tab["em3"], band=tab["band"], data_spec=np.stack(data), mean_spec=np.stack(mu_cur),
+               cov_spec=np.stack(cov_bin), errcorr_spec=ec, out_resid=np.stack(res), out_mean=np.stack(mu),
+               out_cov=np.stack(cov), nfail=nfail, is4d=1)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
 def simulation_case(name, inv, seed):
     nxp, nyp, nzp = int(inv["nxp"]), int(inv["nyp"]), int(inv["nzp"])
     noise = O.ref_fill_complex_noise(nxp, nyp, nzp, seed, 3)
@@ -84,6 +120,8 @@ def main():
     sc8 = S.make_scenario(9, 10, 12, [5.0 * i for i in range(8)], 35.0, nxp=12, nyp=14, nzp=15, sn=2.5, seed=5)
     inversion_case("inversion_n8odd.npz", sc8)
     simulation_case("simulation_c0small.npz", inv, 231171)
+    tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=8)
+    inversion_4d_case("inversion_4d_n4.npz", tl)
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

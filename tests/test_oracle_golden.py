@@ -35,15 +35,16 @@ def test_fft_matches_reference_fftw(oracle, case):
         assert rel(r[:, :, :nxp], g["c2r_cov"][:, :, :nxp]) < tol
 
 
-@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz",
+                                  "inversion_4d_n4.npz"])
 def test_bin_loop_bit_exact_vs_reference(oracle, case):
-    """Same spectra in -> the FP32 restatement reproduces lib_matr bit for bit."""
+    """Same spectra in -> the FP32 restatement reproduces lib_matr bit for bit (3D and 4D branches)."""
     g = golden(case)
     tab = {k: g[k] for k in ("K", "em1", "em2", "em3", "band")}
     tab["nxp"] = int(g["nxp"])
     res, mu, cov, nf = oracle.invert_bins(list(g["data_spec"]), list(g["mean_spec"]), list(g["cov_spec"]),
                                           g["errcorr_spec"], tab, g["err_theta_cov"], g["sigma0"], float(g["wnc"]),
-                                          prec="f")
+                                          is4d=bool(int(g["is4d"])), prec="f")
     assert nf == int(g["nfail"])
     np.testing.assert_array_equal(np.stack(res), g["out_resid"])
     np.testing.assert_array_equal(np.stack(mu), g["out_mean"])

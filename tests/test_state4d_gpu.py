@@ -59,3 +59,71 @@ def test_split_matches_oracle(cuda, oracle):
     print("split vs FP64 oracle:", errs, "fails", int(nfail.item()), nf)
     assert int(nfail.item()) == nf == 0
     assert max(errs) < 2e-5
+
+
+def _oracle_timelapse_chain(oracle, tl, state, errc, tables, prec="d"):
+    """merge -> bin loop (4D branch) -> split per vintage, all in the oracle."""
+    from crava_gb300.pipeline import MERGE_TO_BIN
+    mu_s, mu_d, ss, sd, dd = [list(g) for g in state]
+    tab = dict(tables, nxp=tl.nxp)
+    for v in tl.vintages:
+        mu_cur, cov_cur = oracle.state4d_merge(mu_s, mu_d, ss, sd, dd, prec=prec)
+        data = [oracle.fft3d_r2c(d, tl.nxp, oracle.DATA, prec) for d in v["data"]]
+        _, mu_post, cov_bin, _ = oracle.invert_bins(data, mu_cur, [cov_cur[t] for t in MERGE_TO_BIN], errc, tab,
+                                                    v["err_theta_cov"], tl.sigma_current(), tl.wnc, is4d=True,
+                                                    prec=prec)
+        cov_post = [None] * 6
+        for k, t in enumerate(MERGE_TO_BIN):
+            cov_post[t] = cov_bin[k]
+        (mu_s, mu_d, ss, sd, dd), _ = oracle.state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, prec=prec)
+    return mu_s, mu_d, ss, sd, dd
+
+
+def test_timelapse_two_vintages_matches_fp64_oracle_chain(cuda, oracle):
+    """Two vintages x 4 stacks: merge -> forward transforms -> plain bin loop (4D branch) -> split on the GPU
+    against the same chain in the FP64 oracle, from the same initial state spectra."""
+    from crava_gb300 import api, synthetic as S
+    from crava_gb300.pipeline import TimeLapse
+    tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=7)
+    run = TimeLapse(tl)
+    run.restore()
+    state0 = run.state()
+    errc = api.as_spectrum(run.errcorr).cpu().numpy()
+    run.run()
+    torch.cuda.synchronize()
+    got = run.state()
+    ref = _oracle_timelapse_chain(oracle, tl, state0, errc, run.tables)
+    names = ["mu_s", "mu_d", "ss", "sd", "dd"]
+    errs = {nm: rel(np.stack(a), np.stack(b)) for nm, a, b in zip(names, got, ref)}
+    upd = rel(np.stack(got[1]) - np.stack(state0[1]), np.stack(ref[1]) - np.stack(state0[1]))
+    print("timelapse vs FP64 oracle chain:", errs, "dynamic update", upd,
+          "split fails", [int(x.item()) for x in run.nfail_split])
+    assert all(int(x.item()) == 0 for x in run.nfail_split)
+    assert errs["mu_s"] < 1e-6 and errs["mu_d"] < 1e-4 and upd < 1e-4
+    assert errs["ss"] < 1e-5 and errs["sd"] < 1e-5 and errs["dd"] < 1e-5
+    # the posterior covariance of every block shrinks
+    assert all(np.abs(np.stack(g)).sum() <= np.abs(np.stack(s0)).sum() for g, s0 in zip(got[2:], state0[2:]))
+
+
+def test_plain_4d_bin_loop_matches_reference_lib_matr(cuda):
+    """The 4D branch of the plain bin loop against the reference's own lib_matr run on the same spectra."""
+    from conftest import golden
+    from crava_gb300 import api
+    g = golden("inversion_4d_n4.npz")
+    n = len(g["theta_deg"])
+    ws = api.Workspace(int(g["nxp"]), int(g["nyp"]), int(g["nzp"]), n)
+    tab = {k: g[k] for k in ("K", "em1", "em2", "em3", "band")}
+    ws.set_model(tab, g["err_theta_cov"], g["sigma0"], float(g["wnc"]), is4d=True)
+    data = [to_cube(x) for x in g["data_spec"]]
+    mean = [to_cube(x) for x in g["mean_spec"]]
+    cov = [to_cube(x) for x in g["cov_spec"]]
+    ws.invert_plain(data, mean, cov, to_cube(g["errcorr_spec"]))
+    torch.cuda.synchronize()
+    res = np.stack([from_cube(x) for x in data])
+    mu = np.stack([from_cube(x) for x in mean])
+    cv = np.stack([from_cube(x) for x in cov])
+    e_upd = rel(mu - g["mean_spec"], g["out_mean"] - g["mean_spec"])
+    e_res, e_cov = rel(res, g["out_resid"]), rel(cv, g["out_cov"])
+    print("4D plain vs reference: update", e_upd, "resid", e_res, "cov", e_cov)
+    assert e_upd < 1e-4 and e_res < 1e-5 and e_cov < 1e-5
+    assert ws.stats()["failed"] == int(g["nfail"])
