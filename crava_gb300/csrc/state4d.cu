@@ -27,18 +27,22 @@ struct S4Args {
   int *nfail;
 };
 
-__constant__ int c_ssi[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
-__constant__ int c_sdi[9][2] = {{0, 3}, {0, 4}, {0, 5}, {1, 3}, {1, 4}, {1, 5}, {2, 3}, {2, 4}, {2, 5}};
-__constant__ int c_ddi[6][2] = {{3, 3}, {3, 4}, {3, 5}, {4, 4}, {4, 5}, {5, 5}};
+// (row, column) of stored entry t of each block as compile-time functions: in
+// unrolled loops they fold to constants, so the 6x6 matrices stay in registers
+// (a table in memory would force them to local memory)
+__host__ __device__ constexpr int tri_r(int t) { return t < 3 ? 0 : t < 5 ? 1 : 2; }   // 00 01 02 11 12 22
+__host__ __device__ constexpr int tri_c(int t) { return t < 3 ? t : t < 5 ? t - 2 : 2; }
+__host__ __device__ constexpr int sd_r(int t) { return t / 3; }                        // (0,3) (0,4) ... (2,5)
+__host__ __device__ constexpr int sd_c(int t) { return 3 + t % 3; }
 
 __device__ __forceinline__ void load_full6(const S4Args &a, long b, float2 (*F)[6])
 {
 #pragma unroll
-  for (int t = 0; t < 6; t++) F[c_ssi[t][0]][c_ssi[t][1]] = a.ss[t][b];
+  for (int t = 0; t < 6; t++) F[tri_r(t)][tri_c(t)] = a.ss[t][b];
 #pragma unroll
-  for (int t = 0; t < 9; t++) F[c_sdi[t][0]][c_sdi[t][1]] = a.sd[t][b];
+  for (int t = 0; t < 9; t++) F[sd_r(t)][sd_c(t)] = a.sd[t][b];
 #pragma unroll
-  for (int t = 0; t < 6; t++) F[c_ddi[t][0]][c_ddi[t][1]] = a.dd[t][b];
+  for (int t = 0; t < 6; t++) F[3 + tri_r(t)][3 + tri_c(t)] = a.dd[t][b];
 #pragma unroll
   for (int l = 0; l < 6; l++)
 #pragma unroll
@@ -56,10 +60,9 @@ __global__ void k_state4d_merge(S4Args a)
   }
   float2 F[6][6];
   load_full6(a, b, F);
-  const int out[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
 #pragma unroll
   for (int t = 0; t < 6; t++) {
-    const int l = out[t][0], m = out[t][1];
+    const int l = tri_r(t), m = tri_c(t);
     float re = F[l][m].x;
     re += F[l + 3][m + 3].x;
     re += F[l + 3][m].x;
@@ -72,7 +75,7 @@ __global__ void k_state4d_merge(S4Args a)
   }
 }
 
-__global__ void __launch_bounds__(128) k_state4d_split(S4Args a)
+__global__ void __launch_bounds__(128, 3) k_state4d_split(S4Args a)
 {
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.csize) return;
@@ -166,11 +169,11 @@ __global__ void __launch_bounds__(128) k_state4d_split(S4Args a)
     if (a.nfail) atomicAdd(a.nfail, 1);
   }
 #pragma unroll
-  for (int t = 0; t < 6; t++) a.ss[t][b] = out[c_ssi[t][0]][c_ssi[t][1]];
+  for (int t = 0; t < 6; t++) a.ss[t][b] = out[tri_r(t)][tri_c(t)];
 #pragma unroll
-  for (int t = 0; t < 9; t++) a.sd[t][b] = out[c_sdi[t][0]][c_sdi[t][1]];
+  for (int t = 0; t < 9; t++) a.sd[t][b] = out[sd_r(t)][sd_c(t)];
 #pragma unroll
-  for (int t = 0; t < 6; t++) a.dd[t][b] = out[c_ddi[t][0]][c_ddi[t][1]];
+  for (int t = 0; t < 6; t++) a.dd[t][b] = out[3 + tri_r(t)][3 + tri_c(t)];
 #pragma unroll
   for (int l = 0; l < 3; l++) { a.mu_s[l][b] = muFpost[l]; a.mu_d[l][b] = muFpost[l + 3]; }
 }

@@ -66,6 +66,7 @@ def _oracle_timelapse_chain(oracle, tl, state, errc, tables, prec="d"):
     from crava_gb300.pipeline import MERGE_TO_BIN
     mu_s, mu_d, ss, sd, dd = [list(g) for g in state]
     tab = dict(tables, nxp=tl.nxp)
+    nfails = []
     for v in tl.vintages:
         mu_cur, cov_cur = oracle.state4d_merge(mu_s, mu_d, ss, sd, dd, prec=prec)
         data = [oracle.fft3d_r2c(d, tl.nxp, oracle.DATA, prec) for d in v["data"]]
@@ -75,8 +76,9 @@ def _oracle_timelapse_chain(oracle, tl, state, errc, tables, prec="d"):
         cov_post = [None] * 6
         for k, t in enumerate(MERGE_TO_BIN):
             cov_post[t] = cov_bin[k]
-        (mu_s, mu_d, ss, sd, dd), _ = oracle.state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, prec=prec)
-    return mu_s, mu_d, ss, sd, dd
+        (mu_s, mu_d, ss, sd, dd), nf = oracle.state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, prec=prec)
+        nfails.append(nf)
+    return (mu_s, mu_d, ss, sd, dd), nfails
 
 
 def test_timelapse_two_vintages_matches_fp64_oracle_chain(cuda, oracle):
@@ -92,17 +94,22 @@ def test_timelapse_two_vintages_matches_fp64_oracle_chain(cuda, oracle):
     run.run()
     torch.cuda.synchronize()
     got = run.state()
-    ref = _oracle_timelapse_chain(oracle, tl, state0, errc, run.tables)
+    ref, ref_fails = _oracle_timelapse_chain(oracle, tl, state0, errc, run.tables)
     names = ["mu_s", "mu_d", "ss", "sd", "dd"]
     errs = {nm: rel(np.stack(a), np.stack(b)) for nm, a, b in zip(names, got, ref)}
     upd = rel(np.stack(got[1]) - np.stack(state0[1]), np.stack(ref[1]) - np.stack(state0[1]))
     print("timelapse vs FP64 oracle chain:", errs, "dynamic update", upd,
           "split fails", [int(x.item()) for x in run.nfail_split])
-    assert all(int(x.item()) == 0 for x in run.nfail_split)
+    # bins with a zero prior (the temporal spectrum is cut to zero at k <= lowIntCut) keep their prior in
+    # split, exactly as in the reference; the counts agree
+    assert [int(x.item()) for x in run.nfail_split] == ref_fails
     assert errs["mu_s"] < 1e-6 and errs["mu_d"] < 1e-4 and upd < 1e-4
     assert errs["ss"] < 1e-5 and errs["sd"] < 1e-5 and errs["dd"] < 1e-5
-    # the posterior covariance of every block shrinks
-    assert all(np.abs(np.stack(g)).sum() <= np.abs(np.stack(s0)).sum() for g, s0 in zip(got[2:], state0[2:]))
+    # posterior variances (diagonal spectra of the static and dynamic blocks) never exceed the prior ones
+    for blk in (2, 4):
+        for t in (0, 3, 5):
+            post, prior = got[blk][t].real, state0[blk][t].real
+            assert np.all(post <= prior + 1e-6 * np.abs(prior).max())
 
 
 def test_plain_4d_bin_loop_matches_reference_lib_matr(cuda):
