@@ -171,6 +171,8 @@ def _declare(L):
         "cg_inversion_create": ([ct.POINTER(V), I, I, I, I, I, I, V], I),
         "cg_inversion_destroy": ([V], None),
         "cg_inversion_run_host": ([V, PP, PP, PP, PP, V, I], I),
+        "cg_inversion_submit_host": ([V, PP, PP, PP, PP, PP, PP, V, I], I),
+        "cg_inversion_wait": ([V], I),
         "cg_inversion_stats": ([V, ct.POINTER(I), ct.POINTER(I), ct.POINTER(I)], I),
         "cg_batch_create": ([ct.POINTER(V), V, I, I], I),
         "cg_batch_destroy": ([V], None),

@@ -282,6 +282,24 @@ class HostInversion:
         pe = ct.c_void_p(err_corr_real.ctypes.data) if err_corr_real is not None else None
         check(lib().cg_inversion_run_host(self.h, pd, pm, pc, pp, pe, self.FORMS[form]), "cg_inversion_run_host")
 
+    def submit(self, data, mean, resid_out, mean_out, cov_out, form="mixed", prior_cov_real=None,
+               err_corr_real=None):
+        """Queue one inversion (cg_inversion_submit_host); the buffers stay in use until wait()."""
+        def ptrs(xs):
+            arr = (ct.c_void_p * len(xs))(*[(x.data_ptr() if isinstance(x, torch.Tensor) else x.ctypes.data)
+                                            for x in xs])
+            return ct.cast(arr, ct.POINTER(ct.c_void_p)), arr
+        keep = [ptrs(x) for x in (data, mean, resid_out, mean_out, cov_out)]
+        pp, k4 = ptrs(prior_cov_real) if prior_cov_real is not None else (None, None)
+        pe = ct.c_void_p(err_corr_real.ctypes.data) if err_corr_real is not None else None
+        self._inflight = (keep, k4)
+        check(lib().cg_inversion_submit_host(self.h, *[k[0] for k in keep], pp, pe, self.FORMS[form]),
+              "cg_inversion_submit_host")
+
+    def wait(self):
+        check(lib().cg_inversion_wait(self.h), "cg_inversion_wait")
+        self._inflight = None
+
     def stats(self):
         a, b, c = ct.c_int(), ct.c_int(), ct.c_int()
         check(lib().cg_inversion_stats(self.h, ct.byref(a), ct.byref(b), ct.byref(c)), "cg_inversion_stats")

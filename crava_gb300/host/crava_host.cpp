@@ -264,6 +264,8 @@ struct cg_inversion_s {
   cudaStream_t stream = nullptr;
   cudaStream_t out_stream = nullptr;  // residual and covariance copies, beside the mean inverse transforms
   cudaEvent_t bins_done = nullptr;
+  cudaEvent_t out_done = nullptr;     // the last submit's output copies have read the device cubes
+  bool out_pending = false;
 };
 
 #define CG_TRY(...)                                    \
@@ -310,6 +312,7 @@ extern "C" int cg_inversion_create(cg_inversion *out, int nx, int ny, int nz, in
       cuda_check(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking), "stream");
       cuda_check(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking), "stream");
       cuda_check(cudaEventCreateWithFlags(&h->bins_done, cudaEventDisableTiming), "event");
+      cuda_check(cudaEventCreateWithFlags(&h->out_done, cudaEventDisableTiming), "event");
     } catch (...) {
       cg_inversion_destroy(h);
       throw;
@@ -330,56 +333,93 @@ extern "C" void cg_inversion_destroy(cg_inversion h)
   if (h->stream) cudaStreamDestroy(h->stream);
   if (h->out_stream) cudaStreamDestroy(h->out_stream);
   if (h->bins_done) cudaEventDestroy(h->bins_done);
+  if (h->out_done) cudaEventDestroy(h->out_done);
   delete h;
+}
+
+static void submit_host(cg_inversion h, const float *const *seis_data, const float *const *mean,
+                        float *const *resid_out, float *const *mean_out, float *const *post_cov,
+                        const float *const *prior_cov_real, const float *err_corr_real, int form)
+{
+  const size_t bytes = sizeof(float) * (size_t)h->data[0]->getrsize();
+  cudaStream_t st = h->stream, os = h->out_stream;
+  // the previous submit's output copies (on the output stream) read the same device cubes
+  if (h->out_pending) cuda_check(cudaStreamWaitEvent(st, h->out_done, 0), "wait previous outputs");
+  {
+    cg::TraceScope ts("copy_h2d", st, (double)bytes * (h->ntheta + 3));
+    for (int l = 0; l < h->ntheta; l++) {
+      cuda_check(cudaMemcpyAsync(h->data[l]->devicePtr(), seis_data[l], bytes, cudaMemcpyHostToDevice, st), "H2D data");
+      h->data[l]->setTransformedStatus(false);
+    }
+    for (int p = 0; p < 3; p++) {
+      cuda_check(cudaMemcpyAsync(h->mean[p]->devicePtr(), mean[p], bytes, cudaMemcpyHostToDevice, st), "H2D mean");
+      h->mean[p]->setTransformedStatus(false);
+    }
+  }
+  Crava::Form f = form == 0 ? Crava::PLAIN : form == 1 ? Crava::FUSED_FP32 : Crava::FUSED_MIXED;
+  if (f == Crava::PLAIN) {
+    if (!prior_cov_real || !err_corr_real) throw Error(CG_ERR_ARG, "the plain form needs the real prior covariance cubes");
+    if (!h->errcorr) { h->errcorr = new FFTGrid(h->nx, h->ny, h->nz, h->nxp, h->nyp, h->nzp); h->errcorr->setType(FFTGrid::COVARIANCE); }
+    for (int t = 0; t < 6; t++) {
+      cuda_check(cudaMemcpyAsync(h->cov[t]->devicePtr(), prior_cov_real[t], bytes, cudaMemcpyHostToDevice, st), "H2D cov");
+      h->cov[t]->setTransformedStatus(false);
+    }
+    cuda_check(cudaMemcpyAsync(h->errcorr->devicePtr(), err_corr_real, bytes, cudaMemcpyHostToDevice, st), "H2D errCorr");
+    h->errcorr->setTransformedStatus(false);
+  }
+  FFTGrid *a = h->mean[0], *b = h->mean[1], *c = h->mean[2];
+  h->crava->computePostMeanResidAndFFTCov(h->data.data(), a, b, c, h->cov.data(), h->errcorr, f, st, h->bins_done);
+  // residual and covariance spectra leave while the posterior means are transformed back
+  cuda_check(cudaStreamWaitEvent(os, h->bins_done, 0), "wait bins");
+  {
+    cg::TraceScope ts("copy_d2h_resid_cov", os, (double)bytes * (h->ntheta + 6));
+    for (int l = 0; l < h->ntheta; l++)
+      cuda_check(cudaMemcpyAsync(resid_out[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H residual");
+    for (int t = 0; t < 6; t++)
+      cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H cov");
+  }
+  {
+    cg::TraceScope ts("copy_d2h_mean", st, (double)bytes * 3);
+    for (int p = 0; p < 3; p++)
+      cuda_check(cudaMemcpyAsync(mean_out[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
+  }
+  cuda_check(cudaEventRecord(h->out_done, os), "outputs-done event");
+  h->out_pending = true;
+}
+
+static void check_host_args(cg_inversion h, const void *a, const void *b, const void *c, const void *d, const void *e)
+{
+  if (!h || !a || !b || !c || !d || !e) throw Error(CG_ERR_ARG, "null argument");
 }
 
 extern "C" int cg_inversion_run_host(cg_inversion h, float *const *seis_data, float *const *mean, float *const *post_cov,
                                      const float *const *prior_cov_real, const float *err_corr_real, int form)
 {
-  if (!h || !seis_data || !mean || !post_cov) { cg::set_error("null argument"); return CG_ERR_ARG; }
   CG_TRY({
-    const size_t bytes = sizeof(float) * (size_t)h->data[0]->getrsize();
-    cudaStream_t st = h->stream;
-    {
-      cg::TraceScope ts("copy_h2d", st, (double)bytes * (h->ntheta + 3));
-      for (int l = 0; l < h->ntheta; l++) {
-        cuda_check(cudaMemcpyAsync(h->data[l]->devicePtr(), seis_data[l], bytes, cudaMemcpyHostToDevice, st), "H2D data");
-        h->data[l]->setTransformedStatus(false);
-      }
-      for (int p = 0; p < 3; p++) {
-        cuda_check(cudaMemcpyAsync(h->mean[p]->devicePtr(), mean[p], bytes, cudaMemcpyHostToDevice, st), "H2D mean");
-        h->mean[p]->setTransformedStatus(false);
-      }
-    }
-    Crava::Form f = form == 0 ? Crava::PLAIN : form == 1 ? Crava::FUSED_FP32 : Crava::FUSED_MIXED;
-    if (f == Crava::PLAIN) {
-      if (!prior_cov_real || !err_corr_real) throw Error(CG_ERR_ARG, "the plain form needs the real prior covariance cubes");
-      if (!h->errcorr) { h->errcorr = new FFTGrid(h->nx, h->ny, h->nz, h->nxp, h->nyp, h->nzp); h->errcorr->setType(FFTGrid::COVARIANCE); }
-      for (int t = 0; t < 6; t++) {
-        cuda_check(cudaMemcpyAsync(h->cov[t]->devicePtr(), prior_cov_real[t], bytes, cudaMemcpyHostToDevice, st), "H2D cov");
-        h->cov[t]->setTransformedStatus(false);
-      }
-      cuda_check(cudaMemcpyAsync(h->errcorr->devicePtr(), err_corr_real, bytes, cudaMemcpyHostToDevice, st), "H2D errCorr");
-      h->errcorr->setTransformedStatus(false);
-    }
-    FFTGrid *a = h->mean[0], *b = h->mean[1], *c = h->mean[2];
-    h->crava->computePostMeanResidAndFFTCov(h->data.data(), a, b, c, h->cov.data(), h->errcorr, f, st, h->bins_done);
-    // residual and covariance spectra leave while the posterior means are transformed back
-    cudaStream_t os = h->out_stream;
-    cuda_check(cudaStreamWaitEvent(os, h->bins_done, 0), "wait bins");
-    {
-      cg::TraceScope ts("copy_d2h_resid_cov", os, (double)bytes * (h->ntheta + 6));
-      for (int l = 0; l < h->ntheta; l++)
-        cuda_check(cudaMemcpyAsync(seis_data[l], h->data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H residual");
-      for (int t = 0; t < 6; t++)
-        cuda_check(cudaMemcpyAsync(post_cov[t], h->cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost, os), "D2H cov");
-    }
-    {
-      cg::TraceScope ts("copy_d2h_mean", st, (double)bytes * 3);
-      for (int p = 0; p < 3; p++)
-        cuda_check(cudaMemcpyAsync(mean[p], h->mean[p]->devicePtr(), bytes, cudaMemcpyDeviceToHost, st), "D2H mean");
-    }
-    const cudaError_t e1 = cudaStreamSynchronize(st), e2 = cudaStreamSynchronize(os);
+    check_host_args(h, seis_data, mean, post_cov, seis_data, mean);
+    submit_host(h, seis_data, mean, seis_data, mean, post_cov, prior_cov_real, err_corr_real, form);
+    const cudaError_t e1 = cudaStreamSynchronize(h->stream), e2 = cudaStreamSynchronize(h->out_stream);
+    cuda_check(e1 != cudaSuccess ? e1 : e2, "inversion");
+    return CG_OK;
+  })
+}
+
+extern "C" int cg_inversion_submit_host(cg_inversion h, const float *const *seis_data, const float *const *mean,
+                                        float *const *resid_out, float *const *mean_out, float *const *post_cov,
+                                        const float *const *prior_cov_real, const float *err_corr_real, int form)
+{
+  CG_TRY({
+    check_host_args(h, seis_data, mean, resid_out, mean_out, post_cov);
+    submit_host(h, seis_data, mean, resid_out, mean_out, post_cov, prior_cov_real, err_corr_real, form);
+    return CG_OK;
+  })
+}
+
+extern "C" int cg_inversion_wait(cg_inversion h)
+{
+  if (!h) { cg::set_error("null argument"); return CG_ERR_ARG; }
+  CG_TRY({
+    const cudaError_t e1 = cudaStreamSynchronize(h->stream), e2 = cudaStreamSynchronize(h->out_stream);
     cuda_check(e1 != cudaSuccess ? e1 : e2, "inversion");
     return CG_OK;
   })

@@ -288,6 +288,21 @@ void cg_inversion_destroy(cg_inversion inv);
 int cg_inversion_run_host(cg_inversion inv, float *const *seis_data, float *const *mean, float *const *post_cov,
                           const float *const *prior_cov_real, const float *err_corr_real, int form);
 
+/* No reference counterpart: cg_inversion_run_host split in two so that a
+ * caller with a sequence of inversions (several cubes, vintages or
+ * realisations of the inputs) can keep the link busy in both directions.
+ * submit queues the whole inversion on the context's streams and returns at
+ * once; wait blocks until its outputs are in host memory.  Inputs are read
+ * from seis_data / mean and outputs written to resid_out / mean_out, which may
+ * be the same buffers (the reference's in-place semantics).  Host buffers must
+ * stay untouched until wait returns.  Two contexts used in turn overlap one
+ * inversion's output copies with the next one's input copies and compute;
+ * submits on one context run in order. */
+int cg_inversion_submit_host(cg_inversion inv, const float *const *seis_data, const float *const *mean,
+                             float *const *resid_out, float *const *mean_out, float *const *post_cov,
+                             const float *const *prior_cov_real, const float *err_corr_real, int form);
+int cg_inversion_wait(cg_inversion inv);
+
 /* Counters of the last runs (see cg_workspace_stats). */
 int cg_inversion_stats(cg_inversion inv, int *flagged, int *failed, int *overflow);
 

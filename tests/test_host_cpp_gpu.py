@@ -56,3 +56,35 @@ def test_kernel_copy_between_host_and_device(cuda, native):
     assert native.cg_copy(d.data_ptr(), h.data_ptr(), 20, None) == -1          # size not a multiple of 16
     assert native.cg_copy(None, h.data_ptr(), 16, None) == -1
     assert native.cg_host_access() >= 0
+
+
+def test_submit_wait_pipeline_equals_synchronous_calls(cuda):
+    """Two contexts used in turn through cg_inversion_submit_host / cg_inversion_wait (out of place, inputs
+    untouched) give bit-identical outputs to one synchronous in-place cg_inversion_run_host per input set."""
+    from crava_gb300 import api
+    from crava_gb300 import synthetic as S
+    scs = [S.scaled_config1(48, 40, 64, seed=s) for s in (11, 12, 13)]
+    ctx = [api.HostInversion(scs[0]), api.HostInversion(scs[0])]
+    n = scs[0].ntheta
+    pinned = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()  # noqa: E731
+    ins = [[pinned(x) for x in list(sc.data) + list(sc.mean)] for sc in scs]
+    keep = [[x.clone() for x in s] for s in ins]
+    outs = [[torch.zeros_like(ins[0][0]).pin_memory() for _ in range(n + 3 + 6)] for _ in scs]
+    got = []
+    for i, sc in enumerate(scs):
+        c = ctx[i % 2]
+        if i >= 2:
+            c.wait()
+            got.append([x.clone() for x in outs[i - 2]])
+        c.submit(ins[i][:n], ins[i][n:], outs[i][:n], outs[i][n:n + 3], outs[i][n + 3:], "mixed")
+    for i in (1, 2):
+        ctx[i % 2].wait()
+        got.append([x.clone() for x in outs[i]])
+    for i in range(3):
+        assert all(torch.equal(a, b) for a, b in zip(ins[i], keep[i])), "inputs must stay untouched"
+        data = [x.numpy().copy() for x in keep[i][:n]]
+        mean = [x.numpy().copy() for x in keep[i][n:]]
+        cov = [np.zeros_like(data[0]) for _ in range(6)]
+        ctx[0].run(data, mean, cov, "mixed")
+        ref = data + mean + cov
+        assert all(np.array_equal(g.numpy(), r) for g, r in zip(got[i], ref)), i
