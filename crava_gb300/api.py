@@ -216,6 +216,35 @@ def simulate_fields(chol, fields, nxp, seed=0, real0=0, noise=None, post_mean=No
                                    _stream(stream)), "cg_simulate_fields")
 
 
+def exp_transform(t: torch.Tensor, stream=None):
+    """FFTGrid::expTransf in place (cg_exp_transform)."""
+    check(lib().cg_exp_transform(_vp(t), t.numel(), _stream(stream)), "cg_exp_transform")
+
+
+def log_transform(t: torch.Tensor, stream=None):
+    """FFTGrid::logTransf in place (cg_log_transform)."""
+    check(lib().cg_log_transform(_vp(t), t.numel(), _stream(stream)), "cg_log_transform")
+
+
+def inv_fft_exp_batch(cubes, nxp: int, cubetype: int, stream=None):
+    """Inverse transforms with expTransf fused into the last pass (cg_fft3d_c2r_exp_batch)."""
+    nzp, nyp, _ = cubes[0].shape
+    p, k = _pp(cubes)
+    check(lib().cg_fft3d_c2r_exp_batch(p, len(cubes), nxp, nyp, nzp, cubetype, _stream(stream)),
+          "cg_fft3d_c2r_exp_batch")
+
+
+def cov_origin(cov_real, nxp: int, nz: int, stream=None):
+    """(postVar0 3x3 float64, postCov00 (3, nz) float32) from real-domain covariance grids (00 11 22 01 02 12)."""
+    nzp, nyp, _ = cov_real[0].shape
+    v0 = np.zeros(9, dtype=np.float64)
+    c00 = np.zeros((3, nz), dtype=np.float32)
+    p, k = _pp(cov_real)
+    check(lib().cg_cov_origin(p, nxp, nyp, nzp, nz, v0.ctypes.data, c00.ctypes.data, _stream(stream)),
+          "cg_cov_origin")
+    return v0.reshape(3, 3), c00
+
+
 def state4d_merge(mu_s, mu_d, ss, sd, dd, mu_cur, cov_cur, nxp, stream=None):
     """State4D::merge/mergeCov into mu_cur[3], cov_cur[6] (order 00 01 02 11 12 22)."""
     nzp, nyp, _ = mu_s[0].shape

@@ -37,6 +37,21 @@ __host__ __device__ __forceinline__ C2<T> cconj(C2<T> a) { return mk<T>(a.x, -a.
 template <typename T>
 __host__ __device__ __forceinline__ C2<T> cscale(C2<T> a, T s) { return mk<T>(a.x * s, a.y * s); }
 
+// Output epilogues of the inverse transform's last pass.  kEpiExp is
+// FFTGrid::expTransf (src/fftgrid.cpp:1726-1743): every value but RMISSING
+// becomes exp(value).
+constexpr int kEpiNone = 0, kEpiExp = 1;
+constexpr float kRMissing = -99999.0f;
+template <typename T>
+__device__ __forceinline__ T epilogue(T v, int epi)
+{
+  if (epi == kEpiExp && v != (T)kRMissing) {
+    if constexpr (sizeof(T) == 4) return expf(v);
+    else return exp(v);
+  }
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // error plumbing for the C-ABI
 // ---------------------------------------------------------------------------

@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p
 template <typename T>
 __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet addend, AxisPlan p,
                                                           const C2<T> *__restrict__ twg, int nxp, int nrows,
-                                                          T postscale)
+                                                          T postscale, int epi)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int m = p.n;
@@ -261,6 +261,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet ad
         z.x += a.x;
         z.y += a.y;
       }
+      z.x = epilogue<T>(z.x, epi);
+      z.y = epilogue<T>(z.y, epi);
       ((C2<T> *)(base + (long)row * rnxp))[e] = z;
     }
   } else {
@@ -269,7 +271,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet ad
       int row = t / rnxp, e = t - row * rnxp;
       T v = (e < nxp) ? res[e * ldw + row].x * postscale : (T)0;
       if (add) v += add[(long)row * rnxp + e];
-      base[(long)row * rnxp + e] = v;
+      base[(long)row * rnxp + e] = epilogue<T>(v, epi);
     }
   }
 }
@@ -281,7 +283,7 @@ namespace {
 
 template <typename T>
 int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nyp, int nzp,
-                T scale, cudaStream_t st)
+                T scale, cudaStream_t st, int epi = kEpiNone)
 {
   const bool even = (nxp % 2) == 0;
   const int m = even ? nxp / 2 : nxp;
@@ -294,7 +296,7 @@ int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncub
   if (!tw) return cuda_status(cudaGetLastError(), "twiddle table");
   const int nrows = nyp * nzp;
   if constexpr (sizeof(T) == 4) {
-    const int rc = fast_rows(forward, cs, addend, ncubes, nxp, nrows, (float)scale, (const float2 *)tw, st);
+    const int rc = fast_rows(forward, cs, addend, ncubes, nxp, nrows, (float)scale, (const float2 *)tw, st, epi);
     if (rc < 0) return rc;
     if (rc == 1) return CG_OK;
   }
@@ -315,7 +317,7 @@ int launch_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncub
   } else {
     static bool attr[64] = {};
     CG_CUDA(smem_limit_once(k_c2r_rows<T>, kMaxSmem, attr));
-    k_c2r_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, addend, p, tw, nxp, nrows, scale);
+    k_c2r_rows<T><<<grid, kFFTThreads, smem, st>>>(cs, addend, p, tw, nxp, nrows, scale, epi);
   }
   CG_CHECK_LAUNCH(forward ? "k_r2c_rows" : "k_c2r_rows");
   return CG_OK;
@@ -405,8 +407,14 @@ int fft3d_c2r_add(void *const *bufs, const void *const *addends, int count, int 
 }
 
 template <typename T>
+int fft3d_c2r_epi(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, int epi, cudaStream_t st)
+{
+  return fft3d_add<T>(bufs, nullptr, count, nxp, nyp, nzp, cubetype, false, st, epi);
+}
+
+template <typename T>
 int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
-              bool forward, cudaStream_t st)
+              bool forward, cudaStream_t st, int epi)
 {
   int rc = check_dims(nxp, nyp, nzp, count);
   if (rc) return rc;
@@ -438,7 +446,7 @@ int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp,
       T post = covlike ? (T)(1.0 / N) : (T)(1.0 / sqrt(N));
       if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, +1, st))) return rc;
       if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, +1, st))) return rc;
-      if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st))) return rc;
+      if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st, epi))) return rc;
     }
   }
   return CG_OK;
@@ -446,6 +454,7 @@ int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp,
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_c2r_add<float>(void *const *, const void *const *, int, int, int, int, int, cudaStream_t);
+template int fft3d_c2r_epi<float>(void *const *, int, int, int, int, int, int, cudaStream_t);
 
 }  // namespace cg
 

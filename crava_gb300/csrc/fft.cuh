@@ -44,7 +44,10 @@ template <typename T>
 int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st);
 template <typename T>
 int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
-              bool forward, cudaStream_t st);
+              bool forward, cudaStream_t st, int epi = kEpiNone);
+// inverse transform whose last pass applies an output epilogue (kEpiExp: FFTGrid::expTransf fused)
+template <typename T>
+int fft3d_c2r_epi(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, int epi, cudaStream_t st);
 // inverse transform with a real cube added to each result (FFTGrid::add fused)
 template <typename T>
 int fft3d_c2r_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,

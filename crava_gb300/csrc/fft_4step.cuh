@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const f
 template <int M>
 __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet addend,
                                                              const float2 *__restrict__ twg, int nrows,
-                                                             float postscale)
+                                                             float postscale, int epi)
 {
   constexpr int N1 = fs_n1(M), N2 = M / N1;
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet
             z.x += s.x;
             z.y += s.y;
           }
-          op[e] = z;
+          op[e] = make_float2(epilogue<float>(z.x, epi), epilogue<float>(z.y, epi));
         }
         if (k1 == 0) {
           // the row's padding pair: zero, plus the addend's padding
@@ -362,7 +362,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet
             z.x += s.x;
             z.y += s.y;
           }
-          op[M] = z;
+          op[M] = make_float2(epilogue<float>(z.x, epi), epilogue<float>(z.y, epi));
         }
       }
     }

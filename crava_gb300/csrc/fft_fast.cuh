@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_fast(CubeSet cs, const
 template <int M>
 __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeSet addend,
                                                                const float2 *__restrict__ twg, int nrows,
-                                                               float postscale)
+                                                               float postscale, int epi)
 {
   constexpr int LDW = kRows + 1;
   constexpr int NX = 2 * M, CN = M + 1, RN = 2 * CN;
@@ -508,6 +508,8 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeS
       z.x += a.x;
       z.y += a.y;
     }
+    z.x = epilogue<float>(z.x, epi);
+    z.y = epilogue<float>(z.y, epi);
     ((float2 *)(base + (long)row * RN))[e] = z;
   }
 }
@@ -516,11 +518,11 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeS
 int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
               int sign, const float2 *tw, cudaStream_t st, int *done_cols);
 int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
-              const float2 *tw, cudaStream_t st);
+              const float2 *tw, cudaStream_t st, int epi = kEpiNone);
 // four-step kernels (fft_4step_*.cu); chosen by the tuning table
 int four_step_cols(int minb, const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride,
                    int nbatch, int sign, const float2 *tw, cudaStream_t st);
 int four_step_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
-                   const float2 *tw, cudaStream_t st);
+                   const float2 *tw, cudaStream_t st, int epi = kEpiNone);
 
 }  // namespace cg

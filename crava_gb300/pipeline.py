@@ -112,6 +112,28 @@ class Inversion:
         else:
             raise ValueError(form)
 
+    # -- output grids (the steps after the bin loop) ------------------------
+    def outputs(self, form, stream=None):
+        """The reference's steps after the inversion, on the working cubes of ``form``:
+        invFFTCovGrids (the 6 posterior covariance spectra to the real domain, in place), updatePriorVar +
+        createPostCov00 (src/seismicparametersholder.cpp:771-807), the residual spectra to the real domain
+        (src/crava.cpp:229-244, in place), and Vp / Vs / density = exp(posterior mean) as new cubes
+        (ParameterOutput::writeParameters, src/parameteroutput.cpp:87-108).
+        Returns (post_var0 (3,3), post_cov00 (3, nz), [Vp, Vs, rho] device cubes)."""
+        sc = self.sc
+        nxp = sc.nxp
+        cov = self.cov64 if form == "fp64" else self.cov
+        data = self.data64 if form == "fp64" else self.data
+        if form == "fp64":
+            raise ValueError("output grids are produced from the FP32 forms")
+        api.fft_in_place_batch(cov, nxp, api.COVARIANCE, inverse=True, stream=stream)
+        post_var0, post_cov00 = api.cov_origin(cov, nxp, sc.nz, stream=stream)
+        api.fft_in_place_batch(data, nxp, api.DATA, inverse=True, stream=stream)
+        elastic = [m.clone() for m in self.mean]
+        for e in elastic:
+            api.exp_transform(e, stream=stream)
+        return post_var0, post_cov00, elastic
+
     # -- results -----------------------------------------------------------
     def results(self, form):
         """(posterior-mean real cubes, residual spectra, posterior-cov spectra) as numpy."""

@@ -162,6 +162,31 @@ int cg_scale(float *buf, long n, float scalar, void *stream);
  * 16-byte aligned). */
 int cg_add(float *y, const float *x, long n, void *stream);
 
+/* ========================================================================
+ * Output grids after the bin loop
+ * ======================================================================== */
+
+/* FFTGrid::expTransf / logTransf (src/fftgrid.cpp:1726-1763) over n floats
+ * (device, 16-byte aligned).  exp keeps RMISSING (-99999) values; log maps
+ * RMISSING and values <= 0 to 0. */
+int cg_exp_transform(float *buf, long n, void *stream);
+int cg_log_transform(float *buf, long n, void *stream);
+
+/* invFFTInPlace of count cubes followed by expTransf, the exp fused into the
+ * transform's last pass (ParameterOutput::writeParameters,
+ * src/parameteroutput.cpp:87-108, on the log-domain posterior means). */
+int cg_fft3d_c2r_exp_batch(float *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, void *stream);
+
+/* SeismicParametersHolder::updatePriorVar + createPostCov00
+ * (src/seismicparametersholder.cpp:771-807) on the real-domain posterior
+ * covariance grids cov_real[6] (order 00 11 22 01 02 12, after the
+ * COVARIANCE inverse transforms of invFFTCovGrids): post_var0 receives the
+ * symmetric 3x3 lag-0 matrix (row-major), post_cov00 (may be NULL) the
+ * values (0,0,k), k < nz, of the alpha, beta and rho grids ([3][nz]).
+ * Synchronous. */
+int cg_cov_origin(const float *const *cov_real, int nxp, int nyp, int nzp, int nz, double *post_var0,
+                  float *post_cov00, void *stream);
+
 /* Page-lock a caller's host buffer (e.g. an FFTGrid's fftw_malloc block) so
  * the _host entry points copy it at full link speed; undo with
  * cg_host_unregister. */
