@@ -62,6 +62,16 @@ __host__ __device__ constexpr int fs_n1(int n)
   return n;
 }
 
+// N1 for the x-row passes: the smallest EVEN divisor of M not below sqrt(M)
+// (the R2C unpack pairs column k1 with N1 - k1); M is even for every row
+// specialisation
+__host__ __device__ constexpr int fs_n1_rows(int m)
+{
+  for (int d = 2; d <= m; d += 2)
+    if (m % d == 0 && d * d >= m) return d;
+  return m;
+}
+
 // column tile width: 16 columns when both factors are >= 16 (256 items per
 // pass), else 32
 __host__ __device__ constexpr int fs_cols_w(int n)
@@ -153,7 +163,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
 // items for the 256 threads of both passes
 __host__ __device__ constexpr int fs_rows_per_cta(int m)
 {
-  const int a = kFFTThreads / (m / fs_n1(m)), b = 2 * kFFTThreads / fs_n1(m);
+  const int a = kFFTThreads / (m / fs_n1_rows(m)), b = 2 * kFFTThreads / fs_n1_rows(m);
   return a > b ? a : b;
 }
 
@@ -161,7 +171,7 @@ __host__ __device__ constexpr int fs_rows_per_cta(int m)
 // two rows a half-warp touches fall in opposite bank halves
 __host__ __device__ constexpr int fs_row_pitch(int m)
 {
-  const int need = (m / fs_n1(m)) * (fs_n1(m) + 1);
+  const int need = (m / fs_n1_rows(m)) * (fs_n1_rows(m) + 1);
   return need + ((8 - need % 16) + 16) % 16;
 }
 
@@ -177,7 +187,7 @@ template <int M>
 __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const float2 *__restrict__ twg, int nrows,
                                                              float prescale)
 {
-  constexpr int N1 = fs_n1(M), N2 = M / N1;
+  constexpr int N1 = fs_n1_rows(M), N2 = M / N1;
   static_assert(N1 % 2 == 0, "the R2C pairing needs an even N1");
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
   constexpr int NX = 2 * M, CN = M + 1;
@@ -277,7 +287,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet
                                                              const float2 *__restrict__ twg, int nrows,
                                                              float postscale, int epi)
 {
-  constexpr int N1 = fs_n1(M), N2 = M / N1;
+  constexpr int N1 = fs_n1_rows(M), N2 = M / N1;
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
   constexpr int NX = 2 * M, CN = M + 1;
   constexpr int P1 = RPC * N2, P2 = RPC * N1;

@@ -1,0 +1,67 @@
+// Launch helpers of the four-step kernels (fft_4step.cuh), shared by the
+// translation units that instantiate them for different lengths.
+#pragma once
+
+#include "fft_4step.cuh"
+#include "trace.cuh"
+
+namespace cg {
+
+template <int N, int MINB>
+int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+                   const float2 *tw, cudaStream_t st)
+{
+  constexpr int W = fs_cols_w(N);
+  const size_t smem = ((size_t)N * W + N) * sizeof(float2);
+  static bool attr_set[64] = {};
+  cudaError_t e = smem_limit_once(k_fft_cols_4s<N, W, MINB>, smem, attr_set);
+  if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_4s attribute");
+  ColsGeom g;
+  g.axis_stride = axis_stride;
+  g.batch_stride = batch_stride;
+  g.nfull = ncols / W;
+  g.ntail = ncols - g.nfull * W;
+  g.nbatch = nbatch;
+  const int groups = ceil_div(nbatch, W);
+  const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
+  dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
+  TraceScope ts("k_fft_cols_4s", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
+  k_fft_cols_4s<N, W, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_4s");
+  return 1;
+}
+
+template <int M>
+int launch_rows_4s(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nrows, float scale,
+                   const float2 *tw, cudaStream_t st, int epi)
+{
+  constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M);
+  const size_t smem = ((size_t)RPC * P + 2 * M) * sizeof(float2);
+  dim3 grid(ceil_div(nrows, RPC), 1, ncubes);
+  const double bytes = (double)ncubes * nrows * (2.0 * M * sizeof(float) + (M + 1.0) * sizeof(float2));
+  static bool attr_fwd[64] = {}, attr_inv[64] = {};
+  cudaError_t e;
+  if (forward) {
+    e = smem_limit_once(k_r2c_rows_4s<M>, smem, attr_fwd);
+    if (e != cudaSuccess) return cuda_status(e, "k_r2c_rows_4s attribute");
+    TraceScope ts("k_r2c_rows_4s", st, bytes);
+    k_r2c_rows_4s<M><<<grid, kFFTThreads, smem, st>>>(cs, tw, nrows, scale);
+  } else {
+    e = smem_limit_once(k_c2r_rows_4s<M>, smem, attr_inv);
+    if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_4s attribute");
+    TraceScope ts("k_c2r_rows_4s", st, bytes);
+    k_c2r_rows_4s<M><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale, epi);
+  }
+  CG_CHECK_LAUNCH(forward ? "k_r2c_rows_4s" : "k_c2r_rows_4s");
+  return 1;
+}
+
+// further lengths (fft_4step_cols_ext*.cu, fft_4step_rows_ext*.cu): 0 when not handled
+int four_step_cols_ext0(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
+int four_step_cols_ext1(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
+int four_step_cols_ext2(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
+int four_step_cols_ext3(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
+int four_step_rows_ext0(bool, const CubeSet &, const CubeSet &, int, int, int, float, const float2 *, cudaStream_t, int);
+int four_step_rows_ext1(bool, const CubeSet &, const CubeSet &, int, int, int, float, const float2 *, cudaStream_t, int);
+
+}  // namespace cg

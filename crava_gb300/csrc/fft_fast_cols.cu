@@ -135,7 +135,9 @@ int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride,
     CG_COLS(64) CG_COLS(80) CG_COLS(96) CG_COLS(100) CG_COLS(120) CG_COLS(128) CG_COLS(160) CG_COLS(192)
     CG_COLS(200) CG_COLS(240) CG_COLS(256) CG_COLS(320) CG_COLS(384) CG_COLS(400) CG_COLS(480) CG_COLS(512)
 #undef CG_COLS
-    default: return 0;
+    default:  // further lengths exist only as four-step kernels
+      rc = four_step_cols(minb_for(n), cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+      break;
   }
   if (rc == 1) *done_cols = ncols;
   return rc;

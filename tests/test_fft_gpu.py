@@ -173,3 +173,21 @@ def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
         from crava_gb300 import _native
         native.cg_tune_clear()
         _native._apply_tuning(native)
+
+
+# four-step kernels of the further 7-smooth lengths (columns 16..504, even x rows up to nxp = 504)
+EXT_SIZES = [(42, 54, 90), (126, 189, 144), (36, 500, 21), (180, 35, 405), (56, 243, 16), (504, 98, 75),
+             (432, 448, 18), (84, 27, 441), (252, 150, 49), (300, 225, 28), (216, 63, 486), (448, 125, 32),
+             (196, 336, 20), (288, 81, 360), (140, 392, 45), (112, 270, 105)]
+
+
+@pytest.mark.parametrize("dims", EXT_SIZES)
+def test_extended_lengths_match_oracle(cuda, oracle, dims):
+    from crava_gb300 import api
+    nxp, nyp, nzp = dims
+    x, ref = _variant_case(oracle, nxp, nyp, nzp)
+    t = torch.from_numpy(x.copy()).cuda()
+    api.fft_in_place(t, nxp, api.DATA)
+    assert rel(from_cube(t), ref) < FFT_TOL
+    api.inv_fft_in_place(t, nxp, api.DATA)
+    assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL
