@@ -82,27 +82,35 @@ __device__ __forceinline__ void bin_normals(uint64_t seed, int realisation, long
   for (int t = 0; t < 6; t++) g6[t] = g[t];
 }
 
-// complex noise of the three parameters at flat bin index i, following the
-// structure of FFTGrid::fillInComplexNoise: bins of the x=0 plane (and of the
-// last x plane where the flat index is odd) are real when self-conjugate and
-// the conjugate of their partner's draw when the partner comes first in the
-// flat order; every other bin is an independent complex draw of variance 1.
-__device__ __forceinline__ void noise3_at(uint64_t seed, int realisation, long i, int cnxp, int nyp, int nzp,
-                                          float2 *s)
+// Structure of FFTGrid::fillInComplexNoise at flat bin index i: bins of the
+// x=0 plane (and of the last x plane where the flat index is odd) are real
+// when self-conjugate and the conjugate of their partner's draw when the
+// partner comes first in the flat order; every other bin is an independent
+// complex draw of variance 1.  The structure does not depend on the
+// realisation, so it is worked out once per bin: *src is the bin whose draw
+// is used, the return value the kind (0 complex draw, 1 real draw, 2
+// conjugate of the partner's draw).
+__device__ __forceinline__ int noise_kind(long i, int cnxp, int nyp, int nzp, long *src)
 {
-  const float sd = 0.70710678118654752f;
   const long xshift = i % cnxp;
-  long src = i;
-  int kind = 0;  // 0 complex draw, 1 real draw, 2 conjugate of partner
+  *src = i;
   if (xshift == 0 || (xshift == cnxp - 1 && (i % 2) == 1)) {
     const long jk = (i - xshift) / cnxp;
     const long j = jk % nyp, k = jk / nyp;
     const long jcc = j == 0 ? 0 : nyp - j;
     const long kcc = k == 0 ? 0 : nzp - k;
     const long jkcc = jcc + kcc * nyp;
-    if (jkcc == jk) kind = 1;
-    else if (jkcc < jk) { kind = 2; src = jkcc * cnxp + xshift; }
+    if (jkcc == jk) return 1;
+    if (jkcc < jk) { *src = jkcc * cnxp + xshift; return 2; }
   }
+  return 0;
+}
+
+// complex noise of the three parameters for one realisation, given the bin's
+// noise_kind
+__device__ __forceinline__ void noise3_from(uint64_t seed, int realisation, long src, int kind, float2 *s)
+{
+  const float sd = 0.70710678118654752f;
   float g[6];
   bin_normals(seed, realisation, src, g);
 #pragma unroll
@@ -206,13 +214,15 @@ __global__ void k_sim_apply(ApplyArgs a)
   for (int t = 0; t < 9; t++) l[t] = a.L[(long)t * a.csize + b];
   const float2 L00 = make_float2(l[0], 0), L11 = make_float2(l[1], 0), L22 = make_float2(l[2], 0);
   const float2 L10 = make_float2(l[3], l[4]), L20 = make_float2(l[5], l[6]), L21 = make_float2(l[7], l[8]);
+  long src = b;
+  const int kind = a.noise[0] ? 0 : noise_kind(b, a.cnxp, a.nyp, a.nzp, &src);
   for (int r = 0; r < a.nreal; r++) {
     float2 s[3];
     if (a.noise[0]) {
 #pragma unroll
       for (int p = 0; p < 3; p++) s[p] = a.noise[p][b];
     } else {
-      noise3_at(a.seed, a.real0 + r, b, a.cnxp, a.nyp, a.nzp, s);
+      noise3_from(a.seed, a.real0 + r, src, kind, s);
     }
     float2 o[3];
     o[0] = cmul<float>(L00, s[0]);

@@ -246,8 +246,18 @@ def main():
             ms.append(e0.elapsed_time(e1))
         bins = a._batch.bins
         best = min(ms)
+        # per-kernel view: one eager (not graph-replayed) run under the launch tracer
+        a._batch.reset()
+        torch.cuda.synchronize()
+        _native.trace_enable(True)
+        a._batch.run(a.form, use_graph=False)
+        torch.cuda.synchronize()
+        tr = _native.trace_collect()
+        _native.trace_enable(False)
         print(json.dumps({"case": {k: v for k, v in vars(a).items() if not k.startswith("_")}, "bins": bins,
-                          "ms_per_batch": ms, "Mbins_per_s": bins / (best * 1e-3) / 1e6}))
+                          "ms_per_batch": ms, "Mbins_per_s": bins / (best * 1e-3) / 1e6,
+                          "eager_kernels": {k: {"launches": v[0], "ms": v[1],
+                                                "GBps": v[2] / max(v[1], 1e-12) / 1e6} for k, v in tr.items()}}))
         return
     run = {"fft": fft_case, "invert": invert_case, "batch": batch_case}[a.what]
     if a.what == "batch":

@@ -47,7 +47,7 @@ def test_inversion_outputs_match_oracle(cuda, oracle):
 
 def test_fused_inverse_exp_equals_inverse_then_exp(cuda):
     from crava_gb300 import api
-    for n in ((256, 64, 40), (90, 50, 36), (255, 21, 16)):   # four-step rows, generic even, generic odd
+    for n in ((256, 64, 40), (90, 50, 36), (245, 21, 16)):   # four-step rows, generic even, generic odd
         nxp, nyp, nzp = n
         _, rnxp = api.dims(nxp)
         g = torch.Generator(device="cuda").manual_seed(nxp)
