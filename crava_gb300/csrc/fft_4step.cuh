@@ -62,15 +62,20 @@ __host__ __device__ constexpr int fs_n1(int n)
   return n;
 }
 
-// N1 for the x-row passes: the smallest EVEN divisor of M not below sqrt(M)
-// (the R2C unpack pairs column k1 with N1 - k1); M is even for every row
-// specialisation
+// N1 for the x-row passes: for even M the smallest EVEN divisor not below
+// sqrt(M) (the R2C unpack then pairs column 0 with N1/2), for odd M the
+// smallest divisor not below sqrt(M) (column 0 is then unpaired)
 __host__ __device__ constexpr int fs_n1_rows(int m)
 {
+  if (m % 2) return fs_n1(m);
   for (int d = 2; d <= m; d += 2)
     if (m % d == 0 && d * d >= m) return d;
   return m;
 }
+
+// pass-2 items per row of the R2C pass: column pairs (k1, N1 - k1), with
+// column 0 paired with N1/2 (even N1) or alone (odd N1)
+__host__ __device__ constexpr int fs_r2c_items(int m) { return (fs_n1_rows(m) + 1) / 2; }
 
 // column tile width: 16 columns when both factors are >= 16 (256 items per
 // pass), else 32
@@ -80,9 +85,11 @@ __host__ __device__ constexpr int fs_cols_w(int n)
 }
 
 // ---------------------------------------------------------------------------
-// strided column pass.  Tiles and the column tail follow ColsGeom exactly as
-// in k_fft_cols_fast: full tiles of W adjacent columns, then the tail columns
-// gathered W batch rows at a time.
+// strided column pass.  Full tiles are W adjacent columns of one batch row.
+// The ntail columns left over in each batch row form tail tiles of
+// ntail x trows columns (trows = W / ntail consecutive batch rows), so a tail
+// tile still reads runs of ntail adjacent elements.  Grid columns x >= nfull
+// hold the tail tiles, numbered (x - nfull)*nbatch + y.
 // Shared layout: buf[(k1*N2 + n2)*W + c] (conflict-free for both passes).
 // ---------------------------------------------------------------------------
 template <int N, int W, int MINB>
@@ -96,33 +103,33 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + N * W;
   float2 *cube = (float2 *)cs.ptr[blockIdx.z];
-  long cstride;
-  int cvalid;
   float2 *base;
+  int tdiv, tvalid;  // lane c -> column c % tdiv of batch row c / tdiv; lanes c >= tvalid idle
   if ((int)blockIdx.x < g.nfull) {
     base = cube + (long)blockIdx.y * g.batch_stride + (long)blockIdx.x * W;
-    cstride = 1;
-    cvalid = W;
+    tdiv = W;
+    tvalid = W;
   } else {
-    const int groups = (g.nbatch + W - 1) / W;
     const int tt = ((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
-    const int tcol = tt / groups, grp = tt % groups;
-    if (tcol >= g.ntail) return;
-    base = cube + (long)g.nfull * W + tcol + (long)grp * W * g.batch_stride;
-    cstride = g.batch_stride;
-    cvalid = g.nbatch - grp * W;
+    const int r0 = tt * g.trows;
+    if (r0 >= g.nbatch) return;
+    base = cube + (long)g.nfull * W + (long)r0 * g.batch_stride;
+    tdiv = g.ntail;
+    tvalid = g.ntail * min(g.trows, g.nbatch - r0);
   }
-  const long as = g.axis_stride;
+  const long as = g.axis_stride, bs = g.batch_stride;
+  auto coff = [&](int c) -> long { return (long)(c % tdiv) + (long)(c / tdiv) * bs; };
   for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
   // pass 1, one item at a time (registers hold one item); the first item's
   // loads are issued before the barrier that publishes the twiddle table
   auto load1 = [&](int q, float2 *v) {
     const int t = q * kFFTThreads + threadIdx.x;
     const int c = t % W, n2 = t / W;
-    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && c < cvalid;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && c < tvalid;
+    const long o = ok ? coff(c) : 0;
 #pragma unroll
     for (int n1 = 0; n1 < N1; n1++)
-      v[n1] = ok ? base[(long)(N2 * n1 + n2) * as + (long)c * cstride] : make_float2(0.f, 0.f);
+      v[n1] = ok ? base[(long)(N2 * n1 + n2) * as + o] : make_float2(0.f, 0.f);
   };
   float2 v[N1];
   load1(0, v);
@@ -151,9 +158,10 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
 #pragma unroll
       for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[(k1 * N2 + n2) * W + c];
       reg_fft<float, N2, N1>(u, sign, tw);
-      if (c < cvalid) {
+      if (c < tvalid) {
+        const long o = coff(c);
 #pragma unroll
-        for (int k2 = 0; k2 < N2; k2++) base[(long)(k1 + N1 * k2) * as + (long)c * cstride] = u[k2];
+        for (int k2 = 0; k2 < N2; k2++) base[(long)(k1 + N1 * k2) * as + o] = u[k2];
       }
     }
   }
@@ -163,7 +171,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
 // items for the 256 threads of both passes
 __host__ __device__ constexpr int fs_rows_per_cta(int m)
 {
-  const int a = kFFTThreads / (m / fs_n1_rows(m)), b = 2 * kFFTThreads / fs_n1_rows(m);
+  const int a = kFFTThreads / (m / fs_n1_rows(m)), b = kFFTThreads / fs_r2c_items(m);
   return a > b ? a : b;
 }
 
@@ -181,17 +189,17 @@ __host__ __device__ constexpr int fs_row_pitch(int m)
 // M-point four-step gives Z[k], and the half-length unpack
 //   X[k] = E + W_2M^k O,  E = (Z[k] + conj Z[M-k])/2,  O = -i (Z[k] - conj Z[M-k])/2
 // needs Z[k] and Z[M-k] together: a pass-2 thread transforms the two columns
-// k1 and N1-k1 (k1 = 0 pairs with N1/2), which hold exactly those partners.
+// k1 and N1-k1, which hold exactly those partners; column 0 holds its own
+// partners and is paired with N1/2 when N1 is even, alone when N1 is odd.
 // ---------------------------------------------------------------------------
 template <int M>
 __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const float2 *__restrict__ twg, int nrows,
                                                              float prescale)
 {
-  constexpr int N1 = fs_n1_rows(M), N2 = M / N1;
-  static_assert(N1 % 2 == 0, "the R2C pairing needs an even N1");
+  constexpr int N1 = fs_n1_rows(M), N2 = M / N1, NI = fs_r2c_items(M);
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = N1 + 1;
   constexpr int NX = 2 * M, CN = M + 1;
-  constexpr int P1 = RPC * N2, P2 = RPC * (N1 / 2);
+  constexpr int P1 = RPC * N2, P2 = RPC * NI;
   constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
@@ -229,8 +237,10 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const f
   for (int q = 0; q < B2; q++) {
     const int t = q * kFFTThreads + threadIdx.x;
     if (P2 % kFFTThreads == 0 || t < P2) {
-      const int ka = t % (N1 / 2), row = t / (N1 / 2);
-      const int kb = ka == 0 ? N1 / 2 : N1 - ka;
+      const int ka = t % NI, row = t / NI;
+      // partner column (none for column 0 when N1 is odd: it is read but not used)
+      const bool has_b = ka != 0 || N1 % 2 == 0;
+      const int kb = ka == 0 ? (N1 % 2 == 0 ? N1 / 2 : 0) : N1 - ka;
       float2 a[N2], b[N2];
 #pragma unroll
       for (int n2 = 0; n2 < N2; n2++) {
@@ -238,7 +248,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const f
         b[n2] = buf[row * P + n2 * Q + kb];
       }
       reg_fft<float, N2, 2 * N1>(a, -1, tw);
-      reg_fft<float, N2, 2 * N1>(b, -1, tw);
+      if (has_b) reg_fft<float, N2, 2 * N1>(b, -1, tw);
       if (row < nr) {
         float2 *op = base + (long)row * CN;
         // Z[M-k] for k = ka + N1*k2 sits in b[N2-1-k2]; for ka = 0 it is a[(N2-k2) % N2]
@@ -255,7 +265,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const f
             float2 X = cadd<float>(E, cmul<float>(tw[k], O));
             op[k] = make_float2(X.x * prescale, X.y * prescale);
           }
-          {
+          if (has_b) {
             const int k = kb + N1 * k2;
             const float2 A = b[k2];
             const float2 Bc = ka == 0 ? b[N2 - 1 - k2] : a[N2 - 1 - k2];

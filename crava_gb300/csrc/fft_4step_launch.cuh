@@ -22,8 +22,9 @@ int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, l
   g.nfull = ncols / W;
   g.ntail = ncols - g.nfull * W;
   g.nbatch = nbatch;
-  const int groups = ceil_div(nbatch, W);
-  const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
+  g.trows = g.ntail > 0 ? W / g.ntail : 1;
+  const int tail_tiles = g.ntail > 0 ? ceil_div(nbatch, g.trows) : 0;
+  const int tail_cols = ceil_div(tail_tiles, nbatch);
   dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
   TraceScope ts("k_fft_cols_4s", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
   k_fft_cols_4s<N, W, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
@@ -63,5 +64,6 @@ int four_step_cols_ext2(const CubeSet &, int, int, int, long, long, int, int, co
 int four_step_cols_ext3(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
 int four_step_rows_ext0(bool, const CubeSet &, const CubeSet &, int, int, int, float, const float2 *, cudaStream_t, int);
 int four_step_rows_ext1(bool, const CubeSet &, const CubeSet &, int, int, int, float, const float2 *, cudaStream_t, int);
+int four_step_rows_ext2(bool, const CubeSet &, const CubeSet &, int, int, int, float, const float2 *, cudaStream_t, int);
 
 }  // namespace cg

@@ -19,7 +19,8 @@ int four_step_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int n
   }
   int rc;
   if ((rc = four_step_rows_ext0(forward, cs, addend, ncubes, m, nrows, scale, tw, st, epi))) return rc;
-  return four_step_rows_ext1(forward, cs, addend, ncubes, m, nrows, scale, tw, st, epi);
+  if ((rc = four_step_rows_ext1(forward, cs, addend, ncubes, m, nrows, scale, tw, st, epi))) return rc;
+  return four_step_rows_ext2(forward, cs, addend, ncubes, m, nrows, scale, tw, st, epi);
 }
 
 }  // namespace cg

@@ -120,6 +120,7 @@ struct ColsGeom {
   int nfull;          // full W-column tiles per batch row (grid.x = nfull + 1 when ntail > 0)
   int ntail;          // leftover columns after the full tiles
   int nbatch;
+  int trows;          // four-step kernel: batch rows per tail tile (its tail tiles are ntail x trows blocks)
 };
 
 template <int N, int W, int MINB>

@@ -28,6 +28,7 @@ int launch_v(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long ba
   g.nfull = ncols / kW;
   g.ntail = ncols - g.nfull * kW;
   g.nbatch = nbatch;
+  g.trows = 1;
   const int groups = ceil_div(nbatch, kW);
   const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
   dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
@@ -69,6 +70,7 @@ int launch_pipe(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long
   g.nfull = ncols / kW;
   g.ntail = ncols - g.nfull * kW;
   g.nbatch = nbatch;
+  g.trows = 1;
   const long groups = ceil_div(nbatch, kW);
   const long ntiles = (long)ncubes * ((long)nbatch * g.nfull + (long)g.ntail * groups);
   if (ntiles > 0x7fffffffL) { set_error("too many column tiles"); return CG_ERR_UNSUPPORTED; }
@@ -94,6 +96,7 @@ int launch_rd(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long b
   g.nfull = ncols / kW;
   g.ntail = ncols - g.nfull * kW;
   g.nbatch = nbatch;
+  g.trows = 1;
   const int groups = ceil_div(nbatch, kW);
   const int tail_cols = g.ntail > 0 ? ceil_div((long)g.ntail * groups, nbatch) : 0;
   dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
