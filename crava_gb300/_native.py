@@ -153,6 +153,7 @@ def _declare(L):
         "cg_invert_bins_plain": ([V, PP, PP, PP, V, V], I),
         "cg_prior_spectra": ([V, V, V, I, V], I),
         "cg_invert_bins_fused": ([V, PP, PP, PP, I, V], I),
+        "cg_invert_cubes_fused": ([V, PP, PP, PP, I, V], I),
         "cg_invert_bins_fused_f64": ([V, PP, PP, PP, V], I),
         "cg_operator_tables": ([I, I, I, V, V, F, F, F, F, V, V, V, V, V], I),
         "cg_find_closest_factorable": ([I], I),

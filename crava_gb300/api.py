@@ -184,6 +184,13 @@ class Workspace:
         check(lib().cg_prior_spectra(self.h, _vp(corr_xy), _vp(circ_corr_t), precision, _stream(stream)),
               "cg_prior_spectra")
 
+    def invert_cubes(self, data, mean, cov, precision=PREC_MIXED, stream=None):
+        """Whole fused inversion from real-domain cubes (cg_invert_cubes_fused)."""
+        pd, k1 = _pp(data)
+        pm, k2 = _pp(mean)
+        pc, k3 = _pp(cov)
+        check(lib().cg_invert_cubes_fused(self.h, pd, pm, pc, precision, _stream(stream)), "cg_invert_cubes_fused")
+
     def invert_fused(self, data, mean, cov, precision=PREC_MIXED, stream=None):
         pd, k1 = _pp(data)
         pm, k2 = _pp(mean)

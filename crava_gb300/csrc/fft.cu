@@ -451,7 +451,44 @@ int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp,
   }
   return CG_OK;
 }
+// The x and z passes of a 3D transform only (forward: x rows then z columns;
+// inverse: z columns then x rows), with the full 3D scaling.  The y pass is
+// left to the caller (the fused y-transform + bin kernel).
+template <typename T>
+int fft3d_xz(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st)
+{
+  int rc = check_dims(nxp, nyp, nzp, count);
+  if (rc) return rc;
+  if (cubetype < CG_DATA || cubetype > CG_OPERATOR) {
+    set_error("cubetype %d is not one of DATA/PARAMETER/COVARIANCE/VELOCITY/OPERATOR", cubetype);
+    return CG_ERR_ARG;
+  }
+  const int cnxp = nxp / 2 + 1;
+  const double N = (double)nxp * nyp * nzp;
+  const bool covlike = (cubetype == CG_COVARIANCE || cubetype == CG_OPERATOR);
+  for (int b0 = 0; b0 < count; b0 += kMaxBatch) {
+    const int nb = count - b0 < kMaxBatch ? count - b0 : kMaxBatch;
+    CubeSet cs, ad;
+    for (int i = 0; i < kMaxBatch; i++) { cs.ptr[i] = nullptr; ad.ptr[i] = nullptr; }
+    for (int i = 0; i < nb; i++) {
+      if (!bufs[b0 + i]) { set_error("null buffer %d", b0 + i); return CG_ERR_ARG; }
+      cs.ptr[i] = bufs[b0 + i];
+    }
+    if (forward) {
+      const T pre = covlike ? (T)1 : (T)(1.0 / sqrt(N));
+      if ((rc = launch_rows<T>(true, cs, ad, nb, nxp, nyp, nzp, pre, st))) return rc;
+      if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, -1, st))) return rc;
+    } else {
+      const T post = covlike ? (T)(1.0 / N) : (T)(1.0 / sqrt(N));
+      if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, +1, st))) return rc;
+      if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st))) return rc;
+    }
+  }
+  return CG_OK;
+}
+
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
+template int fft3d_xz<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_c2r_add<float>(void *const *, const void *const *, int, int, int, int, int, cudaStream_t);
 template int fft3d_c2r_epi<float>(void *const *, int, int, int, int, int, int, cudaStream_t);

@@ -45,6 +45,9 @@ int fft3d(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype,
 template <typename T>
 int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp, int nyp, int nzp, int cubetype,
               bool forward, cudaStream_t st, int epi = kEpiNone);
+// x and z passes only (see fft.cu)
+template <typename T>
+int fft3d_xz(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, bool forward, cudaStream_t st);
 // inverse transform whose last pass applies an output epilogue (kEpiExp: FFTGrid::expTransf fused)
 template <typename T>
 int fft3d_c2r_epi(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubetype, int epi, cudaStream_t st);

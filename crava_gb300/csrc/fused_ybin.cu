@@ -1,0 +1,66 @@
+// The fused inversion entry point (cg_invert_cubes_fused); kernel in fused_ybin.cuh.
+#include <cstring>
+
+#include "fused_ybin.cuh"
+#include "fused_entry.h"
+
+namespace cg {
+
+// y lengths with a fused kernel
+static bool ybin_length(int n) { return n == 256 || n == 128 || n == 200; }
+
+}  // namespace cg
+
+using namespace cg;
+
+int cg::invert_cubes_fused(cg_workspace w, float *const *data, float *const *mean, float *const *cov, int precision,
+                           void *stream, cudaEvent_t bins_done)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!data || !mean || !cov) { set_error("null buffer argument"); return CG_ERR_ARG; }
+  if (w->is4d) { set_error("the fused form needs a separable 3-parameter prior; use cg_invert_bins_plain for 4D"); return CG_ERR_UNSUPPORTED; }
+  if (precision != CG_PREC_FP32 && precision != CG_PREC_MIXED) { set_error("precision %d not valid for FP32 buffers", precision); return CG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nt = w->ntheta, nxp = w->nxp, nyp = w->nyp, nzp = w->nzp;
+  void *fwd[kMaxTheta + 3];
+  for (int l = 0; l < nt; l++) { if (!data[l]) { set_error("null data[%d]", l); return CG_ERR_ARG; } fwd[l] = data[l]; }
+  for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } fwd[nt + p] = mean[p]; }
+  for (int t = 0; t < 6; t++) if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; }
+  if (!ybin_length(nyp)) {
+    // no fused kernel for this y length: three-pass transforms around the bin kernel
+    if ((rc = fft3d<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;
+    if ((rc = cg_invert_bins_fused(w, data, mean, cov, precision, stream))) return rc;
+    if (bins_done) CG_CUDA(cudaEventRecord(bins_done, st));
+    return fft3d<float>((void *const *)mean, 3, nxp, nyp, nzp, CG_PARAMETER, false, st);
+  }
+  // DATA and PARAMETER share the 1/sqrt(N) forward scaling: one batched x + z pass over the n+3 cubes
+  if ((rc = fft3d_xz<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;
+  YBinArgs a;
+  memset(&a, 0, sizeof(a));
+  rc = fill_fused_args(w, (void *const *)data, (void *const *)mean, (void *const *)cov, &a.f);
+  if (rc) return rc;
+  a.ktab_d = w->ktab_d;
+  const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
+  for (int t = 0; t < 6; t++) a.sig0d[t] = (double)w->sigma0f[pq[t][0] * 3 + pq[t][1]];
+  a.tw = (const float2 *)twiddle_table<float>(nyp);
+  if (!a.tw) return cuda_status(cudaGetLastError(), "twiddle table");
+  a.mixed = precision == CG_PREC_MIXED;
+  CG_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(int), st));
+  const int tiles = ceil_div(a.f.cnxp, kYW);
+  const double bytes = 8.0 * (double)a.f.plane * nzp * ((nt + 3) + (nt + 3 + 6));
+  switch (nyp) {
+    case 256: rc = launch_ybin_256(a, nt, tiles, nzp, bytes, st); break;
+    case 200: rc = launch_ybin_200(a, nt, tiles, nzp, bytes, st); break;
+    default: rc = launch_ybin_128(a, nt, tiles, nzp, bytes, st); break;
+  }
+  if (rc) return rc;
+  if (bins_done) CG_CUDA(cudaEventRecord(bins_done, st));
+  return fft3d_xz<float>((void *const *)mean, 3, nxp, nyp, nzp, CG_PARAMETER, false, st);
+}
+
+extern "C" int cg_invert_cubes_fused(cg_workspace w, float *const *data, float *const *mean, float *const *cov,
+                                     int precision, void *stream)
+{
+  return cg::invert_cubes_fused(w, data, mean, cov, precision, stream, nullptr);
+}

@@ -63,3 +63,6 @@ struct Workspace {
 };
 
 }  // namespace cg
+
+// the C-ABI handle is the workspace itself
+struct cg_workspace_s : public cg::Workspace {};

@@ -11,6 +11,7 @@
 #include "cravagpu.h"
 #include "cravagpu_host.hpp"
 #include "../csrc/trace.cuh"
+#include "../csrc/fused_entry.h"
 
 namespace cg {
 void set_error(const char *fmt, ...);
@@ -205,13 +206,13 @@ int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha
     if (mean[p]->getIsTransformed()) throw Error(CG_ERR_STATE, "prior mean already transformed");
     fwd.push_back(mean[p]->devicePtr());
   }
-  // DATA and PARAMETER share the 1/sqrt(N) scaling: one batched transform
-  check(cg_fft3d_r2c_batch(fwd.data(), (int)fwd.size(), nxp_, nyp_, nzp_, CG_DATA, stream), "forward transforms");
   float *d[8], *mu[3], *cv[6];
   for (int l = 0; l < n; l++) { d[l] = seisData[l]->devicePtr(); seisData[l]->setTransformedStatus(true); }
   for (int p = 0; p < 3; p++) { mu[p] = mean[p]->devicePtr(); mean[p]->setTransformedStatus(true); }
   for (int t = 0; t < 6; t++) cv[t] = postCov[t]->devicePtr();
   if (form == PLAIN) {
+    // DATA and PARAMETER share the 1/sqrt(N) scaling: one batched transform
+    check(cg_fft3d_r2c_batch(fwd.data(), (int)fwd.size(), nxp_, nyp_, nzp_, CG_DATA, stream), "forward transforms");
     if (!errCorr) throw Error(CG_ERR_ARG, "the plain form needs the error-correlation cube");
     std::vector<float *> covs(cv, cv + 6);
     covs.push_back(errCorr->devicePtr());
@@ -222,8 +223,13 @@ int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha
     if (m_.corrGradI != 0.0f || m_.corrGradJ != 0.0f)
       throw Error(CG_ERR_UNSUPPORTED, "the fused form needs zero correlation gradients; use the plain form");
     check(cg_prior_spectra(ws_, d_corr_xy_, d_circ_t_, CG_PREC_FP32, stream), "prior spectra");
-    check(cg_invert_bins_fused(ws_, d, mu, cv, form == FUSED_MIXED ? CG_PREC_MIXED : CG_PREC_FP32, stream),
-          "bin loop (fused)");
+    // transforms, bin loop and inverse transforms of the means in one call (the y passes fused with the bins)
+    check(cg::invert_cubes_fused(ws_, d, mu, cv, form == FUSED_MIXED ? CG_PREC_MIXED : CG_PREC_FP32, stream,
+                                 (cudaEvent_t)binsDone),
+          "fused inversion");
+    for (int t = 0; t < 6; t++) { postCov[t]->setType(FFTGrid::COVARIANCE); postCov[t]->setTransformedStatus(true); }
+    for (int p = 0; p < 3; p++) mean[p]->setTransformedStatus(false);
+    return 0;
   }
   for (int t = 0; t < 6; t++) { postCov[t]->setType(FFTGrid::COVARIANCE); postCov[t]->setTransformedStatus(true); }
   if (binsDone) cuda_check(cudaEventRecord((cudaEvent_t)binsDone, (cudaStream_t)stream), "bins-done event");

@@ -15,8 +15,13 @@ place).  ``run(form)`` executes one inversion:
 * ``"plain"``  -- the reference dataflow on the GPU, all FP32: 5+3+7 forward
   transforms, the reference-order bin kernel, 3 inverse transforms;
 * ``"fp32"`` / ``"mixed"`` -- the fused form: the separable prior spectra are
-  rebuilt (two tiny transforms), 5+3 forward transforms, the fused bin kernel
-  (mixed: plus the FP64 fix-up pass), 3 inverse transforms;
+  rebuilt (two tiny transforms), then cg_invert_cubes_fused: x and z passes of
+  the 5+3 forward transforms, one kernel doing the y pass, the bin loop (mixed:
+  FP64 for guarded bins) and the inverse y pass of the means, then the z and x
+  passes of the 3 inverse transforms;
+* ``"fp32_3pass"`` / ``"mixed_3pass"`` -- the same arithmetic with three-pass
+  transforms around the stand-alone fused bin kernel (and the FP64 fix-up
+  pass);
 * ``"fp64"`` -- the fused form entirely in FP64 (accuracy reference).
 """
 from __future__ import annotations
@@ -95,6 +100,10 @@ class Inversion:
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
         elif form in ("fp32", "mixed"):
             prec = api.PREC_MIXED if form == "mixed" else api.PREC_FP32
+            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
+            self.ws.invert_cubes(self.data, self.mean, self.cov, prec, stream=stream)
+        elif form in ("fp32_3pass", "mixed_3pass"):
+            prec = api.PREC_MIXED if form == "mixed_3pass" else api.PREC_FP32
             self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
             api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, stream=stream)

@@ -276,6 +276,18 @@ int cg_prior_spectra(cg_workspace ws, const float *corr_xy, const float *circ_co
 int cg_invert_bins_fused(cg_workspace ws, float *const *data, float *const *mean, float *const *cov,
                          int precision, void *stream);
 
+/* The whole fused inversion from real-domain cubes (the transforms and bin
+ * loop of Crava::computePostMeanResidAndFFTCov, src/crava.cpp:177-184 and
+ * :975-1285): data[ntheta] real DATA cubes in, residual spectra out; mean[3]
+ * real prior-mean cubes in, real posterior means out; cov[6] posterior
+ * covariance spectra out.  For y lengths 128, 200 and 256 the forward
+ * transform runs its axes as x, z, y and the y pass is fused with the bin
+ * loop and the inverse y pass of the means (one HBM round trip fewer for
+ * every cube); other sizes run the three-pass transforms around
+ * cg_invert_bins_fused.  Needs cg_prior_spectra first. */
+int cg_invert_cubes_fused(cg_workspace ws, float *const *data, float *const *mean, float *const *cov,
+                          int precision, void *stream);
+
 /* Fused posterior on FP64 spectra (needs cg_prior_spectra with CG_PREC_FP64). */
 int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,
                              void *stream);

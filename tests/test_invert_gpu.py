@@ -78,7 +78,7 @@ def test_fused_matches_fp64_oracle_on_reference_inputs(cuda, oracle, case, form)
     assert e_upd < 1e-4 and e_res < 1e-5 and e_cov < 1e-4
 
 
-@pytest.mark.parametrize("form", ["plain", "fp32", "mixed", "fp64"])
+@pytest.mark.parametrize("form", ["plain", "fp32", "mixed", "fp64", "mixed_3pass"])
 def test_pipeline_matches_fp64_oracle(cuda, oracle, form):
     """Whole inversion from real-domain cubes (config-1 physics on a 40x36x48 cube)."""
     from crava_gb300 import synthetic as S
@@ -99,3 +99,31 @@ def test_pipeline_matches_fp64_oracle(cuda, oracle, form):
     tol = 1e-10 if form == "fp64" else 1e-4
     assert e_mean < (1e-12 if form == "fp64" else 1e-6)
     assert e_upd < tol and e_res < tol and e_cov < tol
+
+
+# y lengths with the fused y-transform + bin-loop kernel (cg_invert_cubes_fused), tail x tiles included
+@pytest.mark.parametrize("dims,cond", [((64, 128, 48), 0.0), ((40, 200, 32), 0.0), ((48, 256, 24), 0.0),
+                                       ((64, 128, 48), 1.0001), ((30, 256, 20), 1.0001)])
+def test_fused_y_kernel_matches_fp64_oracle(cuda, oracle, dims, cond):
+    """cond = 1.0001 sends almost every in-band bin through the in-kernel FP64 path."""
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    nxp, nyp, nzp = dims
+    sc = S.scaled_config1(nxp, nyp, nzp, seed=nyp + nzp)
+    inv = Inversion(sc, forms=("mixed",), cond_threshold=cond)
+    inv.restore("mixed")
+    inv.ws.reset_stats()
+    inv.run("mixed")
+    torch.cuda.synchronize()
+    st = inv.ws.stats()
+    pm, res, cov = inv.results("mixed")
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    e = (rel(pm, post64), rel(pm - prior, post64 - prior), rel(res, res64), rel(cov, cov64))
+    print(dims, cond, "fused y kernel vs FP64 oracle (mean, update, resid, cov):", e, st)
+    assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
+    inband = int(inv.tables["band"].sum()) * sc.cnxp * sc.nyp
+    if cond > 0:
+        assert st["flagged"] > inband // 2   # the FP64 path ran for most in-band bins
+    else:
+        assert st["flagged"] == 0
