@@ -124,6 +124,8 @@ def _apply_tuning(L):
             L.cg_tune_set(2, int(n), int(v["minb"]))
         for n, v in t.get("rows", {}).items():
             L.cg_tune_set(3, int(n), int(v["kernel"]))
+        for n, v in t.get("fused_y", {}).items():
+            L.cg_tune_set(4, int(n), int(v["fused"]))
     except (OSError, ValueError, KeyError):
         pass  # a damaged table leaves the built-in defaults
 

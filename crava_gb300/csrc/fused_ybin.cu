@@ -6,8 +6,13 @@
 
 namespace cg {
 
-// y lengths with a fused kernel
-static bool ybin_length(int n) { return n == 256 || n == 128 || n == 200; }
+// y lengths with a fused kernel, and whether the tuning table selects it
+// (CG_TUNE_FUSED_Y; off by default: measured slower than the three passes
+// around the stand-alone bin kernel at 256^3, see cg_tune_set)
+static bool ybin_length(int n)
+{
+  return (n == 256 || n == 128 || n == 200) && cg_tune_get(CG_TUNE_FUSED_Y, n) == 1;
+}
 
 }  // namespace cg
 

@@ -1,7 +1,7 @@
 // Tuning table: launch variants chosen per transform length or stack count.
 // Defaults are built in (measured on GB300); cg_tune_set overrides them, and
-// the environment variables CRAVA_COLS_MINB, CRAVA_COLS_PIPE, CRAVA_BIN_MINB
-// and CRAVA_ROWS_KERNEL override both (used by ad-hoc sweeps).
+// the environment variables CRAVA_COLS_MINB, CRAVA_COLS_PIPE, CRAVA_BIN_MINB,
+// CRAVA_ROWS_KERNEL and CRAVA_FUSED_Y override both (used by ad-hoc sweeps).
 #include <cstdlib>
 #include <map>
 #include <mutex>
@@ -21,6 +21,7 @@ const char *env_name(int key)
     case CG_TUNE_COLS_PIPE: return "CRAVA_COLS_PIPE";
     case CG_TUNE_BIN_MINB: return "CRAVA_BIN_MINB";
     case CG_TUNE_ROWS_KERNEL: return "CRAVA_ROWS_KERNEL";
+    case CG_TUNE_FUSED_Y: return "CRAVA_FUSED_Y";
     default: return nullptr;
   }
 }
@@ -47,11 +48,12 @@ using namespace cg;
 
 extern "C" int cg_tune_set(int key, int n, int value)
 {
-  if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_ROWS_KERNEL || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
+  if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_FUSED_Y || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
   const bool ok = (key == CG_TUNE_COLS_MINB && (value == 2 || value == 3)) ||
                   (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 3)) ||
                   (key == CG_TUNE_BIN_MINB && (value == 1 || value == 6)) ||
-                  (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1));
+                  (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||
+                  (key == CG_TUNE_FUSED_Y && (value == 0 || value == 1));
   if (!ok) { set_error("cg_tune_set: value %d not valid for key %d", value, key); return CG_ERR_ARG; }
   std::lock_guard<std::mutex> lk(g_mu);
   g_table[((long)key << 32) | (unsigned)n] = value;
@@ -72,6 +74,7 @@ extern "C" int cg_tune_get(int key, int n)
     case CG_TUNE_COLS_PIPE: return tune_get(key, n, n == 256 ? 2 : 3);  // register-direct at 256, four-step elsewhere
     case CG_TUNE_BIN_MINB: return tune_get(key, n, n <= 5 ? 6 : 1);
     case CG_TUNE_ROWS_KERNEL: return tune_get(key, n, 1);  // four-step
+    case CG_TUNE_FUSED_Y: return tune_get(key, n, 0);
     default: set_error("cg_tune_get: bad key"); return CG_ERR_ARG;
   }
 }

@@ -108,13 +108,20 @@ def test_fused_y_kernel_matches_fp64_oracle(cuda, oracle, dims, cond):
     """cond = 1.0001 sends almost every in-band bin through the in-kernel FP64 path."""
     from crava_gb300 import synthetic as S
     from crava_gb300.pipeline import Inversion
+    from crava_gb300 import _native
     nxp, nyp, nzp = dims
     sc = S.scaled_config1(nxp, nyp, nzp, seed=nyp + nzp)
     inv = Inversion(sc, forms=("mixed",), cond_threshold=cond)
     inv.restore("mixed")
     inv.ws.reset_stats()
-    inv.run("mixed")
-    torch.cuda.synchronize()
+    L = _native.lib()
+    assert L.cg_tune_set(4, nyp, 1) == 0   # CG_TUNE_FUSED_Y on for this y length
+    try:
+        inv.run("mixed")
+        torch.cuda.synchronize()
+    finally:
+        L.cg_tune_clear()
+        _native._apply_tuning(L)
     st = inv.ws.stats()
     pm, res, cov = inv.results("mixed")
     post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
