@@ -221,21 +221,20 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_ybin(YBinArgs a)
   }
 }
 
-// launch for one y length: stack-count dispatch, register cap from the tuning
-// table (CG_TUNE_BIN_MINB 6 -> 3 resident CTAs of 256 threads, else 2)
+// launch for one y length, dispatched on the stack count.  Two resident CTAs
+// of 256 threads (128 registers): the 85-register build spills in the bin
+// loop and measured 1.4x slower.
 template <int N>
 int launch_ybin_n(const YBinArgs &a, int nt, int ncols_tiles, int nzp, double bytes, cudaStream_t st)
 {
-  const bool tight = cg_tune_get(CG_TUNE_BIN_MINB, nt) == 6;
   return dispatch_nt(nt, [&](auto NTc) -> int {
     constexpr int NT = decltype(NTc)::value;
     const size_t smem = ((size_t)(NT + 3) * N * kYW + N) * sizeof(float2) + sizeof(KTab<float>);
-    static bool attr3[64] = {}, attr2[64] = {};
-    cudaError_t e = tight ? smem_limit_once(k_ybin<N, NT, 3>, smem, attr3) : smem_limit_once(k_ybin<N, NT, 2>, smem, attr2);
+    static bool attr_set[64] = {};
+    cudaError_t e = smem_limit_once(k_ybin<N, NT, 2>, smem, attr_set);
     if (e != cudaSuccess) return cuda_status(e, "k_ybin attribute");
     TraceScope ts("k_ybin", st, bytes);
-    if (tight) k_ybin<N, NT, 3><<<dim3(ncols_tiles, nzp), kFFTThreads, smem, st>>>(a);
-    else k_ybin<N, NT, 2><<<dim3(ncols_tiles, nzp), kFFTThreads, smem, st>>>(a);
+    k_ybin<N, NT, 2><<<dim3(ncols_tiles, nzp), kFFTThreads, smem, st>>>(a);
     CG_CHECK_LAUNCH("k_ybin");
     return CG_OK;
   });
