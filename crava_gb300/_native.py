@@ -170,6 +170,7 @@ def _declare(L):
         "cg_host_register": ([V, ct.c_size_t], I),
         "cg_copy": ([V, V, ct.c_size_t, V], I),
         "cg_exp_transform": ([V, ct.c_long, V], I),
+        "cg_fill_in_data": ([V, I, I, I, I, I, V, I, V, V, V, V, F, F, V, V], I),
         "cg_log_transform": ([V, ct.c_long, V], I),
         "cg_fft3d_c2r_exp_batch": ([PP, I, I, I, I, I, V], I),
         "cg_cov_origin": ([PP, I, I, I, I, V, V, V], I),

@@ -223,6 +223,18 @@ def simulate_fields(chol, fields, nxp, seed=0, real0=0, noise=None, post_mean=No
                                    _stream(stream)), "cg_simulate_fields")
 
 
+def fill_in_data(buf: torch.Tensor, nxp: int, nz: int, cubetype: int, traces: torch.Tensor, state: torch.Tensor,
+                 z0_data: torch.Tensor, z0_grid: torch.Tensor, dz_grid: torch.Tensor, dz_data: float,
+                 smooth_length: float, stream=None):
+    """FFTGrid::fillInData's per-trace core (cg_fill_in_data); returns the extrapolation counts."""
+    nzp, nyp, _ = buf.shape
+    ext = (ct.c_int * 2)()
+    check(lib().cg_fill_in_data(_vp(buf), nxp, nyp, nzp, nz, cubetype, _vp(traces), traces.shape[1], _vp(state),
+                                _vp(z0_data), _vp(z0_grid), _vp(dz_grid), float(dz_data), float(smooth_length),
+                                ext, _stream(stream)), "cg_fill_in_data")
+    return [ext[0], ext[1]]
+
+
 def exp_transform(t: torch.Tensor, stream=None):
     """FFTGrid::expTransf in place (cg_exp_transform)."""
     check(lib().cg_exp_transform(_vp(t), t.numel(), _stream(stream)), "cg_exp_transform")

@@ -487,8 +487,22 @@ int fft3d_xz(void *const *bufs, int count, int nxp, int nyp, int nzp, int cubety
   return CG_OK;
 }
 
+// 1D real transforms of nrows rows of length nx in the FFTW in-place row
+// layout (pitch 2*(nx/2+1) floats); scale multiplies the input (forward) or
+// the output (inverse)
+template <typename T>
+int fft_rows(void *buf, int nx, int nrows, bool forward, T scale, cudaStream_t st)
+{
+  if (!buf || nx < 1 || nrows < 1) { set_error("fft_rows: bad argument"); return CG_ERR_ARG; }
+  CubeSet cs, ad;
+  for (int i = 0; i < kMaxBatch; i++) { cs.ptr[i] = nullptr; ad.ptr[i] = nullptr; }
+  cs.ptr[0] = buf;
+  return launch_rows<T>(forward, cs, ad, 1, nx, nrows, 1, scale, st);
+}
+
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_xz<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
+template int fft_rows<float>(void *, int, int, bool, float, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_c2r_add<float>(void *const *, const void *const *, int, int, int, int, int, cudaStream_t);
 template int fft3d_c2r_epi<float>(void *const *, int, int, int, int, int, int, cudaStream_t);

@@ -5,6 +5,7 @@
     python -m crava_gb300.microbench copy  --mb 512 --reps 5
     python -m crava_gb300.microbench simulate --nreal 128 --reps 3
     python -m crava_gb300.microbench timelapse --reps 3
+    python -m crava_gb300.microbench ingest --reps 3
 
 Inputs are seeded random cubes (fft) or a scaled config-1 scenario (invert).
 Prints one JSON line with per-kernel launch times and algorithmic bandwidth
@@ -206,9 +207,48 @@ def timelapse_case(a):
                                   for k, v in tr.items()}}))
 
 
+def ingest_case(a):
+    """Data ingest of one 256^3 DATA cube: 258 x 256 column traces of 205 samples (4 ms) resampled onto the
+    grid (transforms of length 210 and 840), timed with CUDA events."""
+    nxp = nyp = nzp = 256
+    nz, n_data = 205, 205
+    _, rnxp = api.dims(nxp)
+    ncol = rnxp * nyp
+    g = torch.Generator(device="cuda").manual_seed(3)
+    traces = torch.randn((ncol, n_data), device="cuda", generator=g)
+    state = torch.zeros(ncol, dtype=torch.uint8, device="cuda")
+    z0d = torch.full((ncol,), 1000.0, device="cuda")
+    z0g = z0d + 20.0
+    dzg = torch.full((ncol,), 4.0, device="cuda")
+    buf = torch.empty((nzp, nyp, rnxp), device="cuda")
+
+    def run():
+        api.fill_in_data(buf, nxp, nz, api.DATA, traces, state, z0d, z0g, dzg, 4.0, 40.0)
+    run()
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(a.reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    _native.trace_enable(True)
+    run()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    best = min(ms)
+    print(json.dumps({"case": {"what": "ingest", "workload": "256^3 DATA cube from 66048 traces of 205 samples"},
+                      "ms_per_cube": ms, "Mtraces_per_s": ncol / (best * 1e-3) / 1e6,
+                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
+                                  for k, v in tr.items()}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse"])
+    ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse", "ingest"])
     ap.add_argument("--nreal", type=int, default=128)
     ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
@@ -229,6 +269,9 @@ def main():
         return
     if a.what == "timelapse":
         timelapse_case(a)
+        return
+    if a.what == "ingest":
+        ingest_case(a)
         return
     if a.what == "batch":
         # graph replays: time the whole batch with CUDA events

@@ -166,6 +166,28 @@ int cg_scale(float *buf, long n, float scalar, void *stream);
 int cg_add(float *y, const float *x, long n, void *stream);
 
 /* ========================================================================
+ * Data ingest before the inversion
+ * ======================================================================== */
+
+/* FFTGrid::fillInData (src/fftgrid.cpp:138-370), the per-trace numerical
+ * core, for every column c = i + rnxp*j (i < rnxp, j < nyp) of the padded real
+ * cube buf (device, rnxp*nyp*nzp floats, written).  traces (device,
+ * [rnxp*nyp][n_data]) hold one trace per column, found by the caller's
+ * geometry lookup (getFillNumber, Simbox::getCoord, the nearest SegY or STORM
+ * trace); state[c] != 0 marks a dead or outside trace (its column is set to
+ * 0); z0_data[c] is the time of the trace's first sample, z0_grid[c] and
+ * dz_grid[c] the column's simbox top and cell thickness, dz_data the sample
+ * interval.  DATA cubes get the guard-zone taper over smooth_length; other
+ * cube types the end extrapolation and trend removal/restoration.  Traces are
+ * resampled through transforms of length findClosestFactorableNumber(n_data)
+ * and 4x that, then interpolated onto the cells.  extrap_out (host, may be
+ * NULL; the call then waits for the stream) receives the largest leading and
+ * trailing extrapolation. */
+int cg_fill_in_data(float *buf, int nxp, int nyp, int nzp, int nz, int cubetype, const float *traces, int n_data,
+                    const unsigned char *state, const float *z0_data, const float *z0_grid, const float *dz_grid,
+                    float dz_data, float smooth_length, int *extrap_out, void *stream);
+
+/* ========================================================================
  * Output grids after the bin loop
  * ======================================================================== */
 

@@ -90,6 +90,9 @@ def lib():
                 ct.c_int, ct.c_int, ct.c_int, ct.c_int, PPR, PPR, PPR, PR, PR, PR, PR, PR,
                 ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_float, ct.c_int, ct.POINTER(ct.c_int), ct.c_int]
             getattr(L, "or_simulate_bins" + sfx).argtypes = [ct.c_size_t, PPR, PPR, ct.c_int]
+            getattr(L, "or_fill_in_data" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int,
+                                                            PR, ct.c_int, ct.c_void_p, PR, PR, PR, R, R,
+                                                            ct.POINTER(ct.c_int), ct.c_int]
             getattr(L, "or_state4d_merge" + sfx).argtypes = [ct.c_size_t, PPR, PPR, PPR, PPR, PPR, PPR, PPR, ct.c_int]
             getattr(L, "or_state4d_split" + sfx).argtypes = [ct.c_size_t, PPR, PPR, PPR, PPR, PPR, PPR, PPR,
                                                              ct.POINTER(ct.c_int), ct.c_int]
@@ -316,6 +319,26 @@ def fill_param_corr(nxp, nyp, nzp, corrXY, circCorrT, gradI=0.0, gradJ=0.0, scal
     getattr(lib(), "or_fill_param_corr_" + prec)(_ptr(buf, R), nxp, nyp, nzp, _ptr(cxy, R), _ptr(ct_, R),
                                                  gradI, gradJ, scalar)
     return buf
+
+
+def fill_in_data(nxp, nyp, nzp, nz, is_data, traces, state, z0_data, z0_grid, dz_grid, dz_data, smooth_length,
+                 prec="f", nthreads=None):
+    """FFTGrid::fillInData's per-trace core: traces (nyp*rnxp, n_data), one per column i + rnxp*j.
+    Returns (padded real cube (nzp, nyp, rnxp), [max leading, max trailing extrapolation])."""
+    import os
+    R = ct.c_float if prec == "f" else ct.c_double
+    _, rnxp = dims(nxp)
+    tr = np.ascontiguousarray(traces, dtype=_rdt(prec))
+    ncol, n_data = tr.shape
+    assert ncol == rnxp * nyp
+    st = np.ascontiguousarray(state, dtype=np.uint8)
+    z0d, z0g, dzg = (np.ascontiguousarray(x, dtype=_rdt(prec)) for x in (z0_data, z0_grid, dz_grid))
+    buf = np.zeros((nzp, nyp, rnxp), dtype=_rdt(prec))
+    ext = (ct.c_int * 2)()
+    getattr(lib(), "or_fill_in_data_" + prec)(_ptr(buf, R), nxp, nyp, nzp, nz, int(is_data), _ptr(tr, R), n_data,
+                                              st.ctypes.data, _ptr(z0d, R), _ptr(z0g, R), _ptr(dzg, R),
+                                              dz_data, smooth_length, ext, nthreads or os.cpu_count())
+    return buf, [ext[0], ext[1]]
 
 
 def fill_err_corr(nxp, nyp, nzp, corrXY, gradI=0.0, gradJ=0.0, prec="f"):
