@@ -49,7 +49,7 @@ def tune_cols(lengths, L):
             api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
         best = None
         for pipe in (0, 1, 2, 3):
-            for minb in (2, 3):
+            for minb in ((2, 3, 4) if pipe in (2, 3) and n <= 256 else (2, 3)):
                 L.cg_tune_set(KEY_COLS_PIPE, n, pipe)
                 L.cg_tune_set(KEY_COLS_MINB, n, minb)
                 ms = _time_kernels(run, "k_fft_cols")

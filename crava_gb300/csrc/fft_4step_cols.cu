@@ -9,6 +9,8 @@ template <int N>
 int launch_minb(int minb, const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch,
                 int sign, const float2 *tw, cudaStream_t st)
 {
+  if constexpr (N <= 256)
+    if (minb == 4) return launch_cols_4s<N, 4>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   if (minb == 3) return launch_cols_4s<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   return launch_cols_4s<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
 }

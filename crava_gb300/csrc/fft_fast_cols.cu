@@ -113,6 +113,8 @@ int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batc
   const int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
   if (kind == 3) return four_step_cols(minb_for(N), cs, ncubes, N, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   if (kind == 2) {
+    if constexpr (N <= 256)
+      if (minb_for(N) == 4) return launch_rd<N, 4>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     if (minb_for(N) == 3) return launch_rd<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     return launch_rd<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   }

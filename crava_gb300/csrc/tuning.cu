@@ -49,7 +49,7 @@ using namespace cg;
 extern "C" int cg_tune_set(int key, int n, int value)
 {
   if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_FUSED_Y || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
-  const bool ok = (key == CG_TUNE_COLS_MINB && (value == 2 || value == 3)) ||
+  const bool ok = (key == CG_TUNE_COLS_MINB && (value >= 2 && value <= 4)) ||
                   (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 3)) ||
                   (key == CG_TUNE_BIN_MINB && (value == 1 || value == 6)) ||
                   (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||

@@ -64,7 +64,8 @@ int cg_trace_collect(void);
 int cg_trace_entry(int index, char *name, int name_len, long *launches, double *ms_total, double *bytes_total);
 
 /* Launch-variant tuning table.  Keys: CG_TUNE_COLS_MINB (resident CTAs the
- * column-pass build targets, 2 or 3, per axis length n), CG_TUNE_COLS_PIPE
+ * column-pass build targets, 2, 3 or 4 (4: lengths up to 256, register-
+ * direct and four-step kernels), per axis length n), CG_TUNE_COLS_PIPE
  * (column-pass kernel per n: 0 shared-memory staged, 1 persistent
  * double-buffered, 2 first and last stages in registers, 3 four-step),
  * CG_TUNE_BIN_MINB (fused bin kernel register cap: 1 = none, 6 = 85

@@ -155,13 +155,13 @@ def _variant_case(oracle, nxp, nyp, nzp):
 
 
 @pytest.mark.parametrize("pipe", [0, 1, 2, 3])
-@pytest.mark.parametrize("minb", [2, 3])
+@pytest.mark.parametrize("minb", [2, 3, 4])
 def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
     from crava_gb300 import api
     native.cg_tune_clear()
     try:
         assert native.cg_tune_set(1, 0, pipe) == 0 and native.cg_tune_set(0, 0, minb) == 0
-        assert native.cg_tune_set(3, 0, minb - 2) == 0   # staged rows with minb 2, four-step rows with 3
+        assert native.cg_tune_set(3, 0, minb % 2) == 0   # four-step rows with minb 3, staged rows otherwise
         for nxp, nyp, nzp in VARIANT_SIZES:
             x, ref = _variant_case(oracle, nxp, nyp, nzp)
             t = torch.from_numpy(x.copy()).cuda()
