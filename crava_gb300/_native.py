@@ -171,6 +171,11 @@ def _declare(L):
         "cg_copy": ([V, V, ct.c_size_t, V], I),
         "cg_exp_transform": ([V, ct.c_long, V], I),
         "cg_fill_in_data": ([V, I, I, I, I, I, V, I, V, V, V, V, F, F, V, V], I),
+        "cg_crava_file_write": ([ct.c_char_p, V, I, I, I, V, V], I),
+        "cg_crava_file_read": ([ct.c_char_p, V, I, I, I, V, V], I),
+        "cg_storm_write": ([ct.c_char_p, V, I, I, I, V], I),
+        "cg_storm_read_header": ([ct.c_char_p, V, V, V, V], I),
+        "cg_storm_read": ([ct.c_char_p, V, ct.c_long], I),
         "cg_log_transform": ([V, ct.c_long, V], I),
         "cg_fft3d_c2r_exp_batch": ([PP, I, I, I, I, I, V], I),
         "cg_cov_origin": ([PP, I, I, I, I, V, V, V], I),

@@ -235,6 +235,56 @@ def fill_in_data(buf: torch.Tensor, nxp: int, nz: int, cubetype: int, traces: to
     return [ext[0], ext[1]]
 
 
+# ---------------------------------------------------------------------------
+# file formats (host memory)
+# ---------------------------------------------------------------------------
+class StormHeader(ct.Structure):
+    _fields_ = [("zone_number", ct.c_int), ("model_file", ct.c_char * 256), ("missing_code", ct.c_float),
+                ("variable", ct.c_char * 256), ("x_min", ct.c_double), ("lx", ct.c_double), ("y_min", ct.c_double),
+                ("ly", ct.c_double), ("z_top", ct.c_double), ("z_bot", ct.c_double), ("erosion_top", ct.c_double),
+                ("erosion_bot", ct.c_double), ("lz", ct.c_double), ("angle_deg", ct.c_double)]
+
+
+def write_crava_file(path, cube: np.ndarray, geom, nx: int, ny: int):
+    """FFTGrid::writeCravaFile: cube (nzp, nyp, rnxp) float32, geom 11 doubles (x0 y0 dx dy IL0 XL0 ILStepX
+    ILStepY XLStepX XLStepY angle)."""
+    c = np.ascontiguousarray(cube, dtype=np.float32)
+    g = np.ascontiguousarray(geom, dtype=np.float64)
+    n = np.array([nx, ny], dtype=np.int32)
+    nzp, nyp, rnxp = c.shape
+    check(lib().cg_crava_file_write(str(path).encode(), c.ctypes.data, rnxp, nyp, nzp, g.ctypes.data, n.ctypes.data),
+          "cg_crava_file_write")
+
+
+def read_crava_file(path, nxp: int, nyp: int, nzp: int):
+    """FFTGrid::readCravaFile: (cube (nzp, nyp, rnxp), geom (11,), (nx, ny))."""
+    _, rnxp = dims(nxp)
+    c = np.empty((nzp, nyp, rnxp), dtype=np.float32)
+    g = np.empty(11, dtype=np.float64)
+    n = np.empty(2, dtype=np.int32)
+    check(lib().cg_crava_file_read(str(path).encode(), c.ctypes.data, rnxp, nyp, nzp, g.ctypes.data, n.ctypes.data),
+          "cg_crava_file_read")
+    return c, g, (int(n[0]), int(n[1]))
+
+
+def write_storm(path, values: np.ndarray, header: StormHeader):
+    """STORM binary grid; values (nk, nj, ni) float32 (i fastest)."""
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    nk, nj, ni = v.shape
+    check(lib().cg_storm_write(str(path).encode(), v.ctypes.data, ni, nj, nk, ct.byref(header)), "cg_storm_write")
+
+
+def read_storm(path):
+    """STORM binary grid with constant surfaces: (values (nk, nj, ni), StormHeader)."""
+    h = StormHeader()
+    ni, nj, nk = ct.c_int(), ct.c_int(), ct.c_int()
+    check(lib().cg_storm_read_header(str(path).encode(), ct.byref(h), ct.byref(ni), ct.byref(nj), ct.byref(nk)),
+          "cg_storm_read_header")
+    v = np.empty((nk.value, nj.value, ni.value), dtype=np.float32)
+    check(lib().cg_storm_read(str(path).encode(), v.ctypes.data, v.size), "cg_storm_read")
+    return v, h
+
+
 def exp_transform(t: torch.Tensor, stream=None):
     """FFTGrid::expTransf in place (cg_exp_transform)."""
     check(lib().cg_exp_transform(_vp(t), t.numel(), _stream(stream)), "cg_exp_transform")

@@ -189,6 +189,38 @@ int cg_fill_in_data(float *buf, int nxp, int nyp, int nzp, int nz, int cubetype,
                     float dz_data, float smooth_length, int *extrap_out, void *stream);
 
 /* ========================================================================
+ * File formats either side of the path (host memory, synchronous)
+ * ======================================================================== */
+
+/* FFTGrid::writeCravaFile / readCravaFile (src/fftgrid.cpp:2410-2493): the
+ * padded real cube rvalue (rnxp*nyp*nzp floats) with its simbox geometry.
+ * geom[11] = x0 y0 dx dy IL0 XL0 ILStepX ILStepY XLStepX XLStepY angle,
+ * nxny[2] = nx ny.  Reading fails (CG_ERR_ARG) when the file's padded size
+ * differs from rnxp x nyp x nzp, as the reference does; geom and nxny may be
+ * NULL when reading. */
+int cg_crava_file_write(const char *path, const float *rvalue, int rnxp, int nyp, int nzp, const double *geom,
+                        const int *nxny);
+int cg_crava_file_read(const char *path, float *rvalue, int rnxp, int nyp, int nzp, double *geom, int *nxny);
+
+/* STORM binary grids (NRLib StormContGrid, libs/nrlib/stormgrid/
+ * stormcontgrid.cpp:72-200) with constant surfaces: values are ni*nj*nk
+ * floats, i fastest.  Grids whose surfaces are files, ASCII grids and grids
+ * with barriers give CG_ERR_UNSUPPORTED. */
+typedef struct {
+  int zone_number;
+  char model_file[256];
+  float missing_code;
+  char variable[256];
+  double x_min, lx, y_min, ly;
+  double z_top, z_bot, erosion_top, erosion_bot;  /* constant surfaces */
+  double lz, angle_deg;
+} cg_storm_header;
+
+int cg_storm_write(const char *path, const float *values, int ni, int nj, int nk, const cg_storm_header *header);
+int cg_storm_read_header(const char *path, cg_storm_header *header, int *ni, int *nj, int *nk);
+int cg_storm_read(const char *path, float *values, long n);
+
+/* ========================================================================
  * Output grids after the bin loop
  * ======================================================================== */
 
