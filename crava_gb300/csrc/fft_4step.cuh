@@ -389,4 +389,165 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet
   }
 }
 
+// ---------------------------------------------------------------------------
+// x rows of ODD length NX (no half-length trick): the real row is transformed
+// as a complex row with zero imaginary part, and the first cnxp = (NX+1)/2
+// bins are kept (R2C); the inverse rebuilds the Hermitian row from those bins
+// (Im of DC dropped, as rfftw_c2hc does) and keeps the real part (C2R).
+// Rows have pitch NX + 1 floats = cnxp complex.
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int fs_odd_rows_per_cta(int nx)
+{
+  return kFFTThreads / (nx / fs_n1(nx)) < 1 ? 1 : kFFTThreads / (nx / fs_n1(nx));
+}
+__host__ __device__ constexpr int fs_odd_row_pitch(int nx)
+{
+  const int need = (nx / fs_n1(nx)) * (fs_n1(nx) + 1);
+  return need + ((8 - need % 16) + 16) % 16;
+}
+
+template <int NX>
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_odd(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+                                                              float prescale)
+{
+  constexpr int N1 = fs_n1(NX), N2 = NX / N1, CN = (NX + 1) / 2, RN = NX + 1;
+  constexpr int RPC = fs_odd_rows_per_cta(NX), P = fs_odd_row_pitch(NX), Q = N1 + 1;
+  constexpr int P1 = RPC * N2, P2 = RPC * N1;
+  constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + RPC * P;
+  const int r0 = blockIdx.x * RPC;
+  const int nr = min(RPC, nrows - r0);
+  float *rbase = (float *)cs.ptr[blockIdx.z] + (long)r0 * RN;
+  float2 *cbase = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  auto load1 = [&](int q, float2 *v) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int n2 = t % N2, row = t / N2;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && row < nr;
+    const float *rp = rbase + (long)row * RN;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) v[n1] = make_float2(ok ? rp[N2 * n1 + n2] : 0.f, 0.f);
+  };
+  float2 v[N1];
+  load1(0, v);
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < B1; q++) {
+    if (q > 0) load1(q, v);
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P1 % kFFTThreads == 0 || t < P1) {
+      const int n2 = t % N2, row = t / N2;
+      reg_fft<float, N1, N2>(v, -1, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw[n2 * k1]);
+#pragma unroll
+      for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < B2; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P2 % kFFTThreads == 0 || t < P2) {
+      const int k1 = t % N1, row = t / N1;
+      float2 u[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[row * P + n2 * Q + k1];
+      reg_fft<float, N2, N1>(u, -1, tw);
+      if (row < nr) {
+        float2 *op = cbase + (long)row * CN;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+          const int k = k1 + N1 * k2;
+          if (k < CN) op[k] = make_float2(u[k2].x * prescale, u[k2].y * prescale);
+        }
+      }
+    }
+  }
+}
+
+template <int NX>
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_odd(CubeSet cs, CubeSet addend,
+                                                              const float2 *__restrict__ twg, int nrows,
+                                                              float postscale, int epi)
+{
+  constexpr int N1 = fs_n1(NX), N2 = NX / N1, CN = (NX + 1) / 2, RN = NX + 1;
+  constexpr int RPC = fs_odd_rows_per_cta(NX), P = fs_odd_row_pitch(NX), Q = N1 + 1;
+  constexpr int P1 = RPC * N2, P2 = RPC * N1;
+  constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + RPC * P;
+  const int r0 = blockIdx.x * RPC;
+  const int nr = min(RPC, nrows - r0);
+  float *rbase = (float *)cs.ptr[blockIdx.z] + (long)r0 * RN;
+  const float2 *cbase = (const float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
+  for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  // Hermitian row from the half spectrum: Z[k] = X[k] (k < CN), conj X[NX-k] above; Im X[0] dropped
+  auto load1 = [&](int q, float2 *v) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    const int n2 = t % N2, row = t / N2;
+    const bool ok = (P1 % kFFTThreads == 0 || t < P1) && row < nr;
+    const float2 *cp = cbase + (long)row * CN;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) {
+      const int k = N2 * n1 + n2;
+      float2 z = make_float2(0.f, 0.f);
+      if (ok) {
+        if (k < CN) {
+          z = __ldg(cp + k);
+          if (k == 0) z.y = 0.f;
+        } else {
+          const float2 x = __ldg(cp + (NX - k));
+          z = make_float2(x.x, -x.y);
+        }
+      }
+      v[n1] = z;
+    }
+  };
+  float2 v[N1];
+  load1(0, v);
+  __syncthreads();  // twiddles staged; every thread's row reads done before the exchange
+#pragma unroll
+  for (int q = 0; q < B1; q++) {
+    if (q > 0) load1(q, v);
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P1 % kFFTThreads == 0 || t < P1) {
+      const int n2 = t % N2, row = t / N2;
+      reg_fft<float, N1, N2>(v, +1, tw);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw_at<float>(tw, n2 * k1, +1));
+#pragma unroll
+      for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
+    }
+  }
+  __syncthreads();
+  const float *add = addend.ptr[blockIdx.z] ? (const float *)addend.ptr[blockIdx.z] + (long)r0 * RN : nullptr;
+#pragma unroll
+  for (int q = 0; q < B2; q++) {
+    const int t = q * kFFTThreads + threadIdx.x;
+    if (P2 % kFFTThreads == 0 || t < P2) {
+      const int k1 = t % N1, row = t / N1;
+      float2 u[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[row * P + n2 * Q + k1];
+      reg_fft<float, N2, N1>(u, +1, tw);
+      if (row < nr) {
+        float *op = rbase + (long)row * RN;
+        const float *ap = add ? add + (long)row * RN : nullptr;
+#pragma unroll
+        for (int k2 = 0; k2 < N2; k2++) {
+          const int e = k1 + N1 * k2;
+          float x = u[k2].x * postscale;
+          if (ap) x += ap[e];
+          op[e] = epilogue<float>(x, epi);
+        }
+        if (k1 == 0) op[NX] = epilogue<float>(ap ? ap[NX] : 0.f, epi);  // the row's padding float
+      }
+    }
+  }
+}
+
 }  // namespace cg

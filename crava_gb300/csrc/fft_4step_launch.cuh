@@ -57,6 +57,35 @@ int launch_rows_4s(bool forward, const CubeSet &cs, const CubeSet &addend, int n
   return 1;
 }
 
+template <int NX>
+int launch_rows_odd(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nrows, float scale,
+                    const float2 *tw, cudaStream_t st, int epi)
+{
+  constexpr int RPC = fs_odd_rows_per_cta(NX), P = fs_odd_row_pitch(NX);
+  const size_t smem = ((size_t)RPC * P + NX) * sizeof(float2);
+  dim3 grid(ceil_div(nrows, RPC), 1, ncubes);
+  const double bytes = (double)ncubes * nrows * (NX * sizeof(float) + (NX + 1) / 2 * sizeof(float2));
+  static bool attr_fwd[64] = {}, attr_inv[64] = {};
+  cudaError_t e;
+  if (forward) {
+    e = smem_limit_once(k_r2c_rows_odd<NX>, smem, attr_fwd);
+    if (e != cudaSuccess) return cuda_status(e, "k_r2c_rows_odd attribute");
+    TraceScope ts("k_r2c_rows_odd", st, bytes);
+    k_r2c_rows_odd<NX><<<grid, kFFTThreads, smem, st>>>(cs, tw, nrows, scale);
+  } else {
+    e = smem_limit_once(k_c2r_rows_odd<NX>, smem, attr_inv);
+    if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_odd attribute");
+    TraceScope ts("k_c2r_rows_odd", st, bytes);
+    k_c2r_rows_odd<NX><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale, epi);
+  }
+  CG_CHECK_LAUNCH(forward ? "k_r2c_rows_odd" : "k_c2r_rows_odd");
+  return 1;
+}
+
+// odd x lengths (fft_4step_rows_odd.cu): 0 when not handled
+int four_step_rows_odd(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows,
+                       float scale, const float2 *tw, cudaStream_t st, int epi);
+
 // further lengths (fft_4step_cols_ext*.cu, fft_4step_rows_ext*.cu): 0 when not handled
 int four_step_cols_ext0(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);
 int four_step_cols_ext1(const CubeSet &, int, int, int, long, long, int, int, const float2 *, cudaStream_t);

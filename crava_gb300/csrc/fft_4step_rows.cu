@@ -8,7 +8,7 @@ namespace cg {
 int four_step_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
                    const float2 *tw, cudaStream_t st, int epi)
 {
-  if (nxp % 2) return 0;
+  if (nxp % 2) return four_step_rows_odd(forward, cs, addend, ncubes, nxp, nrows, scale, tw, st, epi);
   const int m = nxp / 2;
   switch (m) {
 #define CG_ROWS(MM) case MM: return launch_rows_4s<MM>(forward, cs, addend, ncubes, nrows, scale, tw, st, epi);

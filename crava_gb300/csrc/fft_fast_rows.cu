@@ -37,7 +37,8 @@ int launch(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, i
 int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
               const float2 *tw, cudaStream_t st, int epi)
 {
-  if (nxp % 2) return 0;
+  if (nxp % 2)  // odd x lengths exist only as four-step kernels (tuning key n = nxp)
+    return cg_tune_get(CG_TUNE_ROWS_KERNEL, nxp) == 1 ? four_step_rows(forward, cs, addend, ncubes, nxp, nrows, scale, tw, st, epi) : 0;
   if (cg_tune_get(CG_TUNE_ROWS_KERNEL, nxp / 2) == 1)
     return four_step_rows(forward, cs, addend, ncubes, nxp, nrows, scale, tw, st, epi);
   switch (nxp / 2) {

@@ -70,7 +70,8 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
  * double-buffered, 2 first and last stages in registers, 3 four-step),
  * CG_TUNE_BIN_MINB (fused bin kernel register cap: 1 = none, 6 = 85
  * registers, per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per
- * half length n = nxp/2: 0 shared-memory staged, 1 four-step),
+ * half length n = nxp/2, or n = nxp for odd nxp: 0 shared-memory staged or
+ * generic, 1 four-step),
  * CG_TUNE_FUSED_Y (cg_invert_cubes_fused per y length n: 0 three-pass
  * transforms around the bin kernel, 1 y pass fused with the bin loop).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores

@@ -180,7 +180,9 @@ EXT_SIZES = [(42, 54, 90), (126, 189, 144), (36, 500, 21), (180, 35, 405), (56, 
              (432, 448, 18), (84, 27, 441), (252, 150, 49), (300, 225, 28), (216, 63, 486), (448, 125, 32),
              (196, 336, 20), (288, 81, 360), (140, 392, 45), (112, 270, 105),
              # odd half lengths (nxp = 2M, M odd) and narrow cubes (every column a tail column)
-             (54, 54, 90), (150, 25, 36), (270, 18, 49), (378, 20, 15), (90, 100, 64), (250, 64, 30), (30, 45, 63)]
+             (54, 54, 90), (150, 25, 36), (270, 18, 49), (378, 20, 15), (90, 100, 64), (250, 64, 30), (30, 45, 63),
+             # odd x lengths
+             (15, 20, 16), (63, 40, 30), (75, 18, 28), (125, 32, 20), (189, 24, 16), (243, 16, 18), (45, 60, 21)]
 
 
 @pytest.mark.parametrize("dims", EXT_SIZES)
