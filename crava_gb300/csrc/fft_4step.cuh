@@ -86,10 +86,10 @@ __host__ __device__ constexpr int fs_cols_w(int n)
 
 // ---------------------------------------------------------------------------
 // strided column pass.  Full tiles are W adjacent columns of one batch row.
-// The ntail columns left over in each batch row form tail tiles of
-// ntail x trows columns (trows = W / ntail consecutive batch rows), so a tail
-// tile still reads runs of ntail adjacent elements.  Grid columns x >= nfull
-// hold the tail tiles, numbered (x - nfull)*nbatch + y.
+// The ntail columns left over in each batch row, taken row after row, form a
+// list of ntail*nbatch columns cut into tail tiles of W: a tail tile reads runs
+// of ntail adjacent elements and every lane but those of the last tile works.
+// Grid columns x >= nfull hold the tail tiles, numbered (x - nfull)*nbatch + y.
 // Shared layout: buf[(k1*N2 + n2)*W + c] (conflict-free for both passes).
 // ---------------------------------------------------------------------------
 template <int N, int W, int MINB>
@@ -104,21 +104,23 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, c
   float2 *tw = buf + N * W;
   float2 *cube = (float2 *)cs.ptr[blockIdx.z];
   float2 *base;
-  int tdiv, tvalid;  // lane c -> column c % tdiv of batch row c / tdiv; lanes c >= tvalid idle
+  int e0, tdiv, tvalid;  // lane c -> column (e0 + c) % tdiv of batch row (e0 + c) / tdiv; lanes c >= tvalid idle
   if ((int)blockIdx.x < g.nfull) {
     base = cube + (long)blockIdx.y * g.batch_stride + (long)blockIdx.x * W;
+    e0 = 0;
     tdiv = W;
     tvalid = W;
   } else {
-    const int tt = ((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
-    const int r0 = tt * g.trows;
-    if (r0 >= g.nbatch) return;
-    base = cube + (long)g.nfull * W + (long)r0 * g.batch_stride;
+    const long tt = (long)((int)blockIdx.x - g.nfull) * g.nbatch + (int)blockIdx.y;
+    const long ntot = (long)g.ntail * g.nbatch;
+    if (tt * W >= ntot) return;
+    base = cube + (long)g.nfull * W;
+    e0 = (int)(tt * W);
     tdiv = g.ntail;
-    tvalid = g.ntail * min(g.trows, g.nbatch - r0);
+    tvalid = (int)min((long)W, ntot - tt * W);
   }
   const long as = g.axis_stride, bs = g.batch_stride;
-  auto coff = [&](int c) -> long { return (long)(c % tdiv) + (long)(c / tdiv) * bs; };
+  auto coff = [&](int c) -> long { return (long)((e0 + c) % tdiv) + (long)((e0 + c) / tdiv) * bs; };
   for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
   // pass 1, one item at a time (registers hold one item); the first item's
   // loads are issued before the barrier that publishes the twiddle table

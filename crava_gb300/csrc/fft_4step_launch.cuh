@@ -22,9 +22,9 @@ int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, l
   g.nfull = ncols / W;
   g.ntail = ncols - g.nfull * W;
   g.nbatch = nbatch;
-  g.trows = g.ntail > 0 ? W / g.ntail : 1;
-  const int tail_tiles = g.ntail > 0 ? ceil_div(nbatch, g.trows) : 0;
-  const int tail_cols = ceil_div(tail_tiles, nbatch);
+  g.trows = 1;
+  const long tail_tiles = ceil_div((long)g.ntail * nbatch, (long)W);
+  const int tail_cols = (int)ceil_div(tail_tiles, (long)nbatch);
   dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
   TraceScope ts("k_fft_cols_4s", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
   k_fft_cols_4s<N, W, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
