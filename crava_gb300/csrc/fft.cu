@@ -500,8 +500,21 @@ int fft_rows(void *buf, int nx, int nrows, bool forward, T scale, cudaStream_t s
   return launch_rows<T>(forward, cs, ad, 1, nx, nrows, 1, scale, st);
 }
 
+// one column pass (length n, ncols columns of nbatch batch rows) over count
+// cubes given by their first element
+template <typename T>
+int fft_cols(void *const *bufs, int count, int n, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+             cudaStream_t st)
+{
+  if (!bufs || count < 1 || count > kMaxBatch) { set_error("fft_cols: bad argument"); return CG_ERR_ARG; }
+  CubeSet cs;
+  for (int i = 0; i < kMaxBatch; i++) cs.ptr[i] = i < count ? bufs[i] : nullptr;
+  return launch_cols<T>(cs, count, n, ncols, axis_stride, batch_stride, nbatch, sign, st);
+}
+
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_xz<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
+template int fft_cols<float>(void *const *, int, int, int, long, long, int, int, cudaStream_t);
 template int fft_rows<float>(void *, int, int, bool, float, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_c2r_add<float>(void *const *, const void *const *, int, int, int, int, int, cudaStream_t);

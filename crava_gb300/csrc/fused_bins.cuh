@@ -51,6 +51,8 @@ struct FusedArgs {
   int *queue;
   int queue_cap;
   int *counters;
+  int k0;       // first z-plane of the launch (a launch covers planes k0 .. k0 + grid.y - 1)
+  int chunked;  // MIXED fix-up of one z-chunk: queue entries from counters[3] on
 };
 
 // prior scale s = |Re(Cxy Ct)| and error eigenvalue lam = |Re Cxy| of one bin
@@ -249,6 +251,9 @@ __device__ __forceinline__ void write_prior_cov(const FusedArgs<T> &a, long b, T
 }
 
 int check_ws(Workspace *w);
+// the fused bin kernel (and, MIXED, the FP64 fix-up) over z-planes k0 .. k0 + nk - 1 (posterior.cu)
+int fused_bins_range(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision, int k0,
+                     int nk, bool chunked, cudaStream_t st);
 template <typename T>
 int fill_fused_args(Workspace *w, void *const *data, void *const *mean, void *const *cov, FusedArgs<T> *out);
 

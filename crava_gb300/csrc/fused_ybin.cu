@@ -14,6 +14,38 @@ static bool ybin_length(int n)
   return (n == 256 || n == 128 || n == 200) && cg_tune_get(CG_TUNE_FUSED_Y, n) == 1;
 }
 
+// Forward y pass, bins and inverse y pass per chunk of zc z-planes after one
+// batched x + z pass: a chunk of the n + 3 spectra (zc * cnxp * nyp complex
+// values each) is written by the y pass, read by the bin kernel and, for the
+// three means, read again by the inverse y pass while it is still in L2.  An
+// even zc keeps every chunk's first element 16-byte aligned.
+static int chunked_y(cg_workspace w, float *const *data, float *const *mean, float *const *cov, int precision, int zc,
+                     cudaStream_t st, cudaEvent_t bins_done)
+{
+  const int nt = w->ntheta, nxp = w->nxp, nyp = w->nyp, nzp = w->nzp;
+  const int cnxp = nxp / 2 + 1;
+  const long plane = (long)cnxp * nyp;  // complex values per z-plane
+  int rc;
+  void *fwd[kMaxTheta + 3];
+  for (int l = 0; l < nt; l++) fwd[l] = data[l];
+  for (int p = 0; p < 3; p++) fwd[nt + p] = mean[p];
+  if ((rc = fft3d_xz<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;
+  if (precision == CG_PREC_MIXED) CG_CUDA(cudaMemsetAsync(w->counters, 0, sizeof(int), st));
+  for (int k0 = 0; k0 < nzp; k0 += zc) {
+    const int nk = nzp - k0 < zc ? nzp - k0 : zc;
+    void *cf[kMaxTheta + 3], *cm[3];
+    for (int i = 0; i < nt + 3; i++) cf[i] = (float2 *)fwd[i] + k0 * plane;
+    for (int p = 0; p < 3; p++) cm[p] = (float2 *)mean[p] + k0 * plane;
+    if ((rc = fft_cols<float>(cf, nt + 3, nyp, cnxp, cnxp, plane, nk, -1, st))) return rc;
+    if ((rc = fused_bins_range(w, (void *const *)data, (void *const *)mean, (void *const *)cov, precision, k0, nk, true,
+                               st)))
+      return rc;
+    if ((rc = fft_cols<float>(cm, 3, nyp, cnxp, cnxp, plane, nk, +1, st))) return rc;
+  }
+  if (bins_done) CG_CUDA(cudaEventRecord(bins_done, st));
+  return fft3d_xz<float>((void *const *)mean, 3, nxp, nyp, nzp, CG_PARAMETER, false, st);
+}
+
 }  // namespace cg
 
 using namespace cg;
@@ -32,6 +64,8 @@ int cg::invert_cubes_fused(cg_workspace w, float *const *data, float *const *mea
   for (int l = 0; l < nt; l++) { if (!data[l]) { set_error("null data[%d]", l); return CG_ERR_ARG; } fwd[l] = data[l]; }
   for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } fwd[nt + p] = mean[p]; }
   for (int t = 0; t < 6; t++) if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; }
+  const int zc = cg_tune_get(CG_TUNE_FUSED_Y, nyp);
+  if (zc >= 2 && nt + 3 <= kMaxBatch) return chunked_y(w, data, mean, cov, precision, zc, st, bins_done);
   if (!ybin_length(nyp)) {
     // no fused kernel for this y length: three-pass transforms around the bin kernel
     if ((rc = fft3d<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;

@@ -242,7 +242,7 @@ template <typename T, int NT, int MODE, int MINB = 1>
 __global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a)
 {
   __shared__ KTab<T> kt;
-  const int k = blockIdx.y;
+  const int k = a.k0 + blockIdx.y;
   {
     const int *src = (const int *)&a.ktab[k];
     int *dst = (int *)&kt;
@@ -308,7 +308,8 @@ __global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, cons
 {
   const double *sig0d = s0.v;
   const int nq = min(*((volatile int *)&a.counters[0]), a.queue_cap);
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+  const int q0 = a.chunked ? *((volatile int *)&a.counters[3]) : 0;
+  for (int q = q0 + blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
     const long b = a.queue[q];
     const int k = (int)(b / a.plane);
     const int ij = (int)(b - (long)k * a.plane);
@@ -640,6 +641,8 @@ int fill_fused_args(Workspace *w, void *const *data, void *const *mean, void *co
   a.queue = w->queue;
   a.queue_cap = w->queue_cap;
   a.counters = w->counters;
+  a.k0 = 0;
+  a.chunked = 0;
   return CG_OK;
 }
 template int fill_fused_args<float>(Workspace *, void *const *, void *const *, void *const *, FusedArgs<float> *);
@@ -648,25 +651,32 @@ template int fill_fused_args<double>(Workspace *, void *const *, void *const *, 
 
 template <typename T>
 static int fused_launch(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision,
-                        cudaStream_t st)
+                        cudaStream_t st, int k0 = 0, int nk = -1, bool chunked = false)
 {
   const int nt = w->ntheta;
   FusedArgs<T> a;
   int rc = fill_fused_args(w, data, mean, cov, &a);
   if (rc) return rc;
+  if (nk < 0) nk = w->nzp;
+  if (k0 < 0 || nk < 1 || k0 + nk > w->nzp) { set_error("z-plane range %d + %d outside 0..%d", k0, nk, w->nzp); return CG_ERR_ARG; }
+  a.k0 = k0;
+  a.chunked = chunked ? 1 : 0;
   const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   const int threads = 128;
-  dim3 grid(ceil_div(a.plane, threads), w->nzp);
+  dim3 grid(ceil_div(a.plane, threads), nk);
   const long outband = (long)a.plane * w->nzp - w->inband_bins;
-  const double fbytes = (double)sizeof(C2<T>) * (w->inband_bins * (double)((nt + 3) + (nt + 3 + 6)) + outband * 6.0);
+  const double fbytes = (double)sizeof(C2<T>) * (w->inband_bins * (double)((nt + 3) + (nt + 3 + 6)) + outband * 6.0) *
+                        ((double)nk / w->nzp);
   return dispatch_nt(nt, [&](auto NTc) -> int {
     constexpr int NT = decltype(NTc)::value;
     if constexpr (sizeof(T) == 8) {
       TraceScope ts("k_invert_fused_fp64", st, fbytes);
       k_invert_fused<T, NT, 2><<<grid, threads, 0, st>>>(a);
     } else if (precision == CG_PREC_MIXED) {
-      // the queue position counter starts at zero for every inversion (stream ordered)
-      cudaError_t me = cudaMemsetAsync(w->counters, 0, sizeof(int), st);
+      // the queue position counter starts at zero for every inversion (stream ordered); a z-chunk of a
+      // chunked inversion appends to the queue and its fix-up starts where the chunk's entries start
+      cudaError_t me = chunked ? cudaMemcpyAsync(w->counters + 3, w->counters, sizeof(int), cudaMemcpyDeviceToDevice, st)
+                               : cudaMemsetAsync(w->counters, 0, sizeof(int), st);
       if (me != cudaSuccess) return cuda_status(me, "queue reset");
       {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
@@ -690,6 +700,12 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
     CG_CHECK_LAUNCH("k_invert_fused");
     return CG_OK;
   });
+}
+
+int cg::fused_bins_range(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision, int k0,
+                         int nk, bool chunked, cudaStream_t st)
+{
+  return fused_launch<float>(w, data, mean, cov, precision, st, k0, nk, chunked);
 }
 
 extern "C" int cg_invert_bins_fused(cg_workspace w, float *const *data, float *const *mean, float *const *cov,

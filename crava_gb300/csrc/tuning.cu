@@ -25,6 +25,14 @@ const char *env_name(int key)
     default: return nullptr;
   }
 }
+bool valid_value(int key, int value)
+{
+  return (key == CG_TUNE_COLS_MINB && (value >= 2 && value <= 4)) ||
+         (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 3)) ||
+         (key == CG_TUNE_BIN_MINB && (value == 1 || value == 6)) ||
+         (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||
+         (key == CG_TUNE_FUSED_Y && (value == 0 || value == 1 || (value >= 2 && value <= 4096 && value % 2 == 0)));
+}
 }  // namespace
 
 int tune_get(int key, int n, int dflt)
@@ -32,7 +40,7 @@ int tune_get(int key, int n, int dflt)
   const char *en = env_name(key);
   if (en) {
     const char *e = getenv(en);
-    if (e && *e) return atoi(e);
+    if (e && *e && valid_value(key, atoi(e))) return atoi(e);  // an invalid value is ignored
   }
   std::lock_guard<std::mutex> lk(g_mu);
   auto it = g_table.find(((long)key << 32) | (unsigned)n);
@@ -49,12 +57,7 @@ using namespace cg;
 extern "C" int cg_tune_set(int key, int n, int value)
 {
   if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_FUSED_Y || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
-  const bool ok = (key == CG_TUNE_COLS_MINB && (value >= 2 && value <= 4)) ||
-                  (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 3)) ||
-                  (key == CG_TUNE_BIN_MINB && (value == 1 || value == 6)) ||
-                  (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||
-                  (key == CG_TUNE_FUSED_Y && (value == 0 || value == 1));
-  if (!ok) { set_error("cg_tune_set: value %d not valid for key %d", value, key); return CG_ERR_ARG; }
+  if (!valid_value(key, value)) { set_error("cg_tune_set: value %d not valid for key %d", value, key); return CG_ERR_ARG; }
   std::lock_guard<std::mutex> lk(g_mu);
   g_table[((long)key << 32) | (unsigned)n] = value;
   return CG_OK;

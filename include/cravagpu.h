@@ -73,7 +73,9 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
  * half length n = nxp/2, or n = nxp for odd nxp: 0 shared-memory staged or
  * generic, 1 four-step),
  * CG_TUNE_FUSED_Y (cg_invert_cubes_fused per y length n: 0 three-pass
- * transforms around the bin kernel, 1 y pass fused with the bin loop).  n = 0 sets the value for every n.  Built-in defaults were
+ * transforms around the bin kernel, 1 y pass fused with the bin loop, an even
+ * c >= 2: forward y pass, bins and inverse y pass run per chunk of c z-planes
+ * so that the chunk's spectra stay in L2).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0

@@ -82,5 +82,8 @@ def test_tuning_table_defaults_overrides_and_validation(native):
     assert native.cg_tune_get(3, 128) == 1 and native.cg_tune_set(3, 128, 0) == 0  # x-row kernel 0/1
     assert native.cg_tune_get(3, 128) == 0 and native.cg_tune_set(3, 128, 2) == -1
     assert native.cg_tune_set(9, 1, 1) == -1
+    # fused-form y handling: 0 three passes, 1 fused y kernel, an even z-chunk size >= 2 the chunked pipeline
+    assert native.cg_tune_get(4, 256) == 0 and native.cg_tune_set(4, 256, 16) == 0 and native.cg_tune_get(4, 256) == 16
+    assert native.cg_tune_set(4, 256, 15) == -1 and native.cg_tune_set(4, 256, 8192) == -1
     native.cg_tune_clear()
     assert native.cg_tune_get(0, 256) == 3
