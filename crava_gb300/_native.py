@@ -171,6 +171,12 @@ def _declare(L):
         "cg_copy": ([V, V, ct.c_size_t, V], I),
         "cg_exp_transform": ([V, ct.c_long, V], I),
         "cg_fill_in_data": ([V, I, I, I, I, I, V, I, V, V, V, V, F, F, V, V], I),
+        "cg_operator_tables_ex": ([I, I, I, V, V, F, F, F, F, I, V, V, V, V, V], I),
+        "cg_scale_wavelet_table_size": ([I], I),
+        "cg_scale_wavelet_tables": ([I, I, I, V, V, V, V, V, F, F, F, F, F, V], I),
+        "cg_divide_by_scale_wavelet": ([PP, I, I, I, I, I, I, I, V, V, V, V, F, F, F, F, F, V, V], I),
+        "cg_multiply_by_scale_wavelet": ([PP, I, I, I, I, I, I, V, V, V, V, F, V], I),
+        "cg_interpolate_seismic": ([V, I, I, I, I, I, I, F, V, V], I),
         "cg_crava_file_write": ([ct.c_char_p, V, I, I, I, V, V], I),
         "cg_crava_file_read": ([ct.c_char_p, V, I, I, I, V, V], I),
         "cg_storm_write": ([ct.c_char_p, V, I, I, I, V], I),

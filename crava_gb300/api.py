@@ -131,6 +131,75 @@ def operator_tables(wavelets, A, nz, nzp, dt_ms, low_cut, high_cut, min_rel_thic
     return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band}
 
 
+def operator_tables_nct(wavelets, A, nz, nzp, dt_ms, low_cut, high_cut, min_rel_thick):
+    """fillErrMultVectors tables, non-constant-thickness branch (cg_operator_tables_ex)."""
+    w = np.ascontiguousarray(wavelets, dtype=np.float32)
+    n = w.shape[0]
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    K = np.zeros((nzp, n, 3), dtype=np.complex64)
+    e1 = np.zeros((nzp, n), dtype=np.complex64)
+    e2 = np.zeros((nzp, n), dtype=np.complex64)
+    e3 = np.zeros((nzp, n), dtype=np.complex64)
+    band = np.zeros(nzp, dtype=np.uint8)
+    check(lib().cg_operator_tables_ex(n, nz, nzp, w.ctypes.data, A32.ctypes.data, dt_ms, min_rel_thick, low_cut,
+                                      high_cut, 0, K.ctypes.data, e1.ctypes.data, e2.ctypes.data, e3.ctypes.data,
+                                      band.ctypes.data), "cg_operator_tables_ex")
+    return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band}
+
+
+def scale_wavelet_tables(wavelets, A, prior_var0, circ_corr_t, err_theta_cov, nz, dz_ms, lz_ms, low_cut, high_cut,
+                         wnc):
+    """Per-angle tables of Crava::computeAdjustmentFactor (host, C++): (ntheta, table_size) float32."""
+    w = np.ascontiguousarray(wavelets, dtype=np.float32)
+    n, nzp = w.shape
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    pv = np.ascontiguousarray(prior_var0, dtype=np.float64)
+    cc = np.ascontiguousarray(circ_corr_t, dtype=np.float32)
+    etc = np.ascontiguousarray(err_theta_cov, dtype=np.float64)
+    ts = lib().cg_scale_wavelet_table_size(nzp)
+    out = np.zeros((n, ts), dtype=np.float32)
+    check(lib().cg_scale_wavelet_tables(n, nz, nzp, w.ctypes.data, A32.ctypes.data, pv.ctypes.data, cc.ctypes.data,
+                                        etc.ctypes.data, dz_ms, lz_ms, low_cut, high_cut, wnc, out.ctypes.data),
+          "cg_scale_wavelet_tables")
+    return out
+
+
+def divide_by_scale_wavelet(cubes, nx, ny, nz, nxp, tables: torch.Tensor, rel_thick: torch.Tensor, dz_ms, lz_ms,
+                            low_cut, high_cut, energy_threshold=0.0, shift=None, gain=None, stream=None):
+    """Crava::divideDataByScaleWavelet (+ interpolateSeismic unless energy_threshold < 0) on real padded
+    DATA cubes in place (cg_divide_by_scale_wavelet); returns the per-cube count of traces at or below
+    the energy limit."""
+    nzp, nyp, _ = cubes[0].shape
+    pc, keep = _pp(cubes)
+    nbad = (ct.c_int * len(cubes))()
+    check(lib().cg_divide_by_scale_wavelet(pc, len(cubes), nx, ny, nz, nxp, nyp, nzp, _vp(tables), _vp(rel_thick),
+                                           _vp(shift) if shift is not None else None,
+                                           _vp(gain) if gain is not None else None, float(dz_ms), float(lz_ms),
+                                           float(low_cut), float(high_cut), float(energy_threshold), nbad,
+                                           _stream(stream)), "cg_divide_by_scale_wavelet")
+    return list(nbad)
+
+
+def multiply_by_scale_wavelet(cubes, nx, ny, nxp, tables: torch.Tensor, rel_thick: torch.Tensor, dz_ms, shift=None,
+                              gain=None, stream=None):
+    """The per-trace product of Crava::multiplyDataByScaleWaveletAndWriteToFile on real padded cubes in place."""
+    nzp, nyp, _ = cubes[0].shape
+    pc, keep = _pp(cubes)
+    check(lib().cg_multiply_by_scale_wavelet(pc, len(cubes), nx, ny, nxp, nyp, nzp, _vp(tables), _vp(rel_thick),
+                                             _vp(shift) if shift is not None else None,
+                                             _vp(gain) if gain is not None else None, float(dz_ms),
+                                             _stream(stream)), "cg_multiply_by_scale_wavelet")
+
+
+def interpolate_seismic(cube: torch.Tensor, nx, ny, nz, nxp, energy_threshold=0.0, stream=None):
+    """FFTGrid::interpolateSeismic on one real padded DATA cube in place; returns the count of bad traces."""
+    nzp, nyp, _ = cube.shape
+    nbad = ct.c_int()
+    check(lib().cg_interpolate_seismic(_vp(cube), nx, ny, nz, nxp, nyp, nzp, float(energy_threshold), ct.byref(nbad),
+                                       _stream(stream)), "cg_interpolate_seismic")
+    return nbad.value
+
+
 class _Model(ct.Structure):
     _fields_ = [("ntheta", ct.c_int), ("wnc", ct.c_float), ("is4d", ct.c_int), ("K", ct.c_void_p),
                 ("em1", ct.c_void_p), ("em2", ct.c_void_p), ("em3", ct.c_void_p), ("band", ct.c_void_p),

@@ -13,8 +13,13 @@
 // src/wavelet.cpp:246-325) and e3_l = central(backward(forward(w_l)))
 // (Crava::makeErrorSmooth, src/crava.cpp:1289-1323, Wavelet1D ctor
 // src/wavelet1D.cpp:419-479), plus the inversion band of
-// src/crava.cpp:1104-1105.  Spectra are computed in double by a small
-// mixed-radix FFT and rounded to float.
+// src/crava.cpp:1104-1105.  The non-constant-thickness branch
+// (src/crava.cpp:1362-1385) has K = kD * A, errMult1 = 1/||w||,
+// errMult2 = kD3/||e3|| (kD3: the third-difference operator) and errMult3 =
+// 1/max(|W(k)|, |W(k/0.999)|) (fillInverseAbskWRobust, :1493-1519).
+// Spectra are computed in double by a small mixed-radix FFT and rounded to
+// float.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <vector>
@@ -68,9 +73,9 @@ double norm2(const std::vector<double> &x)
 
 }  // namespace
 
-extern "C" int cg_operator_tables(int ntheta, int nz, int nzp, const float *wavelets, const float *A, float dt_ms,
-                                  float min_rel_thick, float low_cut, float high_cut, float *K, float *em1,
-                                  float *em2, float *em3, unsigned char *band)
+extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *wavelets, const float *A, float dt_ms,
+                                     float min_rel_thick, float low_cut, float high_cut, int constant_thickness,
+                                     float *K, float *em1, float *em2, float *em3, unsigned char *band)
 {
   if (ntheta < 1 || nzp < 2 || nz < 1 || !wavelets || !A || !K || !em1 || !em2 || !em3 || !band) {
     cg::set_error("cg_operator_tables: bad argument");
@@ -80,7 +85,16 @@ extern "C" int cg_operator_tables(int ntheta, int nz, int nzp, const float *wave
   d1[0] = -1.0;
   d1[nzp - 1] = 1.0;
   const std::vector<cd> kD = rfft(d1);
+  // third-difference operator central(backward(d1)) for the non-constant-thickness errMult2
+  std::vector<double> d2(nzp), d3(nzp);
+  for (int i = 0; i < nzp; i++) d2[i] = (float)((i == 0) ? d1[0] - d1[nzp - 1] : d1[i] - d1[i - 1]);
+  for (int i = 0; i < nzp; i++) {
+    const double v = (i == 0) ? 0.5 * (d2[1] - d2[nzp - 1]) : (i == nzp - 1) ? 0.5 * (d2[0] - d2[i - 1]) : 0.5 * (d2[i + 1] - d2[i - 1]);
+    d3[i] = (float)v;
+  }
+  const std::vector<cd> kD3 = rfft(d3);
   const float lz = nz * dt_ms;
+  const int cnzp = nzp / 2 + 1;
   for (int l = 0; l < ntheta; l++) {
     std::vector<double> w(nzp), f(nzp), b(nzp), e3(nzp);
     for (int i = 0; i < nzp; i++) w[i] = wavelets[(long)l * nzp + i];
@@ -93,27 +107,141 @@ extern "C" int cg_operator_tables(int ntheta, int nz, int nzp, const float *wave
     const double wn = (float)norm2(w), en = (float)norm2(e3);
     const std::vector<cd> W = rfft(w), E = rfft(e3);
     for (int k = 0; k < nzp; k++) {
-      // the full spectrum already holds getCAmp's reflected/conjugated values for k >= nzp/2+1
-      const cd kw = std::conj(W[k]);
-      const cd p = kD[k] * kw;
-      for (int q = 0; q < 3; q++) {
-        const long o = (((long)k * ntheta + l) * 3 + q) * 2;
-        K[o] = (float)(p.real() * (double)A[l * 3 + q]);
-        K[o + 1] = (float)(p.imag() * (double)A[l * 3 + q]);
-      }
       const long o = ((long)k * ntheta + l) * 2;
-      em1[o] = (float)(W[k].real() / wn);
-      em1[o + 1] = (float)(-W[k].imag() / wn);
-      em2[o] = (float)(E[k].real() / en);
-      em2[o + 1] = (float)(-E[k].imag() / en);
-      em3[o] = 1.0f;
-      em3[o + 1] = 0.0f;
+      if (constant_thickness) {
+        // the full spectrum already holds getCAmp's reflected/conjugated values for k >= nzp/2+1
+        const cd kw = std::conj(W[k]);
+        const cd p = kD[k] * kw;
+        for (int q = 0; q < 3; q++) {
+          const long oq = (((long)k * ntheta + l) * 3 + q) * 2;
+          K[oq] = (float)(p.real() * (double)A[l * 3 + q]);
+          K[oq + 1] = (float)(p.imag() * (double)A[l * 3 + q]);
+        }
+        em1[o] = (float)(W[k].real() / wn);
+        em1[o + 1] = (float)(-W[k].imag() / wn);
+        em2[o] = (float)(E[k].real() / en);
+        em2[o + 1] = (float)(-E[k].imag() / en);
+        em3[o] = 1.0f;
+        em3[o + 1] = 0.0f;
+      } else {
+        // K = kD A, errMult1 = 1/||w||, errMult2 = kD3/||e3||, errMult3 = fillInverseAbskWRobust
+        for (int q = 0; q < 3; q++) {
+          const long oq = (((long)k * ntheta + l) * 3 + q) * 2;
+          K[oq] = (float)(kD[k].real() * (double)A[l * 3 + q]);
+          K[oq + 1] = (float)(kD[k].imag() * (double)A[l * 3 + q]);
+        }
+        em1[o] = (float)(1.0 / wn);
+        em1[o + 1] = 0.0f;
+        em2[o] = (float)(kD3[k].real() / en);
+        em2[o + 1] = (float)(kD3[k].imag() / en);
+        // |W| at k and at the spectrum stretched by 0.999 (Wavelet::getCAmp(k, 0.999f)), the larger one
+        const int kk = k < cnzp ? k : nzp - k;
+        const float omega = (float)kk / 0.999f;
+        double modf = 0.0;
+        if (omega < (float)cnzp) {
+          const int omL = (int)std::floor(omega);
+          const int omU = omL + 1 < cnzp ? omL + 1 : omL;
+          const float d = omega - (float)omL;
+          const cd v = W[omL] * (double)(1.0f - d) + W[omU] * (double)d;
+          modf = std::norm(v);
+        }
+        const double maxMod = std::max(std::norm(W[kk]), modf);
+        em3[o] = maxMod > 0.0 ? (float)(1.0 / std::sqrt(maxMod)) : (float)(wn * nzp * nzp * 100.0);
+        em3[o + 1] = 0.0f;
+      }
     }
   }
   for (int k = 0; k < nzp; k++) {
     const int kk = k < nzp - k ? k : nzp - k;
     const float f = (float)((nz * 1000.0f) / (lz * nzp) * kk);
     band[k] = (f > low_cut * min_rel_thick && f < high_cut) ? 1 : 0;
+  }
+  return CG_OK;
+}
+
+extern "C" int cg_operator_tables(int ntheta, int nz, int nzp, const float *wavelets, const float *A, float dt_ms,
+                                  float min_rel_thick, float low_cut, float high_cut, float *K, float *em1,
+                                  float *em2, float *em3, unsigned char *band)
+{
+  return cg_operator_tables_ex(ntheta, nz, nzp, wavelets, A, dt_ms, min_rel_thick, low_cut, high_cut, 1, K, em1, em2,
+                               em3, band);
+}
+
+// ---------------------------------------------------------------------------
+// Per-angle tables of Crava::computeAdjustmentFactor (src/crava.cpp:807-903)
+// for the non-constant-thickness data scaling (divideDataByScaleWavelet) and
+// its inverse (multiplyDataByScaleWaveletAndWriteToFile).  Per angle, with
+// c = nzp/2 + 1 frequency bins:
+//   [0, 2c)    W     spectrum of the global wavelet (R2C, unnormalised)
+//   [2c, 4c)   E3    spectrum of central(backward(forward(w))) divided by its
+//                    band-limited norm (Wavelet::findNormWithinFrequencyBand);
+//                    the device lookup replaces the floats past nzp by
+//                    RMISSING, as Wavelet::multiplyRAmpByConstant leaves them
+//   [4c, 5c)   tau2  |Re| of the FFT of the reflection-coefficient time
+//                    covariance (computeReflectionCoefficientTimeCovariance)
+//   5c + 0..3  ||w||^2, modW (mean squared wavelet amplitude up to highCut),
+//              errThetaCov[l][l], wnc
+// ---------------------------------------------------------------------------
+extern "C" int cg_scale_wavelet_table_size(int nzp) { return ((5 * (nzp / 2 + 1) + 4) + 3) & ~3; }
+
+extern "C" int cg_scale_wavelet_tables(int ntheta, int nz, int nzp, const float *wavelets, const float *A,
+                                       const double *prior_var0, const float *circ_corr_t,
+                                       const double *err_theta_cov, float dz_ms, float lz_ms, float low_cut,
+                                       float high_cut, float wnc, float *tables)
+{
+  if (ntheta < 1 || nz < 1 || nzp < 2 || !wavelets || !A || !prior_var0 || !circ_corr_t || !err_theta_cov ||
+      !tables || !(dz_ms > 0) || !(lz_ms > 0) || !(high_cut > 0)) {
+    cg::set_error("cg_scale_wavelet_tables: bad argument");
+    return CG_ERR_ARG;
+  }
+  const int c = nzp / 2 + 1, ts = cg_scale_wavelet_table_size(nzp);
+  for (int l = 0; l < ntheta; l++) {
+    float *t = tables + (long)l * ts;
+    for (int i = 0; i < ts; i++) t[i] = 0.0f;
+    std::vector<double> w(nzp), f(nzp), b(nzp), e3(nzp), rc(nzp);
+    for (int i = 0; i < nzp; i++) w[i] = wavelets[(long)l * nzp + i];
+    const std::vector<cd> W = rfft(w);
+    for (int k = 0; k < c; k++) { t[2 * k] = (float)W[k].real(); t[2 * k + 1] = (float)W[k].imag(); }
+    for (int i = 0; i < nzp; i++) f[i] = (float)((i == nzp - 1) ? w[0] - w[i] : w[i + 1] - w[i]);
+    for (int i = 0; i < nzp; i++) b[i] = (float)((i == 0) ? f[0] - f[nzp - 1] : f[i] - f[i - 1]);
+    for (int i = 0; i < nzp; i++) {
+      const double v = (i == 0) ? 0.5 * (b[1] - b[nzp - 1]) : (i == nzp - 1) ? 0.5 * (b[0] - b[i - 1]) : 0.5 * (b[i + 1] - b[i - 1]);
+      e3[i] = (float)v;
+    }
+    const std::vector<cd> E = rfft(e3);
+    // band-limited norm of E3 (dOmega in float as the reference computes it)
+    const float dOmega = 1.0f / ((float)nzp * dz_ms * 0.001f);
+    const int loI = std::max(0, (int)std::floor(low_cut / dOmega));
+    const int hiI = std::min(c, (int)std::ceil(high_cut / dOmega));
+    double n2 = 0.0;
+    for (int i = loI; i < hiI; i++) n2 += 2.0 / nzp * std::norm(E[i]);
+    if (loI == 0) n2 -= 1.0 / nzp * std::norm(E[0]);
+    const double normF3 = std::sqrt(n2);
+    float *te = t + 2 * c;
+    for (int i = 0; i < 2 * c; i++) {
+      const cd v = E[i / 2];
+      te[i] = (float)((i % 2 ? v.imag() : v.real()) / normF3);
+    }
+    // reflection-coefficient time covariance: eiVar * corrT filtered to refk < nz, then 2 c_i - c_{i+1} - c_{i-1}
+    double eiVar = 0.0;
+    for (int p = 0; p < 3; p++)
+      for (int q = 0; q < 3; q++) eiVar += (double)A[l * 3 + p] * prior_var0[p * 3 + q] * (double)A[l * 3 + q];
+    std::vector<double> ei(nzp);
+    for (int k = 0; k < nzp; k++) {
+      const int refk = k < c ? k : nzp - k;
+      ei[k] = refk < nz ? eiVar * (double)circ_corr_t[refk] : 0.0;
+    }
+    for (int i = 0; i < nzp; i++) rc[i] = 2.0 * ei[i] - ei[(i + 1) % nzp] - ei[(i + nzp - 1) % nzp];
+    const std::vector<cd> RC = rfft(rc);
+    for (int k = 0; k < c; k++) t[4 * c + k] = (float)std::fabs(RC[k].real());
+    const float wn = (float)norm2(w);
+    float modW = wn * wn;
+    const float maxfrequency = (float)((nzp / 2) * 1000.0 * nz) / (float)((double)lz_ms * nzp);
+    modW *= maxfrequency / high_cut;
+    t[5 * c + 0] = wn * wn;
+    t[5 * c + 1] = modW;
+    t[5 * c + 2] = (float)err_theta_cov[(long)l * ntheta + l];
+    t[5 * c + 3] = wnc;
   }
   return CG_OK;
 }

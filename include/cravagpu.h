@@ -192,6 +192,61 @@ int cg_fill_in_data(float *buf, int nxp, int nyp, int nzp, int nz, int cubetype,
                     float dz_data, float smooth_length, int *extrap_out, void *stream);
 
 /* ========================================================================
+ * Non-constant simbox thickness (the relative thickness varies laterally).
+ * ======================================================================== */
+
+/* fillErrMultVectors tables with the thickness branch chosen: constant_thickness
+ * != 0 is cg_operator_tables; 0 the non-constant branch (src/crava.cpp:1362-1385):
+ * K = kD*A, errMult1 = 1/||w||, errMult2 = kD3/||e3||, errMult3 =
+ * fillInverseAbskWRobust (:1493-1519).  min_rel_thick: smallest relative
+ * thickness of the simbox (the band's lower edge is lowCut*min_rel_thick). */
+int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *wavelets, const float *A, float dt_ms,
+                          float min_rel_thick, float low_cut, float high_cut, int constant_thickness, float *K,
+                          float *em1, float *em2, float *em3, unsigned char *band);
+
+/* Floats per angle of the scale-wavelet tables (a multiple of 4). */
+int cg_scale_wavelet_table_size(int nzp);
+
+/* Per-angle tables of Crava::computeAdjustmentFactor (src/crava.cpp:807-903),
+ * HOST arrays: wavelets [ntheta][nzp] (time samples in FFT order), A
+ * [ntheta][3], prior_var0 [3][3] (Crava::priorVar0_), circ_corr_t [nzp] (cyclic
+ * prior temporal correlation, 1 at lag 0; filtered to lags < nz as
+ * getPriorCorrTFiltered), err_theta_cov [ntheta][ntheta].  dz_ms: the
+ * wavelet's sample interval, lz_ms: the simbox's time thickness.  tables:
+ * [ntheta][cg_scale_wavelet_table_size(nzp)] floats. */
+int cg_scale_wavelet_tables(int ntheta, int nz, int nzp, const float *wavelets, const float *A,
+                            const double *prior_var0, const float *circ_corr_t, const double *err_theta_cov,
+                            float dz_ms, float lz_ms, float low_cut, float high_cut, float wnc, float *tables);
+
+/* Crava::divideDataByScaleWavelet (src/crava.cpp:678-804) on ntheta real
+ * padded DATA cubes (device, in place; ntheta <= 16), followed per cube by
+ * FFTGrid::interpolateSeismic with energy_threshold (skipped when negative).
+ * tables: device copy of cg_scale_wavelet_tables; rel_thick: [nyp][nxp]
+ * (device) Simbox::getRelThick at every padded trace (must be positive);
+ * shift, gain: [ntheta][ny][nx] (device) local wavelet time shift (ms) and
+ * gain surfaces, or NULL for none.  n_bad (host, ntheta ints, may be NULL):
+ * traces at or below the energy limit.  The slack floats of each row (x >=
+ * nxp) are overwritten.  Waits for the stream when interpolating. */
+int cg_divide_by_scale_wavelet(float *const *data, int ntheta, int nx, int ny, int nz, int nxp, int nyp, int nzp,
+                               const float *tables, const float *rel_thick, const float *shift, const float *gain,
+                               float dz_ms, float lz_ms, float low_cut, float high_cut, float energy_threshold,
+                               int *n_bad, void *stream);
+
+/* The product of Crava::multiplyDataByScaleWaveletAndWriteToFile (src/crava.cpp:
+ * 906-968) on ncubes real padded cubes (device, in place): every simbox trace
+ * (i < nx, j < ny) times the conjugate of its stretched local wavelet
+ * spectrum; cube l uses angle l of the tables. */
+int cg_multiply_by_scale_wavelet(float *const *data, int ncubes, int nx, int ny, int nxp, int nyp, int nzp,
+                                 const float *tables, const float *rel_thick, const float *shift, const float *gain,
+                                 float dz_ms, void *stream);
+
+/* FFTGrid::interpolateSeismic + extrapolateSeismic (src/fftgrid.cpp:2576-2738)
+ * on one real padded DATA cube (device, in place).  n_bad (host, may be NULL):
+ * traces at or below the energy limit.  Synchronous. */
+int cg_interpolate_seismic(float *data, int nx, int ny, int nz, int nxp, int nyp, int nzp, float energy_threshold,
+                           int *n_bad, void *stream);
+
+/* ========================================================================
  * File formats either side of the path (host memory, synchronous)
  * ======================================================================== */
 

@@ -104,6 +104,18 @@ def lib():
                 ct.c_int, ct.c_int, ct.c_int, PR, ct.c_void_p, ct.c_float, ct.c_float, ct.c_float, ct.c_float,
                 ct.c_float, PR, PR, PR, PR, ct.c_void_p]
             getattr(L, "or_circ_corr_t" + sfx).argtypes = [ct.c_void_p, ct.c_int, ct.c_int, ct.c_int, PR]
+            getattr(L, "or_k_tables_nct" + sfx).argtypes = [
+                ct.c_int, ct.c_int, ct.c_int, PR, ct.c_void_p, ct.c_float, ct.c_float, ct.c_float, ct.c_float,
+                PR, PR, PR, PR, ct.c_void_p]
+            FP = ct.POINTER(ct.c_float)
+            getattr(L, "or_divide_scale_wavelet" + sfx).argtypes = [
+                PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, PR, FP, ct.POINTER(ct.c_double), PR,
+                ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float, FP, FP, FP, ct.c_int]
+            getattr(L, "or_multiply_scale_wavelet" + sfx).argtypes = [
+                PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, PR, ct.c_float, FP, FP, FP, ct.c_int]
+            getattr(L, "or_interpolate_seismic" + sfx).argtypes = [
+                PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_float]
+            getattr(L, "or_interpolate_seismic" + sfx).restype = ct.c_int
             getattr(L, "or_circ_corr_t" + sfx).restype = ct.c_int
         L.or_fill_complex_noise.argtypes = [ct.POINTER(ct.c_float), ct.c_int, ct.c_int, ct.c_int,
                                             ct.POINTER(ct.c_uint)]
@@ -367,6 +379,74 @@ def k_tables(nxp, wavelets, A, nz, nzp, dt_ms, lowCut, highCut, minRelThick=1.0,
                                           lowCut, highCut, _ptr(_real_view(K), R), _ptr(_real_view(e1), R),
                                           _ptr(_real_view(e2), R), _ptr(_real_view(e3), R), band.ctypes.data)
     return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band, "nxp": nxp}
+
+
+def k_tables_nct(nxp, wavelets, A, nz, nzp, lz, lowCut, highCut, minRelThick, prec="f"):
+    """fillErrMultVectors for every k, non-constant-thickness branch (K = kD*A, errMult1 = 1/||w||,
+    errMult2 = kD3/||e3||, errMult3 = 1/|W| robust)."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    cdt = np.complex64 if prec == "f" else np.complex128
+    w = np.ascontiguousarray(wavelets, dtype=_rdt(prec))
+    n = w.shape[0]
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    K = np.zeros((nzp, n, 3), dtype=cdt)
+    e1 = np.zeros((nzp, n), dtype=cdt)
+    e2 = np.zeros((nzp, n), dtype=cdt)
+    e3 = np.zeros((nzp, n), dtype=cdt)
+    band = np.zeros(nzp, dtype=np.uint8)
+    getattr(lib(), "or_k_tables_nct_" + prec)(n, nz, nzp, _ptr(w, R), A32.ctypes.data, lz, minRelThick, lowCut,
+                                              highCut, _ptr(_real_view(K), R), _ptr(_real_view(e1), R),
+                                              _ptr(_real_view(e2), R), _ptr(_real_view(e3), R), band.ctypes.data)
+    return {"K": K, "em1": e1, "em2": e2, "em3": e3, "band": band, "nxp": nxp}
+
+
+def _fptr(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32).ctypes.data_as(ct.POINTER(ct.c_float))
+
+
+def divide_scale_wavelet(buf, nx, ny, nz, wavelet, A, prior_var0, circ_corr_t, dz, lz, low_cut, high_cut, wnc,
+                         err_var, rel_thick, shift=None, gain=None, prec="f", nthreads=None):
+    """Crava::divideDataByScaleWavelet on one real padded angle cube (returns a new cube; the
+    interpolateSeismic step is separate)."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    nzp, nyp, rnxp = buf.shape
+    nxp = rel_thick.shape[1]
+    out = np.array(buf, dtype=_rdt(prec), order="C")
+    w = np.ascontiguousarray(wavelet, dtype=_rdt(prec))
+    cc = np.ascontiguousarray(circ_corr_t, dtype=_rdt(prec))
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    pv = np.ascontiguousarray(prior_var0, dtype=np.float64)
+    rt = np.ascontiguousarray(rel_thick, dtype=np.float32)
+    keep = [np.ascontiguousarray(x, dtype=np.float32) if x is not None else None for x in (shift, gain)]
+    getattr(lib(), "or_divide_scale_wavelet_" + prec)(
+        _ptr(out, R), nx, ny, nz, nxp, nyp, nzp, _ptr(w, R), A32.ctypes.data_as(ct.POINTER(ct.c_float)),
+        pv.ctypes.data_as(ct.POINTER(ct.c_double)), _ptr(cc, R), dz, lz, low_cut, high_cut, wnc, err_var,
+        rt.ctypes.data_as(ct.POINTER(ct.c_float)), _fptr(keep[0]), _fptr(keep[1]), nthreads or os.cpu_count())
+    return out
+
+
+def multiply_scale_wavelet(buf, nx, ny, wavelet, dz, rel_thick, shift=None, gain=None, prec="f", nthreads=None):
+    """Crava::multiplyDataByScaleWaveletAndWriteToFile's per-trace product on one real padded cube."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    nzp, nyp, rnxp = buf.shape
+    nxp = rel_thick.shape[1]
+    out = np.array(buf, dtype=_rdt(prec), order="C")
+    w = np.ascontiguousarray(wavelet, dtype=_rdt(prec))
+    rt = np.ascontiguousarray(rel_thick, dtype=np.float32)
+    keep = [np.ascontiguousarray(x, dtype=np.float32) if x is not None else None for x in (shift, gain)]
+    getattr(lib(), "or_multiply_scale_wavelet_" + prec)(
+        _ptr(out, R), nx, ny, nxp, nyp, nzp, _ptr(w, R), dz, rt.ctypes.data_as(ct.POINTER(ct.c_float)),
+        _fptr(keep[0]), _fptr(keep[1]), nthreads or os.cpu_count())
+    return out
+
+
+def interpolate_seismic(buf, nx, ny, nz, nxp, energy_threshold=0.0, prec="f"):
+    """FFTGrid::interpolateSeismic + extrapolateSeismic on one real padded cube; returns (cube, n_bad)."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    nzp, nyp, rnxp = buf.shape
+    out = np.array(buf, dtype=_rdt(prec), order="C")
+    n = getattr(lib(), "or_interpolate_seismic_" + prec)(_ptr(out, R), nx, ny, nz, nxp, nyp, nzp, energy_threshold)
+    return out, n
 
 
 def circ_corr_t(priorCorrT, minIntFq, nzp, prec="f"):
