@@ -177,6 +177,8 @@ def _declare(L):
         "cg_divide_by_scale_wavelet": ([PP, I, I, I, I, I, I, I, V, V, V, V, F, F, F, F, F, V, V], I),
         "cg_multiply_by_scale_wavelet": ([PP, I, I, I, I, I, I, V, V, V, V, F, V], I),
         "cg_interpolate_seismic": ([V, I, I, I, I, I, I, F, V, V], I),
+        "cg_correct_alpha_beta_rho": ([PP, PP, I, I, I, I, I, I, I, V, V, V, V, V, V, V], I),
+        "cg_apply_trace_matrices": ([PP, PP, V, I, I, I, I, I, I, V], I),
         "cg_crava_file_write": ([ct.c_char_p, V, I, I, I, V, V], I),
         "cg_crava_file_read": ([ct.c_char_p, V, I, I, I, V, V], I),
         "cg_storm_write": ([ct.c_char_p, V, I, I, I, V], I),

@@ -200,6 +200,72 @@ def interpolate_seismic(cube: torch.Tensor, nx, ny, nz, nxp, energy_threshold=0.
     return nbad.value
 
 
+def _sort3x3(ev, V):
+    """NRLib::Sort3x3 (libs/nrlib/flens/nrlib_flens.cpp:211-245): eigenvalues in decreasing order, the
+    first of equal values first, eigenvectors permuted alike."""
+    idx = []
+    for _ in range(3):
+        best, bi = -100000.0, -1
+        for i in range(3):
+            if i not in idx and ev[i] > best:
+                best, bi = ev[i], i
+        idx.append(bi)
+    return ev[idx], V[:, idx]
+
+
+def _eig(M):
+    """NRLib::ComputeEigenVectors: the general LAPACK eigen solver (geev) on a symmetric matrix, real parts."""
+    w, V = np.linalg.eig(np.asarray(M, dtype=np.float64))
+    return np.real(w), np.real(V)
+
+
+def local_noise_g(err_theta_cov, prior_var0, post_var0):
+    """Crava::computeG (src/crava.cpp:2261-2343) on the host with LAPACK's geev through numpy, as the
+    reference's NRLib::ComputeEigenVectors does: G (ntheta, 3) for cg_correct_alpha_beta_rho.  The
+    correction depends on the signs of the eigenvectors of Sm^-1/2 (Sm - Spost) Sm^-1/2, which are the
+    eigen routine's choice."""
+    E = np.asarray(err_theta_cov, dtype=np.float64)
+    n = E.shape[0]
+    Sm = np.asarray(prior_var0, dtype=np.float64)
+    Sdelta = Sm - np.asarray(post_var0, dtype=np.float64)
+    ev, V = _eig(Sdelta)
+    Sdelta = V @ np.diag(np.where(ev > 0.0, ev, 0.0)) @ V.T
+    ev, V = _eig(Sm)
+    Sinv = V @ np.diag(np.where(ev > 0.0000001, 1.0 / np.sqrt(np.abs(ev)), 0.0)) @ V.T
+    A = Sinv @ Sdelta @ Sinv
+    ev, V = _sort3x3(*_eig(A))
+    Lg = np.zeros((n, 3))
+    for i in range(min(n, 3)):
+        Lg[i, i] = np.sqrt(ev[i] / (1.0 - ev[i]))
+    eve, Ve = _eig(E)
+    Esq = Ve @ np.diag(np.where(eve > 0.0, np.sqrt(np.abs(eve)), 0.0)) @ Ve.T
+    return Esq @ Lg @ V.T @ Sinv
+
+
+def correct_alpha_beta_rho(post, mean, nx, ny, nz, nxp, G, err_theta_cov, prior_var0, post_var0,
+                           noise_scale: torch.Tensor, sigmamd: torch.Tensor | None = None, stream=None):
+    """Crava::correctAlphaBetaRho on 3 real padded posterior-mean cubes in place (cg_correct_alpha_beta_rho).
+    noise_scale: (ntheta, ny, nx) float64 device tensor; sigmamd: optional (ny, nx, 9) float64 device tensor."""
+    nzp, nyp, _ = post[0].shape
+    pp, k1 = _pp(post)
+    pm, k2 = _pp(mean)
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    h = [np.ascontiguousarray(x, dtype=np.float64) for x in (err_theta_cov, prior_var0, post_var0)]
+    check(lib().cg_correct_alpha_beta_rho(pp, pm, nx, ny, nz, nxp, nyp, nzp, G.shape[0], G.ctypes.data,
+                                          h[0].ctypes.data, h[1].ctypes.data, h[2].ctypes.data, _vp(noise_scale),
+                                          _vp(sigmamd) if sigmamd is not None else None, _stream(stream)),
+          "cg_correct_alpha_beta_rho")
+
+
+def apply_trace_matrices(fields, mats: torch.Tensor, nx, ny, nz, nxp, mean=None, stream=None):
+    """The local-noise step of Crava::simulate: simbox cells times the trace's 3x3 matrix, then + mean."""
+    nzp, nyp, _ = fields[0].shape
+    pf, k1 = _pp(fields)
+    pm, k2 = _pp(mean) if mean is not None else (None, None)
+    check(lib().cg_apply_trace_matrices(pf, pm, _vp(mats), nx, ny, nz, nxp, nyp, nzp, _stream(stream)),
+          "cg_apply_trace_matrices")
+
+
 class _Model(ct.Structure):
     _fields_ = [("ntheta", ct.c_int), ("wnc", ct.c_float), ("is4d", ct.c_int), ("K", ct.c_void_p),
                 ("em1", ct.c_void_p), ("em2", ct.c_void_p), ("em3", ct.c_void_p), ("band", ct.c_void_p),

@@ -23,6 +23,29 @@ int cuda_status(cudaError_t e, const char *where)
   return CG_ERR_CUDA;
 }
 
+// Stream-ordered scratch allocation.  The device's default memory pool
+// returns its memory at every synchronisation unless told otherwise, and the
+// next cudaMallocAsync then maps it again; the library's pool keeps what it
+// has (release threshold: unlimited), set once per device.  The attribute
+// belongs to this process's pool, not to the GPU.
+cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st)
+{
+  static bool done[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev >= 0 && dev < 64 && !done[dev]) {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      unsigned long long keep = ~0ULL;
+      (void)cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    (void)cudaGetLastError();
+    done[dev] = true;
+  }
+  return cudaMallocAsync(p, bytes, st);
+}
+
 }  // namespace cg
 
 extern "C" const char *cg_last_error(void) { return cg::g_err; }

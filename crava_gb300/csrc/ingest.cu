@@ -180,10 +180,10 @@ extern "C" int cg_fill_in_data(float *buf, int nxp, int nyp, int nzp, int nz, in
   float *coarse = nullptr, *fine = nullptr;
   float2 *trend = nullptr;
   int *ext = nullptr;
-  CG_CUDA(cudaMallocAsync((void **)&coarse, sizeof(float) * (size_t)a.ncol * a.rnt, st));
-  cudaError_t e = cudaMallocAsync((void **)&fine, sizeof(float) * (size_t)a.ncol * a.rmt, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **)&trend, sizeof(float2) * (size_t)a.ncol, st);
-  if (e == cudaSuccess) e = cudaMallocAsync((void **)&ext, 2 * sizeof(int), st);
+  CG_CUDA(scratch_alloc((void **)&coarse, sizeof(float) * (size_t)a.ncol * a.rnt, st));
+  cudaError_t e = scratch_alloc((void **)&fine, sizeof(float) * (size_t)a.ncol * a.rmt, st);
+  if (e == cudaSuccess) e = scratch_alloc((void **)&trend, sizeof(float2) * (size_t)a.ncol, st);
+  if (e == cudaSuccess) e = scratch_alloc((void **)&ext, 2 * sizeof(int), st);
   int rc = CG_OK;
   if (e != cudaSuccess) rc = cuda_status(e, "ingest buffers");
   if (!rc) {

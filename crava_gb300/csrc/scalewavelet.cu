@@ -40,11 +40,13 @@
 namespace cg {
 namespace {
 
-struct SwTrace {
+struct __align__(16) SwTrace {
   float sf;    // stretch = relative thickness
   float gain;  // local gain
   float ahi;   // iShift / nzp = ahi + alo, ahi with at most 11 significant bits
   float alo;
+  float2 step; // exp(-2 pi i iShift / nzp): the shift phase of one bin
+  float2 pad;
 };
 
 // FFTGrid::getDistToBoundary (src/fftgrid.cpp:1353-1389)
@@ -133,6 +135,10 @@ __global__ void k_sw_params(SwTrace *__restrict__ tp, int2 *__restrict__ kb, con
     t.gain = g;
     t.ahi = (float)hi;
     t.alo = (float)(a - hi);
+    float sn, cs;
+    sincospif(2.0f * ((t.ahi - rintf(t.ahi)) + t.alo), &sn, &cs);
+    t.step = make_float2(cs, -sn);
+    t.pad = make_float2(0.0f, 0.0f);
     tp[idx] = t;
   }
 }
@@ -176,22 +182,25 @@ __device__ __forceinline__ float2 phasor_at(const SwTrace &t, int m)
   return make_float2(1.0f, 0.0f);
 }
 
-// computeAdjustmentFactor at bin k < nzp/2 + 1 for one trace
+// computeAdjustmentFactor at bin k < nzp/2 + 1 for one trace: the
+// reference's (wLoc/(tau2 wLoc2Adj + sigma2Loc)) / (wGlob2Adj/(tau2 wGlob2 +
+// sigma2Glob)) as one quotient
 template <bool SHIFT>
-__device__ float2 adjustment(const float *tab, int nzp, const SwTrace &t, int k)
+__device__ float2 adjustment(const float *tab, int nzp, const SwTrace &t, int k, float inv_wn2)
 {
   const int cnzp = nzp / 2 + 1;
   const float2 *W = (const float2 *)tab;
   const float2 *E = W + cnzp;
   const float *tau = (const float *)(E + cnzp);
-  const float wn2 = tau[cnzp], modW = tau[cnzp + 1], ev = tau[cnzp + 2], wnc = tau[cnzp + 3];
+  const float modW = tau[cnzp + 1], ev = tau[cnzp + 2], wnc = tau[cnzp + 3];
   float2 wLoc = make_float2(0.0f, 0.0f), eLoc = make_float2(0.0f, 0.0f);
   const float omega = (float)k / t.sf;
   if (omega < (float)cnzp) {
     const int omL = (int)floorf(omega);
     const int omU = omL + 1 < cnzp ? omL + 1 : omL;
     const float d = omega - (float)omL, d1 = 1.0f - d;
-    const float2 pL = phasor_at<SHIFT>(t, omL), pU = phasor_at<SHIFT>(t, omU);
+    const float2 pL = phasor_at<SHIFT>(t, omL);
+    const float2 pU = (SHIFT && omU != omL) ? cmulf(pL, t.step) : pL;
     const float2 wa = wl_val(W, omL, pL, t.gain, nzp), wb = wl_val(W, omU, pU, t.gain, nzp);
     wLoc = make_float2(wa.x * d1 + wb.x * d, wa.y * d1 + wb.y * d);
     const float2 ea = e3_val(E, omL, pL, nzp), eb = e3_val(E, omU, pU, nzp);
@@ -200,10 +209,10 @@ __device__ float2 adjustment(const float *tab, int nzp, const SwTrace &t, int k)
   const float wLoc2 = wLoc.x * wLoc.x + wLoc.y * wLoc.y;
   const float2 wG = W[k];
   const float wGlob2 = wG.x * wG.x + wG.y * wG.y;
-  const float sLoc = wLoc2 / wn2 + (eLoc.x * eLoc.x + eLoc.y * eLoc.y);
+  const float sLoc = wLoc2 * inv_wn2 + (eLoc.x * eLoc.x + eLoc.y * eLoc.y);
   const float2 pk = phasor_at<SHIFT>(t, k);
   const float2 gl = wl_val(W, k, pk, t.gain, nzp), eg = e3_val(E, k, pk, nzp);
-  const float sGlob = (gl.x * gl.x + gl.y * gl.y) / wn2 + (eg.x * eg.x + eg.y * eg.y);
+  const float sGlob = (gl.x * gl.x + gl.y * gl.y) * inv_wn2 + (eg.x * eg.x + eg.y * eg.y);
   float s2L = ev * (wnc + (1.0f - wnc) * 0.5f * sLoc);
   const float s2G = ev * (wnc + (1.0f - wnc) * 0.5f * sGlob);
   const float tau2 = tau[k];
@@ -214,9 +223,9 @@ __device__ float2 adjustment(const float *tab, int nzp, const SwTrace &t, int k)
     wL2A = 0.5f * (wLoc2 + tol * wG2A);
     s2L *= wL2A / wLoc2;
   }
-  const float den = wG2A / (tau2 * wGlob2 + s2G);
   const float q = tau2 * wL2A + s2L;
-  return make_float2((wLoc.x / q) / den, (wLoc.y / q) / den);
+  const float f = (tau2 * wGlob2 + s2G) / (wG2A * q);
+  return make_float2(wLoc.x * f, wLoc.y * f);
 }
 
 // the stretched local wavelet spectrum at bin k (getCAmp(k, sf) of the local wavelet)
@@ -230,8 +239,10 @@ __device__ float2 local_wavelet(const float *tab, int nzp, const SwTrace &t, int
   const int omL = (int)floorf(omega);
   const int omU = omL + 1 < cnzp ? omL + 1 : omL;
   const float d = omega - (float)omL, d1 = 1.0f - d;
-  const float2 wa = wl_val(W, omL, phasor_at<SHIFT>(t, omL), t.gain, nzp);
-  const float2 wb = wl_val(W, omU, phasor_at<SHIFT>(t, omU), t.gain, nzp);
+  const float2 pL = phasor_at<SHIFT>(t, omL);
+  const float2 pU = (SHIFT && omU != omL) ? cmulf(pL, t.step) : pL;
+  const float2 wa = wl_val(W, omL, pL, t.gain, nzp);
+  const float2 wb = wl_val(W, omU, pU, t.gain, nzp);
   return make_float2(wa.x * d1 + wb.x * d, wa.y * d1 + wb.y * d);
 }
 
@@ -239,14 +250,14 @@ enum { kSwDivide = 0, kSwMultiply = 1 };
 
 template <int MODE, bool SHIFT>
 __device__ __forceinline__ float2 trace_factor(const float *tab, const SwTrace *tp, const int2 *kb, int l, int x, int j,
-                                               int k, int nx, int ny, int nxp, int nyp, int nzp)
+                                               int k, int nx, int ny, int nxp, int nyp, int nzp, float inv_wn2)
 {
   if (x >= nxp) return make_float2(0.0f, 0.0f);  // slack column of the in-place layout
   const long tix = (long)j * nxp + x;
   if constexpr (MODE == kSwDivide) {
     const int2 b = kb[tix];
     if (k < b.x || k > b.y) return make_float2(0.0f, 0.0f);
-    return adjustment<SHIFT>(tab, nzp, tp[(long)l * nxp * nyp + tix], k);
+    return adjustment<SHIFT>(tab, nzp, tp[(long)l * nxp * nyp + tix], k, inv_wn2);
   } else {
     if (x >= nx || j >= ny) return make_float2(1.0f, 0.0f);
     const float2 v = local_wavelet<SHIFT>(tab, nzp, tp[(long)l * nxp * nyp + tix], k);
@@ -279,8 +290,9 @@ __global__ void __launch_bounds__(256) k_sw_spectral(CubeSet cs, int ncubes, con
     const float2 X = make_float2(0.5f * (z1.x + z2.x), 0.5f * (z1.y - z2.y));
     const float2 Y = make_float2(0.5f * (z1.y + z2.y), -0.5f * (z1.x - z2.x));
     const float *tab = tables + (long)l * tstride;
-    const float2 a0 = trace_factor<MODE, SHIFT>(tab, tp, kb, l, 2 * c, j, k, nx, ny, nxp, nyp, nzp);
-    const float2 a1 = trace_factor<MODE, SHIFT>(tab, tp, kb, l, 2 * c + 1, j, k, nx, ny, nxp, nyp, nzp);
+    const float inv_wn2 = MODE == kSwDivide ? 1.0f / tab[5 * cnzp] : 0.0f;
+    const float2 a0 = trace_factor<MODE, SHIFT>(tab, tp, kb, l, 2 * c, j, k, nx, ny, nxp, nyp, nzp, inv_wn2);
+    const float2 a1 = trace_factor<MODE, SHIFT>(tab, tp, kb, l, 2 * c + 1, j, k, nx, ny, nxp, nyp, nzp, inv_wn2);
     float2 xp = cmulf(X, a0), yp = cmulf(Y, a1);
     xp.x *= scale; xp.y *= scale;
     yp.x *= scale; yp.y *= scale;
@@ -352,27 +364,38 @@ __global__ void k_sw_zero_apply(CubeSet cs, int ncubes, int nxp, int nyp, int nz
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long ntr = (long)nxp * nyp;
-  const long total = ntr * nzp * ncubes;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
-    const long c = idx % ntr;
-    const long r = idx / ntr;
-    const int k = (int)(r % nzp), l = (int)(r / nzp);
-    if (zf[(long)l * ntr + c]) ((float *)cs.ptr[l])[((long)k * nyp + c / nxp) * rnxp + c % nxp] = 0.0f;
+  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < ntr * ncubes; idx += (long)gridDim.x * blockDim.x) {
+    if (!zf[idx]) continue;
+    const int l = (int)(idx / ntr);
+    const long c = idx - (long)l * ntr;
+    float *b = (float *)cs.ptr[l] + (c / nxp) * rnxp + (c % nxp);
+    for (int k = 0; k < nzp; k++) b[(long)k * nyp * rnxp] = 0.0f;
   }
 }
 
 // per-trace energy over the simbox (FFTGrid::interpolateSeismic, src/fftgrid.cpp:2587-2598):
-// sequential float sum, no fused multiply-add
-__global__ void k_trace_energy(const float *__restrict__ buf, float *__restrict__ energy, int nx, int ny, int nz,
-                               int nxp, int nyp)
+// sequential float sum, no fused multiply-add; loads issued eight at a time
+__global__ void k_trace_energy(CubeSet cs, int ncubes, float *__restrict__ energy, int nx, int ny, int nz, int nxp,
+                               int nyp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long n = (long)nx * ny;
-  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(t % nx), j = (int)(t / nx);
+  const long pstride = (long)nyp * rnxp;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < n * ncubes; t += (long)gridDim.x * blockDim.x) {
+    const int l = (int)(t / n);
+    const long tt = t - (long)l * n;
+    const float *b = (const float *)cs.ptr[l] + (tt / nx) * rnxp + (tt % nx);
     float e = 0.0f;
-    for (int k = 0; k < nz; k++) {
-      const float v = buf[((long)k * nyp + j) * rnxp + i];
+    int k = 0;
+    for (; k + 8 <= nz; k += 8) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) v[u] = __ldg(b + (long)(k + u) * pstride);
+#pragma unroll
+      for (int u = 0; u < 8; u++) e = __fadd_rn(e, __fmul_rn(v[u], v[u]));
+    }
+    for (; k < nz; k++) {
+      const float v = __ldg(b + (long)k * pstride);
       e = __fadd_rn(e, __fmul_rn(v, v));
     }
     energy[t] = e;
@@ -380,16 +403,17 @@ __global__ void k_trace_energy(const float *__restrict__ buf, float *__restrict_
 }
 
 // FFTGrid::interpolateTrace (src/fftgrid.cpp:2668-2707) for one level of
-// independent traces: ops[q] = (trace, neighbour mask: 1 left, 2 right, 4 up, 8 down)
-__global__ void k_interp_traces(float *__restrict__ buf, const int2 *__restrict__ ops, int nops, int nx, int nxp,
-                                int nyp, int nzp)
+// independent traces: ops[q] = (cube, trace, neighbour mask: 1 left, 2 right,
+// 4 up, 8 down)
+__global__ void k_interp_traces(CubeSet cs, const int4 *__restrict__ ops, int nops, int nx, int nxp, int nyp, int nzp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long total = (long)nops * nzp;
   for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
     const int q = (int)(idx / nzp), k = (int)(idx % nzp);
-    const int2 op = ops[q];
-    const int i = op.x % nx, j = op.x / nx, m = op.y;
+    const int4 op = ops[q];
+    float *buf = (float *)cs.ptr[op.x];
+    const int i = op.y % nx, j = op.y / nx, m = op.z;
     const long base = (long)k * nyp * rnxp;
     float s = (m & 1) ? buf[base + (long)j * rnxp + i - 1] : 0.0f;
     if (m & 2) s = __fadd_rn(s, buf[base + (long)j * rnxp + i + 1]);
@@ -399,30 +423,55 @@ __global__ void k_interp_traces(float *__restrict__ buf, const int2 *__restrict_
   }
 }
 
-// FFTGrid::extrapolateSeismic (src/fftgrid.cpp:2710-2738): traces outside the box of good traces
-__global__ void k_extrapolate(float *__restrict__ buf, int nx, int ny, int nz, int nxp, int nyp, int nzp, int imin,
-                              int imax, int jmin, int jmax)
+// FFTGrid::extrapolateSeismic (src/fftgrid.cpp:2710-2738): every trace outside
+// the box of good traces (box[l] = imin, imax, jmin, jmax; skipped when
+// empty) becomes its clamped fill-number reference trace times
+// max(1 - dx^2 - dy^2 - dz^2, 0)^3 (double, as the reference); one thread per
+// trace, the z loop inside
+__global__ void k_extrapolate(CubeSet cs, int ncubes, const int4 *__restrict__ box, int nx, int ny, int nz, int nxp,
+                              int nyp, int nzp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
-  const long total = (long)nxp * nyp * nzp;
-  for (long idx = (long)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
-    const int i = (int)(idx % nxp);
-    const long r = idx / nxp;
-    const int j = (int)(r % nyp), k = (int)(r / nyp);
-    if (!(i < imin || i > imax || j < jmin || j > jmax)) continue;
+  const long ntr = (long)nxp * nyp;
+  const long pstride = (long)nyp * rnxp;
+  for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < ntr * ncubes; t += (long)gridDim.x * blockDim.x) {
+    const int l = (int)(t / ntr);
+    const long c = t - (long)l * ntr;
+    const int i = (int)(c % nxp), j = (int)(c / nxp);
+    const int4 bx = box[l];
+    if (bx.x > bx.y || bx.z > bx.w) continue;
+    if (!(i < bx.x || i > bx.y || j < bx.z || j > bx.w)) continue;
     int refj = fill_number(j, ny, nyp);
-    if (refj < jmin) refj = jmin;
-    else if (refj > jmax) refj = jmax;
+    if (refj < bx.z) refj = bx.z;
+    else if (refj > bx.w) refj = bx.w;
     int refi = fill_number(i, nx, nxp);
-    if (refi < imin) refi = imin;
-    else if (refi > imax) refi = imax;
-    const float value = buf[((long)k * nyp + refj) * rnxp + refi];
-    const float dx = dist_to_boundary(i, nx, nxp), dy = dist_to_boundary(j, ny, nyp),
-                dzz = dist_to_boundary(k, nz, nzp);
-    double t = 1.0 - (double)__fmul_rn(dx, dx) - (double)__fmul_rn(dy, dy) - (double)__fmul_rn(dzz, dzz);
-    t = t > 0.0 ? t : 0.0;
-    const float mult = (float)(t * t * t);
-    buf[((long)k * nyp + j) * rnxp + i] = __fmul_rn(mult, value);
+    if (refi < bx.x) refi = bx.x;
+    else if (refi > bx.y) refi = bx.y;
+    float *buf = (float *)cs.ptr[l];
+    const float *src = buf + (long)refj * rnxp + refi;
+    float *dst = buf + (long)j * rnxp + i;
+    const float dx = dist_to_boundary(i, nx, nxp), dy = dist_to_boundary(j, ny, nyp);
+    const double sxy = 1.0 - (double)__fmul_rn(dx, dx) - (double)__fmul_rn(dy, dy);
+    // inside the simbox in z (k < nz) the distance in z is 0: one factor for those cells
+    double w0 = sxy - 0.0;
+    w0 = w0 > 0.0 ? w0 : 0.0;
+    const float m0 = (float)(w0 * w0 * w0);
+    const int kz = nz < nzp ? nz : nzp;
+    int k = 0;
+    for (; k + 8 <= kz; k += 8) {  // eight loads in flight
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; u++) v[u] = src[(long)(k + u) * pstride];
+#pragma unroll
+      for (int u = 0; u < 8; u++) dst[(long)(k + u) * pstride] = __fmul_rn(m0, v[u]);
+    }
+    for (; k < kz; k++) dst[(long)k * pstride] = __fmul_rn(m0, src[(long)k * pstride]);
+    for (k = kz; k < nzp; k++) {
+      const float dzz = dist_to_boundary(k, nz, nzp);
+      double w = sxy - (double)__fmul_rn(dzz, dzz);
+      w = w > 0.0 ? w : 0.0;
+      dst[(long)k * pstride] = __fmul_rn((float)(w * w * w), src[(long)k * pstride]);
+    }
   }
 }
 
@@ -469,9 +518,9 @@ int sw_apply(int mode, float *const *data, int ncubes, int nx, int ny, int nz, i
   SwTrace *tp = nullptr;
   int2 *kb = nullptr;
   unsigned char *zf = nullptr;
-  CG_CUDA(cudaMallocAsync((void **)&tp, sizeof(SwTrace) * ntr * ncubes, st));
-  cudaError_t e = cudaMallocAsync((void **)&kb, sizeof(int2) * ntr, st);
-  if (e == cudaSuccess && mode == kSwDivide) e = cudaMallocAsync((void **)&zf, (size_t)ntr * ncubes, st);
+  CG_CUDA(scratch_alloc((void **)&tp, sizeof(SwTrace) * ntr * ncubes, st));
+  cudaError_t e = scratch_alloc((void **)&kb, sizeof(int2) * ntr, st);
+  if (e == cudaSuccess && mode == kSwDivide) e = scratch_alloc((void **)&zf, (size_t)ntr * ncubes, st);
   if (e != cudaSuccess) {
     cudaFreeAsync(tp, st);
     if (kb) cudaFreeAsync(kb, st);
@@ -515,7 +564,7 @@ int sw_apply(int mode, float *const *data, int ncubes, int nx, int ny, int nz, i
     }
     if ((rc = fft_cols<float>(ptrs, ncubes, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, +1, st))) break;
     if (zf) {
-      k_sw_zero_apply<<<grid_for(ntr * nzp * ncubes), 256, 0, st>>>(cs, ncubes, nxp, nyp, nzp, zf);
+      k_sw_zero_apply<<<grid_for(ntr * ncubes), 256, 0, st>>>(cs, ncubes, nxp, nyp, nzp, zf);
       if ((e = cudaGetLastError()) != cudaSuccess) break;
     }
   } while (false);
@@ -596,55 +645,65 @@ void interp_plan(const std::vector<float> &energy, int nx, int ny, float thr, In
     }
 }
 
-int interpolate_one(float *buf, int nx, int ny, int nz, int nxp, int nyp, int nzp, float thr, int *nbad,
-                    cudaStream_t st)
+// FFTGrid::interpolateSeismic on ncubes cubes: one energy launch, one wait
+// for the energies, host plans, then per level one launch over all cubes and
+// one extrapolation launch
+int interpolate_cubes(float *const *cubes, int ncubes, int nx, int ny, int nz, int nxp, int nyp, int nzp, float thr,
+                      int *nbad, cudaStream_t st)
 {
+  CubeSet cs;
+  for (int i = 0; i < kMaxBatch; i++) cs.ptr[i] = i < ncubes ? cubes[i] : nullptr;
   const long n = (long)nx * ny;
   float *energy_d = nullptr;
-  CG_CUDA(cudaMallocAsync((void **)&energy_d, sizeof(float) * n, st));
-  std::vector<float> energy(n);
+  CG_CUDA(scratch_alloc((void **)&energy_d, sizeof(float) * n * ncubes, st));
+  std::vector<float> energy(n * ncubes);
   cudaError_t e;
   {
-    TraceScope ts("k_trace_energy", st, 4.0 * (double)n * nz);
-    k_trace_energy<<<grid_for(n), 256, 0, st>>>(buf, energy_d, nx, ny, nz, nxp, nyp);
+    TraceScope ts("k_trace_energy", st, 4.0 * (double)n * nz * ncubes);
+    k_trace_energy<<<grid_for(n * ncubes), 256, 0, st>>>(cs, ncubes, energy_d, nx, ny, nz, nxp, nyp);
   }
   e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(energy.data(), energy_d, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(energy.data(), energy_d, sizeof(float) * n * ncubes, cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   cudaFreeAsync(energy_d, st);
   if (e != cudaSuccess) return cuda_status(e, "trace energies");
-  InterpPlan plan;
-  interp_plan(energy, nx, ny, thr, &plan);
-  if (nbad) *nbad = plan.nbad;
-  long nops = 0;
-  for (auto &lv : plan.levels) nops += (long)lv.size();
-  if (nops > 0) {
-    std::vector<int2> ops;
-    ops.reserve(nops);
-    for (auto &lv : plan.levels) ops.insert(ops.end(), lv.begin(), lv.end());
-    int2 *ops_d = nullptr;
-    CG_CUDA(cudaMallocAsync((void **)&ops_d, sizeof(int2) * nops, st));
-    e = cudaMemcpyAsync(ops_d, ops.data(), sizeof(int2) * nops, cudaMemcpyHostToDevice, st);
-    long off = 0;
-    for (size_t l = 0; l < plan.levels.size() && e == cudaSuccess; l++) {
-      const int cnt = (int)plan.levels[l].size();
-      if (cnt == 0) continue;
-      k_interp_traces<<<grid_for((long)cnt * nzp), 256, 0, st>>>(buf, ops_d + off, cnt, nx, nxp, nyp, nzp);
-      e = cudaGetLastError();
-      off += cnt;
-    }
-    cudaFreeAsync(ops_d, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // ops is a pageable host buffer
-    if (e != cudaSuccess) return cuda_status(e, "trace interpolation");
+  // ops grouped by level across cubes, then the boxes: one upload
+  std::vector<std::vector<int4>> by_level;
+  std::vector<int4> boxes(ncubes);
+  for (int l = 0; l < ncubes; l++) {
+    InterpPlan plan;
+    std::vector<float> el(energy.begin() + (long)l * n, energy.begin() + (long)(l + 1) * n);
+    interp_plan(el, nx, ny, thr, &plan);
+    if (nbad) nbad[l] = plan.nbad;
+    boxes[l] = make_int4(plan.imin, plan.imax, plan.jmin, plan.jmax);
+    if (by_level.size() < plan.levels.size()) by_level.resize(plan.levels.size());
+    for (size_t v = 0; v < plan.levels.size(); v++)
+      for (const int2 &op : plan.levels[v]) by_level[v].push_back(make_int4(l, op.x, op.y, 0));
   }
-  // no trace above the limit: the reference's extrapolation would read the
-  // padding it is overwriting; the cube is left as it is
-  if (plan.imin <= plan.imax && plan.jmin <= plan.jmax) {
+  std::vector<int4> upload(boxes);
+  std::vector<long> off;
+  for (auto &lv : by_level) {
+    off.push_back((long)upload.size());
+    upload.insert(upload.end(), lv.begin(), lv.end());
+  }
+  int4 *up_d = nullptr;
+  CG_CUDA(scratch_alloc((void **)&up_d, sizeof(int4) * upload.size(), st));
+  e = cudaMemcpyAsync(up_d, upload.data(), sizeof(int4) * upload.size(), cudaMemcpyHostToDevice, st);
+  for (size_t v = 0; v < by_level.size() && e == cudaSuccess; v++) {
+    const int cnt = (int)by_level[v].size();
+    if (cnt == 0) continue;
+    k_interp_traces<<<grid_for((long)cnt * nzp), 256, 0, st>>>(cs, up_d + off[v], cnt, nx, nxp, nyp, nzp);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) {
     TraceScope ts("k_extrapolate", st, 0.0);
-    k_extrapolate<<<grid_for((long)nxp * nyp * nzp), 256, 0, st>>>(buf, nx, ny, nz, nxp, nyp, nzp, plan.imin,
-                                                                   plan.imax, plan.jmin, plan.jmax);
-    CG_CHECK_LAUNCH("k_extrapolate");
+    k_extrapolate<<<grid_for((long)nxp * nyp * ncubes), 256, 0, st>>>(cs, ncubes, up_d, nx, ny, nz, nxp, nyp, nzp);
+    e = cudaGetLastError();
   }
+  cudaFreeAsync(up_d, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // upload is a pageable host buffer
+  if (e != cudaSuccess) return cuda_status(e, "trace interpolation");
   return CG_OK;
 }
 
@@ -659,11 +718,8 @@ extern "C" int cg_interpolate_seismic(float *data, int nx, int ny, int nz, int n
   int rc = check_sw_dims(1, nx, ny, nxp, nyp, nzp);
   if (rc) return rc;
   if (!data || nz < 1 || nz > nzp) { set_error("cg_interpolate_seismic: bad argument"); return CG_ERR_ARG; }
-  cudaStream_t st = (cudaStream_t)stream;
-  rc = interpolate_one(data, nx, ny, nz, nxp, nyp, nzp, energy_threshold, n_bad, st);
-  if (rc) return rc;
-  CG_CUDA(cudaStreamSynchronize(st));
-  return CG_OK;
+  float *cubes[1] = {data};
+  return interpolate_cubes(cubes, 1, nx, ny, nz, nxp, nyp, nzp, energy_threshold, n_bad, (cudaStream_t)stream);
 }
 
 extern "C" int cg_divide_by_scale_wavelet(float *const *data, int ntheta, int nx, int ny, int nz, int nxp, int nyp,
@@ -676,12 +732,7 @@ extern "C" int cg_divide_by_scale_wavelet(float *const *data, int ntheta, int nx
                     low_cut, high_cut, st);
   if (rc) return rc;
   if (energy_threshold < 0.0f) return CG_OK;  // interpolation left to the caller
-  for (int l = 0; l < ntheta; l++) {
-    if ((rc = interpolate_one(data[l], nx, ny, nz, nxp, nyp, nzp, energy_threshold, n_bad ? n_bad + l : nullptr, st)))
-      return rc;
-  }
-  CG_CUDA(cudaStreamSynchronize(st));
-  return CG_OK;
+  return interpolate_cubes(data, ntheta, nx, ny, nz, nxp, nyp, nzp, energy_threshold, n_bad, st);
 }
 
 extern "C" int cg_multiply_by_scale_wavelet(float *const *data, int ncubes, int nx, int ny, int nxp, int nyp, int nzp,

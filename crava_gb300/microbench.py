@@ -246,9 +246,108 @@ def ingest_case(a):
                                   for k, v in tr.items()}}))
 
 
+def thickness_case(a):
+    """Non-constant simbox thickness on the 256^3 five-stack workload: the scale-wavelet division of the five
+    DATA cubes with dead-trace interpolation (16 dead traces), the whole mixed inversion on that simbox,
+    and the scale-wavelet product of five residual cubes; timed with CUDA events (inputs restored outside
+    the timed region; cubes of 67.6 MB, five of them exceed L2)."""
+    from . import synthetic as S
+    from .pipeline import Inversion
+    sc = S.variable_thickness(S.config1(seed=9), amp=0.3, surfaces=True, dead_traces=16, seed=2)
+    inv = Inversion(sc, forms=("mixed",))
+
+    def timed(fn, reps):
+        ms = []
+        for _ in range(reps):
+            inv.restore("mixed")
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return ms
+
+    def multiply():
+        api.multiply_by_scale_wavelet(inv.data, sc.nx, sc.ny, sc.nxp, inv.sw_tables, inv.rel_thick, sc.dt_ms,
+                                      shift=inv.wshift, gain=inv.wgain)
+    for fn in (inv.scale_data, lambda: inv.run("mixed"), multiply):
+        timed(fn, 2)
+    res = {"divide": timed(inv.scale_data, a.reps), "inversion": timed(lambda: inv.run("mixed"), a.reps),
+           "multiply": timed(multiply, a.reps)}
+    inv.restore("mixed")
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    inv.scale_data()
+    multiply()
+    torch.cuda.synchronize()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    cube_bytes = 4.0 * sc.rnxp * sc.nyp * sc.nzp
+    n = sc.ntheta
+    out = {"case": {"what": "thickness", "workload": "256^3 padded cubes, 5 stacks, relative thickness 1 +- 0.3, "
+                                                     "local wavelet shift/gain surfaces, 16 dead traces"},
+           "ms": res, "n_bad": inv.n_bad,
+           # one read and one write of every cell: the per-trace operation's lower bound
+           "divide_algorithmic_GBps": 2 * n * cube_bytes / (min(res["divide"]) * 1e-3) / 1e9,
+           "multiply_algorithmic_GBps": 2 * n * cube_bytes / (min(res["multiply"]) * 1e-3) / 1e9,
+           "inversion_Mbins_per_s": sc.nbins / (min(res["inversion"]) * 1e-3) / 1e6,
+           "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
+                       for k, v in tr.items()}}
+    print(json.dumps(out))
+
+
+def localnoise_case(a):
+    """Local-noise correction (correctAlphaBetaRho) after a 256^3 five-stack inversion: per-trace matrices for
+    205 x 205 traces (FP64, one eigen-decomposition of a 5x5 and three of 3x3 matrices per trace) and the
+    update of 205^3 cells of the three posterior-mean cubes; timed with CUDA events."""
+    from . import synthetic as S
+    sc = S.config1(seed=9)
+    n = sc.ntheta
+    Sm = sc.sigma0.astype(np.float64)
+    Smd = 0.45 * Sm + 0.05 * np.diag(np.diag(Sm))
+    G = api.local_noise_g(sc.err_theta_cov, Sm, Smd)
+    yy, xx = np.mgrid[0:sc.ny, 0:sc.nx]
+    scale = torch.from_numpy(np.stack([1.0 + 0.5 * (1 + np.sin(xx / 9.0 + l) * np.cos(yy / 7.0))
+                                       for l in range(n)])).cuda()
+    mean = [torch.from_numpy(np.ascontiguousarray(m)).cuda() for m in sc.mean]
+    post0 = [m + 0.01 for m in mean]
+    post = [m.clone() for m in post0]
+    smd = torch.empty((sc.ny, sc.nx, 9), dtype=torch.float64, device="cuda")
+
+    def run():
+        api.correct_alpha_beta_rho(post, mean, sc.nx, sc.ny, sc.nz, sc.nxp, G, sc.err_theta_cov, Sm, Smd, scale, smd)
+    ms = []
+    for r in range(a.reps + 2):
+        for p, q in zip(post, post0):
+            p.copy_(q)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run()
+        e1.record()
+        torch.cuda.synchronize()
+        if r >= 2:
+            ms.append(e0.elapsed_time(e1))
+    _native.trace_enable(True)
+    run()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    cells = sc.nx * sc.ny * sc.nz
+    print(json.dumps({"case": {"what": "localnoise", "workload": "205^3 simbox in 256^3 padded cubes, 5 stacks"},
+                      "ms": ms, "traces": sc.nx * sc.ny,
+                      "update_algorithmic_GBps": 36.0 * cells / (min(ms) * 1e-3) / 1e9,
+                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
+                                  for k, v in tr.items()}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse", "ingest"])
+    ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse", "ingest",
+                                     "thickness", "localnoise"])
     ap.add_argument("--nreal", type=int, default=128)
     ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
@@ -272,6 +371,12 @@ def main():
         return
     if a.what == "ingest":
         ingest_case(a)
+        return
+    if a.what == "thickness":
+        thickness_case(a)
+        return
+    if a.what == "localnoise":
+        localnoise_case(a)
         return
     if a.what == "batch":
         # graph replays: time the whole batch with CUDA events

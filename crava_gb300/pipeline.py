@@ -23,6 +23,13 @@ place).  ``run(form)`` executes one inversion:
   transforms around the stand-alone fused bin kernel (and the FP64 fix-up
   pass);
 * ``"fp64"`` -- the fused form entirely in FP64 (accuracy reference).
+
+On a simbox of non-constant thickness (``sc.rel_thick`` set) every run starts
+with the per-trace scale-wavelet division of the data and the dead-trace
+interpolation (Crava::divideDataByScaleWavelet, src/crava.cpp:174-175; FP32
+in every form), the operator tables take the non-constant-thickness branch
+of fillErrMultVectors, and ``outputs`` multiplies the residuals back by the
+scale wavelet (multiplyDataByScaleWaveletAndWriteToFile, src/crava.cpp:231-232).
 """
 from __future__ import annotations
 
@@ -41,8 +48,21 @@ class Inversion:
         self.forms = set(forms)
         self.dev = torch.device(device)
         nxp, nyp, nzp, n = sc.nxp, sc.nyp, sc.nzp, sc.ntheta
-        self.tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
-                                          sc.min_rel_thick)
+        self.thick = sc.rel_thick is not None
+        if self.thick:
+            self.tables = api.operator_tables_nct(sc.wavelets, sc.A, sc.nz, nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
+                                                  sc.min_rel_thick)
+            swt = api.scale_wavelet_tables(sc.wavelets, sc.A, sc.sigma0, sc.circ_corr_t, sc.err_theta_cov, sc.nz,
+                                           sc.dt_ms, sc.nz * sc.dt_ms, sc.low_cut, sc.high_cut, sc.wnc)
+            dev32 = lambda a: None if a is None else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(self.dev)  # noqa: E731
+            self.sw_tables = dev32(swt)
+            self.rel_thick = dev32(sc.rel_thick)
+            self.wshift = dev32(sc.wavelet_shift)
+            self.wgain = dev32(sc.wavelet_gain)
+            self.n_bad = None
+        else:
+            self.tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
+                                              sc.min_rel_thick)
         self.ws = api.Workspace(nxp, nyp, nzp, n)
         self.ws.set_model(self.tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=cond_threshold)
         f32 = dict(dtype=torch.float32, device=self.dev)
@@ -78,6 +98,9 @@ class Inversion:
                 d.copy_(self.data_in[l])
             for p, m in enumerate(self.mean64):
                 m.copy_(self.mean_in[p])
+            if self.thick:   # the FP32 data scaling feeds the FP64 cubes
+                for l, d in enumerate(self.data):
+                    d.copy_(self.data_in[l])
             return
         for l, d in enumerate(self.data):
             d.copy_(self.data_in[l])
@@ -89,9 +112,22 @@ class Inversion:
             self.errcorr.copy_(self.err_in)
 
     # -- one inversion -----------------------------------------------------
+    def scale_data(self, stream=None):
+        """Crava::divideDataByScaleWavelet + interpolateSeismic on the FP32 working data cubes."""
+        sc = self.sc
+        self.n_bad = api.divide_by_scale_wavelet(self.data, sc.nx, sc.ny, sc.nz, sc.nxp, self.sw_tables,
+                                                 self.rel_thick, sc.dt_ms, sc.nz * sc.dt_ms, sc.low_cut,
+                                                 sc.high_cut, sc.energy_threshold, shift=self.wshift,
+                                                 gain=self.wgain, stream=stream)
+
     def run(self, form, stream=None):
         sc = self.sc
         nxp = sc.nxp
+        if self.thick:
+            self.scale_data(stream)
+            if form == "fp64":
+                for l, d in enumerate(self.data64):
+                    d.copy_(self.data[l])
         if form == "plain":
             api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, stream=stream)
@@ -138,10 +174,31 @@ class Inversion:
         api.fft_in_place_batch(cov, nxp, api.COVARIANCE, inverse=True, stream=stream)
         post_var0, post_cov00 = api.cov_origin(cov, nxp, sc.nz, stream=stream)
         api.fft_in_place_batch(data, nxp, api.DATA, inverse=True, stream=stream)
+        if self.thick:
+            api.multiply_by_scale_wavelet(data, sc.nx, sc.ny, nxp, self.sw_tables, self.rel_thick, sc.dt_ms,
+                                          shift=self.wshift, gain=self.wgain, stream=stream)
         elastic = [m.clone() for m in self.mean]
         for e in elastic:
             api.exp_transform(e, stream=stream)
         return post_var0, post_cov00, elastic
+
+    # -- local noise -------------------------------------------------------
+    def correct_local_noise(self, form, noise_scale: torch.Tensor, post_var0, G=None, stream=None):
+        """Crava::correctAlphaBetaRho (src/crava.cpp:266-282, 2471-2569) on the posterior means of ``form``
+        (real domain, after ``run``): noise_scale (ntheta, ny, nx) float64 device tensor of local noise
+        scales, post_var0 the 3x3 posterior variance at the origin (``outputs``).  G defaults to
+        ``api.local_noise_g``.  Returns the per-trace matrices sigmamd (ny, nx, 9) for simulation."""
+        sc = self.sc
+        if form == "fp64":
+            raise ValueError("the local-noise correction works on the FP32 forms")
+        s0 = np.asarray(sc.sigma0, dtype=np.float64)
+        if G is None:
+            G = api.local_noise_g(sc.err_theta_cov, s0, post_var0)
+        mean0 = [self.mean_in[p] for p in range(3)]
+        sigmamd = torch.empty((sc.ny, sc.nx, 9), dtype=torch.float64, device=self.dev)
+        api.correct_alpha_beta_rho(self.mean, mean0, sc.nx, sc.ny, sc.nz, sc.nxp, G, sc.err_theta_cov, s0, post_var0,
+                                   noise_scale, sigmamd, stream=stream)
+        return sigmamd
 
     # -- results -----------------------------------------------------------
     def results(self, form):

@@ -125,6 +125,15 @@ def genexp_corr_xy(nxp, nyp, dx, dy, range_m, power=1.0) -> np.ndarray:
     return np.exp(-3.0 * d ** power).astype(np.float32)
 
 
+def corr2d_positive_definite(cxy: np.ndarray) -> np.ndarray:
+    """ModelGeneral::makeCorr2DPositiveDefinite (src/modelgeneral.cpp:5132-5170): the lateral correlation with
+    its 2D spectrum replaced by the spectrum's modulus, rescaled to keep the value at lag 0."""
+    c = np.asarray(cxy, dtype=np.float64)
+    spec = np.abs(np.fft.rfft2(c))
+    r = np.fft.irfft2(spec, s=c.shape)
+    return (r * (c[0, 0] / r[0, 0])).astype(np.float32)
+
+
 def genexp_corr_t(n, dt_ms, range_ms, power):
     lag = np.arange(n + 1) * dt_ms
     return np.exp(-3.0 * (lag / range_ms) ** power).astype(np.float32)
@@ -194,6 +203,11 @@ class Scenario:
     min_rel_thick: float = 1.0
     sn: list = field(default_factory=list)
     truth: list | None = None     # 3 x (nzp, nyp, nxp) float64 (log domain)
+    # non-constant simbox thickness (None: constant thickness)
+    rel_thick: np.ndarray | None = None       # (nyp, nxp) float32, Simbox::getRelThick per padded trace
+    wavelet_shift: np.ndarray | None = None   # (n, ny, nx) float32 ms, local wavelet time shift
+    wavelet_gain: np.ndarray | None = None    # (n, ny, nx) float32, local wavelet gain
+    energy_threshold: float = 0.0             # FFTGrid::interpolateSeismic
 
     @property
     def ntheta(self):
@@ -210,6 +224,29 @@ class Scenario:
     @property
     def nbins(self):
         return self.cnxp * self.nyp * self.nzp
+
+
+def variable_thickness(sc: Scenario, amp=0.3, surfaces=True, dead_traces=0, seed=7) -> Scenario:
+    """A copy of ``sc`` on a simbox whose relative thickness varies laterally (1 +- amp, smooth), with
+    optional local wavelet shift (+-4 ms) and gain (0.85..1.2) surfaces and ``dead_traces`` all-zero
+    traces in every angle cube (interpolateSeismic input)."""
+    from dataclasses import replace
+    rng = np.random.default_rng(seed)
+    yy, xx = np.mgrid[0:sc.nyp, 0:sc.nxp]
+    rt = (1.0 + amp * np.sin(2 * np.pi * xx / max(sc.nx, 2) + 0.4) * np.cos(2 * np.pi * yy / max(sc.ny, 2))
+          ).astype(np.float32)
+    shift = gain = None
+    if surfaces:
+        shift = rng.uniform(-4.0, 4.0, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
+        gain = rng.uniform(0.85, 1.2, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
+    data = [d.copy() for d in sc.data]
+    if dead_traces:
+        idx = rng.choice(sc.nx * sc.ny, dead_traces, replace=False)
+        for d in data:
+            for t in idx:
+                d[:, t // sc.nx, t % sc.nx] = 0.0
+    return replace(sc, data=data, rel_thick=rt, wavelet_shift=shift, wavelet_gain=gain,
+                   min_rel_thick=float(rt[:sc.ny, :sc.nx].min()))
 
 
 def _pad_x(cube, nxp):
@@ -260,7 +297,7 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
                   dx=25.0, dy=25.0, sn=4.0, stds=(0.10, 0.07, 0.05), corr=(0.7, 0.3, 0.3),
                   lateral_range=1000.0, temporal_range_ms=20.0, temporal_power=1.5, low_cut=5.0,
                   high_cut=55.0, wnc=0.1, notches_hz=(), std_scale=1.0, seed=20261203,
-                  keep_truth=False) -> Scenario:
+                  keep_truth=False, pd_corr_xy=False) -> Scenario:
     """Build one seeded scenario.  Sizes are log-domain (ln Vp, ln Vs, ln rho)."""
     rng = np.random.default_rng(seed)
     nxp = nxp or padded_size(nx, pad)
@@ -271,6 +308,8 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     wav = np.stack([ricker_fft_order(nzp, dt_ms, f_peak, notches_hz=notches_hz) for _ in range(n)])
     wav = wav.astype(np.float32)
     cxy = genexp_corr_xy(nxp, nyp, dx, dy, lateral_range)
+    if pd_corr_xy:
+        cxy = corr2d_positive_definite(cxy)
     n_corr_t = max(nz, 2)
     corr_t = genexp_corr_t(n_corr_t, dt_ms, temporal_range_ms, temporal_power)
     min_int_fq = int(math.floor(low_cut * (nzp * 0.001 * dt_ms)))

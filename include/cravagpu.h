@@ -247,6 +247,37 @@ int cg_interpolate_seismic(float *data, int nx, int ny, int nz, int nxp, int nyp
                            int *n_bad, void *stream);
 
 /* ========================================================================
+ * Local noise (the error variance scales laterally, per angle).
+ * ======================================================================== */
+
+/* Crava::correctAlphaBetaRho (src/crava.cpp:2471-2569) with
+ * newPosteriorCovPointwise (:2345-2451): every simbox cell of the 3 real padded
+ * posterior-mean cubes post (device, in place) becomes mean + sigmanew (post -
+ * mean), mean the 3 prior-mean cubes; sigmanew per trace = Delta^1/2
+ * (Sm - Spost)^-1/2 with Delta = Sm G^T (G Sm G^T + D Se D)^+ G Sm, D =
+ * diag(sqrt(scale_l / min scale_l)).  HOST inputs: G [ntheta][3] from
+ * Crava::computeG (:2261-2343; its eigenvector signs are the caller's LAPACK
+ * choice and the result depends on them), err_theta_cov [ntheta][ntheta],
+ * prior_var0 and post_var0 [3][3] (Crava::priorVar0_, postVar0_).  Device:
+ * noise_scale [ntheta][ny][nx] doubles (the local noise scale grids; each is
+ * divided by its minimum over values other than RMISSING; a trace whose scale
+ * is RMISSING counts as the minimum, where the reference computes NaN); sigmamd (may be
+ * NULL) [ny][nx][9] doubles receives Crava::sigmamdnew_ (sqrt of the local
+ * posterior covariance times postVar0^-1/2) for simulation. */
+int cg_correct_alpha_beta_rho(float *const *post, const float *const *mean, int nx, int ny, int nz, int nxp, int nyp,
+                              int nzp, int ntheta, const double *G, const double *err_theta_cov,
+                              const double *prior_var0, const double *post_var0, const double *noise_scale,
+                              double *sigmamd, void *stream);
+
+/* The local-noise step of Crava::simulate (src/crava.cpp:1686-1704) on 3 real
+ * padded simulated fields (device, in place): simbox cells x -> M x with the
+ * trace's matrix M (mats [ny][nx][9] doubles, from cg_correct_alpha_beta_rho's
+ * sigmamd), then, when mean is not NULL, every cell plus the posterior mean
+ * (FFTGrid::add). */
+int cg_apply_trace_matrices(float *const *fields, const float *const *mean, const double *mats, int nx, int ny,
+                            int nz, int nxp, int nyp, int nzp, void *stream);
+
+/* ========================================================================
  * File formats either side of the path (host memory, synchronous)
  * ======================================================================== */
 

@@ -122,6 +122,11 @@ def lib():
         L.or_rnorm01.argtypes = [ct.POINTER(ct.c_uint)]
         L.or_rnorm01.restype = ct.c_double
         L.or_find_closest_factorable.argtypes = [ct.c_int]
+        PD = ct.POINTER(ct.c_double)
+        L.or_new_posterior_cov_pointwise.argtypes = [ct.c_int, PD, PD, PD, PD, PD, PD, PD]
+        L.or_correct_alpha_beta_rho.argtypes = [ct.POINTER(ct.POINTER(ct.c_float)), ct.POINTER(ct.POINTER(ct.c_float)),
+                                                ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, PD, PD, PD,
+                                                PD, PD, PD]
         L.or_find_closest_factorable.restype = ct.c_int
         _lib = L
     return _lib
@@ -447,6 +452,42 @@ def interpolate_seismic(buf, nx, ny, nz, nxp, energy_threshold=0.0, prec="f"):
     out = np.array(buf, dtype=_rdt(prec), order="C")
     n = getattr(lib(), "or_interpolate_seismic_" + prec)(_ptr(out, R), nx, ny, nz, nxp, nyp, nzp, energy_threshold)
     return out, n
+
+
+def _dp(a):
+    return None if a is None else a.ctypes.data_as(ct.POINTER(ct.c_double))
+
+
+def new_posterior_cov_pointwise(G, err_theta_cov, prior_var0, post_var0, scales):
+    """Crava::newPosteriorCovPointwise for one trace: (sigmanew, sigmamdnew), 3x3 each."""
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    n = G.shape[0]
+    e = np.ascontiguousarray(err_theta_cov, dtype=np.float64)
+    sm = np.ascontiguousarray(prior_var0, dtype=np.float64)
+    smd = np.ascontiguousarray(post_var0, dtype=np.float64)
+    sc = np.ascontiguousarray(scales, dtype=np.float64)
+    out1 = np.zeros((3, 3))
+    out2 = np.zeros((3, 3))
+    lib().or_new_posterior_cov_pointwise(n, _dp(G), _dp(e), _dp(sm), _dp(smd), _dp(sc), _dp(out1), _dp(out2))
+    return out1, out2
+
+
+def correct_alpha_beta_rho(post, mean, nx, ny, nz, nxp, G, err_theta_cov, prior_var0, post_var0, noise_scale,
+                           want_sigmamd=False):
+    """Crava::correctAlphaBetaRho on copies of 3 real padded posterior-mean cubes; returns (cubes, sigmamd)."""
+    P = [np.array(c, dtype=np.float32, order="C") for c in post]
+    M = [np.ascontiguousarray(c, dtype=np.float32) for c in mean]
+    nzp, nyp, _ = P[0].shape
+    G = np.ascontiguousarray(G, dtype=np.float64)
+    n = G.shape[0]
+    PF = ct.POINTER(ct.c_float)
+    pp = (PF * 3)(*[c.ctypes.data_as(PF) for c in P])
+    mp = (PF * 3)(*[c.ctypes.data_as(PF) for c in M])
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (err_theta_cov, prior_var0, post_var0, noise_scale)]
+    smd = np.zeros((ny, nx, 9)) if want_sigmamd else None
+    lib().or_correct_alpha_beta_rho(pp, mp, nx, ny, nz, nxp, nyp, n, _dp(G), _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]),
+                                    _dp(arrs[3]), _dp(smd))
+    return P, smd
 
 
 def circ_corr_t(priorCorrT, minIntFq, nzp, prec="f"):
