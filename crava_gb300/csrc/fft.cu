@@ -512,8 +512,19 @@ int fft_cols(void *const *bufs, int count, int n, int ncols, long axis_stride, l
   return launch_cols<T>(cs, count, n, ncols, axis_stride, batch_stride, nbatch, sign, st);
 }
 
+// the x pass alone (R2C forward with prescale, C2R inverse with postscale) over count cubes
+template <typename T>
+int fft_x_pass(void *const *bufs, int count, int nxp, int nyp, int nzp, bool forward, T scale, cudaStream_t st)
+{
+  if (!bufs || count < 1 || count > kMaxBatch) { set_error("fft_x_pass: bad argument"); return CG_ERR_ARG; }
+  CubeSet cs, ad;
+  for (int i = 0; i < kMaxBatch; i++) { cs.ptr[i] = i < count ? bufs[i] : nullptr; ad.ptr[i] = nullptr; }
+  return launch_rows<T>(forward, cs, ad, count, nxp, nyp, nzp, scale, st);
+}
+
 template int fft3d<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
 template int fft3d_xz<float>(void *const *, int, int, int, int, int, bool, cudaStream_t);
+template int fft_x_pass<float>(void *const *, int, int, int, int, bool, float, cudaStream_t);
 template int fft_cols<float>(void *const *, int, int, int, long, long, int, int, cudaStream_t);
 template int fft_rows<float>(void *, int, int, bool, float, cudaStream_t);
 template int fft3d<double>(void *const *, int, int, int, int, int, bool, cudaStream_t);

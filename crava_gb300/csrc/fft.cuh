@@ -48,6 +48,9 @@ int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp,
 // 1D real transforms of rows (see fft.cu)
 template <typename T>
 int fft_rows(void *buf, int nx, int nrows, bool forward, T scale, cudaStream_t st);
+// the x pass alone over given cube pointers (see fft.cu)
+template <typename T>
+int fft_x_pass(void *const *bufs, int count, int nxp, int nyp, int nzp, bool forward, T scale, cudaStream_t st);
 // one column pass over given cube pointers (see fft.cu)
 template <typename T>
 int fft_cols(void *const *bufs, int count, int n, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,

@@ -46,6 +46,10 @@ static int chunked_y(cg_workspace w, float *const *data, float *const *mean, flo
   return fft3d_xz<float>((void *const *)mean, 3, nxp, nyp, nzp, CG_PARAMETER, false, st);
 }
 
+bool ysplit_fits(const Workspace *w);
+int invert_cubes_ysplit(Workspace *w, float *const *data, float *const *mean, float *const *cov, int precision,
+                        cudaStream_t st, cudaEvent_t bins_done);
+
 }  // namespace cg
 
 using namespace cg;
@@ -65,7 +69,8 @@ int cg::invert_cubes_fused(cg_workspace w, float *const *data, float *const *mea
   for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } fwd[nt + p] = mean[p]; }
   for (int t = 0; t < 6; t++) if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; }
   const int zc = cg_tune_get(CG_TUNE_FUSED_Y, nyp);
-  if (zc >= 2 && nt + 3 <= kMaxBatch) return chunked_y(w, data, mean, cov, precision, zc, st, bins_done);
+  if (zc == 2 && ysplit_fits(w)) return invert_cubes_ysplit(w, data, mean, cov, precision, st, bins_done);
+  if (zc >= 4 && nt + 3 <= kMaxBatch) return chunked_y(w, data, mean, cov, precision, zc, st, bins_done);
   if (!ybin_length(nyp)) {
     // no fused kernel for this y length: three-pass transforms around the bin kernel
     if ((rc = fft3d<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;

@@ -37,12 +37,13 @@ struct YBinArgs {
   int mixed;
 };
 
-// FP64 redo of one bin (rare: kept out of line so it costs the FP32 path no registers)
+// FP64 redo of one bin (rare: kept out of line so it costs the FP32 path no
+// registers); sig0d: the 6 entries of Sigma0 in bin-loop order
 template <int NT>
-__device__ __noinline__ int bin_fp64(const YBinArgs &a, int k, float sf, float lamf, float2 *d, float2 *mu,
-                                     float2 *cov)
+__device__ __noinline__ int bin_fp64_t(const KTab<double> *__restrict__ ktd, const double *sig0d, int k, float sf,
+                                       float lamf, float2 *d, float2 *mu, float2 *cov)
 {
-  const KTab<double> &kt = a.ktab_d[k];
+  const KTab<double> &kt = ktd[k];
   const double s = sf, lam = lamf;
   double2 dd[NT], md[3], cd[6], L[NT * (NT + 1) / 2];
 #pragma unroll
@@ -53,10 +54,10 @@ __device__ __noinline__ int bin_fp64(const YBinArgs &a, int k, float sf, float l
   double cond, invr[NT];
   if (!chol_std<double, NT>(L, invr, cond)) {
 #pragma unroll
-    for (int t = 0; t < 6; t++) cov[t] = make_float2((float)(s * a.sig0d[t]), 0.0f);
+    for (int t = 0; t < 6; t++) cov[t] = make_float2((float)(s * sig0d[t]), 0.0f);
     return 0;
   }
-  posterior_from_chol<double, NT>(kt, a.sig0d, s, lam, L, invr, dd, md, cd, true);
+  posterior_from_chol<double, NT>(kt, sig0d, s, lam, L, invr, dd, md, cd, true);
 #pragma unroll
   for (int l = 0; l < NT; l++) d[l] = make_float2((float)dd[l].x, (float)dd[l].y);
 #pragma unroll
@@ -64,6 +65,16 @@ __device__ __noinline__ int bin_fp64(const YBinArgs &a, int k, float sf, float l
 #pragma unroll
   for (int t = 0; t < 6; t++) cov[t] = make_float2((float)cd[t].x, (float)cd[t].y);
   return 1;
+}
+
+template <int NT>
+__device__ __forceinline__ int bin_fp64(const YBinArgs &a, int k, float sf, float lamf, float2 *d, float2 *mu,
+                                        float2 *cov)
+{
+  double s0[6];
+#pragma unroll
+  for (int t = 0; t < 6; t++) s0[t] = a.sig0d[t];
+  return bin_fp64_t<NT>(a.ktab_d, s0, k, sf, lamf, d, mu, cov);
 }
 
 template <int N, int NT, int MINB>

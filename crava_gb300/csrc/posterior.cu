@@ -681,6 +681,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
         if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
+        else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 1, 5><<<grid, threads, 0, st>>>(a);
+        else if (bin_minb(NT) == 4) k_invert_fused<T, NT, 1, 4><<<grid, threads, 0, st>>>(a);
         else k_invert_fused<T, NT, 1, 1><<<grid, threads, 0, st>>>(a);
       }
       CG_CHECK_LAUNCH("k_invert_fused");
@@ -694,7 +696,10 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
     } else {
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
-      if (bin_minb(NT) == 6) k_invert_fused<T, NT, 0, 6><<<grid, threads, 0, st>>>(a);
+      // the FP32 mode spills more than MIXED under the 85-register cap (228 B against 128 B at five
+      // stacks; 0.47 against 0.39 ms at 256^3): its tight setting is the 128-register build
+      if (bin_minb(NT) == 6 || bin_minb(NT) == 4) k_invert_fused<T, NT, 0, 4><<<grid, threads, 0, st>>>(a);
+      else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 0, 5><<<grid, threads, 0, st>>>(a);
       else k_invert_fused<T, NT, 0, 1><<<grid, threads, 0, st>>>(a);
     }
     CG_CHECK_LAUNCH("k_invert_fused");

@@ -68,14 +68,17 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
  * direct and four-step kernels), per axis length n), CG_TUNE_COLS_PIPE
  * (column-pass kernel per n: 0 shared-memory staged, 1 persistent
  * double-buffered, 2 first and last stages in registers, 3 four-step),
- * CG_TUNE_BIN_MINB (fused bin kernel register cap: 1 = none, 6 = 85
- * registers, per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per
+ * CG_TUNE_BIN_MINB (fused bin kernel: resident 128-thread CTAs the build
+ * targets, 4, 5 or 6 (128, 96 or 85 registers), 1 = no target; the FP32
+ * mode takes 4 where 6 is set; per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per
  * half length n = nxp/2, or n = nxp for odd nxp: 0 shared-memory staged or
  * generic, 1 four-step),
  * CG_TUNE_FUSED_Y (cg_invert_cubes_fused per y length n: 0 three-pass
- * transforms around the bin kernel, 1 y pass fused with the bin loop, an even
- * c >= 2: forward y pass, bins and inverse y pass run per chunk of c z-planes
- * so that the chunk's spectra stay in L2).  n = 0 sets the value for every n.  Built-in defaults were
+ * transforms around the bin kernel, 1 y pass fused with the bin loop, 2 the
+ * y transform of the means split in two 16-point stages, the first in the x
+ * row kernels, the second in the bin kernel (nxp = nyp = 256), an even c >= 4:
+ * forward y pass, bins and inverse y pass run per chunk of c z-planes so that
+ * the chunk's spectra stay in L2).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0

@@ -140,7 +140,7 @@ def test_fused_y_kernel_matches_fp64_oracle(cuda, oracle, dims, cond):
 # short last chunk and, at cond = 1.0001, a FP64 fix-up queue that grows over the chunks
 @pytest.mark.parametrize("dims,chunk,cond,form", [((64, 128, 48), 16, 0.0, "fp32"), ((40, 200, 36), 16, 0.0, "mixed"),
                                                   ((48, 256, 24), 10, 1.0001, "mixed"),
-                                                  ((30, 120, 20), 2, 1.0001, "mixed"),
+                                                  ((30, 120, 20), 4, 1.0001, "mixed"),
                                                   ((64, 128, 48), 64, 0.0, "mixed")])
 def test_chunked_y_pipeline_matches_fp64_oracle(cuda, oracle, dims, chunk, cond, form):
     from crava_gb300 import synthetic as S
@@ -174,3 +174,35 @@ def test_chunked_y_pipeline_matches_fp64_oracle(cuda, oracle, dims, chunk, cond,
         csize = sc.cnxp * sc.nyp * sc.nzp
         if min(csize, max(1 << 16, csize // 8)) == csize:   # the workspace's queue holds every bin
             assert st["overflow"] == 0
+
+
+# the split y transform of the means (CG_TUNE_FUSED_Y = 2, nxp = nyp = 256): x + y stage 1 in the row
+# kernels, y stage 2 in the bin kernel; in-band and out-of-band planes, in-kernel FP64 bins at cond 1.0001
+@pytest.mark.parametrize("nzp,cond,form", [(24, 0.0, "mixed"), (20, 0.0, "fp32"), (16, 1.0001, "mixed")])
+def test_split_y_pipeline_matches_fp64_oracle(cuda, oracle, nzp, cond, form):
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    from crava_gb300 import _native
+    sc = S.scaled_config1(256, 256, nzp, seed=nzp + 7)
+    inv = Inversion(sc, forms=(form,), cond_threshold=cond)
+    inv.restore(form)
+    inv.ws.reset_stats()
+    L = _native.lib()
+    assert L.cg_tune_set(4, 256, 2) == 0
+    try:
+        inv.run(form)
+        torch.cuda.synchronize()
+    finally:
+        L.cg_tune_clear()
+        _native._apply_tuning(L)
+    st = inv.ws.stats()
+    pm, res, cov = inv.results(form)
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    e = (rel(pm, post64), rel(pm - prior, post64 - prior), rel(res, res64), rel(cov, cov64))
+    print(nzp, cond, form, "split y vs FP64 oracle (mean, update, resid, cov):", e, st)
+    assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
+    band = inv.tables["band"].astype(bool)
+    assert band.any() and not band.all()
+    if cond > 0:
+        assert st["flagged"] > int(band.sum()) * sc.cnxp * sc.nyp // 2

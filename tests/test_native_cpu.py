@@ -85,5 +85,7 @@ def test_tuning_table_defaults_overrides_and_validation(native):
     # fused-form y handling: 0 three passes, 1 fused y kernel, an even z-chunk size >= 2 the chunked pipeline
     assert native.cg_tune_get(4, 256) == 0 and native.cg_tune_set(4, 256, 16) == 0 and native.cg_tune_get(4, 256) == 16
     assert native.cg_tune_set(4, 256, 15) == -1 and native.cg_tune_set(4, 256, 8192) == -1
+    assert native.cg_tune_set(4, 256, 2) == 0 and native.cg_tune_set(4, 256, 3) == -1   # 2: split y of the means
+    assert native.cg_tune_set(2, 5, 5) == 0 and native.cg_tune_set(2, 5, 3) == -1       # bin kernel caps 1, 4-6
     native.cg_tune_clear()
     assert native.cg_tune_get(0, 256) == 3
