@@ -407,6 +407,97 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(CubeSet cs, c
 }
 
 // ---------------------------------------------------------------------------
+// register-direct column pass on persistent CTAs that keep the next tile's
+// loads in flight: CTA b transforms tiles b, b + G, ... of the tile list of
+// k_fft_cols_pipe; before transforming tile i it issues the global loads of
+// tile i + G into a second register set, so the loads of one tile overlap the
+// arithmetic and stores of the previous one.
+// ---------------------------------------------------------------------------
+template <int N, int W, int MINB>
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rdp(CubeSet cs, const float2 *__restrict__ twg,
+                                                                    ColsGeom g, int ntiles, int sign)
+{
+  static_assert(plan_nstages(N) >= 2, "register-direct pass needs two stages or more");
+  constexpr int NST = plan_nstages(N);
+  constexpr int R0 = plan_radix(N, 0);
+  constexpr int NB0 = N / R0;
+  constexpr int TOT0 = NB0 * W;
+  constexpr int BPT0 = (TOT0 + kFFTThreads - 1) / kFFTThreads;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *buf = (float2 *)smem_raw;
+  float2 *tw = buf + N * W;
+  const long as = g.axis_stride;
+  for (int t = threadIdx.x; t < N; t += kFFTThreads) tw[t] = twg[t];
+  auto load0 = [&](const TileRef &ref, float2 (*v)[R0]) {
+#pragma unroll
+    for (int q = 0; q < BPT0; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      const int j = t / W, c = t % W;
+      const bool ok = (TOT0 % kFFTThreads == 0 || t < TOT0) && c < ref.cvalid;
+#pragma unroll
+      for (int r = 0; r < R0; r++) v[q][r] = ok ? ref.base[(long)(j + r * NB0) * as + (long)c * ref.cstride] : make_float2(0.f, 0.f);
+    }
+  };
+  int tile = blockIdx.x;
+  float2 vn[BPT0][R0];
+  if (tile < ntiles) load0(cols_tile<W>(cs, g, tile), vn);
+  __syncthreads();  // twiddles staged
+  for (; tile < ntiles; tile += gridDim.x) {
+    float2 v[BPT0][R0];
+#pragma unroll
+    for (int q = 0; q < BPT0; q++)
+#pragma unroll
+      for (int r = 0; r < R0; r++) v[q][r] = vn[q][r];
+    const TileRef ref = cols_tile<W>(cs, g, tile);
+    const int next = tile + gridDim.x;
+    if (next < ntiles) load0(cols_tile<W>(cs, g, next), vn);  // consumed in the next iteration
+    // first stage: registers -> shared
+#pragma unroll
+    for (int q = 0; q < BPT0; q++) {
+      const int t = q * kFFTThreads + threadIdx.x;
+      if (TOT0 % kFFTThreads == 0 || t < TOT0) {
+        const int j = t / W, c = t % W;
+        dft_any<float, R0>(v[q], sign, tw, NB0);
+#pragma unroll
+        for (int r = 0; r < R0; r++) buf[(j * R0 + r) * W + c] = v[q][r];
+      }
+    }
+    __syncthreads();
+    cstages_range<float, N, W, W, 1, 1, R0, NST - 1>(buf, tw, sign);
+    // last stage: shared -> registers -> global
+    {
+      constexpr int S = NST - 1;
+      constexpr int R = plan_radix(N, S);
+      constexpr int NS = plan_ns_before(N, S);
+      constexpr int NB = N / R;
+      constexpr int SPAN = N / (NS * R);
+      constexpr int TOT = NB * W;
+      constexpr int BPT = (TOT + kFFTThreads - 1) / kFFTThreads;
+#pragma unroll
+      for (int q = 0; q < BPT; q++) {
+        const int t = q * kFFTThreads + threadIdx.x;
+        if (TOT % kFFTThreads == 0 || t < TOT) {
+          const int j = t / W, c = t % W;
+          float2 u[R];
+#pragma unroll
+          for (int r = 0; r < R; r++) u[r] = buf[(j + r * NB) * W + c];
+          const int jm = j % NS;
+#pragma unroll
+          for (int r = 1; r < R; r++) u[r] = cmul<float>(u[r], tw_at<float>(tw, jm * r * SPAN, sign));
+          dft_any<float, R>(u, sign, tw, NB);
+          const int d = (j - jm) * R + jm;
+          if (c < ref.cvalid) {
+#pragma unroll
+            for (int r = 0; r < R; r++) ref.base[(long)(d + r * NS) * as + (long)c * ref.cstride] = u[r];
+          }
+        }
+      }
+    }
+    __syncthreads();  // buf is rewritten by the next tile's first stage
+  }
+}
+
+// ---------------------------------------------------------------------------
 // x rows, real -> half spectrum (even nxp = 2M), prescale applied to X
 // ---------------------------------------------------------------------------
 template <int M>

@@ -106,11 +106,54 @@ int launch_rd(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long b
   return 1;
 }
 
+// register-direct on persistent CTAs with the next tile's loads in flight (tuning value 4)
+template <int N, int MINB>
+int launch_rdp(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+               const float2 *tw, cudaStream_t st)
+{
+  const size_t smem = ((size_t)N * kW + N) * sizeof(float2);
+  static bool attr_set[64] = {};
+  static int slots[64] = {};
+  cudaError_t e = smem_limit_once(k_fft_cols_rdp<N, kW, MINB>, smem, attr_set);
+  if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_rdp attribute");
+  int dev = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+  int &nslots = slots[dev < 64 ? dev : 0];
+  if (nslots == 0) {
+    int per_sm = 0, nsm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fft_cols_rdp<N, kW, MINB>, kFFTThreads, smem)) !=
+        cudaSuccess)
+      return cuda_status(e, "occupancy");
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return cuda_status(e, "SM count");
+    nslots = (per_sm > 0 ? per_sm : 1) * nsm;
+  }
+  ColsGeom g;
+  g.axis_stride = axis_stride;
+  g.batch_stride = batch_stride;
+  g.nfull = ncols / kW;
+  g.ntail = ncols - g.nfull * kW;
+  g.nbatch = nbatch;
+  g.trows = 1;
+  const long groups = ceil_div(nbatch, kW);
+  const long ntiles = (long)ncubes * ((long)nbatch * g.nfull + (long)g.ntail * groups);
+  if (ntiles > 0x7fffffffL) { set_error("too many column tiles"); return CG_ERR_UNSUPPORTED; }
+  const int grid = (int)(ntiles < nslots ? ntiles : nslots);
+  TraceScope ts("k_fft_cols_rdp", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
+  k_fft_cols_rdp<N, kW, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, (int)ntiles, sign);
+  CG_CHECK_LAUNCH("k_fft_cols_rdp");
+  return 1;
+}
+
 template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
   const int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
+  if (kind == 4) {
+    if (minb_for(N) == 3) return launch_rdp<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    return launch_rdp<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  }
   if (kind == 3) return four_step_cols(minb_for(N), cs, ncubes, N, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
   if (kind == 2) {
     if constexpr (N <= 256)

@@ -297,6 +297,161 @@ __global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a)
   for (int t = 0; t < 6; t++) a.cov[t][b] = cov[t];
 }
 
+// Information-form bin solve (FP32; MODE 0 FP32, 1 MIXED with the FP64 queue
+// of k_invert_fixup64, which redoes a queued bin with the Cholesky of Sd).
+// Per in-band bin: w_m = 1/(lam mu_m + 1), Q = Sigma0^-1/s + sum w_m P_m,
+// S+ = Q^-1 from the 3x3 Cholesky of Q (its squared pivot ratio is the
+// condition estimate), r = d - K mu, b = sum_m G_m w_m (v_m^H r),
+// mu+ = mu + S+ b, residual = d - K mu+.  s = 0 keeps the prior (S+ = 0).
+struct InfoArgs {
+  float s0i[6];  // Sigma0^-1, bin order 00 11 22 01 02 12
+};
+
+template <int NT, int MODE, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab,
+                                                           InfoArgs ia)
+{
+  __shared__ ITab it;
+  const int k = a.k0 + blockIdx.y;
+  {
+    const int *src = (const int *)&itab[k];
+    int *dst = (int *)&it;
+    for (int t = threadIdx.x; t < (int)(sizeof(ITab) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+  const int ij = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ij >= a.plane) return;
+  const long b = (long)k * a.plane + ij;
+  float s, lam;
+  bin_scales<float>(a, ij, k, s, lam);
+  if (!it.band) {
+    write_prior_cov<float>(a, b, s);
+    return;
+  }
+  float2 d[NT], mu[3];
+#pragma unroll
+  for (int l = 0; l < NT; l++) d[l] = a.data[l][b];
+#pragma unroll
+  for (int p = 0; p < 3; p++) mu[p] = a.mean[p][b];
+  float2 S01, S02, S12;
+  float S00, S11, S22;
+  if (s > 0.0f) {
+    const float is = 1.0f / s;
+    float w[NT];
+#pragma unroll
+    for (int m = 0; m < NT; m++) w[m] = 1.0f / (lam * it.mu[m] + 1.0f);
+    float q00 = ia.s0i[0] * is, q11 = ia.s0i[1] * is, q22 = ia.s0i[2] * is;
+    float2 q01 = make_float2(ia.s0i[3] * is, 0.0f), q02 = make_float2(ia.s0i[4] * is, 0.0f),
+           q12 = make_float2(ia.s0i[5] * is, 0.0f);
+#pragma unroll
+    for (int m = 0; m < NT; m++) {
+      const float *P = it.P[m];
+      q00 += w[m] * P[0];
+      q11 += w[m] * P[1];
+      q22 += w[m] * P[2];
+      q01.x += w[m] * P[3]; q01.y += w[m] * P[4];
+      q02.x += w[m] * P[5]; q02.y += w[m] * P[6];
+      q12.x += w[m] * P[7]; q12.y += w[m] * P[8];
+    }
+    // Q = L L^H, L lower: L10 = conj(q01)/L00, L20 = conj(q02)/L00, L21 = (conj(q12) - L20 conj(L10))/L11
+    bool ok = q00 > 0.0f;
+    const float r0 = rsqrtf(q00), l00 = q00 * r0;
+    const float2 l10 = make_float2(q01.x * r0, -q01.y * r0), l20 = make_float2(q02.x * r0, -q02.y * r0);
+    const float p1 = q11 - (l10.x * l10.x + l10.y * l10.y);
+    ok = ok && p1 > 0.0f;
+    const float r1 = rsqrtf(p1), l11 = p1 * r1;
+    const float2 t21 = csub<float>(make_float2(q12.x, -q12.y), cmulc<float>(l20, l10));
+    const float2 l21 = make_float2(t21.x * r1, t21.y * r1);
+    const float p2 = q22 - (l20.x * l20.x + l20.y * l20.y) - (l21.x * l21.x + l21.y * l21.y);
+    ok = ok && p2 > 0.0f;
+    const float r2 = rsqrtf(p2), l22 = p2 * r2;
+    const float dmax = fmaxf(l00, fmaxf(l11, l22)), dmin = fminf(l00, fminf(l11, l22));
+    const float cond = (dmax / dmin) * (dmax / dmin);
+    if (MODE == 1) {
+      const bool flag = !ok || cond > a.cond_thr;
+      const unsigned msk = __ballot_sync(__activemask(), flag);
+      if (flag) {
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(msk) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(&a.counters[0], __popc(msk));
+        base = __shfl_sync(msk, base, leader);
+        const int pos = base + __popc(msk & ((1u << lane) - 1u));
+        if (pos < a.queue_cap) {
+          a.queue[pos] = (int)b;
+          return;  // the FP64 pass writes this bin
+        }
+        atomicAdd(&a.counters[2], 1);  // queue full: keep the FP32 answer
+      }
+    }
+    if (!ok) {
+      atomicAdd(&a.counters[1], 1);
+      write_prior_cov<float>(a, b, s);
+      return;
+    }
+    // M = L^-1 (lower), S+ = M^H M
+    const float m00 = r0, m11 = r1, m22 = r2;
+    const float2 m10 = make_float2(-l10.x * m00 * m11, -l10.y * m00 * m11);
+    const float2 m21 = make_float2(-l21.x * m11 * m22, -l21.y * m11 * m22);
+    const float2 t20 = cadd<float>(make_float2(l20.x * m00, l20.y * m00), cmul<float>(l21, m10));
+    const float2 m20 = make_float2(-t20.x * m22, -t20.y * m22);
+    S00 = m00 * m00 + (m10.x * m10.x + m10.y * m10.y) + (m20.x * m20.x + m20.y * m20.y);
+    S11 = m11 * m11 + (m21.x * m21.x + m21.y * m21.y);
+    S22 = m22 * m22;
+    // S01 = conj(m10) m11 + conj(m20) m21, S02 = conj(m20) m22, S12 = conj(m21) m22
+    S01 = cadd<float>(make_float2(m10.x * m11, -m10.y * m11), cmulc<float>(m21, m20));
+    S02 = make_float2(m20.x * m22, -m20.y * m22);
+    S12 = make_float2(m21.x * m22, -m21.y * m22);
+    // r = d - K mu, b = sum_m G_m w_m (v_m^H r), mu+ = mu + S+ b
+    float2 r[NT];
+#pragma unroll
+    for (int l = 0; l < NT; l++) {
+      float2 km = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int p = 0; p < 3; p++) km = cadd<float>(km, cmul<float>(it.K[l][p], mu[p]));
+      r[l] = csub<float>(d[l], km);
+    }
+    float2 bb[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+#pragma unroll
+    for (int m = 0; m < NT; m++) {
+      float2 h = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int l = 0; l < NT; l++) h = cadd<float>(h, cmulc<float>(r[l], it.V[l][m]));  // conj(v) r
+      h = make_float2(h.x * w[m], h.y * w[m]);
+#pragma unroll
+      for (int p = 0; p < 3; p++) bb[p] = cadd<float>(bb[p], cmul<float>(it.G[m][p], h));
+    }
+    // S+ rows: (S00, S01, S02), (conj S01, S11, S12), (conj S02, conj S12, S22)
+    const float2 u0 = cadd<float>(cadd<float>(make_float2(S00 * bb[0].x, S00 * bb[0].y), cmul<float>(S01, bb[1])),
+                                  cmul<float>(S02, bb[2]));
+    const float2 u1 = cadd<float>(cadd<float>(cmulc<float>(bb[0], S01), make_float2(S11 * bb[1].x, S11 * bb[1].y)),
+                                  cmul<float>(S12, bb[2]));
+    const float2 u2 = cadd<float>(cadd<float>(cmulc<float>(bb[0], S02), cmulc<float>(bb[1], S12)),
+                                  make_float2(S22 * bb[2].x, S22 * bb[2].y));
+    mu[0] = cadd<float>(mu[0], u0);
+    mu[1] = cadd<float>(mu[1], u1);
+    mu[2] = cadd<float>(mu[2], u2);
+  } else {
+    S00 = S11 = S22 = 0.0f;
+    S01 = S02 = S12 = make_float2(0.f, 0.f);
+  }
+#pragma unroll
+  for (int l = 0; l < NT; l++) {
+    float2 km = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int p = 0; p < 3; p++) km = cadd<float>(km, cmul<float>(it.K[l][p], mu[p]));
+    a.data[l][b] = csub<float>(d[l], km);
+  }
+#pragma unroll
+  for (int p = 0; p < 3; p++) a.mean[p][b] = mu[p];
+  a.cov[0][b] = make_float2(S00, 0.f);
+  a.cov[1][b] = make_float2(S11, 0.f);
+  a.cov[2][b] = make_float2(S22, 0.f);
+  a.cov[3][b] = S01;
+  a.cov[4][b] = S02;
+  a.cov[5][b] = S12;
+}
+
 struct S0Args {
   double v[9];
 };
@@ -397,6 +552,98 @@ __global__ void k_prep_tables(int nzp, int nt, const float2 *K, const float2 *em
   tf[k] = f;
 }
 
+// Hermitian eigen-decomposition of an n x n matrix (row-major, destroyed):
+// cyclic Jacobi, each rotation the real one on |a_pq| after the phase
+// diag(1, e^-i arg a_pq) on (p, q); eigenvalues Re a_ii, eigenvectors the
+// columns of v.
+__device__ void herm_jacobi(double2 *a, double2 *v, int n)
+{
+  for (int i = 0; i < n * n; i++) v[i] = make_double2(i % (n + 1) == 0 ? 1.0 : 0.0, 0.0);
+  for (int sweep = 0; sweep < 50; sweep++) {
+    double off = 0.0, diag = 0.0;
+    for (int p = 0; p < n; p++) {
+      diag += a[p * n + p].x * a[p * n + p].x;
+      for (int q = p + 1; q < n; q++) off += a[p * n + q].x * a[p * n + q].x + a[p * n + q].y * a[p * n + q].y;
+    }
+    if (off <= 1e-30 * diag || off == 0.0) break;
+    for (int p = 0; p < n - 1; p++)
+      for (int q = p + 1; q < n; q++) {
+        const double2 apq = a[p * n + q];
+        const double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
+        if (mag == 0.0) continue;
+        const double2 e = make_double2(apq.x / mag, -apq.y / mag);  // e^{-i arg a_pq}
+        const double2 ec = make_double2(e.x, -e.y);
+        const double th = (a[q * n + q].x - a[p * n + p].x) / (2.0 * mag);
+        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < n; k++) {
+          const double2 akp = a[k * n + p], akq = cmul<double>(e, a[k * n + q]);
+          a[k * n + p] = make_double2(c * akp.x - sn * akq.x, c * akp.y - sn * akq.y);
+          a[k * n + q] = make_double2(sn * akp.x + c * akq.x, sn * akp.y + c * akq.y);
+        }
+        for (int k = 0; k < n; k++) {
+          const double2 apk = a[p * n + k], aqk = cmul<double>(ec, a[q * n + k]);
+          a[p * n + k] = make_double2(c * apk.x - sn * aqk.x, c * apk.y - sn * aqk.y);
+          a[q * n + k] = make_double2(sn * apk.x + c * aqk.x, sn * apk.y + c * aqk.y);
+        }
+        for (int k = 0; k < n; k++) {
+          const double2 vkp = v[k * n + p], vkq = cmul<double>(e, v[k * n + q]);
+          v[k * n + p] = make_double2(c * vkp.x - sn * vkq.x, c * vkp.y - sn * vkq.y);
+          v[k * n + q] = make_double2(sn * vkp.x + c * vkq.x, sn * vkp.y + c * vkq.y);
+        }
+      }
+  }
+}
+
+// information-form tables of plane k from the FP64 tables; *bad counts
+// in-band planes with a diagonal error term that is not positive
+__global__ void k_prep_info(int nzp, int nt, const KTab<double> *__restrict__ td, ITab *ti, int *bad)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nzp) return;
+  const KTab<double> &t = td[k];
+  ITab o;
+  memset(&o, 0, sizeof(o));
+  o.band = t.band;
+  for (int l = 0; l < nt; l++)
+    for (int p = 0; p < 3; p++) o.K[l][p] = make_float2((float)t.K[l][p].x, (float)t.K[l][p].y);
+  bool ok = true;
+  for (int l = 0; l < nt; l++) ok = ok && t.D[l] > 0.0;
+  if (!ok) {
+    if (t.band) atomicAdd(bad, 1);
+    ti[k] = o;
+    return;
+  }
+  double2 a[kMaxTheta * kMaxTheta], v[kMaxTheta * kMaxTheta];
+  double dm[kMaxTheta];
+  for (int l = 0; l < nt; l++) dm[l] = 1.0 / sqrt(t.D[l]);
+  for (int l = 0; l < nt; l++)
+    for (int m = 0; m < nt; m++) {
+      const double2 e = l >= m ? t.E[tri(l, m)] : make_double2(t.E[tri(m, l)].x, -t.E[tri(m, l)].y);
+      a[l * nt + m] = make_double2(dm[l] * e.x * dm[m], dm[l] * e.y * dm[m]);
+    }
+  herm_jacobi(a, v, nt);
+  for (int m = 0; m < nt; m++) {
+    o.mu[m] = (float)(a[m * nt + m].x > 0.0 ? a[m * nt + m].x : 0.0);
+    double2 g[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
+    for (int l = 0; l < nt; l++) {
+      const double2 vl = make_double2(dm[l] * v[l * nt + m].x, dm[l] * v[l * nt + m].y);
+      o.V[l][m] = make_float2((float)vl.x, (float)vl.y);
+      for (int p = 0; p < 3; p++) g[p] = cadd<double>(g[p], cmul<double>(make_double2(t.K[l][p].x, -t.K[l][p].y), vl));
+    }
+    for (int p = 0; p < 3; p++) o.G[m][p] = make_float2((float)g[p].x, (float)g[p].y);
+    // g g^H: entry (p, q) = g_p conj(g_q)
+    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
+    for (int p = 0; p < 3; p++) o.P[m][p] = (float)(g[p].x * g[p].x + g[p].y * g[p].y);
+    for (int j = 0; j < 3; j++) {
+      const double2 x = cmulc<double>(g[pq[j][0]], g[pq[j][1]]);
+      o.P[m][3 + 2 * j] = (float)x.x;
+      o.P[m][4 + 2 * j] = (float)x.y;
+    }
+  }
+  ti[k] = o;
+}
+
 __global__ void k_f2d(const float *in, double *out, long n)
 {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -452,6 +699,7 @@ extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp,
   WS_ALLOC(w->ct_d, sizeof(double) * 2 * (size_t)cnzp);
   WS_ALLOC(w->queue, sizeof(int) * (size_t)w->queue_cap);
   WS_ALLOC(w->counters, sizeof(int) * 4);
+  WS_ALLOC(w->itab, sizeof(ITab) * nzp);
 #undef WS_ALLOC
   if (e == cudaSuccess) e = cudaMemset(w->counters, 0, sizeof(int) * 4);
   if (e != cudaSuccess) {
@@ -466,7 +714,7 @@ extern "C" void cg_workspace_destroy(cg_workspace w)
 {
   if (!w) return;
   void *ptrs[] = {w->ktab_f, w->ktab_d, w->K, w->em1, w->em2, w->em3, w->band, w->etc,
-                  w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters};
+                  w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters, w->itab};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
@@ -500,6 +748,27 @@ extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
   k_prep_tables<<<ceil_div(nzp, 64), 64>>>(nzp, nt, w->K, w->em1, w->em2, w->em3, w->band, w->etc, s0, w->wnc,
                                            w->ktab_f, w->ktab_d);
   CG_CHECK_LAUNCH("k_prep_tables");
+  // information-form tables (3D model, every in-band D > 0); bad counts planes without them
+  w->info_ok = false;
+  if (!w->is4d) {
+    CG_CUDA(cudaMemset(w->counters + 3, 0, sizeof(int)));
+    k_prep_info<<<ceil_div(nzp, 64), 64>>>(nzp, nt, w->ktab_d, w->itab, w->counters + 3);
+    CG_CHECK_LAUNCH("k_prep_info");
+    int bad = 1;
+    CG_CUDA(cudaMemcpy(&bad, w->counters + 3, sizeof(int), cudaMemcpyDeviceToHost));
+    // Sigma0^-1 (the float prior the tables use) by cofactors in double
+    const double *a = s0.v;
+    const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
+                       a[2] * (a[3] * a[7] - a[4] * a[6]);
+    if (bad == 0 && det > 0.0) {
+      const double i00 = (a[4] * a[8] - a[5] * a[7]) / det, i11 = (a[0] * a[8] - a[2] * a[6]) / det;
+      const double i22 = (a[0] * a[4] - a[1] * a[3]) / det, i01 = -(a[1] * a[8] - a[2] * a[7]) / det;
+      const double i02 = (a[1] * a[5] - a[2] * a[4]) / det, i12 = -(a[0] * a[5] - a[2] * a[3]) / det;
+      const double inv6[6] = {i00, i11, i22, i01, i02, i12};
+      for (int q = 0; q < 6; q++) w->sig0inv[q] = (float)inv6[q];
+      w->info_ok = true;
+    }
+  }
   CG_CUDA(cudaDeviceSynchronize());
   w->model_set = true;
   return CG_OK;
@@ -649,6 +918,20 @@ template int fill_fused_args<float>(Workspace *, void *const *, void *const *, v
 template int fill_fused_args<double>(Workspace *, void *const *, void *const *, void *const *, FusedArgs<double> *);
 }  // namespace cg
 
+// the information form (CG_TUNE_BIN_FORM 1) when the model has its tables
+static bool use_info(const Workspace *w, int nt) { return w->info_ok && cg_tune_get(CG_TUNE_BIN_FORM, nt) == 1; }
+
+template <int NT, int MODE>
+static void launch_info(const FusedArgs<float> &a, const Workspace *w, dim3 grid, int threads, cudaStream_t st)
+{
+  InfoArgs ia;
+  for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
+  const int mb = cg_tune_get(CG_TUNE_BIN_MINB, NT);
+  if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia);
+  else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia);
+  else k_invert_info<NT, MODE, 4><<<grid, threads, 0, st>>>(a, w->itab, ia);
+}
+
 template <typename T>
 static int fused_launch(Workspace *w, void *const *data, void *const *mean, void *const *cov, int precision,
                         cudaStream_t st, int k0 = 0, int nk = -1, bool chunked = false)
@@ -678,7 +961,10 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       cudaError_t me = chunked ? cudaMemcpyAsync(w->counters + 3, w->counters, sizeof(int), cudaMemcpyDeviceToDevice, st)
                                : cudaMemsetAsync(w->counters, 0, sizeof(int), st);
       if (me != cudaSuccess) return cuda_status(me, "queue reset");
-      {
+      if (use_info(w, NT)) {
+        TraceScope ts("k_invert_info_mixed", st, fbytes);
+        launch_info<NT, 1>(a, w, grid, threads, st);
+      } else {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
         if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
         else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 1, 5><<<grid, threads, 0, st>>>(a);
@@ -694,6 +980,9 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
       TraceScope ts("k_invert_fixup64", st, 0.0);
       k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
+    } else if (use_info(w, NT)) {
+      TraceScope ts("k_invert_info_fp32", st, fbytes);
+      launch_info<NT, 0>(a, w, grid, threads, st);
     } else {
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
       // the FP32 mode spills more than MIXED under the 85-register cap (228 B against 128 B at five

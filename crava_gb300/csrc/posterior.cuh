@@ -33,6 +33,21 @@ struct KTab {
   int pad_[3];
 };
 
+// Per-k tables of the information form of the fused bin solve (FP32).  With
+// D^-1/2 E D^-1/2 = U diag(mu) U^H and v_m = D^-1/2 u_m, g_m = K^H v_m:
+//   (lam E + D)^-1 = sum_m v_m v_m^H / (lam mu_m + 1),
+//   S+ = (Sigma0^-1 / s + sum_m g_m g_m^H / (lam mu_m + 1))^-1,
+//   mu+ = mu + S+ sum_m g_m (v_m^H (d - K mu)) / (lam mu_m + 1).
+struct ITab {
+  float2 K[kMaxTheta][3];
+  float2 V[kMaxTheta][kMaxTheta];  // V[l][m]: component l of v_m
+  float2 G[kMaxTheta][3];          // G[m][p] = (K^H v_m)[p]
+  float P[kMaxTheta][9];           // g_m g_m^H: 00 11 22, then 01 02 12 as (re, im)
+  float mu[kMaxTheta];
+  int band;
+  int pad_[3];
+};
+
 // Opaque workspace behind cg_workspace (device buffers of one model).
 struct Workspace {
   int device;
@@ -59,6 +74,10 @@ struct Workspace {
   int queue_cap;
   int *counters;    // [0] flagged, [1] failed cholesky, [2] queue overflow
   long inband_bins;  // bins whose k is inside the inversion band
+  // information-form tables (valid when every in-band D > 0 and the model is 3D)
+  ITab *itab;
+  bool info_ok;
+  float sig0inv[6];  // Sigma0^-1 in bin order 00 11 22 01 02 12
   bool model_set;
 };
 

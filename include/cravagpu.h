@@ -78,7 +78,11 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
  * y transform of the means split in two 16-point stages, the first in the x
  * row kernels, the second in the bin kernel (nxp = nyp = 256), an even c >= 4:
  * forward y pass, bins and inverse y pass run per chunk of c z-planes so that
- * the chunk's spectra stay in L2).  n = 0 sets the value for every n.  Built-in defaults were
+ * the chunk's spectra stay in L2), CG_TUNE_BIN_FORM (fused bin solve per
+ * stack count n: 0 Cholesky of the n x n data covariance, 1 information form:
+ * a 3 x 3 Cholesky per bin from per-k eigen-decompositions of the error
+ * covariance, for models whose every in-band error diagonal is positive;
+ * the default).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0
@@ -86,6 +90,7 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
 #define CG_TUNE_BIN_MINB 2
 #define CG_TUNE_ROWS_KERNEL 3
 #define CG_TUNE_FUSED_Y 4
+#define CG_TUNE_BIN_FORM 5
 int cg_tune_set(int key, int n, int value);
 int cg_tune_get(int key, int n);
 int cg_tune_clear(void);

@@ -154,7 +154,7 @@ def _variant_case(oracle, nxp, nyp, nzp):
     return _VARIANT_REFS[key]
 
 
-@pytest.mark.parametrize("pipe", [0, 1, 2, 3])
+@pytest.mark.parametrize("pipe", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("minb", [2, 3, 4])
 def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
     from crava_gb300 import api
