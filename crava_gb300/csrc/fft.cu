@@ -112,7 +112,7 @@ __host__ __device__ inline size_t c2r_bufb_elems(int m, int cnxp)
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kFFTThreads) k_fft_cols(CubeSet cs, AxisPlan p, const C2<T> *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads) k_fft_cols(const __grid_constant__ CubeSet cs, const __grid_constant__ AxisPlan p, const C2<T> *__restrict__ twg,
                                                           int col0, int ncols, int wfull, int ntiles,
                                                           long axis_stride, long batch_stride, int sign)
 {
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_fft_cols(CubeSet cs, AxisPlan p
 
 // x rows, real -> half spectrum, prescale fused into the load.
 template <typename T>
-__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p, const C2<T> *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(const __grid_constant__ CubeSet cs, const __grid_constant__ AxisPlan p, const C2<T> *__restrict__ twg,
                                                           int nxp, int nrows, T prescale)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows(CubeSet cs, AxisPlan p
 
 // x rows, half spectrum -> real, postscale fused into the store.
 template <typename T>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(CubeSet cs, CubeSet addend, AxisPlan p,
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows(const __grid_constant__ CubeSet cs, const __grid_constant__ CubeSet addend, const __grid_constant__ AxisPlan p,
                                                           const C2<T> *__restrict__ twg, int nxp, int nrows,
                                                           T postscale, int epi)
 {

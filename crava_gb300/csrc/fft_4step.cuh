@@ -93,7 +93,7 @@ __host__ __device__ constexpr int fs_cols_w(int n)
 // Shared layout: buf[(k1*N2 + n2)*W + c] (conflict-free for both passes).
 // ---------------------------------------------------------------------------
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(CubeSet cs, const float2 *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                    ColsGeom g, int sign)
 {
   constexpr int N1 = fs_n1(N), N2 = N / N1;
@@ -195,7 +195,7 @@ __host__ __device__ constexpr int fs_row_pitch(int m)
 // partners and is paired with N1/2 when N1 is even, alone when N1 is odd.
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg, int nrows,
                                                              float prescale)
 {
   constexpr int N1 = fs_n1_rows(M), N2 = M / N1, NI = fs_r2c_items(M);
@@ -295,7 +295,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(CubeSet cs, const f
 // used before the exchange; pass 2 stores z[n] = (x[2n], x[2n+1]).
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(CubeSet cs, CubeSet addend,
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_constant__ CubeSet cs, const __grid_constant__ CubeSet addend,
                                                              const float2 *__restrict__ twg, int nrows,
                                                              float postscale, int epi)
 {
@@ -409,7 +409,7 @@ __host__ __device__ constexpr int fs_odd_row_pitch(int nx)
 }
 
 template <int NX>
-__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_odd(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_odd(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg, int nrows,
                                                               float prescale)
 {
   constexpr int N1 = fs_n1(NX), N2 = NX / N1, CN = (NX + 1) / 2, RN = NX + 1;
@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_odd(CubeSet cs, const 
 }
 
 template <int NX>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_odd(CubeSet cs, CubeSet addend,
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_odd(const __grid_constant__ CubeSet cs, const __grid_constant__ CubeSet addend,
                                                               const float2 *__restrict__ twg, int nrows,
                                                               float postscale, int epi)
 {

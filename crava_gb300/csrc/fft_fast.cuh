@@ -124,7 +124,7 @@ struct ColsGeom {
 };
 
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(CubeSet cs, const float2 *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_fast(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                      ColsGeom g, int sign)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -227,7 +227,7 @@ __device__ __forceinline__ void cols_prefetch(float2 *buf, const TileRef &ref, l
 }
 
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_pipe(CubeSet cs, const float2 *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_pipe(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                      ColsGeom g, int ntiles, int sign)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -318,7 +318,7 @@ __host__ __device__ constexpr int plan_ns_before(int n, int stage)
 }
 
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(CubeSet cs, const float2 *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                    ColsGeom g, int sign)
 {
   static_assert(plan_nstages(N) >= 2, "register-direct pass needs two stages or more");
@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(CubeSet cs, c
 // arithmetic and stores of the previous one.
 // ---------------------------------------------------------------------------
 template <int N, int W, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rdp(CubeSet cs, const float2 *__restrict__ twg,
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rdp(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                     ColsGeom g, int ntiles, int sign)
 {
   static_assert(plan_nstages(N) >= 2, "register-direct pass needs two stages or more");
@@ -501,7 +501,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rdp(CubeSet cs, 
 // x rows, real -> half spectrum (even nxp = 2M), prescale applied to X
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_fast(CubeSet cs, const float2 *__restrict__ twg, int nrows,
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_fast(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg, int nrows,
                                                                float prescale)
 {
   constexpr int LDW = kRows + 1;
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_fast(CubeSet cs, const
 // x rows, half spectrum -> real (even nxp = 2M), postscale and optional add
 // ---------------------------------------------------------------------------
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(CubeSet cs, CubeSet addend,
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(const __grid_constant__ CubeSet cs, const __grid_constant__ CubeSet addend,
                                                                const float2 *__restrict__ twg, int nrows,
                                                                float postscale, int epi)
 {

@@ -78,7 +78,7 @@ __device__ __forceinline__ int bin_fp64(const YBinArgs &a, int k, float sf, floa
 }
 
 template <int N, int NT, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_ybin(YBinArgs a)
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_ybin(const __grid_constant__ YBinArgs a)
 {
   constexpr int W = kYW;
   constexpr int N1 = fs_n1(N), N2 = N / N1;

@@ -40,7 +40,7 @@ struct IngestArgs {
   float dz_data, smooth_length;
 };
 
-__global__ void k_trace_prep(IngestArgs a)
+__global__ void k_trace_prep(const __grid_constant__ IngestArgs a)
 {
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.ncol) return;
@@ -105,7 +105,7 @@ __device__ __forceinline__ float fine_at(const float *f, float dl, int nf)
   return w1 * f[l1] + w2 * f[l2];
 }
 
-__global__ void k_trace_to_grid(IngestArgs a)
+__global__ void k_trace_to_grid(const __grid_constant__ IngestArgs a)
 {
   const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.ncol) return;

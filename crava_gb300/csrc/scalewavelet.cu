@@ -267,7 +267,7 @@ __device__ __forceinline__ float2 trace_factor(const float *tab, const SwTrace *
 
 // One thread per (cube, bin pair k / nzp - k, y, x pair).
 template <int MODE, bool SHIFT>
-__global__ void __launch_bounds__(256) k_sw_spectral(CubeSet cs, int ncubes, const float *__restrict__ tables,
+__global__ void __launch_bounds__(256) k_sw_spectral(const __grid_constant__ CubeSet cs, int ncubes, const float *__restrict__ tables,
                                                      int tstride, const SwTrace *__restrict__ tp,
                                                      const int2 *__restrict__ kb, int nx, int ny, int nxp, int nyp,
                                                      int nzp, float scale)
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256) k_sw_spectral(CubeSet cs, int ncubes, con
 
 // planes k >= k0: taper max(1 - dist^2, 0) (divideDataByScaleWavelet, src/crava.cpp:737-741)
 // and zero slack columns; planes k < k0: slack columns only
-__global__ void k_sw_taper(CubeSet cs, int ncubes, int k0, int nz, int nxp, int nyp, int nzp)
+__global__ void k_sw_taper(const __grid_constant__ CubeSet cs, int ncubes, int k0, int nz, int nxp, int nyp, int nzp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long rows = (long)(nzp - k0) * nyp;
@@ -329,7 +329,7 @@ __global__ void k_sw_taper(CubeSet cs, int ncubes, int k0, int nz, int nxp, int 
   }
 }
 
-__global__ void k_sw_slack(CubeSet cs, int ncubes, int nplanes, int nxp, int nyp)
+__global__ void k_sw_slack(const __grid_constant__ CubeSet cs, int ncubes, int nplanes, int nxp, int nyp)
 {
   const int rnxp = 2 * (nxp / 2 + 1), ns = rnxp - nxp;
   const long rows = (long)nplanes * nyp;
@@ -346,7 +346,7 @@ __global__ void k_sw_slack(CubeSet cs, int ncubes, int nplanes, int nxp, int nyp
 // traces whose padded input is exactly zero: the reference's transforms keep
 // them exactly zero, which the paired transform (rounding from the partner
 // trace) would not; the energy test of interpolateSeismic depends on it
-__global__ void k_sw_zero_flags(CubeSet cs, int ncubes, int nxp, int nyp, int nzp, unsigned char *__restrict__ zf)
+__global__ void k_sw_zero_flags(const __grid_constant__ CubeSet cs, int ncubes, int nxp, int nyp, int nzp, unsigned char *__restrict__ zf)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long ntr = (long)nxp * nyp;
@@ -360,7 +360,7 @@ __global__ void k_sw_zero_flags(CubeSet cs, int ncubes, int nxp, int nyp, int nz
   }
 }
 
-__global__ void k_sw_zero_apply(CubeSet cs, int ncubes, int nxp, int nyp, int nzp, const unsigned char *__restrict__ zf)
+__global__ void k_sw_zero_apply(const __grid_constant__ CubeSet cs, int ncubes, int nxp, int nyp, int nzp, const unsigned char *__restrict__ zf)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long ntr = (long)nxp * nyp;
@@ -375,7 +375,7 @@ __global__ void k_sw_zero_apply(CubeSet cs, int ncubes, int nxp, int nyp, int nz
 
 // per-trace energy over the simbox (FFTGrid::interpolateSeismic, src/fftgrid.cpp:2587-2598):
 // sequential float sum, no fused multiply-add; loads issued eight at a time
-__global__ void k_trace_energy(CubeSet cs, int ncubes, float *__restrict__ energy, int nx, int ny, int nz, int nxp,
+__global__ void k_trace_energy(const __grid_constant__ CubeSet cs, int ncubes, float *__restrict__ energy, int nx, int ny, int nz, int nxp,
                                int nyp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
@@ -405,7 +405,7 @@ __global__ void k_trace_energy(CubeSet cs, int ncubes, float *__restrict__ energ
 // FFTGrid::interpolateTrace (src/fftgrid.cpp:2668-2707) for one level of
 // independent traces: ops[q] = (cube, trace, neighbour mask: 1 left, 2 right,
 // 4 up, 8 down)
-__global__ void k_interp_traces(CubeSet cs, const int4 *__restrict__ ops, int nops, int nx, int nxp, int nyp, int nzp)
+__global__ void k_interp_traces(const __grid_constant__ CubeSet cs, const int4 *__restrict__ ops, int nops, int nx, int nxp, int nyp, int nzp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);
   const long total = (long)nops * nzp;
@@ -428,7 +428,7 @@ __global__ void k_interp_traces(CubeSet cs, const int4 *__restrict__ ops, int no
 // empty) becomes its clamped fill-number reference trace times
 // max(1 - dx^2 - dy^2 - dz^2, 0)^3 (double, as the reference); one thread per
 // trace, the z loop inside
-__global__ void k_extrapolate(CubeSet cs, int ncubes, const int4 *__restrict__ box, int nx, int ny, int nz, int nxp,
+__global__ void k_extrapolate(const __grid_constant__ CubeSet cs, int ncubes, const int4 *__restrict__ box, int nx, int ny, int nz, int nxp,
                               int nyp, int nzp)
 {
   const int rnxp = 2 * (nxp / 2 + 1);

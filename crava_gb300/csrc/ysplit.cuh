@@ -28,7 +28,7 @@ constexpr int kYsNY = 256, kYsN1 = 16, kYsN2 = 16;  // y length and its four-ste
 // x R2C of the 32 rows {16 n1 + n2 : n2 = 2 blockIdx.x + g, g = 0, 1} of
 // z-plane blockIdx.y, then stage 1 of the y transform of those rows
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_r2c_ys(CubeSet cs, const float2 *__restrict__ twg, float prescale)
+__global__ void __launch_bounds__(kFFTThreads) k_r2c_ys(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg, float prescale)
 {
   constexpr int XN1 = fs_n1_rows(M), XN2 = M / XN1, NI = fs_r2c_items(M);
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = XN1 + 1;
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_ys(CubeSet cs, const float2
 
 // inverse of k_r2c_ys: y stage 1 inverse of the 32 rows, then the x C2R with postscale
 template <int M>
-__global__ void __launch_bounds__(kFFTThreads) k_c2r_ys(CubeSet cs, const float2 *__restrict__ twg, float postscale)
+__global__ void __launch_bounds__(kFFTThreads) k_c2r_ys(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg, float postscale)
 {
   constexpr int XN1 = fs_n1_rows(M), XN2 = M / XN1;
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M), Q = XN1 + 1;
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_ys(CubeSet cs, const float2
 // pair moves into the C2R postscale).  Planes outside the band keep the prior
 // means (stage-1 rows untouched) and get the prior covariance.  MIXED: guarded bins are redone in FP64 in place.
 template <int NT, bool MIXED, int MINB>
-__global__ void __launch_bounds__(kFFTThreads, MINB) k_bins_ys(YBinArgs a)
+__global__ void __launch_bounds__(kFFTThreads, MINB) k_bins_ys(const __grid_constant__ YBinArgs a)
 {
   constexpr int W = 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_bins_ys(YBinArgs a)
 // (mu+ - mu) w16^(-n2 k2) / 16 for the bin k1 + 16 k2 (atomically: bins of
 // one row group may share rows).
 template <int NT>
-__global__ void __launch_bounds__(128) k_ys_fixup64(YBinArgs a)
+__global__ void __launch_bounds__(128) k_ys_fixup64(const __grid_constant__ YBinArgs a)
 {
   const int nq = min(*((volatile int *)&a.f.counters[0]), a.f.queue_cap);
   const int cnxp = a.f.cnxp;
