@@ -3,11 +3,13 @@
     python -m crava_gb300.autotune [--out crava_gb300/tuning.json]
 
 Candidates (see cg_tune_set in include/cravagpu.h):
-  * column transform pass, per axis length: resident-CTA target 2 or 3, and
-    the staged (0), persistent double-buffered (1), register-direct (2) or
-    four-step (3) kernel;
+  * column transform pass, per axis length: resident-CTA target 2 or 3 (or 4
+    for the register-direct and four-step kernels up to 256), and the staged
+    (0), persistent double-buffered (1), register-direct (2), four-step (3)
+    or persistent register-prefetch (4) kernel;
   * x-row pass, per half length nxp/2: staged (0) or four-step (1) kernel;
-  * fused bin kernel, per stack count: unconstrained or 85-register build.
+  * fused bin kernel, per stack count: unconstrained build or a 128-, 96- or
+    85-register build (4, 5 or 6 resident 128-thread CTAs).
 Each candidate is timed with the library's launch tracer (CUDA events on the
 launch stream) on cubes larger than L2; the fastest is kept.  The loader
 (crava_gb300._native.lib) applies tuning.json when it is present.
@@ -48,7 +50,7 @@ def tune_cols(lengths, L):
             api.fft_in_place_batch(cubes, nxp, api.DATA)
             api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
         best = None
-        for pipe in (0, 1, 2, 3):
+        for pipe in (0, 1, 2, 3, 4):
             for minb in ((2, 3, 4) if pipe in (2, 3) and n <= 256 else (2, 3)):
                 L.cg_tune_set(KEY_COLS_PIPE, n, pipe)
                 L.cg_tune_set(KEY_COLS_MINB, n, minb)
@@ -99,9 +101,9 @@ def tune_bin(ntheta_list, L):
             inv.restore("mixed")
             inv.run("mixed")
         best = None
-        for minb in (1, 6):
+        for minb in (1, 4, 5, 6):
             L.cg_tune_set(KEY_BIN_MINB, nt, minb)
-            ms = _time_kernels(run, "k_invert_fused")
+            ms = _time_kernels(run, ("k_invert_fused", "k_invert_info"))
             if best is None or ms < best[0]:
                 best = (ms, minb)
         L.cg_tune_set(KEY_BIN_MINB, nt, best[1])
