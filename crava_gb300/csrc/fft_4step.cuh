@@ -311,7 +311,12 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
   const int nr = min(RPC, nrows - r0);
   float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
   for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
-  // X[k] and X[M-k] of the first item are loaded before the twiddle barrier
+  // X[M-k] for k = N2 n1 + n2 (n2 > 0) is X[N2 (N1-1-n1) + (N2-n2)], the
+  // xk[N1-1-n1] of the item (N2-n2, row); when a row's N2 items sit in
+  // consecutive lanes of one warp it is taken from that lane by a shuffle, and
+  // the n2 = 0 item reads its partners from its own xk (X[M] is loaded).
+  // Otherwise X[M-k] is loaded as well (the second read of a row hits L1).
+  constexpr bool kShfl = 32 % N2 == 0 && P1 % 32 == 0;
   auto load1 = [&](int q, float2 *xk, float2 *xm) {
     const int t = q * kFFTThreads + threadIdx.x;
     const int n2 = t % N2, row = t / N2;
@@ -321,23 +326,34 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
     for (int n1 = 0; n1 < N1; n1++) {
       const int k = N2 * n1 + n2;
       xk[n1] = ok ? __ldg(rp + k) : make_float2(0.f, 0.f);
-      xm[n1] = ok ? __ldg(rp + (M - k)) : make_float2(0.f, 0.f);
+      if constexpr (!kShfl) xm[n1] = ok ? __ldg(rp + (M - k)) : make_float2(0.f, 0.f);
     }
+    if constexpr (kShfl) xm[0] = ok && n2 == 0 ? __ldg(rp + M) : make_float2(0.f, 0.f);
   };
-  float2 xk[N1], xm[N1];
+  float2 xk[N1], xm[kShfl ? 1 : N1];
   load1(0, xk, xm);
   __syncthreads();  // twiddles staged
 #pragma unroll
   for (int q = 0; q < B1; q++) {
     if (q > 0) load1(q, xk, xm);
     const int t = q * kFFTThreads + threadIdx.x;
-    if (P1 % kFFTThreads == 0 || t < P1) {
+    if (P1 % kFFTThreads == 0 || t < P1) {  // warp-uniform when kShfl
       const int n2 = t % N2, row = t / N2;
+      const int lane = threadIdx.x & 31;
+      const int partner = (lane & ~(N2 - 1)) | ((N2 - n2) & (N2 - 1));
       float2 v[N1];
 #pragma unroll
       for (int n1 = 0; n1 < N1; n1++) {
         const int k = N2 * n1 + n2;
-        float2 Xk = xk[n1], Xm = xm[n1];
+        float2 Xk = xk[n1], Xm;
+        if constexpr (kShfl) {
+          const float2 mine = xk[N1 - 1 - n1];
+          const float2 other = make_float2(__shfl_sync(0xffffffffu, mine.x, partner),
+                                           __shfl_sync(0xffffffffu, mine.y, partner));
+          Xm = n2 != 0 ? other : (n1 == 0 ? xm[0] : xk[(N1 - n1) % N1]);
+        } else {
+          Xm = xm[n1];
+        }
         if (k == 0) { Xk.y = 0.f; Xm.y = 0.f; }  // rfftw_c2hc keeps only Re of DC and Nyquist
         Xm.y = -Xm.y;
         const float2 E = cadd<float>(Xk, Xm);
