@@ -67,7 +67,8 @@ int cg_trace_entry(int index, char *name, int name_len, long *launches, double *
  * column-pass build targets, 2, 3 or 4 (4: lengths up to 256, register-
  * direct and four-step kernels), per axis length n), CG_TUNE_COLS_PIPE
  * (column-pass kernel per n: 0 shared-memory staged, 1 persistent
- * double-buffered, 2 first and last stages in registers, 3 four-step),
+ * double-buffered, 2 first and last stages in registers, 3 four-step, 4
+ * persistent register prefetch),
  * CG_TUNE_BIN_MINB (fused bin kernel: resident 128-thread CTAs the build
  * targets, 4, 5 or 6 (128, 96 or 85 registers), 1 = no target; the FP32
  * mode takes 4 where 6 is set; per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per
