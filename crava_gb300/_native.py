@@ -206,6 +206,7 @@ def _declare(L):
         "cg_tune_get": ([I, I], I),
         "cg_tune_clear": ([], I),
         "cg_trace_enable": ([I], I),
+        "cg_device_faults": ([ct.POINTER(I)], I),
         "cg_trace_collect": ([], I),
         "cg_trace_entry": ([I, ct.c_char_p, I, ct.POINTER(ct.c_long), ct.POINTER(D), ct.POINTER(D)], I),
     }
@@ -240,6 +241,13 @@ def header_symbols() -> list[str]:
 
 def trace_enable(on: bool = True):
     check(lib().cg_trace_enable(1 if on else 0), "cg_trace_enable")
+
+
+def device_faults() -> int:
+    """1 when a kernel's bounded wait gave up since the last call (the word is cleared), else 0."""
+    v = ct.c_int(0)
+    check(lib().cg_device_faults(ct.byref(v)), "cg_device_faults")
+    return v.value
 
 
 def trace_collect():

@@ -5,8 +5,9 @@
 Candidates (see cg_tune_set in include/cravagpu.h):
   * column transform pass, per axis length: resident-CTA target 2 or 3 (or 4
     for the register-direct and four-step kernels up to 256), and the staged
-    (0), persistent double-buffered (1), register-direct (2), four-step (3)
-    or persistent register-prefetch (4) kernel;
+    (0), persistent double-buffered (1), register-direct (2), four-step (3),
+    persistent register-prefetch (4) or, at length 256, persistent four-step
+    fed by tensor-memory-accelerator loads (5) kernel;
   * x-row pass, per half length nxp/2: staged (0) or four-step (1) kernel;
   * fused bin kernel, per stack count: unconstrained build or a 128-, 96- or
     85-register build (4, 5 or 6 resident 128-thread CTAs).
@@ -50,8 +51,8 @@ def tune_cols(lengths, L):
             api.fft_in_place_batch(cubes, nxp, api.DATA)
             api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
         best = None
-        for pipe in (0, 1, 2, 3, 4):
-            for minb in ((2, 3, 4) if pipe in (2, 3) and n <= 256 else (2, 3)):
+        for pipe in (0, 1, 2, 3, 4) + ((5,) if n == 256 else ()):
+            for minb in ((2, 3, 4) if pipe in (2, 3) and n <= 256 else (3,) if pipe == 5 else (2, 3)):
                 L.cg_tune_set(KEY_COLS_PIPE, n, pipe)
                 L.cg_tune_set(KEY_COLS_MINB, n, minb)
                 ms = _time_kernels(run, "k_fft_cols")

@@ -149,7 +149,16 @@ template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
            const float2 *tw, cudaStream_t st)
 {
-  const int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
+  int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
+  if (kind == 5) {
+    // TMA-fed persistent pass (length 256 along y or z); the register-direct
+    // kernel wherever its geometry or alignment does not fit
+    if constexpr (N == 256) {
+      const int rc = tma_cols(cs, ncubes, N, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+      if (rc != 0) return rc;
+    }
+    kind = 2;
+  }
   if (kind == 4) {
     if (minb_for(N) == 3) return launch_rdp<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     return launch_rdp<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);

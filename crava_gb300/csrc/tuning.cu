@@ -30,7 +30,7 @@ const char *env_name(int key)
 bool valid_value(int key, int value)
 {
   return (key == CG_TUNE_COLS_MINB && (value >= 2 && value <= 4)) ||
-         (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 4)) ||
+         (key == CG_TUNE_COLS_PIPE && (value >= 0 && value <= 5)) ||
          (key == CG_TUNE_BIN_MINB && (value == 1 || (value >= 4 && value <= 6))) ||
          (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||
          (key == CG_TUNE_FUSED_Y && (value >= 0 && value <= 2 || (value >= 4 && value <= 4096 && value % 2 == 0))) ||

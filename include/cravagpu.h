@@ -63,12 +63,19 @@ int cg_trace_enable(int on);
 int cg_trace_collect(void);
 int cg_trace_entry(int index, char *name, int name_len, long *launches, double *ms_total, double *bytes_total);
 
+/* Device fault word of the current device: kernels that wait on an mbarrier
+ * (the TMA-fed column pass) give up after a bounded number of polls, set this
+ * word and return instead of hanging.  Copies it to *flag (0 = no wait gave
+ * up) and clears it; synchronises with the device. */
+int cg_device_faults(int *flag);
+
 /* Launch-variant tuning table.  Keys: CG_TUNE_COLS_MINB (resident CTAs the
  * column-pass build targets, 2, 3 or 4 (4: lengths up to 256, register-
  * direct and four-step kernels), per axis length n), CG_TUNE_COLS_PIPE
  * (column-pass kernel per n: 0 shared-memory staged, 1 persistent
  * double-buffered, 2 first and last stages in registers, 3 four-step, 4
- * persistent register prefetch),
+ * persistent register prefetch, 5 persistent four-step fed by tensor-memory-
+ * accelerator loads (n = 256 along y or z; 2 elsewhere)),
  * CG_TUNE_BIN_MINB (fused bin kernel: resident 128-thread CTAs the build
  * targets, 4, 5 or 6 (128, 96 or 85 registers), 1 = no target; the FP32
  * mode takes 4 where 6 is set; per stack count n), CG_TUNE_ROWS_KERNEL (x-row pass kernel per

@@ -154,7 +154,7 @@ def _variant_case(oracle, nxp, nyp, nzp):
     return _VARIANT_REFS[key]
 
 
-@pytest.mark.parametrize("pipe", [0, 1, 2, 3, 4])
+@pytest.mark.parametrize("pipe", [0, 1, 2, 3, 4, 5])
 @pytest.mark.parametrize("minb", [2, 3, 4])
 def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
     from crava_gb300 import api
@@ -171,6 +171,39 @@ def test_column_pass_variants_match_oracle(cuda, oracle, native, pipe, minb):
             assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL, (nxp, nyp, nzp)
     finally:
         from crava_gb300 import _native
+        native.cg_tune_clear()
+        _native._apply_tuning(native)
+
+
+# the TMA-fed column pass (tuning value 5, length 256 along y or z): odd and even cnxp, odd rows
+# shifted by one column in the z pass, tail column groups, cubes batched in one launch, and an odd
+# nyp that falls back to the register-direct kernel for the z pass
+TMA_SIZES = [(256, 256, 4), (30, 256, 256), (64, 40, 256), (120, 256, 6), (64, 45, 256), (256, 6, 256)]
+
+
+@pytest.mark.parametrize("dims", TMA_SIZES)
+def test_tma_column_pass_matches_oracle(cuda, oracle, native, dims):
+    from crava_gb300 import _native, api
+    nxp, nyp, nzp = dims
+    native.cg_tune_clear()
+    try:
+        assert native.cg_tune_set(1, 256, 5) == 0
+        x, ref = _variant_case(oracle, nxp, nyp, nzp)
+        cubes = [torch.from_numpy(x.copy()).cuda() for _ in range(3)]
+        _native.trace_enable(True)
+        api.fft_in_place_batch(cubes, nxp, api.DATA)
+        for t in cubes:
+            assert rel(from_cube(t), ref) < FFT_TOL, dims
+        api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
+        tr = _native.trace_collect()
+        _native.trace_enable(False)
+        for t in cubes:
+            assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL, dims
+        uses = nyp == 256 or (nzp == 256 and nyp % 2 == 0)
+        assert ("k_fft_cols_tma" in tr) == uses, tr.keys()
+        assert _native.device_faults() == 0
+    finally:
+        _native.trace_enable(False)
         native.cg_tune_clear()
         _native._apply_tuning(native)
 

@@ -78,7 +78,7 @@ def test_tuning_table_defaults_overrides_and_validation(native):
     assert native.cg_tune_get(0, 256) == 2 and native.cg_tune_get(0, 200) == 3   # per-length entry wins
     assert native.cg_tune_set(1, 0, 0) == 0 and native.cg_tune_get(1, 128) == 0  # n = 0: every length
     assert native.cg_tune_set(0, 256, 7) == -1 and native.cg_tune_set(0, 256, 4) == 0  # resident-CTA targets 2-4
-    assert native.cg_tune_set(1, 0, 4) == 0 and native.cg_tune_set(1, 0, 5) == -1  # column kernels 0..4
+    assert native.cg_tune_set(1, 0, 4) == 0 and native.cg_tune_set(1, 0, 6) == -1  # column kernels 0..5
     assert native.cg_tune_get(3, 128) == 1 and native.cg_tune_set(3, 128, 0) == 0  # x-row kernel 0/1
     assert native.cg_tune_get(3, 128) == 0 and native.cg_tune_set(3, 128, 2) == -1
     assert native.cg_tune_set(9, 1, 1) == -1
