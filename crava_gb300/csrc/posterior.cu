@@ -307,8 +307,14 @@ struct InfoArgs {
   float s0i[6];  // Sigma0^-1, bin order 00 11 22 01 02 12
 };
 
+// threads per CTA of k_invert_info: the 85-register build runs 256-thread CTAs
+// (three per SM; each CTA stages the per-k table once for twice the bins),
+// the others 128
+__host__ __device__ constexpr int info_threads(int minb) { return minb == 6 ? 256 : 128; }
+
 template <int NT, int MODE, int MINB>
-__global__ void __launch_bounds__(128, MINB) k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab,
+__global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(MINB))
+    k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab,
                                                            InfoArgs ia)
 {
   __shared__ ITab it;
@@ -927,6 +933,8 @@ static void launch_info(const FusedArgs<float> &a, const Workspace *w, dim3 grid
   InfoArgs ia;
   for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
   const int mb = cg_tune_get(CG_TUNE_BIN_MINB, NT);
+  threads = info_threads(mb == 6 || mb == 5 ? mb : 4);
+  grid.x = ceil_div(a.plane, threads);
   if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia);
   else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia);
   else k_invert_info<NT, MODE, 4><<<grid, threads, 0, st>>>(a, w->itab, ia);
