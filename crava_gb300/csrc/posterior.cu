@@ -307,26 +307,10 @@ struct InfoArgs {
   float s0i[6];  // Sigma0^-1, bin order 00 11 22 01 02 12
 };
 
-// threads per CTA of k_invert_info: the 85-register build runs 256-thread CTAs
-// (three per SM; each CTA stages the per-k table once for twice the bins),
-// the others 128
-__host__ __device__ constexpr int info_threads(int minb) { return minb == 6 ? 256 : 128; }
-
-template <int NT, int MODE, int MINB>
-__global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(MINB))
-    k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab,
-                                                           InfoArgs ia)
+// one bin of k_invert_info (plane k, bin ij of the plane)
+template <int NT, int MODE>
+__device__ __forceinline__ void info_bin(const FusedArgs<float> &a, const ITab &it, const InfoArgs &ia, int k, int ij)
 {
-  __shared__ ITab it;
-  const int k = a.k0 + blockIdx.y;
-  {
-    const int *src = (const int *)&itab[k];
-    int *dst = (int *)&it;
-    for (int t = threadIdx.x; t < (int)(sizeof(ITab) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
-  }
-  __syncthreads();
-  const int ij = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ij >= a.plane) return;
   const long b = (long)k * a.plane + ij;
   float s, lam;
   bin_scales<float>(a, ij, k, s, lam);
@@ -456,6 +440,32 @@ __global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(
   a.cov[3][b] = S01;
   a.cov[4][b] = S02;
   a.cov[5][b] = S12;
+}
+
+// threads per CTA of k_invert_info: the 85-register build runs 256-thread CTAs
+// (three per SM), the others 128; a CTA solves up to kInfoBlocks runs of that
+// many bins of one plane, so the per-k table is staged once for all of them
+__host__ __device__ constexpr int info_threads(int minb) { return minb == 6 ? 256 : 128; }
+constexpr int kInfoBlocks = 8;
+
+template <int NT, int MODE, int MINB>
+__global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(MINB))
+    k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab, InfoArgs ia, int nruns)
+{
+  __shared__ ITab it;
+  const int k = a.k0 + blockIdx.y;
+  {
+    const int *src = (const int *)&itab[k];
+    int *dst = (int *)&it;
+    for (int t = threadIdx.x; t < (int)(sizeof(ITab) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int r = 0; r < nruns; r++) {
+    const int ij = (blockIdx.x * nruns + r) * blockDim.x + threadIdx.x;
+    if (ij >= a.plane) return;
+    info_bin<NT, MODE>(a, it, ia, k, ij);
+  }
 }
 
 struct S0Args {
@@ -934,10 +944,17 @@ static void launch_info(const FusedArgs<float> &a, const Workspace *w, dim3 grid
   for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
   const int mb = cg_tune_get(CG_TUNE_BIN_MINB, NT);
   threads = info_threads(mb == 6 || mb == 5 ? mb : 4);
-  grid.x = ceil_div(a.plane, threads);
-  if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia);
-  else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia);
-  else k_invert_info<NT, MODE, 4><<<grid, threads, 0, st>>>(a, w->itab, ia);
+  // up to kInfoBlocks runs per CTA while the grid keeps about four waves of
+  // 768 threads per SM
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
+  const long runs = (long)ceil_div(a.plane, threads) * grid.y;
+  const long want = 4L * (nsm > 0 ? nsm : 1) * (768 / threads);
+  const int nruns = (int)(runs / want < 1 ? 1 : runs / want > kInfoBlocks ? kInfoBlocks : runs / want);
+  grid.x = ceil_div(a.plane, (long)threads * nruns);
+  if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
+  else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
+  else k_invert_info<NT, MODE, 4><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
 }
 
 template <typename T>
