@@ -206,10 +206,12 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(const __grid_consta
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + RPC * P;
+  float2 *tw1 = tw + NX;  // tw1[k1 * N2 + n2] = W_2M^(2 n2 k1): pass-1 twiddles without bank conflicts
   const int r0 = blockIdx.x * RPC;
   const int nr = min(RPC, nrows - r0);
   float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
   for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  for (int t = threadIdx.x; t < N1 * N2; t += kFFTThreads) tw1[t] = twg[2 * (t % N2) * (t / N2)];
   auto load1 = [&](int q, float2 *v) {
     const int t = q * kFFTThreads + threadIdx.x;
     const int n2 = t % N2, row = t / N2;
@@ -229,7 +231,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(const __grid_consta
       const int n2 = t % N2, row = t / N2;
       reg_fft<float, N1, 2 * N2>(v, -1, tw);
 #pragma unroll
-      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw[2 * n2 * k1]);
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw1[k1 * N2 + n2]);
 #pragma unroll
       for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
     }
@@ -307,10 +309,12 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *buf = (float2 *)smem_raw;
   float2 *tw = buf + RPC * P;
+  float2 *tw1 = tw + NX;  // tw1[k1 * N2 + n2] = W_2M^(2 n2 k1): pass-1 twiddles without bank conflicts
   const int r0 = blockIdx.x * RPC;
   const int nr = min(RPC, nrows - r0);
   float2 *base = (float2 *)cs.ptr[blockIdx.z] + (long)r0 * CN;
   for (int t = threadIdx.x; t < NX; t += kFFTThreads) tw[t] = twg[t];
+  for (int t = threadIdx.x; t < N1 * N2; t += kFFTThreads) tw1[t] = twg[2 * (t % N2) * (t / N2)];
   // X[M-k] for k = N2 n1 + n2 (n2 > 0) is X[N2 (N1-1-n1) + (N2-n2)], the
   // xk[N1-1-n1] of the item (N2-n2, row); when a row's N2 items sit in
   // consecutive lanes of one warp it is taken from that lane by a shuffle, and
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
       }
       reg_fft<float, N1, 2 * N2>(v, +1, tw);
 #pragma unroll
-      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw_at<float>(tw, 2 * n2 * k1, +1));
+      for (int k1 = 1; k1 < N1; k1++) v[k1] = cmul<float>(v[k1], tw_at<float>(tw1, k1 * N2 + n2, +1));
 #pragma unroll
       for (int k1 = 0; k1 < N1; k1++) buf[row * P + n2 * Q + k1] = v[k1];
     }

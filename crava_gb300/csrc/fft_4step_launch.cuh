@@ -37,7 +37,7 @@ int launch_rows_4s(bool forward, const CubeSet &cs, const CubeSet &addend, int n
                    const float2 *tw, cudaStream_t st, int epi)
 {
   constexpr int RPC = fs_rows_per_cta(M), P = fs_row_pitch(M);
-  const size_t smem = ((size_t)RPC * P + 2 * M) * sizeof(float2);
+  const size_t smem = ((size_t)RPC * P + 3 * M) * sizeof(float2);  // exchange, twiddles, pass-1 twiddles
   dim3 grid(ceil_div(nrows, RPC), 1, ncubes);
   const double bytes = (double)ncubes * nrows * (2.0 * M * sizeof(float) + (M + 1.0) * sizeof(float2));
   static bool attr_fwd[64] = {}, attr_inv[64] = {};
