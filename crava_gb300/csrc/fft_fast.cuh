@@ -360,7 +360,10 @@ __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_rd(const __grid_
 #pragma unroll
       for (int r = 0; r < R; r++) v[q][r] = ok ? base[(long)(j + r * NB) * as + (long)c * cstride] : make_float2(0.f, 0.f);
     }
-    __syncthreads();  // twiddles staged (odd radices read them inside the DFT)
+    // odd radices read the twiddle table inside the DFT; radices 2, 4 and 8 use
+    // constants, so their warps start as soon as their own operands arrive (the
+    // barrier after this stage publishes the table to the later stages)
+    if constexpr (R % 2 == 1) __syncthreads();
 #pragma unroll
     for (int q = 0; q < BPT; q++) {
       const int t = q * kFFTThreads + threadIdx.x;
