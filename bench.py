@@ -394,7 +394,7 @@ def run_ours(args, world, rank, local):
     e2e_sync_ms = sum(sync_step() for _ in range(args.steps)) / args.steps
     for c in ctxs:
         c.close()
-    # the spec phrasing of the target: a 256^3 cube with THREE stacks (0/20/40 deg), mixed vs plain,
+    # the three-stack form of the target: a 256^3 cube with THREE stacks (0/20/40 deg), mixed vs plain,
     # timed the same way (restore + L2 flush outside the events), error vs the FP64 GPU form
     sc3 = S.make_scenario(205, 205, 205, [0.0, 20.0, 40.0], 25.0, nxp=256, nyp=256, nzp=256, sn=3.0,
                           notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=20261208 + rank)

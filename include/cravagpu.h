@@ -31,7 +31,7 @@ extern "C" {
 #define CG_OK 0
 #define CG_ERR_ARG (-1)         /* bad argument (size, pointer, type) */
 #define CG_ERR_CUDA (-2)        /* CUDA runtime error */
-#define CG_ERR_UNSUPPORTED (-3) /* valid input this build does not handle */
+#define CG_ERR_UNSUPPORTED (-3) /* valid input the library does not handle */
 #define CG_ERR_STATE (-4)       /* call out of order (e.g. handle not set up) */
 
 /* ---- cube types: the values of FFTGrid::gridTypes (src/fftgrid.h:199) -- */
