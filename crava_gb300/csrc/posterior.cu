@@ -235,22 +235,10 @@ __global__ void __launch_bounds__(128) k_invert_plain(PlainArgs a)
   a.cov[5][b] = S[1][2];
 }
 
-// MODE 0: FP32, 1: MIXED (FP32 + queue), 2: FP64 (T = double).  MINB is the
-// resident-CTA target handed to the register allocator (1 = unconstrained,
-// 6 = at most 85 registers).
-template <typename T, int NT, int MODE, int MINB = 1>
-__global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a)
+// one bin of k_invert_fused (plane k, bin ij of the plane)
+template <typename T, int NT, int MODE>
+__device__ __forceinline__ void fused_bin(const FusedArgs<T> &a, const KTab<T> &kt, int k, int ij)
 {
-  __shared__ KTab<T> kt;
-  const int k = a.k0 + blockIdx.y;
-  {
-    const int *src = (const int *)&a.ktab[k];
-    int *dst = (int *)&kt;
-    for (int t = threadIdx.x; t < (int)(sizeof(KTab<T>) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
-  }
-  __syncthreads();
-  const int ij = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ij >= a.plane) return;
   const long b = (long)k * a.plane + ij;
   T s, lam;
   bin_scales<T>(a, ij, k, s, lam);
@@ -295,6 +283,29 @@ __global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a)
   for (int p = 0; p < 3; p++) a.mean[p][b] = mu[p];
 #pragma unroll
   for (int t = 0; t < 6; t++) a.cov[t][b] = cov[t];
+}
+
+// MODE 0: FP32, 1: MIXED (FP32 + queue), 2: FP64 (T = double).  MINB is the
+// resident-CTA target handed to the register allocator (1 = unconstrained,
+// 6 = at most 85 registers).  A CTA solves nruns runs of blockDim.x bins of
+// one plane, so the per-k table is staged once for all of them.
+template <typename T, int NT, int MODE, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a, int nruns)
+{
+  __shared__ KTab<T> kt;
+  const int k = a.k0 + blockIdx.y;
+  {
+    const int *src = (const int *)&a.ktab[k];
+    int *dst = (int *)&kt;
+    for (int t = threadIdx.x; t < (int)(sizeof(KTab<T>) / sizeof(int)); t += blockDim.x) dst[t] = src[t];
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (int r = 0; r < nruns; r++) {
+    const int ij = (blockIdx.x * nruns + r) * blockDim.x + threadIdx.x;
+    if (ij >= a.plane) return;
+    fused_bin<T, NT, MODE>(a, kt, k, ij);
+  }
 }
 
 // Information-form bin solve (FP32; MODE 0 FP32, 1 MIXED with the FP64 queue
@@ -934,6 +945,17 @@ template int fill_fused_args<float>(Workspace *, void *const *, void *const *, v
 template int fill_fused_args<double>(Workspace *, void *const *, void *const *, void *const *, FusedArgs<double> *);
 }  // namespace cg
 
+// bin runs per CTA: up to kInfoBlocks while the grid of `threads`-thread CTAs
+// over nk planes keeps about four waves of 768 threads per SM
+static int bin_runs(const Workspace *w, long plane, int threads, int nk)
+{
+  int nsm = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
+  const long runs = (long)ceil_div(plane, threads) * nk;
+  const long want = 4L * (nsm > 0 ? nsm : 1) * (768 / threads);
+  return (int)(runs / want < 1 ? 1 : runs / want > kInfoBlocks ? kInfoBlocks : runs / want);
+}
+
 // the information form (CG_TUNE_BIN_FORM 1) when the model has its tables
 static bool use_info(const Workspace *w, int nt) { return w->info_ok && cg_tune_get(CG_TUNE_BIN_FORM, nt) == 1; }
 
@@ -944,13 +966,7 @@ static void launch_info(const FusedArgs<float> &a, const Workspace *w, dim3 grid
   for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
   const int mb = cg_tune_get(CG_TUNE_BIN_MINB, NT);
   threads = info_threads(mb == 6 || mb == 5 ? mb : 4);
-  // up to kInfoBlocks runs per CTA while the grid keeps about four waves of
-  // 768 threads per SM
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
-  const long runs = (long)ceil_div(a.plane, threads) * grid.y;
-  const long want = 4L * (nsm > 0 ? nsm : 1) * (768 / threads);
-  const int nruns = (int)(runs / want < 1 ? 1 : runs / want > kInfoBlocks ? kInfoBlocks : runs / want);
+  const int nruns = bin_runs(w, a.plane, threads, (int)grid.y);
   grid.x = ceil_div(a.plane, (long)threads * nruns);
   if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
   else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
@@ -972,6 +988,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
   const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   const int threads = 128;
   dim3 grid(ceil_div(a.plane, threads), nk);
+  const int fruns = bin_runs(w, a.plane, threads, nk);  // Cholesky-form kernel: runs per CTA
+  const dim3 fgrid(ceil_div(a.plane, (long)threads * fruns), nk);
   const long outband = (long)a.plane * w->nzp - w->inband_bins;
   const double fbytes = (double)sizeof(C2<T>) * (w->inband_bins * (double)((nt + 3) + (nt + 3 + 6)) + outband * 6.0) *
                         ((double)nk / w->nzp);
@@ -979,7 +997,7 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
     constexpr int NT = decltype(NTc)::value;
     if constexpr (sizeof(T) == 8) {
       TraceScope ts("k_invert_fused_fp64", st, fbytes);
-      k_invert_fused<T, NT, 2><<<grid, threads, 0, st>>>(a);
+      k_invert_fused<T, NT, 2><<<fgrid, threads, 0, st>>>(a, fruns);
     } else if (precision == CG_PREC_MIXED) {
       // the queue position counter starts at zero for every inversion (stream ordered); a z-chunk of a
       // chunked inversion appends to the queue and its fix-up starts where the chunk's entries start
@@ -991,10 +1009,10 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
         launch_info<NT, 1>(a, w, grid, threads, st);
       } else {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
-        if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<grid, threads, 0, st>>>(a);
-        else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 1, 5><<<grid, threads, 0, st>>>(a);
-        else if (bin_minb(NT) == 4) k_invert_fused<T, NT, 1, 4><<<grid, threads, 0, st>>>(a);
-        else k_invert_fused<T, NT, 1, 1><<<grid, threads, 0, st>>>(a);
+        if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<fgrid, threads, 0, st>>>(a, fruns);
+        else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 1, 5><<<fgrid, threads, 0, st>>>(a, fruns);
+        else if (bin_minb(NT) == 4) k_invert_fused<T, NT, 1, 4><<<fgrid, threads, 0, st>>>(a, fruns);
+        else k_invert_fused<T, NT, 1, 1><<<fgrid, threads, 0, st>>>(a, fruns);
       }
       CG_CHECK_LAUNCH("k_invert_fused");
       S0Args sd;
@@ -1012,9 +1030,9 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
       // the FP32 mode spills more than MIXED under the 85-register cap (228 B against 128 B at five
       // stacks; 0.47 against 0.39 ms at 256^3): its tight setting is the 128-register build
-      if (bin_minb(NT) == 6 || bin_minb(NT) == 4) k_invert_fused<T, NT, 0, 4><<<grid, threads, 0, st>>>(a);
-      else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 0, 5><<<grid, threads, 0, st>>>(a);
-      else k_invert_fused<T, NT, 0, 1><<<grid, threads, 0, st>>>(a);
+      if (bin_minb(NT) == 6 || bin_minb(NT) == 4) k_invert_fused<T, NT, 0, 4><<<fgrid, threads, 0, st>>>(a, fruns);
+      else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 0, 5><<<fgrid, threads, 0, st>>>(a, fruns);
+      else k_invert_fused<T, NT, 0, 1><<<fgrid, threads, 0, st>>>(a, fruns);
     }
     CG_CHECK_LAUNCH("k_invert_fused");
     return CG_OK;
