@@ -861,6 +861,23 @@ extern "C" int cg_invert_bins_plain(cg_workspace w, float *const *data, float *c
   });
 }
 
+// zero-padded copies of the lateral correlation surface (nxp x nyp at the
+// rnxp pitch, n1 = rnxp * nyp values) and of the temporal correlation (nzp
+// values into the rnzp that follow), in one launch
+__global__ void k_pad_prior(const float *__restrict__ corr_xy, const float *__restrict__ circ_t, float *cxy,
+                            float *ct, int nxp, int nzp, int rnxp, long n1, long n)
+{
+  const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (i < n1) {
+    const int x = (int)(i % rnxp);
+    cxy[i] = x < nxp ? corr_xy[(i / rnxp) * nxp + x] : 0.0f;
+  } else {
+    const int z = (int)(i - n1);
+    ct[z] = z < nzp ? circ_t[z] : 0.0f;
+  }
+}
+
 // pad a real nxp x nyp surface into the FFTGrid layout and transform it
 template <typename T>
 static int prior_tables(Workspace *w, const float *corr_xy, const float *circ_corr_t, T *cxy, T *ct, cudaStream_t st)
@@ -868,11 +885,10 @@ static int prior_tables(Workspace *w, const float *corr_xy, const float *circ_co
   const int nxp = w->nxp, nyp = w->nyp, nzp = w->nzp;
   const int rnxp = 2 * (nxp / 2 + 1), rnzp = 2 * (nzp / 2 + 1);
   if (sizeof(T) == 4) {
-    CG_CUDA(cudaMemsetAsync(cxy, 0, sizeof(T) * (size_t)rnxp * nyp, st));
-    CG_CUDA(cudaMemcpy2DAsync(cxy, sizeof(T) * rnxp, corr_xy, sizeof(float) * nxp, sizeof(float) * nxp, nyp,
-                              cudaMemcpyDeviceToDevice, st));
-    CG_CUDA(cudaMemsetAsync(ct, 0, sizeof(T) * (size_t)rnzp, st));
-    CG_CUDA(cudaMemcpyAsync(ct, circ_corr_t, sizeof(float) * nzp, cudaMemcpyDeviceToDevice, st));
+    const long n1 = (long)rnxp * nyp, n2 = rnzp;
+    k_pad_prior<<<ceil_div(n1 + n2, 256), 256, 0, st>>>(corr_xy, circ_corr_t, (float *)cxy, (float *)ct, nxp, nzp,
+                                                        rnxp, n1, n1 + n2);
+    CG_CHECK_LAUNCH("k_pad_prior");
   } else {
     // float -> double into the padded layout, row by row through the float staging buffers
     CG_CUDA(cudaMemsetAsync(w->cxy_f, 0, sizeof(float) * (size_t)rnxp * nyp, st));
