@@ -210,10 +210,14 @@ def test_split_y_pipeline_matches_fp64_oracle(cuda, oracle, nzp, cond, form):
 
 # the information form of the fused bin solve (CG_TUNE_BIN_FORM = 1, the default): per-k eigen-decompositions of the error
 # covariance, a 3 x 3 Cholesky per bin; guarded bins (cond 1.0001 flags most of them) go to the FP64 fix-up
-@pytest.mark.parametrize("dims,cond,form,nt", [((64, 128, 48), 0.0, "mixed", 5), ((40, 200, 36), 0.0, "fp32", 5),
-                                               ((48, 64, 40), 1.0001, "mixed", 5), ((36, 48, 30), 0.0, "mixed", 3),
-                                               ((30, 40, 32), 0.0, "fp32", 8)])
-def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt):
+# the 128^3 cases give every CTA two runs of bins of its plane (the grid keeps about four waves), for both forms
+@pytest.mark.parametrize("dims,cond,form,nt,bin_form", [((64, 128, 48), 0.0, "mixed", 5, 1), ((40, 200, 36), 0.0, "fp32", 5, 1),
+                                                        ((48, 64, 40), 1.0001, "mixed", 5, 1), ((36, 48, 30), 0.0, "mixed", 3, 1),
+                                                        ((30, 40, 32), 0.0, "fp32", 8, 1),
+                                                        ((128, 128, 128), 0.0, "mixed", 5, 1),
+                                                        ((128, 128, 128), 1.0001, "mixed", 5, 1),
+                                                        ((128, 128, 128), 0.0, "mixed", 5, 0)])
+def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt, bin_form):
     from crava_gb300 import synthetic as S
     from crava_gb300.pipeline import Inversion
     from crava_gb300 import _native
@@ -222,7 +226,7 @@ def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt
                          nxp=nxp, nyp=nyp, nzp=nzp, sn=3.0, notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0,
                          seed=nxp + nzp + nt)
     L = _native.lib()
-    assert L.cg_tune_set(5, 0, 1) == 0
+    assert L.cg_tune_set(5, 0, bin_form) == 0
     try:
         inv = Inversion(sc, forms=(form,), cond_threshold=cond)
         inv.restore(form)
@@ -237,7 +241,7 @@ def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt
     post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
     prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
     e = (rel(pm, post64), rel(pm - prior, post64 - prior), rel(res, res64), rel(cov, cov64))
-    print(dims, cond, form, nt, "information form vs FP64 oracle (mean, update, resid, cov):", e, st)
+    print(dims, cond, form, nt, bin_form, "fused form vs FP64 oracle (mean, update, resid, cov):", e, st)
     assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
     if cond > 0:
         assert st["flagged"] > 0
