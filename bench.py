@@ -17,7 +17,8 @@ a cube; cubes are independent), value = total bins / max time.
 
 --impl reference times the reference algorithm on the host cores (the C
 oracle port: its FFTs and its lib_matr-order bin loop, OpenMP over k like the
-reference) on a bounded sample scaled to a full inversion.
+reference): one complete inversion per step, operator tables from the
+oracle's own restatement.
 """
 from __future__ import annotations
 
@@ -174,71 +175,80 @@ def rel(a, b):
 
 
 # ---------------------------------------------------------------------------
-# CPU reference (oracle port) timing
+# CPU reference (oracle port): one complete inversion on the host cores
 # ---------------------------------------------------------------------------
-def cpu_reference_sample(sc, tables, kplanes=8, threads=None):
-    """Time the reference algorithm on the host on a bounded sample.
+COV_PAIRS = [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]
 
-    Sample: one forward and one inverse 3D transform of a full cube, plus the
-    bin loop over `kplanes` in-band k-planes.  Scaled to one inversion of the
-    reference dataflow: (n + 3 + 6 + 1) forward transforms, 3 inverse
-    transforms, all bins.
-    """
+
+def cpu_inversion(sc, tables, prec="f", threads=None):
+    """The whole inversion of ``sc`` on the CPU oracle, in the reference's dataflow and order
+    (Crava::computePostMeanResidAndFFTCov, src/crava.cpp:975-1285, with the data and prior-mean transforms
+    of src/crava.cpp:177-184): n data + 3 prior-mean forward transforms, the 6 prior covariance cubes
+    (fillInParamCorr) and the error correlation cube (fillInErrCorr) filled and forward transformed, the
+    lib_matr-order bin loop over every bin (OpenMP over k), 3 inverse transforms of the posterior means.
+    prec "f" is the reference's FP32 arithmetic, "d" the FP64 oracle.  ``tables`` are the per-k FP32
+    operator tables.  Returns (seconds per phase, posterior-mean real cubes, residual spectra, covariance
+    spectra, failed-Cholesky count)."""
     import numpy as np
     from oracle import oracle as O
-    threads = threads or os.cpu_count() or 1
-    nxp, nyp, nzp, n = sc.nxp, sc.nyp, sc.nzp, sc.ntheta
+    nt = threads or os.cpu_count() or 1
+    tab = dict(tables)
+    tab["nxp"] = sc.nxp
+    if prec == "d":
+        tab = {k: (v.astype(np.complex128) if hasattr(v, "dtype") and v.dtype == np.complex64 else v)
+               for k, v in tab.items()}
+    t = {}
     t0 = time.perf_counter()
-    spec = O.fft3d_r2c(sc.data[0], nxp, O.DATA, "f", threads)
-    t_fwd = time.perf_counter() - t0
+    data = [O.fft3d_r2c(d, sc.nxp, O.DATA, prec, nt) for d in sc.data]
+    mean = [O.fft3d_r2c(m, sc.nxp, O.PARAMETER, prec, nt) for m in sc.mean]
+    t["data_mean_fft_s"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    O.fft3d_c2r(spec, nxp, O.PARAMETER, "f", threads)
-    t_inv = time.perf_counter() - t0
-    # bin loop on a slab of in-band k-planes (inputs: random spectra of the right shape)
-    ks = [k for k in range(nzp) if tables["band"][k]][:kplanes]
-    rng = np.random.default_rng(1)
-    cnxp = nxp // 2 + 1
-    shp = (len(ks), nyp, cnxp)
+    covs = []
+    for (p, q) in COV_PAIRS:
+        c = O.fill_param_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, sc.circ_corr_t, 0, 0,
+                              float(np.float32(sc.sigma0[p, q])), prec=prec)
+        covs.append(O.fft3d_r2c(c, sc.nxp, O.COVARIANCE, prec, nt))
+    ec = O.fft3d_r2c(O.fill_err_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, prec=prec), sc.nxp, O.COVARIANCE, prec,
+                     nt)
+    t["cov_fill_fft_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s0 = np.asarray(sc.sigma0, dtype=np.float64).astype(np.float32).astype(np.float64)
+    res, mu, cov, nf = O.invert_bins(data, mean, covs, ec, tab, sc.err_theta_cov, s0, sc.wnc, prec=prec,
+                                     nthreads=nt)
+    t["bins_s"] = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    post = np.stack([O.fft3d_c2r(m, sc.nxp, O.PARAMETER, prec, nt)[:, :, :sc.nxp] for m in mu])
+    t["inverse_fft_s"] = time.perf_counter() - t0
+    t["total_s"] = sum(t.values())
+    return t, post, np.stack(res), np.stack(cov), nf
 
-    def rc():
-        return (rng.standard_normal(shp) + 1j * rng.standard_normal(shp)).astype(np.complex64)
-    data = [rc() for _ in range(n)]
-    mean = [rc() for _ in range(3)]
-    # prior spectra of the planes from the separable model (so every Cholesky does its full work)
-    cxy = np.fft.rfft2(sc.corr_xy.astype(np.float64))            # (nyp, cnxp)
-    ctk = np.fft.fft(sc.circ_corr_t.astype(np.float64))[ks]      # (len(ks),)
-    c = (ctk[:, None, None] * cxy[None, :, :]).real.astype(np.float32)
-    s0 = sc.sigma0.astype(np.float32)
-    cov = [(c * s0[p, q]).astype(np.complex64) for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]]
-    ec = np.broadcast_to(cxy.real.astype(np.float32), shp).astype(np.complex64)
-    sub = {"K": tables["K"][ks], "em1": tables["em1"][ks], "em2": tables["em2"][ks], "em3": tables["em3"][ks],
-           "band": np.ones(len(ks), np.uint8), "nxp": nxp}
-    t0 = time.perf_counter()
-    O.invert_bins(data, mean, cov, ec, sub, sc.err_theta_cov, sc.sigma0, sc.wnc, prec="f", nthreads=threads)
-    t_bins = time.perf_counter() - t0
-    inband = int(np.asarray(tables["band"]).sum())
-    t_full = (n + 3 + 6 + 1) * t_fwd + 3 * t_inv + t_bins * inband / max(1, len(ks))
-    sample = (f"1 forward + 1 inverse 256^3 transform and the bin loop over {len(ks)} of {inband} in-band "
-              f"k-planes, scaled to {n + 10} forward + 3 inverse transforms and all bins")
-    return t_full, threads, sample, {"t_fwd_s": t_fwd, "t_inv_s": t_inv, "t_bins_sample_s": t_bins}
+
+def oracle_tables(sc):
+    """The per-k operator tables from the oracle's own restatement (no product code on the CPU arm)."""
+    from oracle import oracle as O
+    return O.k_tables(sc.nxp, sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
+                      sc.min_rel_thick, prec="f")
+
+
+CPU_SAMPLE = ("one complete inversion of the workload: {n} data + 3 prior-mean + 7 prior/error forward 256^3 "
+              "transforms, the bin loop over all bins, 3 inverse transforms (no extrapolation)")
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    import numpy as np
     from crava_gb300 import synthetic as S
-    from crava_gb300 import api
     sc = S.config1()
-    tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut)
+    tables = oracle_tables(sc)
     bins = sc.nbins
+    threads = os.cpu_count() or 1
     for _ in range(args.warmup):
-        cpu_reference_sample(sc, tables, kplanes=2)
+        cpu_inversion(sc, tables, "f", threads)
     times = []
     info = None
     for _ in range(args.steps):
-        t, cores, sample, info = cpu_reference_sample(sc, tables)
-        times.append(t)
+        info = cpu_inversion(sc, tables, "f", threads)[0]
+        times.append(info["total_s"])
     ms = 1e3 * statistics.mean(times)
     value = bins / (ms * 1e-3) / 1e6
     line = {
@@ -247,8 +257,9 @@ def run_reference(args, world, rank):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "nxp": sc.nxp, "nyp": sc.nyp, "nzp": sc.nzp, "ntheta": sc.ntheta,
                    "bins": bins, "form": "reference dataflow on the host (C oracle port, OpenMP)"},
-        "cpu_baseline": {"value": round(value, 4), "unit": "Mbins/s", "cores": cores, "kind": "port",
-                         "sample": sample, **{k: round(v, 4) for k, v in info.items()}},
+        "cpu_baseline": {"value": round(value, 4), "unit": "Mbins/s", "cores": threads, "kind": "port",
+                         "sample": CPU_SAMPLE.format(n=sc.ntheta),
+                         "last_step_phases_s": {k: round(v, 4) for k, v in info.items()}},
         "e2e": {"value": round(value, 4), "unit": "Mbins/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -257,6 +268,73 @@ def run_reference(args, world, rank):
 # ---------------------------------------------------------------------------
 # GPU
 # ---------------------------------------------------------------------------
+COND_BUCKETS = 16
+
+
+def conditioning_case(args, stream, flush, rank):
+    """A workload whose bins do cross the FP64 guard: 8 stacks 0-40 deg (near-collinear Aki-Richards rows),
+    S/N 10 (the reference's maximum), 25 Hz Ricker without notches, band 1-100 Hz, 256x256x128 padded.
+    Times the fused FP32 and mixed forms and reports the FP64 fix-up's share and both errors vs FP64."""
+    import numpy as np
+    import torch
+    from crava_gb300 import _native
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.make_scenario(205, 205, 102, list(np.linspace(0.0, 40.0, 8)), 25.0, nxp=256, nyp=256, nzp=128,
+                         sn=10.0, low_cut=1.0, high_cut=100.0, seed=20261209 + rank)
+    inv = Inversion(sc, forms=("fp32", "mixed", "fp64"))
+    ms = {}
+    for form in ("fp32", "mixed"):
+        for _ in range(max(args.warmup, 1)):
+            inv.restore(form)
+            inv.run(form)
+        ev = []
+        for _ in range(args.steps):
+            inv.restore(form)
+            flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            inv.run(form)
+            e1.record(stream)
+            ev.append((e0, e1))
+        torch.cuda.synchronize()
+        ms[form] = statistics.mean(a.elapsed_time(b) for a, b in ev)
+    inv.restore("fp64")
+    inv.run("fp64")
+    torch.cuda.synchronize()
+    pm64, res64, cov64 = inv.results("fp64")
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    out = {"workload": "256x256x128 padded, 8 stacks 0-40 deg, 25 Hz Ricker, S/N 10, band 1-100 Hz",
+           "bins": sc.nbins, "ms": {k: round(v, 4) for k, v in ms.items()}}
+    for form in ("fp32", "mixed"):
+        inv.restore(form)
+        inv.ws.reset_stats()
+        inv.run(form)
+        torch.cuda.synchronize()
+        pm, res, cov = inv.results(form)
+        st = inv.ws.stats()
+        out[form] = {"mean_rel_err": float(f"{rel(pm, pm64):.3e}"),
+                     "update_rel_err": float(f"{rel(pm - prior, pm64 - prior):.3e}"),
+                     "resid_rel_err": float(f"{rel(res, res64):.3e}"), "cov_rel_err": float(f"{rel(cov, cov64):.3e}"),
+                     "fp64_bins": st["flagged"] if form == "mixed" else 0, "chol_fail": st["failed"]}
+        if form == "mixed":
+            hc, hi = inv.ws.condition_histogram(COND_BUCKETS)
+            out["condition_histogram"] = {"chol_form_fp64": hc, "info_form_fp32": hi}
+    inv.restore("mixed")
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    inv.run("mixed")
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    total = sum(v[1] for v in tr.values())
+    fix = sum(v[1] for k, v in tr.items() if "fixup" in k)
+    out["fixup_ms"] = round(fix, 4)
+    out["fixup_share_of_kernel_time"] = round(fix / total, 4) if total > 0 else None
+    del inv
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -308,6 +386,27 @@ def run_ours(args, world, rank, local):
         torch.cuda.synchronize()
         results[form] = statistics.mean(ms)
 
+    # one-shot inversion of a model seen for the first time (per-model set-up inside the step)
+    def timed_cold(k):
+        evs = []
+        for _ in range(k):
+            inv.restore("mixed")
+            flush.fill_(1.0)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            inv.run_cold("mixed")
+            b.record(stream)
+            evs.append((a, b))
+        torch.cuda.synchronize()
+        return [a.elapsed_time(b) for a, b in evs]
+
+    timed_cold(args.warmup)
+    barrier(world)
+    torch.cuda.synchronize()
+    ms_cold = statistics.mean(timed_cold(args.steps))
+    barrier(world)
+
     # accuracy against the FP64 run on the same inputs
     inv.restore("fp64")
     inv.run("fp64")
@@ -325,7 +424,19 @@ def run_ours(args, world, rank, local):
         acc[form] = {"mean_rel_err": rel(pm, pm64), "update_rel_err": rel(pm - prior, pm64 - prior),
                      "resid_rel_err": rel(res, res64), "cov_rel_err": rel(cov, cov64),
                      "fp64_bins": st["flagged"] if form == "mixed" else 0, "chol_fail": st["failed"]}
+        if form == "mixed":
+            mixed_out = (pm, res, cov)
+            hist_chol, hist_info = inv.ws.condition_histogram(COND_BUCKETS)
         del pm, res, cov
+    inv.restore("mixed")
+    inv.run_cold("mixed")
+    torch.cuda.synchronize()
+    pmc, resc, covc = inv.results("mixed")
+    acc["mixed_cold"] = {"mean_rel_err": rel(pmc, pm64), "update_rel_err": rel(pmc - prior, pm64 - prior),
+                         "resid_rel_err": rel(resc, res64), "cov_rel_err": rel(covc, cov64),
+                         "identical_to_mixed": bool((pmc == mixed_out[0]).all() and (resc == mixed_out[1]).all()
+                                                    and (covc == mixed_out[2]).all())}
+    del pmc, resc, covc, pm64, res64, cov64
 
     # per-kernel launch times and algorithmic bytes, one traced mixed step
     inv.restore("mixed")
@@ -439,11 +550,25 @@ def run_ours(args, world, rank, local):
     total_bins = bins * world
     value = replicas.whole_job_rate(bins, ms_mixed, world)
 
+    cond_case = conditioning_case(args, stream, flush, rank)
+
     cpu = None
+    vs_cpu64 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        t_full, cores, sample, info = cpu_reference_sample(sc, inv.tables)
-        cpu = {"value": round(bins / t_full / 1e6, 4), "unit": "Mbins/s", "cores": cores, "kind": "port",
-               "sample": sample}
+        threads = os.cpu_count() or 1
+        # the posterior of the mixed GPU form against the CPU FP64 oracle on the same inputs and tables
+        t64, post64, r64, c64, nf64 = cpu_inversion(sc, inv.tables, "d", threads)
+        pm, res, cov = mixed_out
+        vs_cpu64 = {"mean_rel_err": float(f"{rel(pm, post64):.3e}"),
+                    "update_rel_err": float(f"{rel(pm - prior, post64 - prior):.3e}"),
+                    "resid_rel_err": float(f"{rel(res, r64):.3e}"), "cov_rel_err": float(f"{rel(cov, c64):.3e}"),
+                    "oracle_chol_fail": int(nf64), "oracle_s": round(t64["total_s"], 2),
+                    "oracle": "C oracle in FP64, reference dataflow, the GPU's operator tables"}
+        del post64, r64, c64, pm, res, cov
+        tcpu = cpu_inversion(sc, oracle_tables(sc), "f", threads)[0]
+        cpu = {"value": round(bins / tcpu["total_s"] / 1e6, 4), "unit": "Mbins/s", "cores": threads, "kind": "port",
+               "sample": CPU_SAMPLE.format(n=sc.ntheta), "phases_s": {k: round(v, 4) for k, v in tcpu.items()}}
+    del mixed_out
 
     if rank == 0:
         line = {
@@ -456,6 +581,15 @@ def run_ours(args, world, rank, local):
                        "l2": "256 MB flush + ~1.3 GB input restore between timed steps; working set 1.4 GB > L2"},
             "forms_ms": {"plain": round(ms_plain, 4), "fp32": round(ms_fp32, 4), "mixed": round(ms_mixed, 4)},
             "speedup_mixed_vs_plain": round(ms_plain / ms_mixed, 3),
+            "cold_one_shot": {"ms": round(ms_cold, 4), "Mbins_per_s": round(bins / (ms_cold * 1e-3) / 1e6, 1),
+                              "vs_repeated_model": round(ms_cold / ms_mixed, 4),
+                              "what": "mixed form with the model's per-k set-up inside the step: host operator "
+                                      "tables built while the forward transforms run, one upload, the per-k "
+                                      "table kernel (cg_workspace_set_model_async)"},
+            "accuracy_vs_cpu_fp64": vs_cpu64,
+            "condition_histogram": {"buckets": "decades of the squared Cholesky pivot ratio, last = failed",
+                                    "threshold": 1.0e3, "chol_form_fp64": hist_chol, "info_form_fp32": hist_info},
+            "conditioning_stress": cond_case,
             "three_stack_256": three_stack,
             "accuracy_vs_fp64": {f: {k: (float(f"{v:.3e}") if isinstance(v, float) else v) for k, v in d.items()}
                                  for f, d in acc.items()},

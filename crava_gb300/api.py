@@ -292,14 +292,29 @@ class Workspace:
         except Exception:
             pass
 
-    def set_model(self, tables, err_theta_cov, sigma0, wnc, is4d=False, cond_threshold=0.0):
-        self._keep = [np.ascontiguousarray(tables[k], dtype=np.complex64) for k in ("K", "em1", "em2", "em3")]
+    def set_model(self, tables, err_theta_cov, sigma0, wnc, is4d=False, cond_threshold=0.0, stream=None,
+                  asynchronous=False):
+        """Upload the model (host arrays) and build the per-k tables.  asynchronous=True queues the
+        upload and the table kernel on ``stream`` (cg_workspace_set_model_async) instead of waiting."""
+        keep = [np.ascontiguousarray(tables[k], dtype=np.complex64) for k in ("K", "em1", "em2", "em3")]
         band = np.ascontiguousarray(tables["band"], dtype=np.uint8)
         etc = np.ascontiguousarray(err_theta_cov, dtype=np.float64)
         s0 = np.ascontiguousarray(sigma0, dtype=np.float64).reshape(9)
-        m = _Model(self.ntheta, float(wnc), int(is4d), *[a.ctypes.data for a in self._keep], band.ctypes.data,
+        m = _Model(self.ntheta, float(wnc), int(is4d), *[a.ctypes.data for a in keep], band.ctypes.data,
                    etc.ctypes.data, s0.ctypes.data, float(cond_threshold))
-        check(lib().cg_workspace_set_model(self.h, ct.byref(m)), "cg_workspace_set_model")
+        if asynchronous:
+            check(lib().cg_workspace_set_model_async(self.h, ct.byref(m), _stream(stream)),
+                  "cg_workspace_set_model_async")
+        else:
+            check(lib().cg_workspace_set_model(self.h, ct.byref(m)), "cg_workspace_set_model")
+
+    def condition_histogram(self, nbuckets=24, stream=None):
+        """Decade histograms of the in-band bins' condition estimates (cg_condition_histogram): the FP64
+        Cholesky of the data covariance and the FP32 3 x 3 information-form matrix.  Needs prior_spectra."""
+        hc = (ct.c_ulonglong * nbuckets)()
+        hi = (ct.c_ulonglong * nbuckets)()
+        check(lib().cg_condition_histogram(self.h, hc, hi, nbuckets, _stream(stream)), "cg_condition_histogram")
+        return list(hc), list(hi)
 
     def reset_stats(self, stream=None):
         check(lib().cg_workspace_reset_stats(self.h, _stream(stream)), "cg_workspace_reset_stats")

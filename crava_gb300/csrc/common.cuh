@@ -57,7 +57,7 @@ __device__ __forceinline__ T epilogue(T v, int epi)
 // ---------------------------------------------------------------------------
 void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *where);
-// cudaMallocAsync from the device's default pool, which keeps its memory between calls
+// stream-ordered allocation from the library's own per-device pool, which keeps its memory between calls
 cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st);
 
 #define CG_CUDA(call)                                           \

@@ -1,6 +1,7 @@
 // Error text and status plumbing shared by every C-ABI entry point.
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -23,27 +24,41 @@ int cuda_status(cudaError_t e, const char *where)
   return CG_ERR_CUDA;
 }
 
-// Stream-ordered scratch allocation.  The device's default memory pool
-// returns its memory at every synchronisation unless told otherwise, and the
-// next cudaMallocAsync then maps it again; the library's pool keeps what it
-// has (release threshold: unlimited), set once per device.  The attribute
-// belongs to this process's pool, not to the GPU.
+// Stream-ordered scratch allocation from a memory pool of the library's own,
+// one per device, created on first use.  A pool returns its memory at every
+// synchronisation unless told otherwise, and the next allocation then maps it
+// again; this pool keeps what it has (release threshold: unlimited).  It is
+// not the device's default pool, so the host application's own
+// cudaMallocAsync memory keeps the release behaviour the application chose.
+// Scratch is returned with cudaFreeAsync, which finds the pool by itself.
 cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st)
 {
-  static bool done[64] = {};
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev >= 0 && dev < 64 && !done[dev]) {
-    cudaMemPool_t pool;
-    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+  if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, st);
+  cudaMemPool_t pool;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+      cudaMemPoolProps props = {};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t np = nullptr;
+      e = cudaMemPoolCreate(&np, &props);
+      if (e != cudaSuccess) return e;
       unsigned long long keep = ~0ULL;
-      (void)cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+      (void)cudaMemPoolSetAttribute(np, cudaMemPoolAttrReleaseThreshold, &keep);
+      (void)cudaGetLastError();
+      pools[dev] = np;
     }
-    (void)cudaGetLastError();
-    done[dev] = true;
+    pool = pools[dev];
   }
-  return cudaMallocAsync(p, bytes, st);
+  return cudaMallocFromPoolAsync(p, bytes, pool, st);
 }
 
 }  // namespace cg

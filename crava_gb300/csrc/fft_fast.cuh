@@ -612,8 +612,10 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_fast(const __grid_cons
 // host-side dispatch (fft_fast_*.cu): return 1 if a specialisation ran the pass
 int tma_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
              int sign, const float2 *tw, cudaStream_t st);
+// no_alloc keeps the pass off kernels that allocate on first use (the TMA
+// column pass and its device fault word)
 int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
-              int sign, const float2 *tw, cudaStream_t st, int *done_cols);
+              int sign, const float2 *tw, cudaStream_t st, int *done_cols, bool no_alloc = false);
 int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
               const float2 *tw, cudaStream_t st, int epi = kEpiNone);
 // four-step kernels (fft_4step_*.cu); chosen by the tuning table

@@ -147,9 +147,10 @@ int launch_rdp(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long 
 
 template <int N>
 int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
-           const float2 *tw, cudaStream_t st)
+           const float2 *tw, cudaStream_t st, bool no_alloc)
 {
   int kind = cg_tune_get(CG_TUNE_COLS_PIPE, N);
+  if (kind == 5 && no_alloc) kind = 2;  // the TMA pass allocates its fault word on first use
   if (kind == 5) {
     // TMA-fed persistent pass (length 256 along y or z); the register-direct
     // kernel wherever its geometry or alignment does not fit
@@ -182,13 +183,13 @@ int launch(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batc
 // Runs a whole column pass when the length has a specialisation; *done_cols
 // receives how many columns were handled (all of them, or 0).
 int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride, int nbatch,
-              int sign, const float2 *tw, cudaStream_t st, int *done_cols)
+              int sign, const float2 *tw, cudaStream_t st, int *done_cols, bool no_alloc)
 {
   *done_cols = 0;
   if (ncols < 1) return 0;
   int rc = 0;
   switch (n) {
-#define CG_COLS(NN) case NN: rc = launch<NN>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st); break;
+#define CG_COLS(NN) case NN: rc = launch<NN>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st, no_alloc); break;
     CG_COLS(64) CG_COLS(80) CG_COLS(96) CG_COLS(100) CG_COLS(120) CG_COLS(128) CG_COLS(160) CG_COLS(192)
     CG_COLS(200) CG_COLS(240) CG_COLS(256) CG_COLS(320) CG_COLS(384) CG_COLS(400) CG_COLS(480) CG_COLS(512)
 #undef CG_COLS

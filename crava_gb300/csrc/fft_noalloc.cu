@@ -18,10 +18,16 @@
 //
 // The first call on a device looks the array's address up for that device
 // (cudaGetSymbolAddress); make that first call before any stream capture.
+//
+// The column passes never take the TMA-fed kernel here (whatever the tuning
+// table says), because that kernel allocates a device fault word on first
+// use, and the launch tracer is off for these calls (it creates CUDA events).
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 #include "fft_fast.cuh"
+#include "trace.cuh"
 
 namespace cg {
 
@@ -30,8 +36,9 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) float2 g_noalloc_twiddles[kNoAllocTwiddles];
 
-// device-side address of g_noalloc_twiddles, per device
+// device-side address of g_noalloc_twiddles, per device, looked up under the lock
 static float2 *g_noalloc_ptr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mu;
 
 // tw[t] = exp(-2 pi i t / n) for the three axis tables laid out back to back
 __global__ void k_noalloc_twiddles(float2 *tw, int n0, int n1, int n2)
@@ -55,6 +62,7 @@ static int noalloc_setup(float2 **ptr)
     set_error("device %d beyond the %d devices the no-allocation transforms support", dev, kNoAllocMaxDevices);
     return CG_ERR_UNSUPPORTED;
   }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
   if (!g_noalloc_ptr[dev]) {
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_twiddles);
@@ -104,6 +112,7 @@ static int noalloc_fft(float *buf, int nxp, int nyp, int nzp, int cubetype, bool
   float2 *tw = nullptr;
   int rc = noalloc_setup(&tw);
   if (rc) return rc;
+  TraceSuppress quiet;
   const float2 *twx = tw, *twy = tw + nxp, *twz = tw + nxp + nyp;
   k_noalloc_twiddles<<<ceil_div((long)nxp + nyp + nzp, 256), 256, 0, st>>>(tw, nxp, nyp, nzp);
   CG_CHECK_LAUNCH("k_noalloc_twiddles");
@@ -116,7 +125,7 @@ static int noalloc_fft(float *buf, int nxp, int nyp, int nzp, int cubetype, bool
   int done = 0;
   auto cols = [&](int n, long axis_stride, long batch_stride, int nbatch, const float2 *t, int sign) -> int {
     if (n == 1) return CG_OK;
-    int r = fast_cols(cs, 1, n, cnxp, axis_stride, batch_stride, nbatch, sign, t, st, &done);
+    int r = fast_cols(cs, 1, n, cnxp, axis_stride, batch_stride, nbatch, sign, t, st, &done, /*no_alloc=*/true);
     if (r < 0) return r;
     if (r == 0 || done != cnxp) {
       set_error("axis length %d has no specialised transform; the no-allocation transforms support 64, 80, 96, "

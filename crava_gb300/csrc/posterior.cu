@@ -522,155 +522,6 @@ __global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, cons
   }
 }
 
-// per-k tables (double), one thread per k
-__global__ void k_prep_tables(int nzp, int nt, const float2 *K, const float2 *em1, const float2 *em2,
-                              const float2 *em3, const unsigned char *band, const double *etc, S0Args s0, float wnc,
-                              KTab<float> *tf, KTab<double> *td)
-{
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nzp) return;
-  KTab<double> t;
-  memset(&t, 0, sizeof(t));
-  for (int l = 0; l < nt; l++)
-    for (int p = 0; p < 3; p++) {
-      float2 v = K[((long)k * nt + l) * 3 + p];
-      t.K[l][p] = make_double2(v.x, v.y);
-    }
-  for (int l = 0; l < nt; l++)
-    for (int p = 0; p < 3; p++) {
-      double2 acc = make_double2(0, 0);
-      for (int q = 0; q < 3; q++) {
-        acc.x += t.K[l][q].x * s0.v[q * 3 + p];
-        acc.y += t.K[l][q].y * s0.v[q * 3 + p];
-      }
-      t.KS0[l][p] = acc;
-    }
-  const double c0 = 0.5 * (1.0 - (double)wnc);
-  for (int l = 0; l < nt; l++) {
-    float2 e1l = em1[(long)k * nt + l], e2l = em2[(long)k * nt + l];
-    for (int m = 0; m <= l; m++) {
-      double2 acc = make_double2(0, 0);
-      for (int p = 0; p < 3; p++) acc = cadd<double>(acc, cmulc<double>(t.KS0[l][p], t.K[m][p]));
-      t.M[tri(l, m)] = acc;
-      float2 e1m = em1[(long)k * nt + m], e2m = em2[(long)k * nt + m];
-      double re = (double)e1l.x * e1m.x + (double)e1l.y * e1m.y + (double)e2l.x * e2m.x + (double)e2l.y * e2m.y;
-      double im = (-(double)e1l.x * e1m.y + (double)e1l.y * e1m.x) + (-(double)e2l.x * e2m.y + (double)e2l.y * e2m.x);
-      double f = c0 * etc[l * nt + m];
-      t.E[tri(l, m)] = l == m ? make_double2(f * re, 0.0) : make_double2(f * re, f * im);
-    }
-    float2 e3 = em3[(long)k * nt + l];
-    t.D[l] = (double)wnc * etc[l * nt + l] * (double)e3.x * (double)e3.x;
-  }
-  t.band = band[k];
-  td[k] = t;
-  KTab<float> f;
-  memset(&f, 0, sizeof(f));
-  for (int l = 0; l < kMaxTheta; l++)
-    for (int p = 0; p < 3; p++) {
-      f.K[l][p] = make_float2((float)t.K[l][p].x, (float)t.K[l][p].y);
-      f.KS0[l][p] = make_float2((float)t.KS0[l][p].x, (float)t.KS0[l][p].y);
-    }
-  for (int q = 0; q < kTri; q++) {
-    f.M[q] = make_float2((float)t.M[q].x, (float)t.M[q].y);
-    f.E[q] = make_float2((float)t.E[q].x, (float)t.E[q].y);
-  }
-  for (int l = 0; l < kMaxTheta; l++) f.D[l] = (float)t.D[l];
-  f.band = t.band;
-  tf[k] = f;
-}
-
-// Hermitian eigen-decomposition of an n x n matrix (row-major, destroyed):
-// cyclic Jacobi, each rotation the real one on |a_pq| after the phase
-// diag(1, e^-i arg a_pq) on (p, q); eigenvalues Re a_ii, eigenvectors the
-// columns of v.
-__device__ void herm_jacobi(double2 *a, double2 *v, int n)
-{
-  for (int i = 0; i < n * n; i++) v[i] = make_double2(i % (n + 1) == 0 ? 1.0 : 0.0, 0.0);
-  for (int sweep = 0; sweep < 50; sweep++) {
-    double off = 0.0, diag = 0.0;
-    for (int p = 0; p < n; p++) {
-      diag += a[p * n + p].x * a[p * n + p].x;
-      for (int q = p + 1; q < n; q++) off += a[p * n + q].x * a[p * n + q].x + a[p * n + q].y * a[p * n + q].y;
-    }
-    if (off <= 1e-30 * diag || off == 0.0) break;
-    for (int p = 0; p < n - 1; p++)
-      for (int q = p + 1; q < n; q++) {
-        const double2 apq = a[p * n + q];
-        const double mag = sqrt(apq.x * apq.x + apq.y * apq.y);
-        if (mag == 0.0) continue;
-        const double2 e = make_double2(apq.x / mag, -apq.y / mag);  // e^{-i arg a_pq}
-        const double2 ec = make_double2(e.x, -e.y);
-        const double th = (a[q * n + q].x - a[p * n + p].x) / (2.0 * mag);
-        const double t = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
-        for (int k = 0; k < n; k++) {
-          const double2 akp = a[k * n + p], akq = cmul<double>(e, a[k * n + q]);
-          a[k * n + p] = make_double2(c * akp.x - sn * akq.x, c * akp.y - sn * akq.y);
-          a[k * n + q] = make_double2(sn * akp.x + c * akq.x, sn * akp.y + c * akq.y);
-        }
-        for (int k = 0; k < n; k++) {
-          const double2 apk = a[p * n + k], aqk = cmul<double>(ec, a[q * n + k]);
-          a[p * n + k] = make_double2(c * apk.x - sn * aqk.x, c * apk.y - sn * aqk.y);
-          a[q * n + k] = make_double2(sn * apk.x + c * aqk.x, sn * apk.y + c * aqk.y);
-        }
-        for (int k = 0; k < n; k++) {
-          const double2 vkp = v[k * n + p], vkq = cmul<double>(e, v[k * n + q]);
-          v[k * n + p] = make_double2(c * vkp.x - sn * vkq.x, c * vkp.y - sn * vkq.y);
-          v[k * n + q] = make_double2(sn * vkp.x + c * vkq.x, sn * vkp.y + c * vkq.y);
-        }
-      }
-  }
-}
-
-// information-form tables of plane k from the FP64 tables; *bad counts
-// in-band planes with a diagonal error term that is not positive
-__global__ void k_prep_info(int nzp, int nt, const KTab<double> *__restrict__ td, ITab *ti, int *bad)
-{
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nzp) return;
-  const KTab<double> &t = td[k];
-  ITab o;
-  memset(&o, 0, sizeof(o));
-  o.band = t.band;
-  for (int l = 0; l < nt; l++)
-    for (int p = 0; p < 3; p++) o.K[l][p] = make_float2((float)t.K[l][p].x, (float)t.K[l][p].y);
-  bool ok = true;
-  for (int l = 0; l < nt; l++) ok = ok && t.D[l] > 0.0;
-  if (!ok) {
-    if (t.band) atomicAdd(bad, 1);
-    ti[k] = o;
-    return;
-  }
-  double2 a[kMaxTheta * kMaxTheta], v[kMaxTheta * kMaxTheta];
-  double dm[kMaxTheta];
-  for (int l = 0; l < nt; l++) dm[l] = 1.0 / sqrt(t.D[l]);
-  for (int l = 0; l < nt; l++)
-    for (int m = 0; m < nt; m++) {
-      const double2 e = l >= m ? t.E[tri(l, m)] : make_double2(t.E[tri(m, l)].x, -t.E[tri(m, l)].y);
-      a[l * nt + m] = make_double2(dm[l] * e.x * dm[m], dm[l] * e.y * dm[m]);
-    }
-  herm_jacobi(a, v, nt);
-  for (int m = 0; m < nt; m++) {
-    o.mu[m] = (float)(a[m * nt + m].x > 0.0 ? a[m * nt + m].x : 0.0);
-    double2 g[3] = {make_double2(0, 0), make_double2(0, 0), make_double2(0, 0)};
-    for (int l = 0; l < nt; l++) {
-      const double2 vl = make_double2(dm[l] * v[l * nt + m].x, dm[l] * v[l * nt + m].y);
-      o.V[l][m] = make_float2((float)vl.x, (float)vl.y);
-      for (int p = 0; p < 3; p++) g[p] = cadd<double>(g[p], cmul<double>(make_double2(t.K[l][p].x, -t.K[l][p].y), vl));
-    }
-    for (int p = 0; p < 3; p++) o.G[m][p] = make_float2((float)g[p].x, (float)g[p].y);
-    // g g^H: entry (p, q) = g_p conj(g_q)
-    const int pq[3][2] = {{0, 1}, {0, 2}, {1, 2}};
-    for (int p = 0; p < 3; p++) o.P[m][p] = (float)(g[p].x * g[p].x + g[p].y * g[p].y);
-    for (int j = 0; j < 3; j++) {
-      const double2 x = cmulc<double>(g[pq[j][0]], g[pq[j][1]]);
-      o.P[m][3 + 2 * j] = (float)x.x;
-      o.P[m][4 + 2 * j] = (float)x.y;
-    }
-  }
-  ti[k] = o;
-}
-
 __global__ void k_f2d(const float *in, double *out, long n)
 {
   long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -714,12 +565,22 @@ extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp,
 #define WS_ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (bytes))
   WS_ALLOC(w->ktab_f, sizeof(KTab<float>) * nzp);
   WS_ALLOC(w->ktab_d, sizeof(KTab<double>) * nzp);
-  WS_ALLOC(w->K, sizeof(float2) * (size_t)nzp * ntheta * 3);
-  WS_ALLOC(w->em1, sizeof(float2) * (size_t)nzp * ntheta);
-  WS_ALLOC(w->em2, sizeof(float2) * (size_t)nzp * ntheta);
-  WS_ALLOC(w->em3, sizeof(float2) * (size_t)nzp * ntheta);
-  WS_ALLOC(w->band, (size_t)nzp);
-  WS_ALLOC(w->etc, sizeof(double) * ntheta * ntheta);
+  // uploaded tables, packed in one block: etc | K | em1 | em2 | em3 | band
+  const size_t o_k = sizeof(double) * ntheta * ntheta, n_k = sizeof(float2) * (size_t)nzp * ntheta * 3;
+  const size_t n_em = sizeof(float2) * (size_t)nzp * ntheta;
+  w->model_bytes = o_k + n_k + 3 * n_em + (size_t)nzp;
+  WS_ALLOC(w->model_dev, w->model_bytes);
+  if (e == cudaSuccess) e = cudaMallocHost(&w->model_host, w->model_bytes);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->model_copied, cudaEventDisableTiming);
+  if (e == cudaSuccess) {
+    char *base = (char *)w->model_dev;
+    w->etc = (double *)base;
+    w->K = (float2 *)(base + o_k);
+    w->em1 = (float2 *)(base + o_k + n_k);
+    w->em2 = (float2 *)(base + o_k + n_k + n_em);
+    w->em3 = (float2 *)(base + o_k + n_k + 2 * n_em);
+    w->band = (unsigned char *)(base + o_k + n_k + 3 * n_em);
+  }
   WS_ALLOC(w->cxy_f, sizeof(float) * 2 * (size_t)cnxp * nyp);
   WS_ALLOC(w->ct_f, sizeof(float) * 2 * (size_t)cnzp);
   WS_ALLOC(w->cxy_d, sizeof(double) * 2 * (size_t)cnxp * nyp);
@@ -740,14 +601,19 @@ extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp,
 extern "C" void cg_workspace_destroy(cg_workspace w)
 {
   if (!w) return;
-  void *ptrs[] = {w->ktab_f, w->ktab_d, w->K, w->em1, w->em2, w->em3, w->band, w->etc,
-                  w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters, w->itab};
+  void *ptrs[] = {w->ktab_f, w->ktab_d, w->model_dev, w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters,
+                  w->itab};
+  if (w->model_copied) {
+    cudaEventSynchronize(w->model_copied);
+    cudaEventDestroy(w->model_copied);
+  }
+  if (w->model_host) cudaFreeHost(w->model_host);
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete w;
 }
 
-extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
+extern "C" int cg_workspace_set_model_async(cg_workspace w, const cg_model *m, void *stream)
 {
   if (!w || !m) { set_error("null argument"); return CG_ERR_ARG; }
   if (m->ntheta != w->ntheta) { set_error("model ntheta %d != workspace ntheta %d", m->ntheta, w->ntheta); return CG_ERR_ARG; }
@@ -755,39 +621,61 @@ extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
     set_error("model table pointer is null");
     return CG_ERR_ARG;
   }
+  int dev = -1;
+  CG_CUDA(cudaGetDevice(&dev));
+  if (dev != w->device) { set_error("workspace belongs to device %d, current device is %d", w->device, dev); return CG_ERR_STATE; }
+  cudaStream_t st = (cudaStream_t)stream;
   const int nt = w->ntheta, nzp = w->nzp;
+  // the previous model's upload must have left the staging copy
+  CG_CUDA(cudaEventSynchronize(w->model_copied));
+  char *h = (char *)w->model_host;
+  const size_t n_etc = sizeof(double) * nt * nt, n_k = sizeof(float2) * (size_t)nzp * nt * 3;
+  const size_t n_em = sizeof(float2) * (size_t)nzp * nt;
+  memcpy(h, m->err_theta_cov, n_etc);
+  memcpy(h + n_etc, m->K, n_k);
+  memcpy(h + n_etc + n_k, m->em1, n_em);
+  memcpy(h + n_etc + n_k + n_em, m->em2, n_em);
+  memcpy(h + n_etc + n_k + 2 * n_em, m->em3, n_em);
+  memcpy(h + n_etc + n_k + 3 * n_em, m->band, (size_t)nzp);
+  CG_CUDA(cudaMemcpyAsync(w->model_dev, w->model_host, w->model_bytes, cudaMemcpyHostToDevice, st));
+  CG_CUDA(cudaEventRecord(w->model_copied, st));
   w->wnc = m->wnc;
   w->is4d = m->is4d;
   w->cond_threshold = m->cond_threshold > 0 ? m->cond_threshold : 1.0e3;
   for (int t = 0; t < 9; t++) { w->sigma0[t] = m->sigma0[t]; w->sigma0f[t] = (float)m->sigma0[t]; }
-  CG_CUDA(cudaMemcpy(w->K, m->K, sizeof(float2) * (size_t)nzp * nt * 3, cudaMemcpyHostToDevice));
-  CG_CUDA(cudaMemcpy(w->em1, m->em1, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
-  CG_CUDA(cudaMemcpy(w->em2, m->em2, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
-  CG_CUDA(cudaMemcpy(w->em3, m->em3, sizeof(float2) * (size_t)nzp * nt, cudaMemcpyHostToDevice));
-  CG_CUDA(cudaMemcpy(w->band, m->band, (size_t)nzp, cudaMemcpyHostToDevice));
   long nb = 0;
   for (int k = 0; k < nzp; k++) nb += m->band[k] ? 1 : 0;
   w->inband_bins = nb * (long)(w->nxp / 2 + 1) * w->nyp;
-  CG_CUDA(cudaMemcpy(w->etc, m->err_theta_cov, sizeof(double) * nt * nt, cudaMemcpyHostToDevice));
-  S0Args s0;
+  PrepArgs pa;
+  pa.nt = nt;
+  pa.wnc = m->wnc;
+  pa.is4d = m->is4d;
+  pa.K = w->K; pa.em1 = w->em1; pa.em2 = w->em2; pa.em3 = w->em3; pa.band = w->band; pa.etc = w->etc;
   // the prior the reference multiplies into the covariance cubes is float(priorVar0)
-  for (int t = 0; t < 9; t++) s0.v[t] = (double)(float)m->sigma0[t];
-  k_prep_tables<<<ceil_div(nzp, 64), 64>>>(nzp, nt, w->K, w->em1, w->em2, w->em3, w->band, w->etc, s0, w->wnc,
-                                           w->ktab_f, w->ktab_d);
-  CG_CHECK_LAUNCH("k_prep_tables");
-  // information-form tables (3D model, every in-band D > 0); bad counts planes without them
+  for (int t = 0; t < 9; t++) pa.s0[t] = (double)(float)m->sigma0[t];
+  pa.tf = w->ktab_f; pa.td = w->ktab_d; pa.ti = w->itab;
+  {
+    TraceScope ts("k_prep_model", st, 0.0);
+    k_prep_model<<<nzp, 32, 0, st>>>(pa);
+    CG_CHECK_LAUNCH("k_prep_model");
+  }
+  // The information form needs a 3D model with a positive error diagonal in every in-band plane
+  // (D_l = wnc errThetaCov_ll (Re e3_l)^2, the product the set-up kernel forms) and an invertible prior.
   w->info_ok = false;
   if (!w->is4d) {
-    CG_CUDA(cudaMemset(w->counters + 3, 0, sizeof(int)));
-    k_prep_info<<<ceil_div(nzp, 64), 64>>>(nzp, nt, w->ktab_d, w->itab, w->counters + 3);
-    CG_CHECK_LAUNCH("k_prep_info");
-    int bad = 1;
-    CG_CUDA(cudaMemcpy(&bad, w->counters + 3, sizeof(int), cudaMemcpyDeviceToHost));
+    bool pos = true;
+    for (int k = 0; k < nzp && pos; k++) {
+      if (!m->band[k]) continue;
+      for (int l = 0; l < nt; l++) {
+        const double e3 = (double)m->em3[2 * ((long)k * nt + l)];
+        if (!((double)m->wnc * m->err_theta_cov[l * nt + l] * e3 * e3 > 0.0)) { pos = false; break; }
+      }
+    }
     // Sigma0^-1 (the float prior the tables use) by cofactors in double
-    const double *a = s0.v;
+    const double *a = pa.s0;
     const double det = a[0] * (a[4] * a[8] - a[5] * a[7]) - a[1] * (a[3] * a[8] - a[5] * a[6]) +
                        a[2] * (a[3] * a[7] - a[4] * a[6]);
-    if (bad == 0 && det > 0.0) {
+    if (pos && det > 0.0) {
       const double i00 = (a[4] * a[8] - a[5] * a[7]) / det, i11 = (a[0] * a[8] - a[2] * a[6]) / det;
       const double i22 = (a[0] * a[4] - a[1] * a[3]) / det, i01 = -(a[1] * a[8] - a[2] * a[7]) / det;
       const double i02 = (a[1] * a[5] - a[2] * a[4]) / det, i12 = -(a[0] * a[5] - a[2] * a[3]) / det;
@@ -796,8 +684,15 @@ extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
       w->info_ok = true;
     }
   }
-  CG_CUDA(cudaDeviceSynchronize());
   w->model_set = true;
+  return CG_OK;
+}
+
+extern "C" int cg_workspace_set_model(cg_workspace w, const cg_model *m)
+{
+  const int rc = cg_workspace_set_model_async(w, m, nullptr);
+  if (rc) return rc;
+  CG_CUDA(cudaDeviceSynchronize());
   return CG_OK;
 }
 
@@ -1082,4 +977,113 @@ extern "C" int cg_invert_bins_fused_f64(cg_workspace w, double *const *data, dou
   if (w->is4d) { set_error("the fused form needs a separable 3-parameter prior"); return CG_ERR_UNSUPPORTED; }
   return fused_launch<double>(w, (void *const *)data, (void *const *)mean, (void *const *)cov, CG_PREC_FP64,
                               (cudaStream_t)stream);
+}
+
+// ---------------------------------------------------------------------------
+// Condition estimates of the in-band bins (diagnostic)
+// ---------------------------------------------------------------------------
+namespace cg {
+
+// One thread per bin of plane blockIdx.y.  hist[0 .. nb-1]: FP64 Cholesky of
+// Sd = s M + lam E + D (the Cholesky form's guard estimate: squared ratio of
+// the largest to the smallest pivot), hist[nb .. 2nb-1]: the 3 x 3
+// information-form matrix in FP32, computed as the default kernel's guard
+// does.  Bucket floor(log10(cond)) clamped to 0 .. nb-2; bucket nb-1 counts
+// failed factorisations.
+template <int NT>
+__global__ void __launch_bounds__(128) k_cond_hist(const float2 *__restrict__ cxy, const float2 *__restrict__ ct,
+                                                   const KTab<double> *__restrict__ ktd, const ITab *__restrict__ itab,
+                                                   InfoArgs ia, int plane, int nzp, bool info,
+                                                   unsigned long long *hist, int nb)
+{
+  __shared__ unsigned int h[2 * kCondBucketsMax];
+  for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const int k = blockIdx.y;
+  const int ij = blockIdx.x * blockDim.x + threadIdx.x;
+  const KTab<double> &kt = ktd[k];
+  if (ij < plane && kt.band) {
+    const int cnzp = nzp / 2 + 1;
+    const float2 cx = cxy[ij];
+    const float2 t = k < cnzp ? ct[k] : make_float2(ct[nzp - k].x, -ct[nzp - k].y);
+    const float sf = fabsf(cx.x * t.x - cx.y * t.y), lamf = fabsf(cx.x);
+    {
+      double2 L[NT * (NT + 1) / 2];
+      double inv[NT], cond = 0.0;
+      build_sd<double, NT>(kt, (double)sf, (double)lamf, L);
+      const bool ok = chol_std<double, NT>(L, inv, cond);
+      const int b = ok ? min(max((int)floor(log10(cond)), 0), nb - 2) : nb - 1;
+      atomicAdd(&h[b], 1u);
+    }
+    if (info && sf > 0.0f) {
+      const ITab &it = itab[k];
+      const float is = 1.0f / sf;
+      float q00 = ia.s0i[0] * is, q11 = ia.s0i[1] * is, q22 = ia.s0i[2] * is;
+      float2 q01 = make_float2(ia.s0i[3] * is, 0.0f), q02 = make_float2(ia.s0i[4] * is, 0.0f),
+             q12 = make_float2(ia.s0i[5] * is, 0.0f);
+#pragma unroll
+      for (int m = 0; m < NT; m++) {
+        const float w = 1.0f / (lamf * it.mu[m] + 1.0f);
+        const float *P = it.P[m];
+        q00 += w * P[0]; q11 += w * P[1]; q22 += w * P[2];
+        q01.x += w * P[3]; q01.y += w * P[4];
+        q02.x += w * P[5]; q02.y += w * P[6];
+        q12.x += w * P[7]; q12.y += w * P[8];
+      }
+      bool ok = q00 > 0.0f;
+      const float r0 = rsqrtf(q00), l00 = q00 * r0;
+      const float2 l10 = make_float2(q01.x * r0, -q01.y * r0), l20 = make_float2(q02.x * r0, -q02.y * r0);
+      const float p1 = q11 - (l10.x * l10.x + l10.y * l10.y);
+      ok = ok && p1 > 0.0f;
+      const float r1 = rsqrtf(p1), l11 = p1 * r1;
+      const float2 t21 = csub<float>(make_float2(q12.x, -q12.y), cmulc<float>(l20, l10));
+      const float2 l21 = make_float2(t21.x * r1, t21.y * r1);
+      const float p2 = q22 - (l20.x * l20.x + l20.y * l20.y) - (l21.x * l21.x + l21.y * l21.y);
+      ok = ok && p2 > 0.0f;
+      const float l22 = p2 * rsqrtf(p2);
+      const float dmax = fmaxf(l00, fmaxf(l11, l22)), dmin = fminf(l00, fminf(l11, l22));
+      const float cond = (dmax / dmin) * (dmax / dmin);
+      const int b = ok ? min(max((int)floorf(log10f(cond)), 0), nb - 2) : nb - 1;
+      atomicAdd(&h[nb + b], 1u);
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < 2 * nb; i += blockDim.x)
+    if (h[i]) atomicAdd(&hist[i], (unsigned long long)h[i]);
+}
+
+}  // namespace cg
+
+extern "C" int cg_condition_histogram(cg_workspace w, unsigned long long *hist_chol, unsigned long long *hist_info,
+                                      int nbuckets, void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (!hist_chol || !hist_info) { set_error("null histogram"); return CG_ERR_ARG; }
+  if (nbuckets < 2 || nbuckets > kCondBucketsMax) { set_error("nbuckets %d outside 2..%d", nbuckets, kCondBucketsMax); return CG_ERR_ARG; }
+  if (w->is4d) { set_error("the condition histogram covers the fused form's 3D model"); return CG_ERR_UNSUPPORTED; }
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long *d = nullptr;
+  CG_CUDA(scratch_alloc((void **)&d, sizeof(unsigned long long) * 2 * nbuckets, st));
+  cudaError_t e = cudaMemsetAsync(d, 0, sizeof(unsigned long long) * 2 * nbuckets, st);
+  InfoArgs ia;
+  for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
+  const int plane = (w->nxp / 2 + 1) * w->nyp;
+  const dim3 grid(ceil_div(plane, 128), w->nzp);
+  if (e == cudaSuccess) {
+    rc = dispatch_nt(w->ntheta, [&](auto NTc) -> int {
+      constexpr int NT = decltype(NTc)::value;
+      k_cond_hist<NT><<<grid, 128, 0, st>>>((const float2 *)w->cxy_f, (const float2 *)w->ct_f, w->ktab_d, w->itab,
+                                            ia, plane, w->nzp, w->info_ok, d, nbuckets);
+      return CG_OK;
+    });
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hist_chol, d, sizeof(unsigned long long) * nbuckets, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hist_info, d + nbuckets, sizeof(unsigned long long) * nbuckets, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(d, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_status(e, "cg_condition_histogram");
+  return rc;
 }

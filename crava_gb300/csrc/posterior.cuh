@@ -8,6 +8,7 @@ namespace cg {
 constexpr int kMaxTheta = 8;
 constexpr int kTri = kMaxTheta * (kMaxTheta + 1) / 2;
 constexpr double kCholTol = 1e-20;  // lib_matr.c:19, applied to the pivots scaled by A00
+constexpr int kCondBucketsMax = 32;  // buckets of cg_condition_histogram
 
 __host__ __device__ constexpr int tri(int l, int m) { return l * (l + 1) / 2 + m; }  // l >= m
 
@@ -48,6 +49,22 @@ struct ITab {
   int pad_[3];
 };
 
+// Arguments of the per-model set-up kernel (prep.cu): the uploaded
+// reference-order tables in, the per-k tables out.
+struct PrepArgs {
+  int nt;
+  float wnc;
+  int is4d;
+  const float2 *K, *em1, *em2, *em3;
+  const unsigned char *band;
+  const double *etc;
+  double s0[9];  // float(priorVar0) widened, row-major
+  KTab<float> *tf;
+  KTab<double> *td;
+  ITab *ti;
+};
+__global__ void k_prep_model(const __grid_constant__ PrepArgs p);
+
 // Opaque workspace behind cg_workspace (device buffers of one model).
 struct Workspace {
   int device;
@@ -60,6 +77,13 @@ struct Workspace {
   // per-model tables (device)
   KTab<float> *ktab_f;
   KTab<double> *ktab_d;
+  // uploaded model tables: one device block and its pinned host staging copy
+  // (one host-to-device copy per model; the event marks when the staging
+  // copy may be rewritten)
+  void *model_dev;
+  void *model_host;
+  size_t model_bytes;
+  cudaEvent_t model_copied;
   float2 *K;        // nzp*ntheta*3 (reference-order tables for the plain path)
   float2 *em1, *em2, *em3;
   unsigned char *band;

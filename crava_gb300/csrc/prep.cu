@@ -1,0 +1,230 @@
+// Per-model set-up of the fused bin kernels: for every temporal frequency k,
+// the operator and error tables of the Cholesky form (KTab, FP64 and FP32)
+// and the information-form tables (ITab).  This is the GPU counterpart of
+// the per-k work the reference does inside its bin loop before the bins of a
+// plane (Crava::fillErrMultVectors products and getNextErrorVariance's
+// per-k factors, src/crava.cpp:1108-1120, :1337-1386, :1442-1469).
+//
+// One warp per k.  The lanes build the table entries in parallel (an entry
+// per lane), and the information form's Hermitian eigen-decomposition is a
+// parallel Jacobi: in each step the lanes compute the rotations of up to four
+// disjoint index pairs at once (round-robin pairing), then apply them to the
+// columns, the eigenvectors and the rows with one matrix element per lane.
+// FP64 throughout; the FP64 rate of this GPU is low, so the work is spread
+// over one warp per plane on all SMs instead of one thread per plane.
+#include "posterior.cuh"
+
+namespace cg {
+
+namespace {
+
+constexpr int kPrepSweeps = 40;
+
+// packed lower-triangle index t -> (l, m), l >= m
+__device__ __forceinline__ void tri_lm(int t, int &l, int &m)
+{
+  l = 0;
+  while ((l + 1) * (l + 2) / 2 <= t) l++;
+  m = t - l * (l + 1) / 2;
+}
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepArgs p)
+{
+  const int k = blockIdx.x;
+  const int lane = threadIdx.x;
+  const int nt = p.nt;
+  __shared__ KTab<double> t;
+  __shared__ KTab<float> f;
+  __shared__ ITab o;
+  __shared__ double2 a[kMaxTheta][kMaxTheta], v[kMaxTheta][kMaxTheta], g[kMaxTheta][3];
+  __shared__ double dm[kMaxTheta];
+  __shared__ double rc[kMaxTheta / 2], rsn[kMaxTheta / 2];
+  __shared__ double2 rph[kMaxTheta / 2];
+  __shared__ int rp[kMaxTheta / 2], rq[kMaxTheta / 2];
+
+  for (int i = lane; i < (int)(sizeof(KTab<double>) / sizeof(double)); i += 32) ((double *)&t)[i] = 0.0;
+  for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) ((float *)&f)[i] = 0.0f;
+  for (int i = lane; i < (int)(sizeof(ITab) / sizeof(float)); i += 32) ((float *)&o)[i] = 0.0f;
+  __syncwarp();
+
+  // K (ntheta x 3) and K S0
+  for (int i = lane; i < nt * 3; i += 32) {
+    const float2 kv = p.K[((long)k * nt) * 3 + i];
+    t.K[i / 3][i % 3] = make_double2(kv.x, kv.y);
+  }
+  __syncwarp();
+  for (int i = lane; i < nt * 3; i += 32) {
+    const int l = i / 3, c = i % 3;
+    double2 acc = make_double2(0, 0);
+    for (int q = 0; q < 3; q++) {
+      acc.x += t.K[l][q].x * p.s0[q * 3 + c];
+      acc.y += t.K[l][q].y * p.s0[q * 3 + c];
+    }
+    t.KS0[l][c] = acc;
+  }
+  __syncwarp();
+  // M = K S0 K^H and E = 0.5 (1 - wnc) errThetaCov (e1 e1^H + e2 e2^H), lower triangles
+  const double c0 = 0.5 * (1.0 - (double)p.wnc);
+  for (int i = lane; i < nt * (nt + 1) / 2; i += 32) {
+    int l, m;
+    tri_lm(i, l, m);
+    double2 acc = make_double2(0, 0);
+    for (int c = 0; c < 3; c++) acc = cadd<double>(acc, cmulc<double>(t.KS0[l][c], t.K[m][c]));
+    t.M[i] = acc;
+    const float2 e1l = p.em1[(long)k * nt + l], e2l = p.em2[(long)k * nt + l];
+    const float2 e1m = p.em1[(long)k * nt + m], e2m = p.em2[(long)k * nt + m];
+    const double re = (double)e1l.x * e1m.x + (double)e1l.y * e1m.y + (double)e2l.x * e2m.x + (double)e2l.y * e2m.y;
+    const double im = (-(double)e1l.x * e1m.y + (double)e1l.y * e1m.x) + (-(double)e2l.x * e2m.y + (double)e2l.y * e2m.x);
+    const double fc = c0 * p.etc[l * nt + m];
+    t.E[i] = l == m ? make_double2(fc * re, 0.0) : make_double2(fc * re, fc * im);
+  }
+  // D = wnc errThetaCov_ll |Re e3_l|^2
+  for (int l = lane; l < nt; l += 32) {
+    const float2 e3 = p.em3[(long)k * nt + l];
+    t.D[l] = (double)p.wnc * p.etc[l * nt + l] * (double)e3.x * (double)e3.x;
+  }
+  if (lane == 0) t.band = p.band[k];
+  __syncwarp();
+
+  // FP32 copy of the tables
+  for (int i = lane; i < kMaxTheta * 3; i += 32) {
+    const int l = i / 3, c = i % 3;
+    f.K[l][c] = make_float2((float)t.K[l][c].x, (float)t.K[l][c].y);
+    f.KS0[l][c] = make_float2((float)t.KS0[l][c].x, (float)t.KS0[l][c].y);
+  }
+  for (int i = lane; i < kTri; i += 32) {
+    f.M[i] = make_float2((float)t.M[i].x, (float)t.M[i].y);
+    f.E[i] = make_float2((float)t.E[i].x, (float)t.E[i].y);
+  }
+  for (int l = lane; l < kMaxTheta; l += 32) f.D[l] = (float)t.D[l];
+  if (lane == 0) f.band = t.band;
+  __syncwarp();
+  {
+    const double *src = (const double *)&t;
+    double *dst = (double *)&p.td[k];
+    for (int i = lane; i < (int)(sizeof(KTab<double>) / sizeof(double)); i += 32) dst[i] = src[i];
+    const float *fs = (const float *)&f;
+    float *fd = (float *)&p.tf[k];
+    for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) fd[i] = fs[i];
+  }
+  if (p.is4d) return;
+
+  // information form: D^-1/2 E D^-1/2 = U diag(mu) U^H, v_m = D^-1/2 u_m, g_m = K^H v_m
+  for (int i = lane; i < nt * 3; i += 32) o.K[i / 3][i % 3] = f.K[i / 3][i % 3];
+  if (lane == 0) o.band = t.band;
+  bool ok = true;
+  for (int l = 0; l < nt; l++) ok = ok && t.D[l] > 0.0;
+  __syncwarp();
+  if (ok) {
+    for (int l = lane; l < nt; l += 32) dm[l] = 1.0 / sqrt(t.D[l]);
+    __syncwarp();
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      const double2 e = l >= m ? t.E[tri(l, m)] : make_double2(t.E[tri(m, l)].x, -t.E[tri(m, l)].y);
+      a[l][m] = make_double2(dm[l] * e.x * dm[m], dm[l] * e.y * dm[m]);
+      v[l][m] = make_double2(l == m ? 1.0 : 0.0, 0.0);
+    }
+    __syncwarp();
+    // parallel cyclic Jacobi over an even number of indices (index nt is a
+    // dummy when nt is odd: its pairs are skipped)
+    const int ne = nt + (nt & 1), np = ne / 2;
+    for (int sweep = 0; sweep < kPrepSweeps; sweep++) {
+      double off = 0.0, diag = 0.0;
+      for (int i = lane; i < nt * nt; i += 32) {
+        const int l = i / nt, m = i % nt;
+        if (l == m) diag += a[l][l].x * a[l][l].x;
+        else if (m > l) off += a[l][m].x * a[l][m].x + a[l][m].y * a[l][m].y;
+      }
+      off = warp_sum(off);
+      diag = warp_sum(diag);
+      if (off <= 1e-30 * diag || off == 0.0) break;
+      for (int r = 0; r < ne - 1; r++) {
+        if (lane < np) {
+          int i0, i1;
+          if (lane == 0) { i0 = ne - 1; i1 = r; }
+          else { i0 = (r + lane) % (ne - 1); i1 = (r - lane + ne - 1) % (ne - 1); }
+          const int pp = min(i0, i1), qq = max(i0, i1);
+          double c = 1.0, s = 0.0;
+          double2 e = make_double2(1.0, 0.0);
+          if (qq < nt) {
+            const double2 apq = a[pp][qq];
+            const double mag2 = apq.x * apq.x + apq.y * apq.y;
+            if (mag2 > 0.0) {
+              const double ri = rsqrt(mag2);
+              e = make_double2(apq.x * ri, -apq.y * ri);  // e^{-i arg a_pq}
+              const double th = (a[qq][qq].x - a[pp][pp].x) * (0.5 * ri);
+              const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+              c = rsqrt(tt * tt + 1.0);
+              s = tt * c;
+            }
+          }
+          rp[lane] = pp; rq[lane] = qq; rc[lane] = c; rsn[lane] = s; rph[lane] = e;
+        }
+        __syncwarp();
+        // columns of a and v: a <- a J, v <- v J
+        for (int i = lane; i < 2 * np * nt; i += 32) {
+          const int which = i / (np * nt), j = (i / nt) % np, row = i % nt;
+          const int pp = rp[j], qq = rq[j];
+          if (qq >= nt) continue;
+          double2 (*x)[kMaxTheta] = which ? v : a;
+          const double c = rc[j], s = rsn[j];
+          const double2 xp = x[row][pp], xq = cmul<double>(rph[j], x[row][qq]);
+          x[row][pp] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
+          x[row][qq] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
+        }
+        __syncwarp();
+        // rows of a: a <- J^H a
+        for (int i = lane; i < np * nt; i += 32) {
+          const int j = i / nt, col = i % nt;
+          const int pp = rp[j], qq = rq[j];
+          if (qq >= nt) continue;
+          const double c = rc[j], s = rsn[j];
+          const double2 xp = a[pp][col], xq = cmul<double>(cconj<double>(rph[j]), a[qq][col]);
+          a[pp][col] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
+          a[qq][col] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
+        }
+        __syncwarp();
+      }
+    }
+    for (int m = lane; m < nt; m += 32) o.mu[m] = (float)(a[m][m].x > 0.0 ? a[m][m].x : 0.0);
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      const double2 vl = make_double2(dm[l] * v[l][m].x, dm[l] * v[l][m].y);
+      v[l][m] = vl;
+      o.V[l][m] = make_float2((float)vl.x, (float)vl.y);
+    }
+    __syncwarp();
+    for (int i = lane; i < nt * 3; i += 32) {
+      const int m = i / 3, c = i % 3;
+      double2 acc = make_double2(0, 0);
+      for (int l = 0; l < nt; l++) acc = cadd<double>(acc, cmul<double>(cconj<double>(t.K[l][c]), v[l][m]));
+      g[m][c] = acc;
+      o.G[m][c] = make_float2((float)acc.x, (float)acc.y);
+    }
+    __syncwarp();
+    // g g^H: entry (p, q) = g_p conj(g_q); 00 11 22, then 01 02 12 as (re, im)
+    for (int m = lane; m < nt; m += 32) {
+      for (int c = 0; c < 3; c++) o.P[m][c] = (float)(g[m][c].x * g[m][c].x + g[m][c].y * g[m][c].y);
+      const double2 x01 = cmulc<double>(g[m][0], g[m][1]), x02 = cmulc<double>(g[m][0], g[m][2]);
+      const double2 x12 = cmulc<double>(g[m][1], g[m][2]);
+      o.P[m][3] = (float)x01.x; o.P[m][4] = (float)x01.y;
+      o.P[m][5] = (float)x02.x; o.P[m][6] = (float)x02.y;
+      o.P[m][7] = (float)x12.x; o.P[m][8] = (float)x12.y;
+    }
+  }
+  __syncwarp();
+  const float *os = (const float *)&o;
+  float *od = (float *)&p.ti[k];
+  for (int i = lane; i < (int)(sizeof(ITab) / sizeof(float)); i += 32) od[i] = os[i];
+}
+
+}  // namespace cg

@@ -42,11 +42,16 @@ struct Agg {
 std::vector<std::pair<std::string, Agg>> g_report;
 }  // namespace
 
+thread_local bool t_suppress = false;
+
 bool trace_on() { return g_on; }
+
+TraceSuppress::TraceSuppress() : prev_(t_suppress) { t_suppress = true; }
+TraceSuppress::~TraceSuppress() { t_suppress = prev_; }
 
 TraceScope::TraceScope(const char *name, cudaStream_t st, double bytes) : name_(name), st_(st), bytes_(bytes)
 {
-  if (!g_on) return;
+  if (!g_on || t_suppress) return;
   std::lock_guard<std::mutex> lk(g_mu);
   a_ = get_event();
   b_ = get_event();

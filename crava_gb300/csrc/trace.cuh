@@ -7,6 +7,18 @@ namespace cg {
 
 bool trace_on();
 
+// While one of these lives on a thread, launches on that thread record no
+// trace events (event creation is kept off the paths that promise to
+// allocate nothing).
+class TraceSuppress {
+ public:
+  TraceSuppress();
+  ~TraceSuppress();
+
+ private:
+  bool prev_;
+};
+
 class TraceScope {
  public:
   TraceScope(const char *name, cudaStream_t st, double bytes);

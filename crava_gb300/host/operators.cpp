@@ -34,35 +34,80 @@ namespace {
 
 typedef std::complex<double> cd;
 
-// recursive mixed-radix DFT, sign -1 (forward), out[k] = sum x[j] e^{-2 pi i jk/n}
+// complex product without the library's inf/NaN recovery call (operands are finite)
+inline cd cmul(cd a, cd b)
+{
+  return cd(a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real());
+}
+
+// recursive mixed-radix DFT, sign -1 (forward), out[k] = sum x[j] e^{-2 pi i jk/n}.
+// tw holds e^{-2 pi i t / N} for the top-level length N; at every level
+// n * twstep = N, so the twiddle indices below stay under N without a modulo.
 void dft_rec(const cd *x, int n, int stride, cd *out, const std::vector<cd> &tw, int twstep)
 {
   if (n == 1) { out[0] = x[0]; return; }
-  int r = 2;
+  int r = n % 4 == 0 ? 4 : 2;
   while (n % r) r++;
   const int m = n / r;
   for (int q = 0; q < r; q++) dft_rec(x + q * stride, m, stride * r, out + q * m, tw, twstep * r);
-  std::vector<cd> t(r);
-  const int N = (int)tw.size();
+  if (r == 2 || r == 4) {
+    // butterflies: W_2 = -1, W_4 = -i
+    for (int k = 0; k < m; k++) {
+      if (r == 2) {
+        const cd a = out[k], b = cmul(out[m + k], tw[(long)k * twstep]);
+        out[k] = a + b;
+        out[m + k] = a - b;
+      } else {
+        const cd t0 = out[k], t1 = cmul(out[m + k], tw[(long)k * twstep]);
+        const cd t2 = cmul(out[2 * m + k], tw[(long)2 * k * twstep]), t3 = cmul(out[3 * m + k], tw[(long)3 * k * twstep]);
+        const cd s02 = t0 + t2, d02 = t0 - t2, s13 = t1 + t3, d13 = t1 - t3;
+        const cd jd13(d13.imag(), -d13.real());  // -i (t1 - t3)
+        out[k] = s02 + s13;
+        out[m + k] = d02 + jd13;
+        out[2 * m + k] = s02 - s13;
+        out[3 * m + k] = d02 - jd13;
+      }
+    }
+    return;
+  }
+  cd tb[16], wb[16];
+  std::vector<cd> th, wh;
+  if (r > 16) { th.resize(r); wh.resize(r); }  // radices above 16 only for lengths with a large prime factor
+  cd *t = r > 16 ? th.data() : tb;
+  cd *wr = r > 16 ? wh.data() : wb;  // the r-th roots of unity e^{-2 pi i j / r}
+  for (int j = 0; j < r; j++) wr[j] = tw[(long)j * m * twstep];
   for (int k = 0; k < m; k++) {
-    for (int q = 0; q < r; q++) t[q] = out[q * m + k] * tw[((long)q * k * twstep) % N];
+    for (int q = 0; q < r; q++) t[q] = cmul(out[q * m + k], tw[(long)q * k * twstep]);
     for (int u = 0; u < r; u++) {
       cd acc = 0;
-      for (int q = 0; q < r; q++) acc += t[q] * tw[((long)q * u * m * twstep) % N];
+      int idx = 0;
+      for (int q = 0; q < r; q++) {
+        acc += cmul(t[q], wr[idx]);
+        idx += u;
+        if (idx >= r) idx -= r;
+      }
       out[u * m + k] = acc;
     }
   }
 }
 
-std::vector<cd> rfft(const std::vector<double> &x)
+std::vector<cd> twiddles(int n)
+{
+  std::vector<cd> tw(n);
+  for (int t = 0; t < n; t++) tw[t] = std::polar(1.0, -2.0 * M_PI * t / n);
+  return tw;
+}
+
+// full spectrum of a real sequence; getCAmp semantics are applied by the caller
+std::vector<cd> rfft(const std::vector<double> &x, const std::vector<cd> &tw)
 {
   const int n = (int)x.size();
-  std::vector<cd> tw(n), in(n), out(n);
-  for (int t = 0; t < n; t++) tw[t] = std::polar(1.0, -2.0 * M_PI * t / n);
-  for (int t = 0; t < n; t++) in[t] = x[t];
+  std::vector<cd> in(x.begin(), x.end()), out(n);
   dft_rec(in.data(), n, 1, out.data(), tw, 1);
-  return out;  // full spectrum; getCAmp semantics are applied by the caller
+  return out;
 }
+
+std::vector<cd> rfft(const std::vector<double> &x) { return rfft(x, twiddles((int)x.size())); }
 
 double norm2(const std::vector<double> &x)
 {
@@ -84,7 +129,8 @@ extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *w
   std::vector<double> d1(nzp, 0.0);
   d1[0] = -1.0;
   d1[nzp - 1] = 1.0;
-  const std::vector<cd> kD = rfft(d1);
+  const std::vector<cd> twz = twiddles(nzp);
+  const std::vector<cd> kD = rfft(d1, twz);
   // third-difference operator central(backward(d1)) for the non-constant-thickness errMult2
   std::vector<double> d2(nzp), d3(nzp);
   for (int i = 0; i < nzp; i++) d2[i] = (float)((i == 0) ? d1[0] - d1[nzp - 1] : d1[i] - d1[i - 1]);
@@ -92,7 +138,7 @@ extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *w
     const double v = (i == 0) ? 0.5 * (d2[1] - d2[nzp - 1]) : (i == nzp - 1) ? 0.5 * (d2[0] - d2[i - 1]) : 0.5 * (d2[i + 1] - d2[i - 1]);
     d3[i] = (float)v;
   }
-  const std::vector<cd> kD3 = rfft(d3);
+  const std::vector<cd> kD3 = rfft(d3, twz);
   const float lz = nz * dt_ms;
   const int cnzp = nzp / 2 + 1;
   for (int l = 0; l < ntheta; l++) {
@@ -105,13 +151,13 @@ extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *w
       e3[i] = (float)v;
     }
     const double wn = (float)norm2(w), en = (float)norm2(e3);
-    const std::vector<cd> W = rfft(w), E = rfft(e3);
+    const std::vector<cd> W = rfft(w, twz), E = rfft(e3, twz);
     for (int k = 0; k < nzp; k++) {
       const long o = ((long)k * ntheta + l) * 2;
       if (constant_thickness) {
         // the full spectrum already holds getCAmp's reflected/conjugated values for k >= nzp/2+1
         const cd kw = std::conj(W[k]);
-        const cd p = kD[k] * kw;
+        const cd p = cmul(kD[k], kw);
         for (int q = 0; q < 3; q++) {
           const long oq = (((long)k * ntheta + l) * 3 + q) * 2;
           K[oq] = (float)(p.real() * (double)A[l * 3 + q]);

@@ -63,6 +63,7 @@ class Inversion:
         else:
             self.tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
                                               sc.min_rel_thick)
+        self.cond_threshold = cond_threshold
         self.ws = api.Workspace(nxp, nyp, nzp, n)
         self.ws.set_model(self.tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=cond_threshold)
         f32 = dict(dtype=torch.float32, device=self.dev)
@@ -156,6 +157,28 @@ class Inversion:
                 api.inv_fft_in_place(m, nxp, api.PARAMETER, stream=stream)
         else:
             raise ValueError(form)
+
+    def run_cold(self, form="mixed", stream=None):
+        """One inversion of a model the workspace has not seen: the per-model work happens inside the call,
+        as the reference does it inside computePostMeanResidAndFFTCov (the per-k operator and error factors,
+        fillErrMultVectors / getNextErrorVariance, src/crava.cpp:1108-1120).  The forward transforms of the
+        data and prior means are queued first; the host builds the operator tables (from the wavelets) while
+        the GPU transforms, then queues their upload and the per-k table kernel
+        (cg_workspace_set_model_async), the prior spectra, the bin kernel and the inverse transforms."""
+        sc = self.sc
+        if self.thick:
+            raise ValueError("run_cold covers the constant-thickness model")
+        prec = {"mixed": api.PREC_MIXED, "fp32": api.PREC_FP32}[form]
+        nxp = sc.nxp
+        api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
+        api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, stream=stream)
+        tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
+                                     sc.min_rel_thick)
+        self.ws.set_model(tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=self.cond_threshold,
+                          stream=stream, asynchronous=True)
+        self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
+        self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=stream)
+        api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
 
     # -- output grids (the steps after the bin loop) ------------------------
     def outputs(self, form, stream=None):

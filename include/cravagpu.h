@@ -142,7 +142,10 @@ int cg_fft3d_c2r_f64(double *buf, int nxp, int nyp, int nzp, int cubetype, void 
  * CG_ERR_ARG or CG_ERR_UNSUPPORTED before the buffer is touched.  Every call
  * rewrites the shared array, so calls that overlap on the GPU race.  The
  * first call on a device looks the array up for that device; make it before
- * any stream capture. */
+ * any stream capture.  The column passes here always use register-direct or
+ * four-step kernels, whatever the tuning table selects (the TMA-fed pass
+ * allocates a fault word on first use), and the launch tracer records
+ * nothing for these calls (it would create CUDA events). */
 int cg_fft3d_r2c_noalloc(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
 int cg_fft3d_c2r_noalloc(float *buf, int nxp, int nyp, int nzp, int cubetype, void *stream);
 
@@ -405,8 +408,16 @@ typedef struct cg_model {
 int cg_workspace_create(cg_workspace *ws, int nxp, int nyp, int nzp, int ntheta);
 void cg_workspace_destroy(cg_workspace ws);
 
-/* Upload the model and build the per-k tables (synchronous). */
+/* Upload the model and build the per-k tables: the per-model work the
+ * reference repeats inside computePostMeanResidAndFFTCov for every k before
+ * its bins (Crava::fillErrMultVectors products and the getNextErrorVariance
+ * factors, src/crava.cpp:1108-1120).  cg_workspace_set_model is synchronous.
+ * cg_workspace_set_model_async copies the model into the workspace's pinned
+ * staging buffer (waiting only for the previous model's copy to have left
+ * it), then queues one host-to-device copy and the table kernel on `stream`;
+ * inversions on other streams must be ordered after it by the caller. */
 int cg_workspace_set_model(cg_workspace ws, const cg_model *model);
+int cg_workspace_set_model_async(cg_workspace ws, const cg_model *model, void *stream);
 
 /* Counters: bins queued for FP64 by the last mixed-precision inversion, and,
  * since the last reset, bins whose Cholesky failed (they keep the prior, like
@@ -450,6 +461,19 @@ int cg_invert_bins_fused(cg_workspace ws, float *const *data, float *const *mean
  * cg_invert_bins_fused.  Needs cg_prior_spectra first. */
 int cg_invert_cubes_fused(cg_workspace ws, float *const *data, float *const *mean, float *const *cov,
                           int precision, void *stream);
+
+/* Condition estimates of the current model's in-band bins, for choosing the
+ * CG_PREC_MIXED threshold (no reference counterpart: the reference runs
+ * every bin in FP32).  Needs cg_prior_spectra.  hist_chol[b] counts the bins
+ * whose FP64 Cholesky of the data covariance Sd has a squared pivot ratio in
+ * [10^b, 10^(b+1)) (the Cholesky form's guard estimate), hist_info[b] the
+ * same for the 3 x 3 information-form matrix in FP32 as the default kernel's
+ * guard computes it (all zero when the model has no information-form
+ * tables); b = 0 also takes ratios below 1, b = nbuckets-2 everything above,
+ * and b = nbuckets-1 counts failed factorisations.  Host arrays of nbuckets
+ * (2..32) entries; synchronises `stream`. */
+int cg_condition_histogram(cg_workspace ws, unsigned long long *hist_chol, unsigned long long *hist_info,
+                           int nbuckets, void *stream);
 
 /* Fused posterior on FP64 spectra (needs cg_prior_spectra with CG_PREC_FP64). */
 int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,

@@ -33,7 +33,8 @@ BUILD_DIR = os.path.join(HERE, "_build")
 ORACLE_SO = os.path.join(BUILD_DIR, "libcravaoracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
 REF_SO = os.path.join(REF_DIR, "libcrava_ref.so")
-REFERENCE_SRC = os.environ.get("CRAVA_REFERENCE_SRC", "/root/reference")
+# the reference checkout, when this machine has one: named by the caller, never assumed
+REFERENCE_SRC = os.environ.get("CRAVA_REFERENCE_SRC", "")
 
 DATA, PARAMETER, COVARIANCE, OPERATOR = 1, 2, 3, 5
 
@@ -60,7 +61,7 @@ def build_oracle(force: bool = False) -> str:
 
 def build_ref() -> str | None:
     """Build oracle/_ref from the reference sources when they are present."""
-    if not os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft")):
+    if not REFERENCE_SRC or not os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft")):
         return None
     repo = os.path.dirname(HERE)
     subprocess.check_call(
@@ -133,7 +134,7 @@ def lib():
 
 
 def ref_available() -> bool:
-    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft"))
+    return os.path.exists(REF_SO) or bool(REFERENCE_SRC) and os.path.isdir(os.path.join(REFERENCE_SRC, "libs", "fft"))
 
 
 def ref():

@@ -245,3 +245,64 @@ def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt
     assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
     if cond > 0:
         assert st["flagged"] > 0
+
+
+@pytest.mark.parametrize("nt", [1, 2, 3, 5, 8])
+def test_cold_inversion_matches_repeated_model_and_fp64_oracle(cuda, oracle, nt):
+    """run_cold (operator tables, cg_workspace_set_model_async and the per-k table kernel inside the call)
+    gives bit-for-bit the three-pass mixed inversion of a workspace whose model was set synchronously, and
+    stays within the FP64 oracle's tolerances; stack counts 1..8 cover the parallel Jacobi's even and odd
+    index sets."""
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.make_scenario(32, 28, 40, list(np.linspace(0.0, 40.0, nt)), 25.0, nxp=40, nyp=36, nzp=48, sn=3.0,
+                         notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=31 + nt)
+    inv = Inversion(sc, forms=("mixed",))
+    inv.restore("mixed")
+    inv.run("mixed_3pass")
+    torch.cuda.synchronize()
+    warm = inv.results("mixed")
+    from crava_gb300 import api
+    inv2 = Inversion(sc, forms=("mixed",))
+    # a stale model in the workspace, which run_cold must replace
+    bad = S.make_scenario(32, 28, 40, list(np.linspace(5.0, 35.0, nt)), 30.0, nxp=40, nyp=36, nzp=48, sn=4.0,
+                          seed=99)
+    bad_tab = api.operator_tables(bad.wavelets, bad.A, bad.nz, bad.nzp, bad.dt_ms, bad.low_cut, bad.high_cut)
+    inv2.ws.set_model(bad_tab, bad.err_theta_cov, bad.sigma0, bad.wnc)
+    inv2.restore("mixed")
+    inv2.run_cold("mixed")
+    torch.cuda.synchronize()
+    cold = inv2.results("mixed")
+    for a, b in zip(cold, warm):
+        assert np.array_equal(a, b)
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    e = (rel(cold[0], post64), rel(cold[0] - prior, post64 - prior), rel(cold[1], res64), rel(cold[2], cov64))
+    print(nt, "cold inversion vs FP64 oracle (mean, update, resid, cov):", e)
+    assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
+
+
+def test_condition_histogram_counts_every_inband_bin(cuda):
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.scaled_config1(48, 40, 64, seed=8)
+    inv = Inversion(sc, forms=("mixed",))
+    inv.restore("mixed")
+    inv.run("mixed")
+    torch.cuda.synchronize()
+    hc, hi = inv.ws.condition_histogram(16)
+    inband = int(inv.tables["band"].sum()) * sc.cnxp * sc.nyp
+    print("condition histograms (Cholesky FP64, information FP32):", hc, hi)
+    assert sum(hc) == inband
+    assert 0 < sum(hi) <= inband
+    assert hc[-1] == 0  # no failed factorisation on this model
+    # a forced guard flags the bins the histogram puts above the threshold
+    inv2 = Inversion(sc, forms=("mixed",), cond_threshold=10.0)
+    inv2.restore("mixed")
+    inv2.ws.reset_stats()
+    inv2.run("mixed")
+    torch.cuda.synchronize()
+    hc2, hi2 = inv2.ws.condition_histogram(16)
+    assert hi2 == hi
+    fl = inv2.ws.stats()["flagged"]
+    assert sum(hi[2:]) <= fl <= sum(hi[1:])  # above the threshold of 10 (decade 1 holds 10 itself)
