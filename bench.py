@@ -271,17 +271,18 @@ def run_reference(args, world, rank):
 COND_BUCKETS = 16
 
 
-def conditioning_case(args, stream, flush, rank):
-    """A workload whose bins do cross the FP64 guard: 8 stacks 0-40 deg (near-collinear Aki-Richards rows),
-    S/N 10 (the reference's maximum), 25 Hz Ricker without notches, band 1-100 Hz, 256x256x128 padded.
-    Times the fused FP32 and mixed forms and reports the FP64 fix-up's share and both errors vs FP64."""
+def conditioning_case(args, stream, flush, rank, sn, wnc):
+    """8 stacks 0-40 deg (near-collinear Aki-Richards rows), 25 Hz Ricker without notches, band 1-100 Hz,
+    256x256x128 padded, at signal-to-noise ratio ``sn`` and white-noise component ``wnc``.  Times the fused
+    FP32 and mixed forms and reports the FP64 fix-up's share, the condition histograms and both forms'
+    errors vs the FP64 form."""
     import numpy as np
     import torch
     from crava_gb300 import _native
     from crava_gb300 import synthetic as S
     from crava_gb300.pipeline import Inversion
     sc = S.make_scenario(205, 205, 102, list(np.linspace(0.0, 40.0, 8)), 25.0, nxp=256, nyp=256, nzp=128,
-                         sn=10.0, low_cut=1.0, high_cut=100.0, seed=20261209 + rank)
+                         sn=sn, wnc=wnc, low_cut=1.0, high_cut=100.0, seed=20261209 + rank)
     inv = Inversion(sc, forms=("fp32", "mixed", "fp64"))
     ms = {}
     for form in ("fp32", "mixed"):
@@ -305,7 +306,7 @@ def conditioning_case(args, stream, flush, rank):
     torch.cuda.synchronize()
     pm64, res64, cov64 = inv.results("fp64")
     prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
-    out = {"workload": "256x256x128 padded, 8 stacks 0-40 deg, 25 Hz Ricker, S/N 10, band 1-100 Hz",
+    out = {"workload": f"256x256x128 padded, 8 stacks 0-40 deg, 25 Hz Ricker, S/N {sn:g}, wnc {wnc:g}, band 1-100 Hz",
            "bins": sc.nbins, "ms": {k: round(v, 4) for k, v in ms.items()}}
     for form in ("fp32", "mixed"):
         inv.restore(form)
@@ -406,6 +407,12 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     ms_cold = statistics.mean(timed_cold(args.steps))
     barrier(world)
+    inv.restore("mixed")
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    inv.run_cold("mixed")
+    tr_cold = _native.trace_collect()
+    _native.trace_enable(False)
 
     # accuracy against the FP64 run on the same inputs
     inv.restore("fp64")
@@ -550,7 +557,10 @@ def run_ours(args, world, rank, local):
     total_bins = bins * world
     value = replicas.whole_job_rate(bins, ms_mixed, world)
 
-    cond_case = conditioning_case(args, stream, flush, rank)
+    # conditioning: the reference accepts 1 < S/N <= 10 (src/modelavodynamic.cpp:1255-1260); at its maximum
+    # no bin crosses the guard, so a second case goes far beyond that range to exercise the FP64 fix-up
+    cond_case = {"sn_10_reference_max": conditioning_case(args, stream, flush, rank, 10.0, 0.1),
+                 "sn_1e5_outside_reference_range": conditioning_case(args, stream, flush, rank, 1.0e5, 1.0e-4)}
 
     cpu = None
     vs_cpu64 = None
@@ -583,6 +593,8 @@ def run_ours(args, world, rank, local):
             "speedup_mixed_vs_plain": round(ms_plain / ms_mixed, 3),
             "cold_one_shot": {"ms": round(ms_cold, 4), "Mbins_per_s": round(bins / (ms_cold * 1e-3) / 1e6, 1),
                               "vs_repeated_model": round(ms_cold / ms_mixed, 4),
+                              "kernels": {k: {"launches": v[0], "ms": round(v[1], 4)}
+                                          for k, v in sorted(tr_cold.items(), key=lambda kv: -kv[1][1])},
                               "what": "mixed form with the model's per-k set-up inside the step: host operator "
                                       "tables built while the forward transforms run, one upload, the per-k "
                                       "table kernel (cg_workspace_set_model_async)"},

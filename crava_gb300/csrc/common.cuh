@@ -59,6 +59,9 @@ void set_error(const char *fmt, ...);
 int cuda_status(cudaError_t e, const char *where);
 // stream-ordered allocation from the library's own per-device pool, which keeps its memory between calls
 cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st);
+// every memory allocation the library makes (device, pinned host, pools) calls this first (cg_alloc_calls)
+void count_alloc();
+cudaError_t dev_malloc(void **p, size_t bytes);  // cudaMalloc, counted
 
 #define CG_CUDA(call)                                           \
   do {                                                          \

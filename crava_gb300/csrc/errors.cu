@@ -1,5 +1,6 @@
 // Error text and status plumbing shared by every C-ABI entry point.
 #include <cstdarg>
+#include <atomic>
 #include <cstdio>
 #include <mutex>
 
@@ -8,6 +9,15 @@
 namespace cg {
 
 static thread_local char g_err[512] = "";
+static std::atomic<long> g_alloc_calls{0};
+
+void count_alloc() { g_alloc_calls.fetch_add(1, std::memory_order_relaxed); }
+
+cudaError_t dev_malloc(void **p, size_t bytes)
+{
+  count_alloc();
+  return cudaMalloc(p, bytes);
+}
 
 void set_error(const char *fmt, ...)
 {
@@ -38,6 +48,7 @@ cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st)
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
+  count_alloc();
   if (dev < 0 || dev >= 64) return cudaMallocAsync(p, bytes, st);
   cudaMemPool_t pool;
   {
@@ -49,6 +60,7 @@ cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st)
       props.location.type = cudaMemLocationTypeDevice;
       props.location.id = dev;
       cudaMemPool_t np = nullptr;
+      count_alloc();
       e = cudaMemPoolCreate(&np, &props);
       if (e != cudaSuccess) return e;
       unsigned long long keep = ~0ULL;
@@ -65,3 +77,4 @@ cudaError_t scratch_alloc(void **p, size_t bytes, cudaStream_t st)
 
 extern "C" const char *cg_last_error(void) { return cg::g_err; }
 extern "C" int cg_version(void) { return 100; }
+extern "C" long cg_alloc_calls(void) { return cg::g_alloc_calls.load(); }

@@ -68,6 +68,7 @@ const C2<T> *twiddle_table(int n)
     h[t] = mk<T>((T)cos(a), (T)sin(a));
   }
   void *d = nullptr;
+  count_alloc();
   if (cudaMalloc(&d, sizeof(C2<T>) * (size_t)n) != cudaSuccess) return nullptr;
   if (cudaMemcpy(d, h.data(), sizeof(C2<T>) * (size_t)n, cudaMemcpyHostToDevice) != cudaSuccess) {
     cudaFree(d);
@@ -584,6 +585,7 @@ static int fft_host(float *hbuf, int nxp, int nyp, int nzp, int cubetype, bool f
   int rc = CG_OK;
   size_t bytes = sizeof(float) * 2 * (size_t)(nxp / 2 + 1) * nyp * nzp;
   float *d = nullptr;
+  count_alloc();
   CG_CUDA(cudaMalloc(&d, bytes));
   cudaError_t e = cudaMemcpy(d, hbuf, bytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) { cudaFree(d); return cuda_status(e, "H2D"); }

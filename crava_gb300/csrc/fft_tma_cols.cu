@@ -55,6 +55,7 @@ int *device_fault_word()
   std::lock_guard<std::mutex> lk(g_fault_mu);
   if (!g_fault[dev]) {
     int *p = nullptr;
+    count_alloc();
     if (cudaMalloc(&p, sizeof(int)) != cudaSuccess) return nullptr;
     if (cudaMemset(p, 0, sizeof(int)) != cudaSuccess) { cudaFree(p); return nullptr; }
     g_fault[dev] = p;

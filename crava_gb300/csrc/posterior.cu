@@ -562,7 +562,7 @@ extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp,
   const long csize = (long)cnxp * nyp * nzp;
   w->queue_cap = (int)std::min<long>(csize, std::max<long>(1 << 16, csize / 8));
   cudaError_t e = cudaSuccess;
-#define WS_ALLOC(ptr, bytes) if (e == cudaSuccess) e = cudaMalloc((void **)&(ptr), (bytes))
+#define WS_ALLOC(ptr, bytes) if (e == cudaSuccess) e = (count_alloc(), cudaMalloc((void **)&(ptr), (bytes)))
   WS_ALLOC(w->ktab_f, sizeof(KTab<float>) * nzp);
   WS_ALLOC(w->ktab_d, sizeof(KTab<double>) * nzp);
   // uploaded tables, packed in one block: etc | K | em1 | em2 | em3 | band
@@ -570,7 +570,7 @@ extern "C" int cg_workspace_create(cg_workspace *out, int nxp, int nyp, int nzp,
   const size_t n_em = sizeof(float2) * (size_t)nzp * ntheta;
   w->model_bytes = o_k + n_k + 3 * n_em + (size_t)nzp;
   WS_ALLOC(w->model_dev, w->model_bytes);
-  if (e == cudaSuccess) e = cudaMallocHost(&w->model_host, w->model_bytes);
+  if (e == cudaSuccess) e = (count_alloc(), cudaMallocHost(&w->model_host, w->model_bytes));
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->model_copied, cudaEventDisableTiming);
   if (e == cudaSuccess) {
     char *base = (char *)w->model_dev;

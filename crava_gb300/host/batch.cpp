@@ -19,6 +19,7 @@
 #include "cravagpu_host.hpp"
 
 namespace cg {
+cudaError_t dev_malloc(void **p, size_t bytes);  // cudaMalloc, counted (cg_alloc_calls)
 void set_error(const char *fmt, ...);
 }
 
@@ -129,14 +130,14 @@ extern "C" int cg_batch_create(cg_batch *out, const cg_batch_cube *cubes, int nc
           c.data.push_back(new FFTGrid(d.nx, d.ny, d.nz, d.nxp, d.nyp, d.nzp));
           c.data.back()->setType(FFTGrid::DATA);
           float *p = nullptr;
-          cuda_check(cudaMalloc((void **)&p, sizeof(float) * c.rsize()), "batch input");
+          cuda_check(cg::dev_malloc((void **)&p, sizeof(float) * c.rsize()), "batch input");
           c.data_in.push_back(p);
         }
         for (int q = 0; q < 3; q++) {
           c.mean.push_back(new FFTGrid(d.nx, d.ny, d.nz, d.nxp, d.nyp, d.nzp));
           c.mean.back()->setType(FFTGrid::PARAMETER);
           float *p = nullptr;
-          cuda_check(cudaMalloc((void **)&p, sizeof(float) * c.rsize()), "batch input");
+          cuda_check(cg::dev_malloc((void **)&p, sizeof(float) * c.rsize()), "batch input");
           c.mean_in.push_back(p);
         }
         for (int t = 0; t < 6; t++) {

@@ -14,6 +14,7 @@
 #include "../csrc/fused_entry.h"
 
 namespace cg {
+cudaError_t dev_malloc(void **p, size_t bytes);  // cudaMalloc, counted (cg_alloc_calls)
 void set_error(const char *fmt, ...);
 }
 
@@ -39,7 +40,7 @@ FFTGrid::FFTGrid(int nx, int ny, int nz, int nxp, int nyp, int nzp)
     : nx_(nx), ny_(ny), nz_(nz), nxp_(nxp), nyp_(nyp), nzp_(nzp)
 {
   if (nxp < 1 || nyp < 1 || nzp < 1) throw Error(CG_ERR_ARG, "FFTGrid: bad padded size");
-  cuda_check(cudaMalloc((void **)&d_, sizeof(float) * (size_t)getrsize()), "FFTGrid allocation");
+  cuda_check(cg::dev_malloc((void **)&d_, sizeof(float) * (size_t)getrsize()), "FFTGrid allocation");
   cuda_check(cudaMemset(d_, 0, sizeof(float) * (size_t)getrsize()), "FFTGrid clear");
 }
 
@@ -175,8 +176,8 @@ Crava::Crava(int nx, int ny, int nz, int nxp, int nyp, int nzp, const InversionM
   cm.sigma0 = m_.sigma0.data();
   cm.cond_threshold = m_.condThreshold;
   check(cg_workspace_set_model(ws_, &cm), "set model");
-  cuda_check(cudaMalloc((void **)&d_corr_xy_, sizeof(float) * m_.corrXY.size()), "corrXY");
-  cuda_check(cudaMalloc((void **)&d_circ_t_, sizeof(float) * m_.circCorrT.size()), "circCorrT");
+  cuda_check(cg::dev_malloc((void **)&d_corr_xy_, sizeof(float) * m_.corrXY.size()), "corrXY");
+  cuda_check(cg::dev_malloc((void **)&d_circ_t_, sizeof(float) * m_.circCorrT.size()), "circCorrT");
   cuda_check(cudaMemcpy(d_corr_xy_, m_.corrXY.data(), sizeof(float) * m_.corrXY.size(), cudaMemcpyHostToDevice),
              "corrXY upload");
   cuda_check(cudaMemcpy(d_circ_t_, m_.circCorrT.data(), sizeof(float) * m_.circCorrT.size(), cudaMemcpyHostToDevice),
@@ -243,7 +244,7 @@ int Crava::simulate(FFTGrid **postCov, FFTGrid *const *postMean, int nSim, unsig
 {
   if (nSim < 1) return 0;
   if (!d_chol_)
-    cuda_check(cudaMalloc((void **)&d_chol_, sizeof(float) * 9 * (size_t)postCov[0]->getcsize()), "factor planes");
+    cuda_check(cg::dev_malloc((void **)&d_chol_, sizeof(float) * 9 * (size_t)postCov[0]->getcsize()), "factor planes");
   float *cv[6];
   for (int t = 0; t < 6; t++) cv[t] = postCov[t]->devicePtr();
   check(cg_posterior_cholesky(cv, d_chol_, nxp_, nyp_, nzp_, nullptr, stream), "posterior factor");

@@ -170,8 +170,8 @@ class Inversion:
             raise ValueError("run_cold covers the constant-thickness model")
         prec = {"mixed": api.PREC_MIXED, "fp32": api.PREC_FP32}[form]
         nxp = sc.nxp
-        api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
-        api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, stream=stream)
+        # DATA and PARAMETER cubes share the 1/sqrt(N) scaling: one batched launch per pass for all of them
+        api.fft_in_place_batch(self.data + self.mean, nxp, api.DATA, stream=stream)
         tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
                                      sc.min_rel_thick)
         self.ws.set_model(tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=self.cond_threshold,

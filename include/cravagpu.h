@@ -51,6 +51,10 @@ extern "C" {
 const char *cg_last_error(void);
 /* Library version, e.g. 100 = 0.1.0. */
 int cg_version(void);
+/* How many memory allocations (device, pinned host, memory pools) the
+ * library has made in this process: a diagnostic for callers that must know
+ * whether a call allocated (no reference counterpart). */
+long cg_alloc_calls(void);
 /* Largest transform length supported along one axis. */
 int cg_fft_max_length(void);
 

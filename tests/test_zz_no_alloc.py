@@ -68,7 +68,7 @@ _CHILD = r"""
 import ctypes as ct, json, sys
 sys.path.insert(0, sys.argv[1])
 import crava_gb300
-L = crava_gb300.lib()          # the library's kernels are registered before the context exists
+L = crava_gb300.lib()
 import torch
 torch.cuda.init()
 nxp, nyp, nzp = 256, 256, 64   # y axis of length 256: the TMA-fed pass when the tuning value is 5
@@ -78,47 +78,49 @@ x0 = x.clone()
 a = x.clone()
 s = ct.c_void_p(0)
 torch.cuda.synchronize()
-free0 = torch.cuda.mem_get_info()[0]
-alloc0 = torch.cuda.memory_allocated()
-rcs = []
-for _ in range(2):
+calls0 = L.cg_alloc_calls()
+rcs, free = [], []
+for _ in range(3):
     rcs.append(L.cg_fft3d_r2c_noalloc(ct.c_void_p(x.data_ptr()), nxp, nyp, nzp, 1, s))
     rcs.append(L.cg_fft3d_c2r_noalloc(ct.c_void_p(x.data_ptr()), nxp, nyp, nzp, 1, s))
-torch.cuda.synchronize()
-free1 = torch.cuda.mem_get_info()[0]
-alloc1 = torch.cuda.memory_allocated()
-# the allocating transform at the same size, for contrast: its first call allocates twiddle tables
+    torch.cuda.synchronize()
+    free.append(torch.cuda.mem_get_info()[0])
+calls1 = L.cg_alloc_calls()
+# the allocating transform at the same size, for contrast: it allocates its twiddle tables and, on the
+# TMA-fed pass, the fault word
 rcs.append(L.cg_fft3d_r2c(ct.c_void_p(a.data_ptr()), nxp, nyp, nzp, 1, s))
 torch.cuda.synchronize()
-free2 = torch.cuda.mem_get_info()[0]
+calls2 = L.cg_alloc_calls()
 flag = ct.c_int(0)
 rcs.append(L.cg_device_faults(ct.byref(flag)))
 err = float(torch.linalg.vector_norm((x - x0)[..., :nxp].double()) / torch.linalg.vector_norm(x0.double()))
-print(json.dumps({"rcs": rcs, "free0": free0, "free1": free1, "free2": free2,
-                  "alloc0": alloc0, "alloc1": alloc1, "faults": flag.value, "roundtrip_err": err}))
+print(json.dumps({"rcs": rcs, "calls": [calls0, calls1, calls2], "free": free, "faults": flag.value,
+                  "roundtrip_err": err}))
 """
 
 
 def test_noalloc_allocates_nothing_with_the_tma_pass_selected(cuda, native):
-    """A fresh process with every kernel loaded at context creation
-    (CUDA_MODULE_LOADING=EAGER, so a first launch maps no code) and the
-    tuning table pointing length-256 column passes at the TMA-fed kernel,
-    whose fault word is allocated on first use.  Device free memory must be
-    the same before and after two rounds of no-allocation transforms."""
+    """A fresh process with the tuning table pointing length-256 column passes at the TMA-fed kernel,
+    whose fault word is allocated on first use.  Three rounds of no-allocation transforms must make no
+    memory allocation of the library's own (cg_alloc_calls counts every one it makes), while one call of
+    the allocating transform at the same size does make some.  Device free memory is also compared
+    across the later rounds: the first launches of kernels may still map memory of the driver's own
+    (code and per-thread local memory are set up lazily), which no library call controls."""
     import json
     import os
     import subprocess
     import sys
     repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    env = dict(os.environ, CUDA_MODULE_LOADING="EAGER", CRAVA_COLS_PIPE="5")
+    env = dict(os.environ, CRAVA_COLS_PIPE="5")
     out = subprocess.run([sys.executable, "-c", _CHILD, repo], env=env, capture_output=True, text=True,
                          timeout=600)
     assert out.returncode == 0, out.stderr[-2000:]
     r = json.loads(out.stdout.strip().splitlines()[-1])
-    assert r["rcs"] == [0] * 6, r
+    print(r)
+    assert r["rcs"] == [0] * 8, r
     assert r["roundtrip_err"] < FFT_TOL, r
     assert r["faults"] == 0, r
-    assert r["alloc1"] == r["alloc0"], r
-    assert r["free1"] == r["free0"], f"the no-allocation transforms changed free device memory: {r}"
-    print(f"free memory: {r['free0']} before, {r['free1']} after the no-allocation calls, "
-          f"{r['free2']} after one allocating call")
+    c0, c1, c2 = r["calls"]
+    assert c1 == c0, f"the no-allocation transforms allocated: {r}"
+    assert c2 > c1, f"the allocating transform was not seen allocating: {r}"
+    assert r["free"][1] == r["free"][2], f"repeated no-allocation calls changed free device memory: {r}"
