@@ -646,8 +646,25 @@ extern "C" int cg_workspace_set_model_async(cg_workspace w, const cg_model *m, v
   long nb = 0;
   for (int k = 0; k < nzp; k++) nb += m->band[k] ? 1 : 0;
   w->inband_bins = nb * (long)(w->nxp / 2 + 1) * w->nyp;
+  // conjugate symmetry in k of everything the set-up kernel reads (K, errMult1..3, band): then it computes
+  // planes 0..nzp/2 and mirrors them
+  bool sym = true;
+  for (int k = 1; k < nzp && sym; k++) {
+    const int km = nzp - k;
+    if (km <= k) break;
+    sym = m->band[k] == m->band[km];
+    const float *arrs[4] = {m->K, m->em1, m->em2, m->em3};
+    const long per[4] = {(long)nt * 3, nt, nt, nt};
+    for (int a = 0; a < 4 && sym; a++)
+      for (long i = 0; i < per[a] && sym; i++) {
+        const float *x = arrs[a] + 2 * ((long)k * per[a] + i), *y = arrs[a] + 2 * ((long)km * per[a] + i);
+        sym = x[0] == y[0] && x[1] == -y[1];
+      }
+  }
   PrepArgs pa;
   pa.nt = nt;
+  pa.nzp = nzp;
+  pa.sym = sym ? 1 : 0;
   pa.wnc = m->wnc;
   pa.is4d = m->is4d;
   pa.K = w->K; pa.em1 = w->em1; pa.em2 = w->em2; pa.em3 = w->em3; pa.band = w->band; pa.etc = w->etc;
@@ -656,7 +673,7 @@ extern "C" int cg_workspace_set_model_async(cg_workspace w, const cg_model *m, v
   pa.tf = w->ktab_f; pa.td = w->ktab_d; pa.ti = w->itab;
   {
     TraceScope ts("k_prep_model", st, 0.0);
-    k_prep_model<<<nzp, 32, 0, st>>>(pa);
+    k_prep_model<<<sym ? nzp / 2 + 1 : nzp, 32, 0, st>>>(pa);
     CG_CHECK_LAUNCH("k_prep_model");
   }
   // The information form needs a 3D model with a positive error diagonal in every in-band plane

@@ -53,6 +53,8 @@ struct ITab {
 // reference-order tables in, the per-k tables out.
 struct PrepArgs {
   int nt;
+  int nzp;
+  int sym;  // the tables of plane nzp-k are the conjugates of plane k's: compute k <= nzp/2 only
   float wnc;
   int is4d;
   const float2 *K, *em1, *em2, *em3;

@@ -5,13 +5,19 @@
 // plane (Crava::fillErrMultVectors products and getNextErrorVariance's
 // per-k factors, src/crava.cpp:1108-1120, :1337-1386, :1442-1469).
 //
-// One warp per k.  The lanes build the table entries in parallel (an entry
+// One warp per k.  The tables of plane nzp-k are the conjugates of plane k's
+// when the uploaded model is conjugate-symmetric in k, as the reference's
+// tables are (Wavelet::getCAmp reflects k >= nzp/2+1); the host checks that
+// and then launches planes 0..nzp/2 only, each writing its mirror plane too.
+// The lanes build the table entries in parallel (an entry
 // per lane), and the information form's Hermitian eigen-decomposition is a
 // parallel Jacobi: in each step the lanes compute the rotations of up to four
 // disjoint index pairs at once (round-robin pairing), then apply them to the
 // columns, the eigenvectors and the rows with one matrix element per lane.
 // FP64 throughout; the FP64 rate of this GPU is low, so the work is spread
-// over one warp per plane on all SMs instead of one thread per plane.
+// over one warp per plane on all SMs instead of one thread per plane, and the
+// rotation's square roots and reciprocal are hardware approximations refined
+// by Newton-Raphson steps.
 #include "posterior.cuh"
 
 namespace cg {
@@ -35,6 +41,33 @@ __device__ __forceinline__ double warp_sum(double v)
   return v;
 }
 
+// x^(-1/2) for normal x > 0: the hardware approximation refined by two Newton-Raphson steps for
+// f(y) = 1/y^2 - x, y <- y (3 - x y^2) / 2 (each step squares the relative error)
+__device__ __forceinline__ double rsqrt_nr(double x)
+{
+  double y;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(x));
+  y = y * (1.5 - 0.5 * x * y * y);
+  return y * (1.5 - 0.5 * x * y * y);
+}
+
+// 1/x for normal x > 0: the hardware approximation refined by two Newton-Raphson steps for
+// f(y) = 1/y - x, y <- y (2 - x y)
+__device__ __forceinline__ double rcp_nr(double x)
+{
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  y = y * (2.0 - x * y);
+  return y * (2.0 - x * y);
+}
+
+// conjugates n complex values in shared memory (lanes in parallel)
+template <typename C>
+__device__ __forceinline__ void conj_all(C *v, int n, int lane)
+{
+  for (int i = lane; i < n; i += 32) v[i].y = -v[i].y;
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepArgs p)
@@ -42,6 +75,8 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
   const int k = blockIdx.x;
   const int lane = threadIdx.x;
   const int nt = p.nt;
+  // with symmetric tables this CTA also writes plane nzp - k, the conjugate of plane k
+  const int km = (p.sym && k > 0 && 2 * k != p.nzp) ? p.nzp - k : -1;
   __shared__ KTab<double> t;
   __shared__ KTab<float> f;
   __shared__ ITab o;
@@ -116,6 +151,32 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
     float *fd = (float *)&p.tf[k];
     for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) fd[i] = fs[i];
   }
+  if (km >= 0) {
+    // plane nzp - k: K, KS0, M, E conjugated, D and the band as they are (the information form below
+    // reads only K, E and D of t: it runs before t is conjugated)
+    __shared__ KTab<float> fm;
+    {
+      const float *fs = (const float *)&f;
+      float *fmw = (float *)&fm;
+      for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) fmw[i] = fs[i];
+    }
+    __syncwarp();
+    conj_all(&fm.K[0][0], kMaxTheta * 3, lane);
+    conj_all(&fm.KS0[0][0], kMaxTheta * 3, lane);
+    conj_all(fm.M, kTri, lane);
+    conj_all(fm.E, kTri, lane);
+    __syncwarp();
+    const float *fs = (const float *)&fm;
+    float *fd = (float *)&p.tf[km];
+    for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) fd[i] = fs[i];
+    const double *src = (const double *)&t;
+    double *dst = (double *)&p.td[km];
+    for (int i = lane; i < (int)(sizeof(KTab<double>) / sizeof(double)); i += 32) {
+      // the complex arrays K, KS0, M, E come first (double2 each): odd words are imaginary parts
+      const int nc = 2 * (2 * kMaxTheta * 3 + 2 * kTri);
+      dst[i] = (i < nc && (i & 1)) ? -src[i] : src[i];
+    }
+  }
   if (p.is4d) return;
 
   // information form: D^-1/2 E D^-1/2 = U diag(mu) U^H, v_m = D^-1/2 u_m, g_m = K^H v_m
@@ -158,12 +219,15 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
           if (qq < nt) {
             const double2 apq = a[pp][qq];
             const double mag2 = apq.x * apq.x + apq.y * apq.y;
-            if (mag2 > 0.0) {
-              const double ri = rsqrt(mag2);
+            // an element below 1e-150 (squared) against the diagonal is left: it is already far under
+            // the stopping criterion, and the refined approximations need normal operands
+            if (mag2 > 1e-300 && mag2 > 1e-40 * (a[pp][pp].x * a[pp][pp].x + a[qq][qq].x * a[qq][qq].x)) {
+              const double ri = rsqrt_nr(mag2);
               e = make_double2(apq.x * ri, -apq.y * ri);  // e^{-i arg a_pq}
               const double th = (a[qq][qq].x - a[pp][pp].x) * (0.5 * ri);
-              const double tt = (th >= 0.0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-              c = rsqrt(tt * tt + 1.0);
+              const double q = th * th + 1.0;
+              const double tt = (th >= 0.0 ? 1.0 : -1.0) * rcp_nr(fabs(th) + q * rsqrt_nr(q));
+              c = rsqrt_nr(tt * tt + 1.0);
               s = tt * c;
             }
           }
@@ -225,6 +289,22 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
   const float *os = (const float *)&o;
   float *od = (float *)&p.ti[k];
   for (int i = lane; i < (int)(sizeof(ITab) / sizeof(float)); i += 32) od[i] = os[i];
+  if (km >= 0) {
+    // plane nzp - k: the conjugate matrix has the conjugate eigenvectors and the same eigenvalues, so
+    // K, V, G and the off-diagonal entries of g g^H are conjugated
+    __syncwarp();
+    conj_all(&o.K[0][0], kMaxTheta * 3, lane);
+    conj_all(&o.V[0][0], kMaxTheta * kMaxTheta, lane);
+    conj_all(&o.G[0][0], kMaxTheta * 3, lane);
+    for (int m = lane; m < kMaxTheta; m += 32) {
+      o.P[m][4] = -o.P[m][4];
+      o.P[m][6] = -o.P[m][6];
+      o.P[m][8] = -o.P[m][8];
+    }
+    __syncwarp();
+    float *odm = (float *)&p.ti[km];
+    for (int i = lane; i < (int)(sizeof(ITab) / sizeof(float)); i += 32) odm[i] = os[i];
+  }
 }
 
 }  // namespace cg

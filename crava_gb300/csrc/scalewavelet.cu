@@ -9,7 +9,8 @@
 // (C2R) and scales by 1/nzp.  The factor compares the inversion of one trace
 // with the local wavelet (the global wavelet shifted by the local time shift,
 // scaled by the local gain and stretched by the relative thickness: getCAmp(k,
-// sf) interpolates the spectrum at k/sf) with the one the global wavelet gives.
+// sf) interpolates the spectrum at k/sf and multiplies by 1/sf) with the one
+// the global wavelet gives.
 // multiplyDataByScaleWaveletAndWriteToFile (:906-968) is the inverse step on
 // output cubes: every simbox trace times the conjugate stretched local wavelet
 // spectrum.  FFTGrid::interpolateSeismic (src/fftgrid.cpp:2576-2738) then
@@ -205,6 +206,9 @@ __device__ float2 adjustment(const float *tab, int nzp, const SwTrace &t, int k,
     wLoc = make_float2(wa.x * d1 + wb.x * d, wa.y * d1 + wb.y * d);
     const float2 ea = e3_val(E, omL, pL, nzp), eb = e3_val(E, omU, pU, nzp);
     eLoc = make_float2(ea.x * d1 + eb.x * d, ea.y * d1 + eb.y * d);
+    // getCAmp(k, sf) returns the interpolated value times 1/sf (src/wavelet.cpp:382-383)
+    wLoc = make_float2(wLoc.x / t.sf, wLoc.y / t.sf);
+    eLoc = make_float2(eLoc.x / t.sf, eLoc.y / t.sf);
   }
   const float wLoc2 = wLoc.x * wLoc.x + wLoc.y * wLoc.y;
   const float2 wG = W[k];
@@ -243,7 +247,8 @@ __device__ float2 local_wavelet(const float *tab, int nzp, const SwTrace &t, int
   const float2 pU = (SHIFT && omU != omL) ? cmulf(pL, t.step) : pL;
   const float2 wa = wl_val(W, omL, pL, t.gain, nzp);
   const float2 wb = wl_val(W, omU, pU, t.gain, nzp);
-  return make_float2(wa.x * d1 + wb.x * d, wa.y * d1 + wb.y * d);
+  // getCAmp(k, sf) returns the interpolated value times 1/sf (src/wavelet.cpp:382-383)
+  return make_float2((wa.x * d1 + wb.x * d) / t.sf, (wa.y * d1 + wb.y * d) / t.sf);
 }
 
 enum { kSwDivide = 0, kSwMultiply = 1 };

@@ -98,12 +98,17 @@ std::vector<cd> twiddles(int n)
   return tw;
 }
 
-// full spectrum of a real sequence; getCAmp semantics are applied by the caller
+// full spectrum of a real sequence with the reference's half-spectrum semantics: the DC (and, for even
+// n, Nyquist) bins are real and bins k >= n/2+1 are the conjugates of bins n-k, as Wavelet::getCAmp
+// reflects them (src/wavelet.cpp:309-325), so every table built from it is exactly conjugate-symmetric
 std::vector<cd> rfft(const std::vector<double> &x, const std::vector<cd> &tw)
 {
   const int n = (int)x.size();
   std::vector<cd> in(x.begin(), x.end()), out(n);
   dft_rec(in.data(), n, 1, out.data(), tw, 1);
+  out[0] = cd(out[0].real(), 0.0);
+  if (n % 2 == 0) out[n / 2] = cd(out[n / 2].real(), 0.0);
+  for (int k = n / 2 + 1; k < n; k++) out[k] = std::conj(out[n - k]);
   return out;
 }
 
@@ -155,7 +160,7 @@ extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *w
     for (int k = 0; k < nzp; k++) {
       const long o = ((long)k * ntheta + l) * 2;
       if (constant_thickness) {
-        // the full spectrum already holds getCAmp's reflected/conjugated values for k >= nzp/2+1
+        // the full spectrum holds getCAmp's reflected/conjugated values for k >= nzp/2+1
         const cd kw = std::conj(W[k]);
         const cd p = cmul(kD[k], kw);
         for (int q = 0; q < 3; q++) {
@@ -188,7 +193,8 @@ extern "C" int cg_operator_tables_ex(int ntheta, int nz, int nzp, const float *w
           const int omL = (int)std::floor(omega);
           const int omU = omL + 1 < cnzp ? omL + 1 : omL;
           const float d = omega - (float)omL;
-          const cd v = W[omL] * (double)(1.0f - d) + W[omU] * (double)d;
+          // getCAmp(k, scale) returns the interpolated value times 1/scale (src/wavelet.cpp:382-383)
+          const cd v = (W[omL] * (double)(1.0f - d) + W[omU] * (double)d) / (double)0.999f;
           modf = std::norm(v);
         }
         const double maxMod = std::max(std::norm(W[kk]), modf);

@@ -208,6 +208,8 @@ class Scenario:
     wavelet_shift: np.ndarray | None = None   # (n, ny, nx) float32 ms, local wavelet time shift
     wavelet_gain: np.ndarray | None = None    # (n, ny, nx) float32, local wavelet gain
     energy_threshold: float = 0.0             # FFTGrid::interpolateSeismic
+    corr_t: np.ndarray | None = None          # the temporal correlation lags circ_corr_t was made from
+    min_int_fq: int = 0                       # the lowest inverted frequency index of computeCircCorrT
 
     @property
     def ntheta(self):
@@ -337,7 +339,7 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     return Scenario(nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, dt_ms=dt_ms, theta_deg=list(theta_deg),
                     A=A, wavelets=wav, corr_xy=cxy, circ_corr_t=cct, sigma0=sig0, err_theta_cov=etc,
                     data=data, mean=mean, wnc=wnc, low_cut=low_cut, high_cut=high_cut, sn=list(snr),
-                    truth=[t for t in truth] if keep_truth else None)
+                    truth=[t for t in truth] if keep_truth else None, corr_t=corr_t, min_int_fq=min_int_fq)
 
 
 # ----------------------------------------------------------------------------

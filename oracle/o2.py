@@ -1,0 +1,144 @@
+"""Driver of oracle/_ref/crava_o2, the harness around the reference's own
+compiled Crava / Wavelet / SeismicParametersHolder / State4D classes -- TEST
+INFRASTRUCTURE ONLY.  tests/golden/make_golden.py calls it where the
+reference checkout exists (CRAVA_REFERENCE_SRC) to write golden fixtures;
+the tests read the fixtures, never this module.
+
+Each call writes the inputs as raw little-endian arrays plus a params.txt
+into a scratch directory, runs ``crava_o2 <command> <dir>`` and reads the
+outputs back (oracle/o2_harness.cpp documents every file).
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+O2_EXE = os.path.join(HERE, "_ref", "crava_o2")
+
+
+def build(reference_src: str) -> str:
+    subprocess.check_call(["make", "-s", "-f", os.path.join(HERE, "Makefile.o2"), f"REF={reference_src}",
+                           f"-j{os.cpu_count() or 4}"], cwd=os.path.dirname(HERE))
+    return O2_EXE
+
+
+def _run(cmd, d):
+    r = subprocess.run([O2_EXE, cmd, d], cwd=d, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"crava_o2 {cmd} failed ({r.returncode}): {r.stderr[-2000:]}")
+
+
+def _params(d, **kw):
+    with open(os.path.join(d, "params.txt"), "w") as f:
+        for k, v in kw.items():
+            f.write(f"{k} {v!r}\n")
+
+
+def _w(d, name, arr, dt):
+    np.ascontiguousarray(arr, dtype=dt).tofile(os.path.join(d, name))
+
+
+def _r(d, name, dt, shape=None):
+    a = np.fromfile(os.path.join(d, name), dtype=dt)
+    return a.reshape(shape) if shape is not None else a
+
+
+def inversion(sc, corr_t, min_int_fq, f_peak, wavelets=None):
+    """Crava::computePostMeanResidAndFFTCov on the scenario's data and prior means, with the reference's
+    own Ricker wavelets (peak frequency f_peak; or, when ``wavelets`` (n, nzp) is given, those resampled
+    samples in the reference's Wavelet objects) and prior/error correlation cubes built from corr_xy and
+    the temporal correlation corr_t.  Returns the reference's intermediate and final arrays (complex
+    spectra as (nzp, nyp, cnxp) complex64, real cubes as (nzp, nyp, rnxp) float32)."""
+    n, nxp, nyp, nzp = sc.ntheta, sc.nxp, sc.nyp, sc.nzp
+    cnxp, rnxp = nxp // 2 + 1, 2 * (nxp // 2 + 1)
+    shape = (nzp, nyp, rnxp)
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=nxp, nyp=nyp, nzp=nzp, ntheta=n, ncorrt=len(corr_t),
+                min_int_fq=int(min_int_fq), dt=float(sc.dt_ms), fpeak=float(f_peak), low_cut=float(sc.low_cut),
+                high_cut=float(sc.high_cut), wnc=float(sc.wnc), given_wavelets=int(wavelets is not None))
+        if wavelets is not None:
+            _w(d, "wavelets_in.f32", wavelets, np.float32)
+        _w(d, "theta.f32", sc.theta_deg, np.float32)
+        _w(d, "A.f32", sc.A, np.float32)
+        _w(d, "etc.f64", sc.err_theta_cov, np.float64)
+        _w(d, "sigma0.f32", np.asarray(sc.sigma0, dtype=np.float64).astype(np.float32), np.float32)
+        _w(d, "corrxy.f64", np.asarray(sc.corr_xy, dtype=np.float32).astype(np.float64), np.float64)
+        _w(d, "corrt.f32", corr_t, np.float32)
+        _w(d, "data.f32", np.stack(sc.data), np.float32)
+        _w(d, "mean.f32", np.stack(sc.mean), np.float32)
+        _run("inversion", d)
+        spec = lambda a: a.view(np.complex64).reshape((nzp, nyp, cnxp))  # noqa: E731
+        out = _r(d, "output.f32", np.float32, (3 + n + 6,) + shape)
+        inp = _r(d, "input_spectra.f32", np.float32, (n + 3,) + shape)
+        res = {
+            "wavelets": _r(d, "wavelets.f32", np.float32, (n, nzp)),
+            "wavelet_norms": _r(d, "wavelet_norms.f32", np.float32),
+            "circ_corr_t": _r(d, "circcorrt.f32", np.float32),
+            "prior_cov_real": _r(d, "prior_cov_real.f32", np.float32, (6,) + shape),
+            "errcorr_real": _r(d, "errcorr_real.f32", np.float32, shape),
+            "errcorr_spec": spec(_r(d, "errcorr_spec.f32", np.float32, shape)),
+            "data_spec": np.stack([spec(x) for x in inp[:n]]),
+            "mean_spec": np.stack([spec(x) for x in inp[n:]]),
+            "out_mean_real": out[:3],
+            "out_resid": np.stack([spec(x) for x in out[3:3 + n]]),
+            "out_cov": np.stack([spec(x) for x in out[3 + n:]]),
+        }
+        for sfx in ("", "_nct"):
+            res["K" + sfx] = _r(d, f"K{sfx}.f32", np.float32).view(np.complex64).reshape(nzp, n, 3)
+            for e in ("em1", "em2", "em3"):
+                res[e + sfx] = _r(d, f"{e}{sfx}.f32", np.float32).view(np.complex64).reshape(nzp, n)
+            res["band" + sfx] = _r(d, f"band{sfx}.u8", np.uint8)
+    return res
+
+
+def state4d(state27, post9, nxp):
+    """State4D::merge then State4D::split.  state27: the 27 state spectra (mu_s 3, mu_d 3, static-static 6,
+    static-dynamic 9, dynamic-dynamic 6), post9: the current state's posterior (mean 3, covariance in the
+    order 00 01 02 11 12 22), all (nzp, nyp, cnxp) complex64.  Returns (merged 9 spectra, split 27)."""
+    state27 = np.ascontiguousarray(state27, dtype=np.complex64)
+    post9 = np.ascontiguousarray(post9, dtype=np.complex64)
+    nzp, nyp, cnxp = state27.shape[1:]
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nxp=nxp, nyp=nyp, nzp=nzp)
+        _w(d, "state.f32", state27.view(np.float32), np.float32)
+        _w(d, "post.f32", post9.view(np.float32), np.float32)
+        _run("state4d", d)
+        merged = _r(d, "merged.f32", np.float32).view(np.complex64).reshape(9, nzp, nyp, cnxp)
+        split = _r(d, "split.f32", np.float32).view(np.complex64).reshape(27, nzp, nyp, cnxp)
+    return merged, split
+
+
+def adjustment(sc, l, corr_t, min_int_fq, f_peak, cases, error_var):
+    """Crava::computeAdjustmentFactor for angle l of the scenario: the reference's Ricker (f_peak) resampled
+    on the grid is the global wavelet; cases: (n, 3) of (time shift ms, gain, stretch).  Returns (the
+    global wavelet samples, the filtered temporal correlation it used, (n, nzp/2+1) complex factors)."""
+    cases = np.ascontiguousarray(cases, dtype=np.float32)
+    nzp = sc.nzp
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=sc.nxp, nyp=sc.nyp, nzp=nzp, ncases=len(cases),
+                ncorrt=len(corr_t), min_int_fq=int(min_int_fq), dt=float(sc.dt_ms), fpeak=float(f_peak),
+                theta=float(sc.theta_deg[l]), error_var=float(error_var), low_cut=float(sc.low_cut),
+                high_cut=float(sc.high_cut), wnc=float(sc.wnc))
+        _w(d, "A.f32", sc.A[l], np.float32)
+        _w(d, "sigma0.f32", np.asarray(sc.sigma0, dtype=np.float64).astype(np.float32), np.float32)
+        _w(d, "corrxy.f64", np.asarray(sc.corr_xy, dtype=np.float32).astype(np.float64), np.float64)
+        _w(d, "corrt.f32", corr_t, np.float32)
+        _w(d, "cases.f32", cases, np.float32)
+        _run("adjust", d)
+        wav = _r(d, "wavelet.f32", np.float32)
+        ct_f = _r(d, "corrt_filtered.f32", np.float32)
+        adj = _r(d, "adjust.f32", np.float32).view(np.complex64).reshape(len(cases), nzp // 2 + 1)
+    return wav, ct_f, adj
+
+
+def closest_factorable(ns):
+    ns = np.asarray(ns, dtype=np.int32)
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, count=len(ns))
+        _w(d, "n.i32", ns, np.int32)
+        _run("factorable", d)
+        return _r(d, "factorable.i32", np.int32)

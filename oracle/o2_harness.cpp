@@ -1,0 +1,441 @@
+// In-process harness around the reference's own compiled classes -- TEST
+// INFRASTRUCTURE ONLY (it generates golden fixtures; nothing in the product
+// links it).  Built by oracle/Makefile.o2 from the unmodified reference
+// sources; runs only where the reference checkout is (x86 build container).
+//
+//   crava_o2 inversion  <dir>   Ricker wavelets (Wavelet1D + Wavelet::resample),
+//                               prior covariance cubes (SeismicParametersHolder::
+//                               initializeCorrelations: computeCircCorrT +
+//                               FFTGrid::fillInParamCorr), error correlation
+//                               (FFTGrid::fillInErrCorr), the data and prior-mean
+//                               transforms (FFTGrid::fftInPlace), then
+//                               Crava::computePostMeanResidAndFFTCov itself
+//                               (src/crava.cpp:975-1285); afterwards the per-k
+//                               tables of Crava::fillErrMultVectors for both
+//                               thickness branches (src/crava.cpp:1337-1386).
+//   crava_o2 state4d    <dir>   State4D::merge and State4D::split
+//                               (src/state4d.cpp:140-580) on given spectra.
+//   crava_o2 adjust     <dir>   Crava::computeAdjustmentFactor (src/crava.cpp:807-903)
+//                               for given local shifts, gains and stretches.
+//   crava_o2 factorable <dir>   FFTGrid::findClosestFactorableNumber.
+//
+// <dir> holds params.txt ("key value" lines) and raw little-endian arrays
+// named in this file; outputs are written to the same directory.  A minimal
+// Crava / ModelGeneral is set up by writing the few members the called
+// methods read (seisData_, ntheta_, nzp_; do4DInversion_), which is why the
+// reference headers are included with their access specifiers opened.
+#include <algorithm>
+#include <cassert>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <csignal>
+#include <execinfo.h>
+#include <unistd.h>
+#include <fstream>
+#include <iostream>
+#include <list>
+#include <new>
+#include <map>
+#include <set>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#define private public
+#define protected public
+#include "src/crava.h"
+#include "src/definitions.h"
+#include "src/fftgrid.h"
+#include "src/modelgeneral.h"
+#include "src/modelsettings.h"
+#include "src/seismicparametersholder.h"
+#include "src/simbox.h"
+#include "src/state4d.h"
+#include "src/wavelet1D.h"
+#undef private
+#undef protected
+
+namespace {
+
+std::string g_dir;
+
+std::map<std::string, double> read_params()
+{
+  std::map<std::string, double> p;
+  std::ifstream f((g_dir + "/params.txt").c_str());
+  std::string k;
+  double v;
+  while (f >> k >> v) p[k] = v;
+  return p;
+}
+
+template <typename T>
+std::vector<T> read_arr(const std::string &name, size_t n)
+{
+  std::vector<T> v(n);
+  FILE *f = fopen((g_dir + "/" + name).c_str(), "rb");
+  if (!f || fread(&v[0], sizeof(T), n, f) != n) {
+    fprintf(stderr, "cannot read %s (%zu values)\n", name.c_str(), n);
+    exit(2);
+  }
+  fclose(f);
+  return v;
+}
+
+void write_raw(const std::string &name, const void *p, size_t bytes)
+{
+  FILE *f = fopen((g_dir + "/" + name).c_str(), "wb");
+  if (!f || fwrite(p, 1, bytes, f) != bytes) {
+    fprintf(stderr, "cannot write %s\n", name.c_str());
+    exit(2);
+  }
+  fclose(f);
+}
+
+// a grid holding `vals` (rsize floats, the FFTGrid in-place layout) in the given domain
+FFTGrid *make_grid(int nx, int ny, int nz, int nxp, int nyp, int nzp, int cubetype, const float *vals, bool transformed)
+{
+  FFTGrid *g = new FFTGrid(nx, ny, nz, nxp, nyp, nzp);
+  g->createRealGrid(false);
+  g->setType(cubetype);
+  if (vals) memcpy(g->rvalue_, vals, sizeof(float) * (size_t)g->rsize_);
+  g->istransformed_ = transformed;
+  return g;
+}
+
+void dump_grid(const std::string &name, FFTGrid *g)
+{
+  write_raw(name, g->rvalue_, sizeof(float) * (size_t)g->rsize_);
+}
+
+int cmd_inversion()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"], n = (int)p["ntheta"];
+  const int ncorrt = (int)p["ncorrt"], min_int_fq = (int)p["min_int_fq"];
+  const float dt = (float)p["dt"], fpeak = (float)p["fpeak"], low_cut = (float)p["low_cut"];
+  const float high_cut = (float)p["high_cut"], wnc = (float)p["wnc"];
+  const int cnxp = nxp / 2 + 1, rnxp = 2 * cnxp;
+  const size_t rsize = (size_t)rnxp * nyp * nzp;
+
+  std::vector<float> theta = read_arr<float>("theta.f32", n);
+  std::vector<float> A = read_arr<float>("A.f32", (size_t)n * 3);
+  std::vector<double> etc = read_arr<double>("etc.f64", (size_t)n * n);
+  std::vector<float> s0 = read_arr<float>("sigma0.f32", 9);
+  std::vector<double> cxy = read_arr<double>("corrxy.f64", (size_t)nxp * nyp);
+  std::vector<float> corrT = read_arr<float>("corrt.f32", ncorrt);
+  std::vector<float> data = read_arr<float>("data.f32", rsize * n);
+  std::vector<float> mean = read_arr<float>("mean.f32", rsize * 3);
+
+  // wavelets: the reference's Ricker (239 taps at 1 ms), resampled onto the grid in FFT order; one set
+  // for the inversion (which transforms them) and one for the table extraction afterwards
+  // (given_wavelets = 1: the resampled samples are replaced by wavelets_in.f32, n x nzp in FFT order, and
+  // the norm recomputed from them as Wavelet::resample computes it, src/wavelet.cpp:442-446)
+  ModelSettings ms;
+  Wavelet **wav = new Wavelet *[n], **wav2 = new Wavelet *[n];
+  std::vector<float> wav_out((size_t)n * nzp), wav_norm(n), given;
+  if (p["given_wavelets"] != 0.0) given = read_arr<float>("wavelets_in.f32", (size_t)n * nzp);
+  for (int set = 0; set < 2; set++)
+    for (int l = 0; l < n; l++) {
+      int err = 0;
+      Wavelet1D *w = new Wavelet1D(&ms, &A[3 * l], theta[l], fpeak, err);
+      if (err) { fprintf(stderr, "wavelet %d: error %d\n", l, err); return 3; }
+      w->resample(dt, nz, nzp);
+      if (!given.empty()) {
+        double norm2 = 0.0;
+        for (int k = 0; k < nzp; k++) {
+          w->rAmp_[k] = given[(size_t)l * nzp + k];
+          norm2 += static_cast<double>(w->rAmp_[k] * w->rAmp_[k]);
+        }
+        w->norm_ = static_cast<float>(sqrt(norm2));
+      }
+      if (set == 0) {
+        for (int k = 0; k < nzp; k++) wav_out[(size_t)l * nzp + k] = w->rAmp_[k];
+        wav_norm[l] = w->norm_;
+        wav[l] = w;
+      } else {
+        wav2[l] = w;
+      }
+    }
+  write_raw("wavelets.f32", &wav_out[0], sizeof(float) * wav_out.size());
+  write_raw("wavelet_norms.f32", &wav_norm[0], sizeof(float) * n);
+
+  // lateral correlation surface (ModelGeneral::findCorrXYGrid's output), nxp x nyp
+  Surface corr_xy(0.0, 0.0, 25.0 * nxp, 25.0 * nyp, nxp, nyp, 0.0);
+  for (int j = 0; j < nyp; j++)
+    for (int i = 0; i < nxp; i++) corr_xy(i + nxp * j) = cxy[(size_t)j * nxp + i];
+
+  // prior covariance cubes: computeCircCorrT + fillInParamCorr x priorVar0
+  SeismicParametersHolder sp;
+  sp.priorVar0_.resize(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) sp.priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
+  sp.createCorrGrids(nx, ny, nz, nxp, nyp, nzp, false);
+  sp.initializeCorrelations(&corr_xy, corrT, 0.0f, 0.0f, min_int_fq, nzp);
+  fftw_real *circ = sp.computeCircCorrT(corrT, min_int_fq, nzp);
+  write_raw("circcorrt.f32", circ, sizeof(float) * nzp);
+  fftw_free(circ);
+  FFTGrid *covs[6] = {sp.covAlpha_, sp.covBeta_, sp.covRho_, sp.crCovAlphaBeta_, sp.crCovAlphaRho_, sp.crCovBetaRho_};
+  {
+    std::vector<float> prior_cov(rsize * 6);
+    for (int t = 0; t < 6; t++) memcpy(&prior_cov[rsize * t], covs[t]->rvalue_, sizeof(float) * rsize);
+    write_raw("prior_cov_real.f32", &prior_cov[0], sizeof(float) * prior_cov.size());
+  }
+
+  FFTGrid *errcorr = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::COVARIANCE, NULL, false);
+  errcorr->fillInErrCorr(&corr_xy, 0.0f, 0.0f);
+  dump_grid("errcorr_real.f32", errcorr);
+
+  // data and prior means, transformed by the reference's own fftInPlace (src/crava.cpp:177-184)
+  FFTGrid **seis = new FFTGrid *[n];
+  for (int l = 0; l < n; l++) {
+    seis[l] = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::DATA, &data[rsize * l], false);
+    seis[l]->fftInPlace();
+  }
+  FFTGrid *mu[3];
+  for (int q = 0; q < 3; q++) {
+    mu[q] = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::PARAMETER, &mean[rsize * q], false);
+    mu[q]->fftInPlace();
+  }
+  {
+    std::vector<float> spec(rsize * (n + 3));
+    for (int l = 0; l < n; l++) memcpy(&spec[rsize * l], seis[l]->rvalue_, sizeof(float) * rsize);
+    for (int q = 0; q < 3; q++) memcpy(&spec[rsize * (n + q)], mu[q]->rvalue_, sizeof(float) * rsize);
+    write_raw("input_spectra.f32", &spec[0], sizeof(float) * spec.size());
+  }
+
+  // the minimal Crava / ModelGeneral / Simbox the inversion reads
+  Crava *crava = static_cast<Crava *>(operator new(sizeof(Crava)));
+  memset((void *)crava, 0, sizeof(Crava));
+  crava->seisData_ = seis;
+  crava->ntheta_ = n;
+  crava->nzp_ = nzp;
+  crava->nz_ = nz;
+  ModelGeneral *mg = static_cast<ModelGeneral *>(operator new(sizeof(ModelGeneral)));
+  memset((void *)mg, 0, sizeof(ModelGeneral));
+  mg->do4DInversion_ = false;
+  Simbox simbox;
+  simbox.lz_ = (double)nz * dt;
+  simbox.constThick_ = true;
+  simbox.minRelThick_ = 1.0;
+
+  double **etcp = new double *[n];
+  float **Ap = new float *[n];
+  for (int l = 0; l < n; l++) { etcp[l] = &etc[(size_t)n * l]; Ap[l] = &A[3 * l]; }
+
+  crava->computePostMeanResidAndFFTCov(mg, &simbox, sp, mu[0], mu[1], mu[2], errcorr, seis, wav, etcp, Ap, &theta[0], n,
+                                       low_cut, high_cut, wnc, nz, nzp, nyp, nxp, 1, false);
+
+  {
+    std::vector<float> out(rsize * (3 + n + 6));
+    for (int q = 0; q < 3; q++) memcpy(&out[rsize * q], mu[q]->rvalue_, sizeof(float) * rsize);
+    for (int l = 0; l < n; l++) memcpy(&out[rsize * (3 + l)], seis[l]->rvalue_, sizeof(float) * rsize);
+    for (int t = 0; t < 6; t++) memcpy(&out[rsize * (3 + n + t)], covs[t]->rvalue_, sizeof(float) * rsize);
+    write_raw("output.f32", &out[0], sizeof(float) * out.size());
+    dump_grid("errcorr_spec.f32", errcorr);
+  }
+
+  // the per-k tables both thickness branches hand to the bin solve, built from the second wavelet set in
+  // the order computePostMeanResidAndFFTCov builds them (src/crava.cpp:1002-1049)
+  Wavelet1D *d1 = new Wavelet1D(Wavelet::FIRSTORDERFORWARDDIFF, nz, nzp);
+  Wavelet1D *d2 = new Wavelet1D(d1, Wavelet::FIRSTORDERBACKWARDDIFF);
+  Wavelet1D *d3 = new Wavelet1D(d2, Wavelet::FIRSTORDERCENTRALDIFF);
+  d1->fft1DInPlace();
+  d3->fft1DInPlace();
+  Wavelet1D **es = new Wavelet1D *[n], **es3 = new Wavelet1D *[n], **wnorm = new Wavelet1D *[n];
+  crava->makeErrorSmooth(es, es3, seis, wav2, &theta[0], n);
+  for (int l = 0; l < n; l++) {
+    wnorm[l] = wav2[l]->createWavelet1DForErrorNorm();
+    wnorm[l]->fft1DInPlace();
+  }
+  for (int branch = 1; branch >= 0; branch--) {  // the non-constant branch reads the wavelets untransformed
+    const bool constant = branch == 0;
+    if (constant)
+      for (int l = 0; l < n; l++) wav2[l]->fft1DInPlace();
+    std::vector<float> K((size_t)nzp * n * 3 * 2), e1((size_t)nzp * n * 2), e2(e1.size()), e3(e1.size());
+    std::vector<unsigned char> band(nzp);
+    fftw_complex *m1 = new fftw_complex[n], *m2 = new fftw_complex[n], *m3 = new fftw_complex[n];
+    fftw_complex **Kk = crava->allocateFFTComplex(n, 3);
+    for (int k = 0; k < nzp; k++) {
+      const float f = static_cast<float>((nz * 1000.0f) / (simbox.getlz() * nzp) * std::min(k, nzp - k));
+      band[k] = (f > low_cut * simbox.getMinRelThick() && f < high_cut) ? 1 : 0;
+      crava->fillErrMultVectors(m1, m2, m3, Kk, d1->getCAmp(k), d3->getCAmp(k), wav2, wnorm, es3, Ap, constant, n, k);
+      for (int l = 0; l < n; l++) {
+        for (int q = 0; q < 3; q++) {
+          K[(((size_t)k * n + l) * 3 + q) * 2] = Kk[l][q].re;
+          K[(((size_t)k * n + l) * 3 + q) * 2 + 1] = Kk[l][q].im;
+        }
+        e1[((size_t)k * n + l) * 2] = m1[l].re; e1[((size_t)k * n + l) * 2 + 1] = m1[l].im;
+        e2[((size_t)k * n + l) * 2] = m2[l].re; e2[((size_t)k * n + l) * 2 + 1] = m2[l].im;
+        e3[((size_t)k * n + l) * 2] = m3[l].re; e3[((size_t)k * n + l) * 2 + 1] = m3[l].im;
+      }
+    }
+    const std::string sfx = constant ? "" : "_nct";
+    write_raw("K" + sfx + ".f32", &K[0], sizeof(float) * K.size());
+    write_raw("em1" + sfx + ".f32", &e1[0], sizeof(float) * e1.size());
+    write_raw("em2" + sfx + ".f32", &e2[0], sizeof(float) * e2.size());
+    write_raw("em3" + sfx + ".f32", &e3[0], sizeof(float) * e3.size());
+    write_raw("band" + sfx + ".u8", &band[0], band.size());
+  }
+  return 0;
+}
+
+int cmd_state4d()
+{
+  std::map<std::string, double> p = read_params();
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"];
+  const int cnxp = nxp / 2 + 1, rnxp = 2 * cnxp;
+  const size_t rsize = (size_t)rnxp * nyp * nzp;
+  // state spectra in: mu_s(3) mu_d(3) ss(6) sd(9) dd(6); posterior of the current state: mu(3) cov(6)
+  std::vector<float> st = read_arr<float>("state.f32", rsize * 27);
+  std::vector<float> post = read_arr<float>("post.f32", rsize * 9);
+  std::vector<FFTGrid *> g(27);
+  for (int t = 0; t < 27; t++)
+    g[t] = make_grid(nxp, nyp, nzp, nxp, nyp, nzp, t < 6 ? FFTGrid::PARAMETER : FFTGrid::COVARIANCE, &st[rsize * t], true);
+  State4D s4;
+  s4.setStaticMu(g[0], g[1], g[2]);
+  s4.setDynamicMu(g[3], g[4], g[5]);
+  s4.setStaticSigma(g[6], g[7], g[8], g[9], g[10], g[11]);
+  s4.setStaticDynamicSigma(g[12], g[13], g[14], g[15], g[16], g[17], g[18], g[19], g[20]);
+  s4.setDynamicSigma(g[21], g[22], g[23], g[24], g[25], g[26]);
+
+  // merge: the current state's prior (means and covariance spectra)
+  SeismicParametersHolder cur;
+  cur.muAlpha_ = make_grid(nxp, nyp, nzp, nxp, nyp, nzp, FFTGrid::PARAMETER, NULL, true);
+  cur.muBeta_ = make_grid(nxp, nyp, nzp, nxp, nyp, nzp, FFTGrid::PARAMETER, NULL, true);
+  cur.muRho_ = make_grid(nxp, nyp, nzp, nxp, nyp, nzp, FFTGrid::PARAMETER, NULL, true);
+  FFTGrid **cg[6] = {&cur.covAlpha_, &cur.crCovAlphaBeta_, &cur.crCovAlphaRho_, &cur.covBeta_, &cur.crCovBetaRho_,
+                     &cur.covRho_};
+  for (int t = 0; t < 6; t++) *cg[t] = make_grid(nxp, nyp, nzp, nxp, nyp, nzp, FFTGrid::COVARIANCE, NULL, true);
+  s4.merge(cur);
+  {
+    std::vector<float> out(rsize * 9);
+    FFTGrid *m[3] = {cur.muAlpha_, cur.muBeta_, cur.muRho_};
+    for (int q = 0; q < 3; q++) memcpy(&out[rsize * q], m[q]->rvalue_, sizeof(float) * rsize);
+    for (int t = 0; t < 6; t++) memcpy(&out[rsize * (3 + t)], (*cg[t])->rvalue_, sizeof(float) * rsize);
+    write_raw("merged.f32", &out[0], sizeof(float) * out.size());
+  }
+  // split with the given posterior of the current state (order: mu 3, then 00 01 02 11 12 22)
+  FFTGrid *m[3] = {cur.muAlpha_, cur.muBeta_, cur.muRho_};
+  for (int q = 0; q < 3; q++) memcpy(m[q]->rvalue_, &post[rsize * q], sizeof(float) * rsize);
+  for (int t = 0; t < 6; t++) memcpy((*cg[t])->rvalue_, &post[rsize * (3 + t)], sizeof(float) * rsize);
+  s4.split(cur);
+  {
+    std::vector<float> out(rsize * 27);
+    for (int t = 0; t < 27; t++) memcpy(&out[rsize * t], g[t]->rvalue_, sizeof(float) * rsize);
+    write_raw("split.f32", &out[0], sizeof(float) * out.size());
+  }
+  return 0;
+}
+
+// Crava::computeAdjustmentFactor (src/crava.cpp:807-903) for a list of (time shift, gain, stretch) cases:
+// the local wavelet is the global Ricker copied and shifted / scaled as createLocalWavelet1D does
+int cmd_adjust()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"], nc = (int)p["ncases"];
+  const int ncorrt = (int)p["ncorrt"], min_int_fq = (int)p["min_int_fq"];
+  const float dt = (float)p["dt"], fpeak = (float)p["fpeak"], theta = (float)p["theta"];
+  const float error_var = (float)p["error_var"];
+  std::vector<float> A = read_arr<float>("A.f32", 3);
+  std::vector<float> s0 = read_arr<float>("sigma0.f32", 9);
+  std::vector<double> cxy = read_arr<double>("corrxy.f64", (size_t)nxp * nyp);
+  std::vector<float> corrT = read_arr<float>("corrt.f32", ncorrt);
+  std::vector<float> cases = read_arr<float>("cases.f32", (size_t)nc * 3);
+
+  ModelSettings ms;
+  int err = 0;
+  Wavelet1D *wglob = new Wavelet1D(&ms, &A[0], theta, fpeak, err);
+  if (err) { fprintf(stderr, "wavelet: error %d\n", err); return 3; }
+  wglob->resample(dt, nz, nzp);
+  write_raw("wavelet.f32", wglob->rAmp_, sizeof(float) * nzp);
+
+  Surface corr_xy(0.0, 0.0, 25.0 * nxp, 25.0 * nyp, nxp, nyp, 0.0);
+  for (int j = 0; j < nyp; j++)
+    for (int i = 0; i < nxp; i++) corr_xy(i + nxp * j) = cxy[(size_t)j * nxp + i];
+  SeismicParametersHolder sp;
+  sp.priorVar0_.resize(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) sp.priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
+  sp.createCorrGrids(nx, ny, nz, nxp, nyp, nzp, false);
+  sp.initializeCorrelations(&corr_xy, corrT, 0.0f, 0.0f, min_int_fq, nzp);
+  float *filtered = sp.getPriorCorrTFiltered(nz, nzp);
+  write_raw("corrt_filtered.f32", filtered, sizeof(float) * nzp);
+  delete[] filtered;
+
+  Simbox simbox;
+  simbox.lz_ = (double)nz * dt;
+  Crava *crava = static_cast<Crava *>(operator new(sizeof(Crava)));
+  memset((void *)crava, 0, sizeof(Crava));
+  crava->nz_ = nz;
+  crava->nzp_ = nzp;
+  crava->lowCut_ = (float)p["low_cut"];
+  crava->highCut_ = (float)p["high_cut"];
+  crava->wnc_ = (float)p["wnc"];
+  crava->simbox_ = &simbox;
+  new (&crava->priorVar0_) NRLib::Matrix(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) crava->priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
+
+  const int cnzp = nzp / 2 + 1;
+  std::vector<float> out((size_t)nc * cnzp * 2);
+  fftw_complex *adj = new fftw_complex[cnzp];
+  for (int c = 0; c < nc; c++) {
+    Wavelet1D *loc = new Wavelet1D(wglob);
+    loc->shiftAndScale(cases[3 * c], cases[3 * c + 1]);
+    crava->computeAdjustmentFactor(adj, loc, (double)cases[3 * c + 2], wglob, sp, &A[0], error_var);
+    for (int k = 0; k < cnzp; k++) {
+      out[((size_t)c * cnzp + k) * 2] = adj[k].re;
+      out[((size_t)c * cnzp + k) * 2 + 1] = adj[k].im;
+    }
+    delete loc;
+  }
+  write_raw("adjust.f32", &out[0], sizeof(float) * out.size());
+  return 0;
+}
+
+int cmd_factorable()
+{
+  std::map<std::string, double> p = read_params();
+  const int n = (int)p["count"];
+  std::vector<int> in = read_arr<int>("n.i32", n), out(n);
+  for (int i = 0; i < n; i++) out[i] = FFTGrid::findClosestFactorableNumber(in[i]);
+  write_raw("factorable.i32", &out[0], sizeof(int) * n);
+  return 0;
+}
+
+}  // namespace
+
+// a reference code path that reaches a left-out routine stops with a backtrace instead of silently
+void on_fault(int sig)
+{
+  void *frames[64];
+  const int n = backtrace(frames, 64);
+  fprintf(stderr, "crava_o2: signal %d\n", sig);
+  backtrace_symbols_fd(frames, n, 2);
+  _exit(128 + sig);
+}
+
+int main(int argc, char **argv)
+{
+  signal(SIGSEGV, on_fault);
+  signal(SIGABRT, on_fault);
+  if (argc != 3) {
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|factorable} <dir>\n");
+    return 1;
+  }
+  g_dir = argv[2];
+  const std::string c = argv[1];
+  if (c == "inversion") return cmd_inversion();
+  if (c == "state4d") return cmd_state4d();
+  if (c == "factorable") return cmd_factorable();
+  if (c == "adjust") return cmd_adjust();
+  fprintf(stderr, "unknown command %s\n", c.c_str());
+  return 1;
+}

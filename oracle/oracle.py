@@ -112,6 +112,9 @@ def lib():
             getattr(L, "or_divide_scale_wavelet" + sfx).argtypes = [
                 PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, PR, FP, ct.POINTER(ct.c_double), PR,
                 ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float, FP, FP, FP, ct.c_int]
+            getattr(L, "or_adjustment_factor" + sfx).argtypes = [
+                PR, PR, FP, ct.POINTER(ct.c_double), PR, ct.c_int, ct.c_int, ct.c_float, ct.c_float, ct.c_float,
+                ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float, ct.c_float]
             getattr(L, "or_multiply_scale_wavelet" + sfx).argtypes = [
                 PR, ct.c_int, ct.c_int, ct.c_int, ct.c_int, ct.c_int, PR, ct.c_float, FP, FP, FP, ct.c_int]
             getattr(L, "or_interpolate_seismic" + sfx).argtypes = [
@@ -429,6 +432,23 @@ def divide_scale_wavelet(buf, nx, ny, nz, wavelet, A, prior_var0, circ_corr_t, d
         pv.ctypes.data_as(ct.POINTER(ct.c_double)), _ptr(cc, R), dz, lz, low_cut, high_cut, wnc, err_var,
         rt.ctypes.data_as(ct.POINTER(ct.c_float)), _fptr(keep[0]), _fptr(keep[1]), nthreads or os.cpu_count())
     return out
+
+
+def adjustment_factor(wavelet, A, prior_var0, circ_corr_t, nz, dz, lz, low_cut, high_cut, wnc, err_var, ts, gain, sf,
+                      prec="f"):
+    """Crava::computeAdjustmentFactor for one local wavelet (the global one shifted by ts ms, scaled by gain,
+    stretched by sf): (nzp/2+1,) complex."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    nzp = len(wavelet)
+    out = np.zeros(2 * (nzp // 2 + 1), dtype=_rdt(prec))
+    w = np.ascontiguousarray(wavelet, dtype=_rdt(prec))
+    cc = np.ascontiguousarray(circ_corr_t, dtype=_rdt(prec))
+    A32 = np.ascontiguousarray(A, dtype=np.float32)
+    pv = np.ascontiguousarray(prior_var0, dtype=np.float64)
+    getattr(lib(), "or_adjustment_factor_" + prec)(
+        _ptr(out, R), _ptr(w, R), A32.ctypes.data_as(ct.POINTER(ct.c_float)), pv.ctypes.data_as(ct.POINTER(ct.c_double)),
+        _ptr(cc, R), nz, nzp, dz, lz, low_cut, high_cut, wnc, err_var, ts, gain, sf)
+    return out.view(np.complex64 if prec == "f" else np.complex128)
 
 
 def multiply_scale_wavelet(buf, nx, ny, wavelet, dz, rel_thick, shift=None, gain=None, prec="f", nthreads=None):
