@@ -1,14 +1,17 @@
 """Generate the golden fixtures in this directory from the reference build.
 
-Run where the CRAVA reference checkout exists (it builds oracle/_ref from the
-reference's own FFTW 2.1.2, lib_matr.c and random.cpp):
+Run where the CRAVA reference checkout exists, naming it:
 
-    python tests/golden/make_golden.py
+    CRAVA_REFERENCE_SRC=<reference checkout> python tests/golden/make_golden.py
 
-Every output array comes from the reference's compiled code (see
-oracle/ref_harness.cpp); the inputs are seeded synthetic cubes.  The fixtures
-are small so the CPU suite stays fast, and they travel to machines without the
-reference checkout, where they are the only reference-generated vectors.
+It builds oracle/_ref from the reference's own sources: the FFTW 2.1.2,
+lib_matr.c and random.cpp pieces with ref_harness.cpp (oracle/Makefile.ref),
+and crava_o2, the reference's whole Crava / Wavelet / SeismicParametersHolder
+/ State4D code with o2_harness.cpp (oracle/Makefile.o2).  Every output array
+comes from the reference's compiled code; the inputs are seeded synthetic
+cubes.  The fixtures are small so the CPU suite stays fast, and they travel to
+machines without the reference checkout, where they are the only
+reference-generated vectors.
 """
 import os
 import sys
@@ -19,8 +22,28 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, REPO)
 
+from oracle import o2  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 from crava_gb300 import synthetic as S  # noqa: E402
+
+NCT = ("K", "em1", "em2", "em3", "band")
+
+
+def reference_tables(wavelets, A, theta_deg, nz, nzp, dt_ms, low_cut, high_cut, wnc=0.1):
+    """The per-k tables of the reference's Crava::fillErrMultVectors for given resampled wavelets (both
+    thickness branches), from a crava_o2 run on a 2 x 1 lateral grid (the tables depend on the wavelets,
+    A, nz, nzp, dt and the band only)."""
+    n = len(theta_deg)
+    rnxp = 4  # 2 * (nxp//2 + 1) for nxp = 2
+    zero = np.zeros((nzp, 1, rnxp), np.float32)
+    sc = S.Scenario(nx=2, ny=1, nz=nz, nxp=2, nyp=1, nzp=nzp, dt_ms=dt_ms, theta_deg=list(theta_deg), A=A,
+                    wavelets=wavelets, corr_xy=np.ones((1, 2), np.float32), circ_corr_t=None,
+                    sigma0=np.diag([0.01, 0.005, 0.0025]), err_theta_cov=np.eye(n) * 1e-3, data=[zero] * n,
+                    mean=[zero] * 3, wnc=wnc, low_cut=low_cut, high_cut=high_cut,
+                    corr_t=S.genexp_corr_t(max(nz, 2), dt_ms, 20.0, 1.5),
+                    min_int_fq=int(np.floor(low_cut * (nzp * 0.001 * dt_ms))))
+    r = o2.inversion(sc, sc.corr_t, sc.min_int_fq, 30.0, wavelets=wavelets)
+    return {k: r[k] for k in NCT}, {k: r[k + "_nct"] for k in NCT}
 
 
 def fft_case(name, nxp, nyp, nzp, seed):
@@ -37,29 +60,73 @@ def fft_case(name, nxp, nyp, nzp, seed):
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
-def inversion_case(name, sc, is4d=False):
-    tab = O.k_tables(sc.nxp, sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut)
-    data = [O.ref_fft3d_r2c(d, sc.nxp, O.DATA) for d in sc.data]
-    mean = [O.ref_fft3d_r2c(m, sc.nxp, O.PARAMETER) for m in sc.mean]
-    covs = []
-    for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]:
-        c = O.fill_param_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, sc.circ_corr_t, 0, 0, np.float32(sc.sigma0[p, q]))
-        covs.append(O.ref_fft3d_r2c(c, sc.nxp, O.COVARIANCE))
-    ec = O.ref_fft3d_r2c(O.fill_err_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy), sc.nxp, O.COVARIANCE)
-    res, mu, cov, nfail = O.ref_invert_bins(data, mean, covs, ec, tab, sc.err_theta_cov, sc.sigma0, sc.wnc,
-                                            is4d=is4d)
+def inversion_case(name, sc, f_peak):
+    """One inversion by the reference's own Crava::computePostMeanResidAndFFTCov (crava_*) on the scenario's
+    inputs, with the scenario's resampled wavelets in the reference's Wavelet objects; the per-k tables
+    (both thickness branches), the prior / error correlation cubes and circCorrT are the reference's.  The
+    bin loop is also run by ref_harness.cpp's glue around the reference's lib_matr on the same spectra
+    (out_*), which keeps the posterior-mean spectra before the inverse transform."""
+    r = o2.inversion(sc, sc.corr_t, sc.min_int_fq, f_peak, wavelets=sc.wavelets)
+    tab = {k: r[k] for k in NCT}
+    data = list(r["data_spec"])
+    mean = list(r["mean_spec"])
+    covs = [O.ref_fft3d_r2c(c, sc.nxp, O.COVARIANCE) for c in r["prior_cov_real"]]
+    ec = O.ref_fft3d_r2c(r["errcorr_real"], sc.nxp, O.COVARIANCE)
+    res, mu, cov, nfail = O.ref_invert_bins(data, mean, covs, ec, dict(tab, nxp=sc.nxp), sc.err_theta_cov,
+                                            sc.sigma0, sc.wnc)
     post_real = [O.ref_fft3d_c2r(m, sc.nxp, O.PARAMETER) for m in mu]
     out = dict(nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=sc.nxp, nyp=sc.nyp, nzp=sc.nzp, dt_ms=sc.dt_ms,
                theta_deg=np.array(sc.theta_deg), A=sc.A, wavelets=sc.wavelets, corr_xy=sc.corr_xy,
-               circ_corr_t=sc.circ_corr_t, sigma0=sc.sigma0, err_theta_cov=sc.err_theta_cov, wnc=sc.wnc,
-               low_cut=sc.low_cut, high_cut=sc.high_cut,
+               corr_t=sc.corr_t, min_int_fq=sc.min_int_fq, circ_corr_t=r["circ_corr_t"], sigma0=sc.sigma0,
+               err_theta_cov=sc.err_theta_cov, wnc=sc.wnc, low_cut=sc.low_cut, high_cut=sc.high_cut,
                data_real=np.stack(sc.data), mean_real=np.stack(sc.mean),
-               K=tab["K"], em1=tab["em1"], em2=tab["em2"], em3=tab["em3"], band=tab["band"],
+               prior_cov_real=r["prior_cov_real"], errcorr_real=r["errcorr_real"],
+               wavelet_norms=r["wavelet_norms"],
                data_spec=np.stack(data), mean_spec=np.stack(mean), cov_spec=np.stack(covs), errcorr_spec=ec,
                out_resid=np.stack(res), out_mean=np.stack(mu), out_cov=np.stack(cov), out_mean_real=np.stack(post_real),
-               nfail=nfail, is4d=int(is4d))
+               nfail=nfail, is4d=0,
+               crava_mean_real=r["out_mean_real"], crava_resid=r["out_resid"], crava_cov=r["out_cov"],
+               **tab, **{k + "_nct": r[k + "_nct"] for k in NCT})
     np.savez_compressed(os.path.join(HERE, name), **out)
     return out
+
+
+def wavelet_case(name):
+    """The reference's own Ricker wavelets (Wavelet1D + Wavelet::resample) on a few grids."""
+    out = {}
+    for i, (nzp, dt, f) in enumerate([(30, 4.0, 30.0), (64, 2.0, 25.0), (45, 4.0, 45.0), (128, 4.0, 15.0)]):
+        sc = S.make_scenario(4, 3, max(2, int(nzp / 1.25)), [0.0, 20.0], f, nxp=4, nyp=3, nzp=nzp, dt_ms=dt, seed=i)
+        r = o2.inversion(sc, sc.corr_t, sc.min_int_fq, f)
+        out[f"case{i}_grid"] = np.array([nzp, dt, f, sc.nz])
+        out[f"case{i}_wavelets"] = r["wavelets"]
+        out[f"case{i}_norms"] = r["wavelet_norms"]
+        out[f"case{i}_corr_t"] = sc.corr_t
+        out[f"case{i}_min_int_fq"] = sc.min_int_fq
+        out[f"case{i}_circ_corr_t"] = r["circ_corr_t"]
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+def adjustment_case(name):
+    """Crava::computeAdjustmentFactor for a grid of local time shifts, gains and relative thicknesses."""
+    sc = S.make_scenario(16, 12, 40, [10.0, 30.0], 30.0, nxp=20, nyp=15, nzp=50, seed=9)
+    cases = np.array([(0.0, 1.0, 1.0), (0.0, 1.0, 0.7), (0.0, 1.0, 1.3), (3.0, 1.2, 0.85), (-2.5, 0.8, 1.15),
+                      (7.0, 1.0, 1.0), (0.0, 0.5, 0.6)], np.float32)
+    out = dict(nz=sc.nz, nzp=sc.nzp, dt_ms=sc.dt_ms, low_cut=sc.low_cut, high_cut=sc.high_cut, wnc=sc.wnc,
+               sigma0=sc.sigma0, cases=cases)
+    for l in range(sc.ntheta):
+        ev = float(sc.err_theta_cov[l, l])
+        wav, ctf, adj = o2.adjustment(sc, l, sc.corr_t, sc.min_int_fq, 30.0, cases, ev)
+        out[f"A{l}"] = sc.A[l]
+        out[f"err_var{l}"] = ev
+        out[f"wavelet{l}"] = wav
+        out[f"corr_t_filtered{l}"] = ctf
+        out[f"adjust{l}"] = adj
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+def factorable_case(name):
+    ns = np.array(list(range(1, 260)) + [341, 343, 500, 511, 625, 1000, 1023, 1025, 2047, 4097, 10000], np.int32)
+    np.savez_compressed(os.path.join(HERE, name), n=ns, closest=o2.closest_factorable(ns))
 
 
 def inversion_4d_case(name, tl, vintage=0):
@@ -84,11 +151,12 @@ def inversion_4d_case(name, tl, vintage=0):
     mu_cur, cov_cur = O.state4d_merge(mu_s, mu_d, ss, sd, dd, prec="f")
     cov_bin = [cov_cur[t] for t in MERGE_TO_BIN]
     v = tl.vintages[vintage]
-    tab = O.k_tables(tl.nxp, tl.wavelets, tl.A, tl.nz, tl.nzp, tl.dt_ms, tl.low_cut, tl.high_cut)
+    tab, _ = reference_tables(tl.wavelets, tl.A, tl.theta_deg, tl.nz, tl.nzp, tl.dt_ms, tl.low_cut, tl.high_cut)
     data = [O.ref_fft3d_r2c(d, tl.nxp, O.DATA) for d in v["data"]]
     ec = O.ref_fft3d_r2c(O.fill_err_corr(tl.nxp, tl.nyp, tl.nzp, tl.corr_xy), tl.nxp, O.COVARIANCE)
     s0 = tl.sigma_current()
-    res, mu, cov, nfail = O.ref_invert_bins(data, mu_cur, cov_bin, ec, tab, v["err_theta_cov"], s0, tl.wnc,
+    res, mu, cov, nfail = O.ref_invert_bins(data, mu_cur, cov_bin, ec, dict(tab, nxp=tl.nxp), v["err_theta_cov"], s0,
+                                            tl.wnc,
                                             is4d=True)
     out = dict(nxp=tl.nxp, nyp=tl.nyp, nzp=tl.nzp, theta_deg=np.array(tl.theta_deg), sigma0=s0,
                err_theta_cov=v["err_theta_cov"], wnc=tl.wnc, K=tab["K"], em1=tab["em1"], em2=tab["em2"],
@@ -96,6 +164,13 @@ def inversion_4d_case(name, tl, vintage=0):
                cov_spec=np.stack(cov_bin), errcorr_spec=ec, out_resid=np.stack(res), out_mean=np.stack(mu),
                out_cov=np.stack(cov), nfail=nfail, is4d=1)
     np.savez_compressed(os.path.join(HERE, name), **out)
+    # State4D::merge and State4D::split by the reference's own code on this state and posterior
+    state27 = np.stack(mu_s + mu_d + ss + sd + dd)
+    bin_to_merge = [0, 3, 4, 1, 5, 2]
+    post9 = np.stack(list(mu) + [cov[t] for t in bin_to_merge])
+    merged, split = o2.state4d(state27, post9, tl.nxp)
+    np.savez_compressed(os.path.join(HERE, "state4d_n4.npz"), nxp=tl.nxp, state=state27, post=post9,
+                        merged=merged, split=split)
 
 
 def simulation_case(name, inv, seed):
@@ -108,17 +183,24 @@ def simulation_case(name, inv, seed):
 
 
 def main():
+    src = os.environ.get("CRAVA_REFERENCE_SRC")
+    if not src:
+        raise SystemExit("set CRAVA_REFERENCE_SRC to the reference checkout")
     O.build_ref()
+    o2.build(src)
     fft_case("fft_even.npz", 16, 12, 20, 11)
     fft_case("fft_odd.npz", 15, 9, 7, 12)
     fft_case("fft_mixed.npz", 40, 21, 25, 13)
     sc = S.make_scenario(16, 12, 20, [10.0, 20.0, 30.0], 30.0, nxp=20, nyp=15, nzp=24, seed=3)
-    inv = inversion_case("inversion_c0small.npz", sc)
+    inv = inversion_case("inversion_c0small.npz", sc, 30.0)
     sc5 = S.make_scenario(20, 16, 26, [0.0, 10.0, 20.0, 30.0, 40.0], 25.0, nxp=24, nyp=20, nzp=32, sn=3.0,
                           notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=4)
-    inversion_case("inversion_c1small.npz", sc5)
+    inversion_case("inversion_c1small.npz", sc5, 25.0)
     sc8 = S.make_scenario(9, 10, 12, [5.0 * i for i in range(8)], 35.0, nxp=12, nyp=14, nzp=15, sn=2.5, seed=5)
-    inversion_case("inversion_n8odd.npz", sc8)
+    inversion_case("inversion_n8odd.npz", sc8, 35.0)
+    wavelet_case("reference_wavelets.npz")
+    adjustment_case("reference_adjustment.npz")
+    factorable_case("reference_factorable.npz")
     simulation_case("simulation_c0small.npz", inv, 231171)
     tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=8)
     inversion_4d_case("inversion_4d_n4.npz", tl)

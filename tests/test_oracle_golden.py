@@ -66,13 +66,18 @@ def test_fp64_oracle_close_to_reference(oracle, case):
     assert rel(np.stack(cov), g["out_cov"]) < 1e-4
 
 
-def test_k_tables_match_fixture(oracle):
-    g = golden("inversion_c1small.npz")
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+def test_k_tables_match_reference_fill_err_mult_vectors(oracle, case):
+    """The oracle's restatement of the per-k tables against the reference's own Crava::fillErrMultVectors
+    (constant-thickness branch) on the same resampled wavelets.  The reference transforms the wavelets in
+    FP32 (FFTW 2.1.2 float), the restatement in FP64 before rounding: entries agree to FP32 rounding of
+    the table's scale."""
+    g = golden(case)
     tab = oracle.k_tables(int(g["nxp"]), g["wavelets"], g["A"], int(g["nz"]), int(g["nzp"]), float(g["dt_ms"]),
                           float(g["low_cut"]), float(g["high_cut"]))
     np.testing.assert_array_equal(tab["band"], g["band"])
     for k in ("K", "em1", "em2", "em3"):
-        np.testing.assert_array_equal(tab[k], g[k])
+        assert np.abs(tab[k] - g[k]).max() <= 1e-6 * np.abs(g[k]).max(), k
 
 
 def test_noise_generator_bit_exact(oracle):

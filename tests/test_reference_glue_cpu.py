@@ -1,0 +1,189 @@
+"""The code around the bin solve against the reference's own compiled classes.
+
+The fixtures come from crava_o2 (oracle/o2_harness.cpp), which runs the
+reference's Wavelet, SeismicParametersHolder, Crava and State4D code compiled
+from its sources (tests/golden/make_golden.py): its Ricker wavelets and
+resampling, computeCircCorrT, the prior and error correlation fills,
+fillErrMultVectors for both thickness branches, the whole
+computePostMeanResidAndFFTCov, computeAdjustmentFactor, State4D::merge and
+::split and findClosestFactorableNumber.  Here the repo's restatements (the
+synthetic-input generator, the C++ host tables, the CPU oracle) are held to
+them; the GPU tests hold the GPU to the same fixtures.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden, oracle_pipeline, rel
+
+CASES = ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"]
+TABLES = ("K", "em1", "em2", "em3")
+
+
+def _scenario(g):
+    """The fixture's inputs as a Scenario (the reference's circCorrT)."""
+    from crava_gb300 import synthetic as S
+    return S.Scenario(nx=int(g["nx"]), ny=int(g["ny"]), nz=int(g["nz"]), nxp=int(g["nxp"]), nyp=int(g["nyp"]),
+                      nzp=int(g["nzp"]), dt_ms=float(g["dt_ms"]), theta_deg=list(g["theta_deg"]), A=g["A"],
+                      wavelets=g["wavelets"], corr_xy=g["corr_xy"], circ_corr_t=g["circ_corr_t"],
+                      sigma0=g["sigma0"], err_theta_cov=g["err_theta_cov"], data=list(g["data_real"]),
+                      mean=list(g["mean_real"]), wnc=float(g["wnc"]), low_cut=float(g["low_cut"]),
+                      high_cut=float(g["high_cut"]))
+
+
+def test_ricker_wavelets_match_reference():
+    """synthetic.ricker_fft_order (Wavelet's Ricker, 239 taps at 1 ms, resampled onto the grid in FFT
+    order, src/wavelet.cpp:130-186, :416-463) and the wavelet norm."""
+    from crava_gb300 import synthetic as S
+    g = golden("reference_wavelets.npz")
+    for i in range(4):
+        nzp, dt, f, _ = g[f"case{i}_grid"]
+        w = S.ricker_fft_order(int(nzp), float(dt), float(f)).astype(np.float32)
+        ref = g[f"case{i}_wavelets"]
+        assert rel(w, ref[0]) < 1e-6 and rel(w, ref[1]) < 1e-6, i
+        norm = np.sqrt(np.sum((w * w).astype(np.float64)))
+        assert abs(norm - g[f"case{i}_norms"][0]) <= 1e-6 * norm
+
+
+def test_circ_corr_t_matches_reference(oracle):
+    """computeCircCorrT + makeCircCorrTPosDef (src/seismicparametersholder.cpp:430-501): the FP64
+    restatement in the input generator and the oracle's FP32 one."""
+    from crava_gb300 import synthetic as S
+    g = golden("reference_wavelets.npz")
+    for i in range(4):
+        nzp = int(g[f"case{i}_grid"][0])
+        ref = g[f"case{i}_circ_corr_t"]
+        c = S.circ_corr_t(g[f"case{i}_corr_t"], int(g[f"case{i}_min_int_fq"]), nzp)
+        assert rel(c, ref) < 1e-6, i
+        assert rel(oracle.circ_corr_t(g[f"case{i}_corr_t"], int(g[f"case{i}_min_int_fq"]), nzp), ref) < 1e-6, i
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_prior_and_error_correlation_fills_bit_exact(oracle, case):
+    """FFTGrid::fillInParamCorr x priorVar0 (initializeCorrelations) and fillInErrCorr."""
+    g = golden(case)
+    nxp, nyp, nzp = int(g["nxp"]), int(g["nyp"]), int(g["nzp"])
+    s0 = np.asarray(g["sigma0"]).astype(np.float32)
+    for t, (p, q) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
+        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], 0, 0, float(s0[p, q]))
+        np.testing.assert_array_equal(c[..., :nxp], g["prior_cov_real"][t][..., :nxp])
+    e = oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"])
+    np.testing.assert_array_equal(e[..., :nxp], g["errcorr_real"][..., :nxp])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_host_operator_tables_match_reference_both_branches(native, oracle, case):
+    """cg_operator_tables / cg_operator_tables_ex (host C++) and the oracle's restatements against the
+    reference's fillErrMultVectors, fillkW, fillkWNorm and fillInverseAbskWRobust (src/crava.cpp:1337-1519)
+    on the same wavelets, both thickness branches.  In band, entries agree to FP32 rounding of the table's
+    scale (the reference's spectra are FP32 FFTW transforms).  Out of band the non-constant branch's
+    errMult3 at the Ricker's DC bin is 1/|W(0)| of a value that is zero up to rounding: it is huge on both
+    sides and never used."""
+    from crava_gb300 import api
+    g = golden(case)
+    args = (g["wavelets"], g["A"], int(g["nz"]), int(g["nzp"]), float(g["dt_ms"]), float(g["low_cut"]),
+            float(g["high_cut"]))
+    band = np.asarray(g["band"]).astype(bool)
+    for branch, sfx in (("constant", ""), ("non-constant", "_nct")):
+        if sfx:
+            host = api.operator_tables_nct(*args, 1.0)
+            orc = oracle.k_tables_nct(int(g["nxp"]), g["wavelets"], g["A"], int(g["nz"]), int(g["nzp"]),
+                                      int(g["nz"]) * float(g["dt_ms"]), float(g["low_cut"]), float(g["high_cut"]), 1.0)
+        else:
+            host = api.operator_tables(*args)
+            orc = oracle.k_tables(int(g["nxp"]), *args)
+        for impl, t in (("host", host), ("oracle", orc)):
+            np.testing.assert_array_equal(t["band"], g["band" + sfx])
+            for k in TABLES:
+                ref = g[k + sfx][band]
+                got = t[k][band]
+                if sfx and k == "em3":
+                    # errMult3 = 1/max|W| (robust): compare the amplitudes, whose FP32 rounding is absolute;
+                    # near the notches of a notched wavelet 1/|W| magnifies it
+                    ref, got = 1.0 / ref.real, 1.0 / got.real
+                assert np.abs(got - ref).max() <= 1e-6 * np.abs(ref).max(), (branch, impl, k)
+
+
+@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("prec", ["f", "d"])
+def test_oracle_pipeline_matches_reference_crava(oracle, case, prec):
+    """The whole inversion: the oracle in the reference's dataflow (its own transforms and bin loop) with
+    the reference's tables against Crava::computePostMeanResidAndFFTCov itself (src/crava.cpp:975-1285),
+    which also ran the reference's findParameterVariances, getNextErrorVariance, band test and
+    lib_matr solves.  FP32 differences only: the update (posterior minus prior mean) is ~60x smaller than
+    the mean, so its relative difference is correspondingly larger."""
+    g = golden(case)
+    sc = _scenario(g)
+    tab = {k: g[k] for k in TABLES + ("band",)}
+    post, res, cov, nf = oracle_pipeline(oracle, sc, prec, tables=tab)
+    nxp = sc.nxp
+    prior = g["mean_real"][..., :nxp]
+    ref_mean = g["crava_mean_real"][..., :nxp]
+    e = (rel(post, ref_mean), rel(post - prior, ref_mean - prior), rel(res, g["crava_resid"]),
+         rel(cov, g["crava_cov"]))
+    print(case, prec, "oracle vs reference Crava (mean, update, resid, cov):", e)
+    assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 2e-5 and e[3] < 2e-5
+    assert nf == int(g["nfail"])
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_bin_loop_glue_matches_reference_crava(case):
+    """ref_harness.cpp's glue around the reference's lib_matr (the fixture's out_* arrays, which keep the
+    posterior-mean spectra) reproduces the reference's own bin loop bit for bit."""
+    g = golden(case)
+    np.testing.assert_array_equal(g["out_resid"], g["crava_resid"])
+    np.testing.assert_array_equal(g["out_cov"], g["crava_cov"])
+    nxp = int(g["nxp"])
+    np.testing.assert_array_equal(g["out_mean_real"][..., :nxp], g["crava_mean_real"][..., :nxp])
+
+
+def test_state4d_merge_and_split_match_reference(oracle):
+    """State4D::merge and State4D::split (src/state4d.cpp:140-580) against the FP32 oracle restatement."""
+    g = golden("state4d_n4.npz")
+    st = list(g["state"])
+    mu_s, mu_d, ss, sd, dd = st[0:3], st[3:6], st[6:12], st[12:21], st[21:27]
+    mu_cur, cov_cur = oracle.state4d_merge(mu_s, mu_d, ss, sd, dd, prec="f")
+    merged = np.stack(list(mu_cur) + list(cov_cur))
+    e_merge = rel(merged, g["merged"])
+    post = list(g["post"])
+    st_out, nfail = oracle.state4d_split(mu_s, mu_d, ss, sd, dd, post[:3], post[3:], prec="f")
+    split = np.stack([x for grp in st_out for x in grp])
+    e_split = rel(split, g["split"])
+    print("State4D oracle vs reference: merge", e_merge, "split", e_split, "split failures", nfail)
+    assert e_merge < 1e-7
+    assert e_split < 1e-5
+
+
+def test_adjustment_factor_matches_reference(oracle):
+    """Crava::computeAdjustmentFactor (src/crava.cpp:807-903) for local time shifts, gains and relative
+    thicknesses 0.6-1.3: the oracle's per-trace restatement that the GPU scale-wavelet division is held to.
+    Compared on the bins divideDataByScaleWavelet uses (lowCut < f_k < highCut with the trace's stretched
+    frequency step, src/crava.cpp:750-770); above highCut, near the Nyquist bin, the global wavelet's
+    spectrum is zero up to FP32 rounding and the factor is that rounding magnified."""
+    g = golden("reference_adjustment.npz")
+    cases = g["cases"]
+    nz, nzp, dt = int(g["nz"]), int(g["nzp"]), float(g["dt_ms"])
+    s0 = np.asarray(g["sigma0"]).astype(np.float32).astype(np.float64)
+    worst = 0.0
+    for l in range(2):
+        for c, (ts, gain, sf) in enumerate(cases):
+            ref = g[f"adjust{l}"][c]
+            got = oracle.adjustment_factor(g[f"wavelet{l}"], g[f"A{l}"], s0, g[f"corr_t_filtered{l}"], nz, dt,
+                                           nz * dt, float(g["low_cut"]), float(g["high_cut"]), float(g["wnc"]),
+                                           float(g[f"err_var{l}"]), float(ts), float(gain), float(sf))
+            f = 1000.0 / (float(sf) * dt * nzp) * np.arange(nzp // 2 + 1)
+            used = (f > float(g["low_cut"])) & (f < float(g["high_cut"]))
+            e = rel(got[used], ref[used])
+            worst = max(worst, e)
+            assert e < 2e-5, (l, c, e)
+    print("adjustment factor vs reference: worst rel err", worst)
+
+
+def test_find_closest_factorable_matches_reference(native, oracle):
+    """FFTGrid::findClosestFactorableNumber (src/fftgrid.cpp:2857-2885): the C-ABI, the oracle and the
+    input generator."""
+    from crava_gb300.synthetic import find_closest_factorable
+    g = golden("reference_factorable.npz")
+    for n, ref in zip(g["n"], g["closest"]):
+        assert native.cg_find_closest_factorable(int(n)) == ref
+        assert oracle.find_closest_factorable(int(n)) == ref
+        assert find_closest_factorable(int(n)) == ref
