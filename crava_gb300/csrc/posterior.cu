@@ -673,7 +673,8 @@ extern "C" int cg_workspace_set_model_async(cg_workspace w, const cg_model *m, v
   pa.tf = w->ktab_f; pa.td = w->ktab_d; pa.ti = w->itab;
   {
     TraceScope ts("k_prep_model", st, 0.0);
-    k_prep_model<<<sym ? nzp / 2 + 1 : nzp, 32, 0, st>>>(pa);
+    const int prc = launch_prep_model(pa, sym ? nzp / 2 + 1 : nzp, st);
+    if (prc) return prc;
     CG_CHECK_LAUNCH("k_prep_model");
   }
   // The information form needs a 3D model with a positive error diagonal in every in-band plane

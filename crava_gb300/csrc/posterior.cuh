@@ -65,7 +65,8 @@ struct PrepArgs {
   KTab<double> *td;
   ITab *ti;
 };
-__global__ void k_prep_model(const __grid_constant__ PrepArgs p);
+// queues the set-up kernel over nplanes planes (prep.cu)
+int launch_prep_model(const PrepArgs &p, int nplanes, cudaStream_t st);
 
 // Opaque workspace behind cg_workspace (device buffers of one model).
 struct Workspace {

@@ -70,11 +70,12 @@ __device__ __forceinline__ void conj_all(C *v, int n, int lane)
 
 }  // namespace
 
+template <int NT>
 __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepArgs p)
 {
   const int k = blockIdx.x;
   const int lane = threadIdx.x;
-  const int nt = p.nt;
+  constexpr int nt = NT;
   // with symmetric tables this CTA also writes plane nzp - k, the conjugate of plane k
   const int km = (p.sym && k > 0 && 2 * k != p.nzp) ? p.nzp - k : -1;
   __shared__ KTab<double> t;
@@ -305,6 +306,23 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
     float *odm = (float *)&p.ti[km];
     for (int i = lane; i < (int)(sizeof(ITab) / sizeof(float)); i += 32) odm[i] = os[i];
   }
+}
+
+// one instantiation per stack count: every index below is then a compile-time expression
+int launch_prep_model(const PrepArgs &p, int nplanes, cudaStream_t st)
+{
+  switch (p.nt) {
+    case 1: k_prep_model<1><<<nplanes, 32, 0, st>>>(p); break;
+    case 2: k_prep_model<2><<<nplanes, 32, 0, st>>>(p); break;
+    case 3: k_prep_model<3><<<nplanes, 32, 0, st>>>(p); break;
+    case 4: k_prep_model<4><<<nplanes, 32, 0, st>>>(p); break;
+    case 5: k_prep_model<5><<<nplanes, 32, 0, st>>>(p); break;
+    case 6: k_prep_model<6><<<nplanes, 32, 0, st>>>(p); break;
+    case 7: k_prep_model<7><<<nplanes, 32, 0, st>>>(p); break;
+    case 8: k_prep_model<8><<<nplanes, 32, 0, st>>>(p); break;
+    default: set_error("ntheta %d outside 1..%d", p.nt, kMaxTheta); return CG_ERR_ARG;
+  }
+  return CG_OK;
 }
 
 }  // namespace cg

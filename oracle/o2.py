@@ -135,6 +135,67 @@ def adjustment(sc, l, corr_t, min_int_fq, f_peak, cases, error_var):
     return wav, ct_f, adj
 
 
+CRAVA_GEOM = ("x0", "y0", "dx", "dy", "il0", "xl0", "ilstepx", "ilstepy", "xlstepx", "xlstepy", "angle")
+
+
+def crava_write(cube, nx, ny, nxp, geom):
+    """FFTGrid::writeCravaFile of the padded real cube (nzp, nyp, rnxp) with simbox geometry geom (the 11
+    values of CRAVA_GEOM); returns the file's bytes."""
+    nzp, nyp, _ = cube.shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=nx, ny=ny, nxp=nxp, nyp=nyp, nzp=nzp, **dict(zip(CRAVA_GEOM, [float(g) for g in geom])))
+        _w(d, "cube.f32", cube, np.float32)
+        _run("crava_write", d)
+        with open(os.path.join(d, "out.crava"), "rb") as f:
+            return f.read()
+
+
+def crava_read(raw, nxp, nyp, nzp):
+    """FFTGrid::readCravaFile of the bytes raw into a grid of padded size nxp x nyp x nzp: the cube, or the
+    reference's error text when the sizes disagree."""
+    rnxp = 2 * (nxp // 2 + 1)
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nxp=nxp, nyp=nyp, nzp=nzp)
+        with open(os.path.join(d, "in.crava"), "wb") as f:
+            f.write(raw)
+        _run("crava_read", d)
+        if os.path.exists(os.path.join(d, "error.txt")):
+            with open(os.path.join(d, "error.txt")) as f:
+                return f.read()
+        return _r(d, "cube_read.f32", np.float32, (nzp, nyp, rnxp))
+
+
+STORM_PARAMS = ("zone", "missing", "x_min", "lx", "y_min", "ly", "z_top", "z_bot", "erosion_top", "erosion_bot",
+                "angle_deg")
+
+
+def storm_write(values, **hdr):
+    """NRLib::StormContGrid::WriteToFile of values (nk, nj, ni) with constant surfaces, model file name
+    "ModelFile" and variable name "Vp"; returns the file's bytes."""
+    nk, nj, ni = values.shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, ni=ni, nj=nj, nk=nk, **{k: float(hdr[k]) for k in STORM_PARAMS})
+        _w(d, "values.f32", values, np.float32)
+        _run("storm_write", d)
+        with open(os.path.join(d, "out.storm"), "rb") as f:
+            return f.read()
+
+
+def storm_read(raw):
+    """NRLib::StormContGrid::ReadFromFile of the bytes raw: (values (nk, nj, ni), header dict)."""
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "in.storm"), "wb") as f:
+            f.write(raw)
+        _run("storm_read", d)
+        hdr = {}
+        with open(os.path.join(d, "header.txt")) as f:
+            for line in f:
+                k, v = line.split()
+                hdr[k] = float(v)
+        v = _r(d, "values_read.f32", np.float32)
+        return v.reshape(int(hdr["nk"]), int(hdr["nj"]), int(hdr["ni"])), hdr
+
+
 def closest_factorable(ns):
     ns = np.asarray(ns, dtype=np.int32)
     with tempfile.TemporaryDirectory() as d:

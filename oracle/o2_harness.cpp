@@ -17,6 +17,11 @@
 //                               (src/state4d.cpp:140-580) on given spectra.
 //   crava_o2 adjust     <dir>   Crava::computeAdjustmentFactor (src/crava.cpp:807-903)
 //                               for given local shifts, gains and stretches.
+//   crava_o2 crava_write / crava_read <dir>
+//                               FFTGrid::writeCravaFile / readCravaFile.
+//   crava_o2 storm_write / storm_read <dir>
+//                               NRLib::StormContGrid::WriteToFile / ReadFromFile
+//                               (constant surfaces).
 //   crava_o2 factorable <dir>   FFTGrid::findClosestFactorableNumber.
 //
 // <dir> holds params.txt ("key value" lines) and raw little-endian arrays
@@ -56,6 +61,8 @@
 #include "src/simbox.h"
 #include "src/state4d.h"
 #include "src/wavelet1D.h"
+#include "nrlib/stormgrid/stormcontgrid.hpp"
+#include "nrlib/surface/surface.hpp"
 #undef private
 #undef protected
 
@@ -400,6 +407,85 @@ int cmd_adjust()
   return 0;
 }
 
+// FFTGrid::writeCravaFile (src/fftgrid.cpp:2410-2441) of the cube cube.f32 with the geometry of params.txt
+int cmd_crava_write()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"];
+  FFTGrid *g = make_grid(nx, ny, nzp, nxp, nyp, nzp, FFTGrid::PARAMETER, NULL, false);
+  std::vector<float> v = read_arr<float>("cube.f32", (size_t)g->rsize_);
+  memcpy(g->rvalue_, &v[0], sizeof(float) * v.size());
+  Simbox sb;
+  sb.x_min_ = p["x0"];
+  sb.y_min_ = p["y0"];
+  sb.dx_ = p["dx"];
+  sb.dy_ = p["dy"];
+  sb.nx_ = nx;
+  sb.ny_ = ny;
+  sb.inLine0_ = p["il0"];
+  sb.crossLine0_ = p["xl0"];
+  sb.ilStepX_ = p["ilstepx"];
+  sb.ilStepY_ = p["ilstepy"];
+  sb.xlStepX_ = p["xlstepx"];
+  sb.xlStepY_ = p["xlstepy"];
+  sb.angle_ = p["angle"];
+  g->writeCravaFile(g_dir + "/out", &sb);
+  return 0;
+}
+
+// FFTGrid::readCravaFile (src/fftgrid.cpp:2445-2493) of in.crava into a grid of the params.txt size
+int cmd_crava_read()
+{
+  std::map<std::string, double> p = read_params();
+  FFTGrid *g = new FFTGrid((int)p["nxp"], (int)p["nyp"], (int)p["nzp"], (int)p["nxp"], (int)p["nyp"], (int)p["nzp"]);
+  std::string err;
+  g->readCravaFile(g_dir + "/in.crava", err, false);
+  if (!err.empty()) {
+    std::ofstream f((g_dir + "/error.txt").c_str());
+    f << err;
+    return 0;
+  }
+  dump_grid("cube_read.f32", g);
+  return 0;
+}
+
+// NRLib::StormContGrid::WriteToFile (libs/nrlib/stormgrid/stormcontgrid.cpp:169-205) of values.f32 with
+// constant surfaces
+int cmd_storm_write()
+{
+  std::map<std::string, double> p = read_params();
+  const size_t ni = (size_t)p["ni"], nj = (size_t)p["nj"], nk = (size_t)p["nk"];
+  std::vector<float> v = read_arr<float>("values.f32", ni * nj * nk);
+  NRLib::StormContGrid g(ni, nj, nk);
+  g.SetDimensions(p["x_min"], p["y_min"], p["lx"], p["ly"]);
+  g.SetAngle(p["angle_deg"] * NRLib::Pi / 180.0);
+  g.SetSurfaces(NRLib::ConstantSurface<double>(p["z_top"]), NRLib::ConstantSurface<double>(p["z_bot"]),
+                NRLib::ConstantSurface<double>(p["erosion_top"]), NRLib::ConstantSurface<double>(p["erosion_bot"]));
+  g.SetZoneNumber((int)p["zone"]);
+  g.SetModelFileName("ModelFile");
+  g.SetMissingCode((float)p["missing"]);
+  g.SetVariableName("Vp");
+  std::copy(v.begin(), v.end(), g.begin());
+  g.WriteToFile(g_dir + "/out.storm");
+  return 0;
+}
+
+// NRLib::StormContGrid::ReadFromFile (libs/nrlib/stormgrid/stormcontgrid.cpp:72-165) of in.storm
+int cmd_storm_read()
+{
+  NRLib::StormContGrid g;
+  g.ReadFromFile(g_dir + "/in.storm");
+  std::vector<float> v(g.begin(), g.end());
+  write_raw("values_read.f32", &v[0], sizeof(float) * v.size());
+  std::ofstream f((g_dir + "/header.txt").c_str());
+  f.precision(17);
+  f << "ni " << g.GetNI() << "\nnj " << g.GetNJ() << "\nnk " << g.GetNK() << "\nzone " << g.GetZoneNumber()
+    << "\nmissing " << g.GetMissingCode() << "\nx_min " << g.GetXMin() << "\ny_min " << g.GetYMin()
+    << "\nlx " << g.GetLX() << "\nly " << g.GetLY() << "\nlz " << g.GetLZ() << "\nangle " << g.GetAngle()
+    << "\nz_top " << g.GetTopSurface().GetZ(0.0, 0.0) << "\nz_bot " << g.GetBotSurface().GetZ(0.0, 0.0) << "\n";
+  return 0;
+}
+
 int cmd_factorable()
 {
   std::map<std::string, double> p = read_params();
@@ -427,7 +513,8 @@ int main(int argc, char **argv)
   signal(SIGSEGV, on_fault);
   signal(SIGABRT, on_fault);
   if (argc != 3) {
-    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|factorable} <dir>\n");
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|crava_write|crava_read|storm_write|storm_read|"
+                    "factorable} <dir>\n");
     return 1;
   }
   g_dir = argv[2];
@@ -436,6 +523,10 @@ int main(int argc, char **argv)
   if (c == "state4d") return cmd_state4d();
   if (c == "factorable") return cmd_factorable();
   if (c == "adjust") return cmd_adjust();
+  if (c == "crava_write") return cmd_crava_write();
+  if (c == "crava_read") return cmd_crava_read();
+  if (c == "storm_write") return cmd_storm_write();
+  if (c == "storm_read") return cmd_storm_read();
   fprintf(stderr, "unknown command %s\n", c.c_str());
   return 1;
 }

@@ -124,6 +124,45 @@ def adjustment_case(name):
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
+def file_format_case(name):
+    """The reference's FFTGrid::writeCravaFile and StormContGrid::WriteToFile bytes for seeded cubes, and
+    its readers' view of the files the library writes (crava_gb300.api.write_crava_file / write_storm)."""
+    from crava_gb300 import api
+    rng = np.random.default_rng(17)
+    nx, ny, nxp, nyp, nzp = 8, 5, 10, 6, 4
+    _, rnxp = api.dims(nxp)
+    cube = rng.standard_normal((nzp, nyp, rnxp)).astype(np.float32)
+    geom = np.array([1000.5, 2000.25, 25.0, 12.5, 100.0, 200.0, 0.5, -0.5, 0.25, 0.75, 0.1])
+    crava_bytes = o2.crava_write(cube, nx, ny, nxp, geom)
+    hdr = dict(zone=0, missing=-999.25, x_min=456000.0, lx=1600.0, y_min=6780000.0, ly=1200.0, z_top=1800.0,
+               z_bot=2400.0, erosion_top=1800.0, erosion_bot=2400.0, angle_deg=30.0)
+    values = rng.standard_normal((3, 4, 5)).astype(np.float32)
+    storm_bytes = o2.storm_write(values, **hdr)
+    # the library's own files, read back by the reference
+    tmp = os.path.join(HERE, "_tmp_grid")
+    api.write_crava_file(tmp + ".crava", cube, list(geom), nx, ny)
+    with open(tmp + ".crava", "rb") as f:
+        ours_crava = f.read()
+    h = api.StormHeader()
+    h.zone_number, h.model_file, h.missing_code, h.variable = 0, b"ModelFile", -999.25, b"Vp"
+    h.x_min, h.lx, h.y_min, h.ly = hdr["x_min"], hdr["lx"], hdr["y_min"], hdr["ly"]
+    h.z_top, h.z_bot, h.erosion_top, h.erosion_bot = hdr["z_top"], hdr["z_bot"], hdr["erosion_top"], hdr["erosion_bot"]
+    h.lz, h.angle_deg = hdr["z_bot"] - hdr["z_top"], hdr["angle_deg"]
+    api.write_storm(tmp + ".storm", values, h)
+    with open(tmp + ".storm", "rb") as f:
+        ours_storm = f.read()
+    os.remove(tmp + ".crava")
+    os.remove(tmp + ".storm")
+    read_crava = o2.crava_read(ours_crava, nxp, nyp, nzp)
+    read_storm, read_hdr = o2.storm_read(ours_storm)
+    np.savez_compressed(os.path.join(HERE, name), cube=cube, geom=geom, nx=nx, ny=ny, nxp=nxp, nyp=nyp, nzp=nzp,
+                        crava_bytes=np.frombuffer(crava_bytes, np.uint8), values=values,
+                        storm_header=np.array([hdr[k] for k in o2.STORM_PARAMS]),
+                        storm_bytes=np.frombuffer(storm_bytes, np.uint8), read_crava=read_crava,
+                        read_storm=read_storm, read_storm_header=np.array([read_hdr[k] for k in sorted(read_hdr)]),
+                        read_storm_keys=np.array(sorted(read_hdr)))
+
+
 def factorable_case(name):
     ns = np.array(list(range(1, 260)) + [341, 343, 500, 511, 625, 1000, 1023, 1025, 2047, 4097, 10000], np.int32)
     np.savez_compressed(os.path.join(HERE, name), n=ns, closest=o2.closest_factorable(ns))
@@ -201,6 +240,7 @@ def main():
     wavelet_case("reference_wavelets.npz")
     adjustment_case("reference_adjustment.npz")
     factorable_case("reference_factorable.npz")
+    file_format_case("reference_file_formats.npz")
     simulation_case("simulation_c0small.npz", inv, 231171)
     tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=8)
     inversion_4d_case("inversion_4d_n4.npz", tl)
