@@ -153,6 +153,7 @@ def _declare(L):
         "cg_workspace_set_model_async": ([V, V, V], I),
         "cg_condition_histogram": ([V, V, V, I, V], I),
         "cg_alloc_calls": ([], ct.c_long),
+        "cg_vintage4d": ([V, V, V, V, V, V, V, V, V, I, V, V], I),
         "cg_workspace_stats": ([V, ct.POINTER(I), ct.POINTER(I), ct.POINTER(I)], I),
         "cg_workspace_reset_stats": ([V, V], I),
         "cg_invert_bins_plain": ([V, PP, PP, PP, V, V], I),

@@ -481,6 +481,17 @@ def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, nxp, stream=None):
     return nfail
 
 
+def vintage4d(ws, mu_s, mu_d, ss, sd, dd, data, errcorr, post_mean, nxp, precision=None, stream=None):
+    """One 4D vintage in one pass (cg_vintage4d): state updated in place, data -> residuals, post_mean <-
+    the current state's posterior mean.  Returns a device counter of bins whose split kept the prior."""
+    prec = PREC_MIXED if precision is None else precision
+    nsplit = torch.zeros(1, dtype=torch.int32, device=mu_s[0].device)
+    keep = [_pp(x) for x in (mu_s, mu_d, ss, sd, dd, data, post_mean)]
+    check(lib().cg_vintage4d(ws.h, *[k[0] for k in keep[:6]], _vp(errcorr), keep[6][0], prec, _vp(nsplit),
+                             _stream(stream)), "cg_vintage4d")
+    return nsplit
+
+
 class _InvModel(ct.Structure):
     _fields_ = [("ntheta", ct.c_int), ("wavelets", ct.c_void_p), ("A", ct.c_void_p), ("err_theta_cov", ct.c_void_p),
                 ("sigma0", ct.c_void_p), ("corr_xy", ct.c_void_p), ("circ_corr_t", ct.c_void_p),

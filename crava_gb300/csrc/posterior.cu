@@ -28,6 +28,7 @@
 #include "posterior.cuh"
 #include "fused_bins.cuh"
 #include "linalg.cuh"
+#include "plain_bin.cuh"
 #include "trace.cuh"
 
 namespace cg {
@@ -60,7 +61,7 @@ __device__ __forceinline__ float2 param_cov_entry(float2 v, float s)
 }
 
 template <int NT>
-__global__ void __launch_bounds__(128) k_invert_plain(PlainArgs a)
+__global__ void __launch_bounds__(128) k_invert_plain(const __grid_constant__ PlainArgs a)
 {
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.csize) return;
@@ -84,141 +85,16 @@ __global__ void __launch_bounds__(128) k_invert_plain(PlainArgs a)
   S[1][2] = c6[5]; S[2][1] = make_float2(c6[5].x, -c6[5].y);
 
   if (a.band[k]) {
-    float2 d[NT], res[NT], mu[3], K[NT][3], KS[NT][3], KScc[3][NT], Sd[NT * (NT + 1) / 2];
+    float2 res[NT], mu[3];
 #pragma unroll
-    for (int l = 0; l < NT; l++) { d[l] = a.data[l][b]; res[l] = d[l]; }
+    for (int l = 0; l < NT; l++) res[l] = a.data[l][b];
 #pragma unroll
     for (int p = 0; p < 3; p++) mu[p] = a.mean[p][b];
     const float2 ec = a.errcorr[b];
     const float lam = sqrtf(ec.x * ec.x);
-#pragma unroll
-    for (int l = 0; l < NT; l++)
-#pragma unroll
-      for (int p = 0; p < 3; p++) K[l][p] = __ldg(&a.K[((long)k * NT + l) * 3 + p]);
-    // KS = K S (lib_matrProdCpx)
-#pragma unroll
-    for (int l = 0; l < NT; l++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          xr += K[l][q].x * S[q][j].x - K[l][q].y * S[q][j].y;
-          xi += K[l][q].y * S[q][j].x + K[l][q].x * S[q][j].y;
-        }
-        KS[l][j] = make_float2(xr, xi);
-      }
-    // Sd = KS K^H + errVar (lower triangle; lib_matrProdAdjointCpx + getNextErrorVariance)
-#pragma unroll
-    for (int l = 0; l < NT; l++) {
-      const float2 e1l = __ldg(&a.em1[(long)k * NT + l]);
-      const float2 e2l = __ldg(&a.em2[(long)k * NT + l]);
-#pragma unroll
-      for (int m = 0; m <= l; m++) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          xr += KS[l][q].x * K[m][q].x + KS[l][q].y * K[m][q].y;
-          xi += KS[l][q].y * K[m][q].x - KS[l][q].x * K[m][q].y;
-        }
-        const float2 e1m = __ldg(&a.em1[(long)k * NT + m]);
-        const float2 e2m = __ldg(&a.em2[(long)k * NT + m]);
-        const float c0 = a.c0[l * NT + m] * lam;
-        float er = c0 * (e1l.x * e1m.x + e1l.y * e1m.y);
-        er += c0 * (e2l.x * e2m.x + e2l.y * e2m.y);
-        float ei;
-        if (l == m) {
-          const float2 e3 = __ldg(&a.em3[(long)k * NT + l]);
-          er += a.cw[l] * e3.x * e3.x;
-          ei = 0.0f;
-        } else {
-          ei = c0 * (-e1l.x * e1m.y + e1l.y * e1m.x);
-          ei += c0 * (-e2l.x * e2m.y + e2l.y * e2m.x);
-        }
-        Sd[tri(l, m)] = make_float2(xr + er, xi + ei);
-      }
-    }
-    if (chol_ref<float, NT>(Sd)) {
-#pragma unroll
-      for (int l = 0; l < NT; l++)
-#pragma unroll
-        for (int p = 0; p < 3; p++) KScc[p][l] = make_float2(KS[l][p].x, -KS[l][p].y);
-      // lib_matrAXeqBMatCpx: KS <- Sd^-1 KS
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-#pragma unroll
-        for (int i = 0; i < NT; i++) {
-          float xr = KS[i][c].x, xi = KS[i][c].y;
-#pragma unroll
-          for (int j = 0; j < i; j++) {
-            xr -= (KS[j][c].x * Sd[tri(i, j)].x - KS[j][c].y * Sd[tri(i, j)].y);
-            xi -= (KS[j][c].y * Sd[tri(i, j)].x + KS[j][c].x * Sd[tri(i, j)].y);
-          }
-          const float2 lii = Sd[tri(i, i)];
-          const float help = lii.x * lii.x + lii.y * lii.y;
-          KS[i][c] = make_float2((xr * lii.x + xi * lii.y) / help, (xi * lii.x - xr * lii.y) / help);
-        }
-#pragma unroll
-        for (int i = NT - 1; i >= 0; i--) {
-          float xr = KS[i][c].x, xi = KS[i][c].y;
-#pragma unroll
-          for (int j = NT - 1; j > i; j--) {
-            xr = xr - (KS[j][c].x * Sd[tri(j, i)].x + KS[j][c].y * Sd[tri(j, i)].y);
-            xi = xi - (-KS[j][c].x * Sd[tri(j, i)].y + KS[j][c].y * Sd[tri(j, i)].x);
-          }
-          const float2 lii = Sd[tri(i, i)];
-          const float help = lii.x * lii.x + lii.y * lii.y;
-          KS[i][c] = make_float2((xr * lii.x - xi * lii.y) / help, (xi * lii.x + xr * lii.y) / help);
-        }
-      }
-      // S -= KScc KS
-#pragma unroll
-      for (int p = 0; p < 3; p++)
-#pragma unroll
-        for (int q = 0; q < 3; q++) {
-          float xr = 0, xi = 0;
-#pragma unroll
-          for (int l = 0; l < NT; l++) {
-            xr += KScc[p][l].x * KS[l][q].x - KScc[p][l].y * KS[l][q].y;
-            xi += KScc[p][l].y * KS[l][q].x + KScc[p][l].x * KS[l][q].y;
-          }
-          S[p][q].x -= xr;
-          S[p][q].y -= xi;
-        }
-      // d -= K mu; ans = KS^H d; mu += ans; res -= K mu
-#pragma unroll
-      for (int l = 0; l < NT; l++) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int p = 0; p < 3; p++) {
-          xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
-          xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
-        }
-        d[l].x -= xr;
-        d[l].y -= xi;
-      }
-#pragma unroll
-      for (int p = 0; p < 3; p++) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int l = 0; l < NT; l++) {
-          xr += KS[l][p].x * d[l].x + KS[l][p].y * d[l].y;
-          xi += -KS[l][p].y * d[l].x + KS[l][p].x * d[l].y;
-        }
-        mu[p].x += xr;
-        mu[p].y += xi;
-      }
-#pragma unroll
-      for (int l = 0; l < NT; l++) {
-        float xr = 0, xi = 0;
-#pragma unroll
-        for (int p = 0; p < 3; p++) {
-          xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
-          xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
-        }
-        res[l].x -= xr;
-        res[l].y -= xi;
-      }
+    float cond;
+    if (plain_solve<float, NT>(a.K + (long)k * NT * 3, a.em1 + (long)k * NT, a.em2 + (long)k * NT,
+                               a.em3 + (long)k * NT, a.c0, a.cw, lam, S, mu, res, &cond)) {
 #pragma unroll
       for (int l = 0; l < NT; l++) a.data[l][b] = res[l];
 #pragma unroll
@@ -642,6 +518,7 @@ extern "C" int cg_workspace_set_model_async(cg_workspace w, const cg_model *m, v
   w->wnc = m->wnc;
   w->is4d = m->is4d;
   w->cond_threshold = m->cond_threshold > 0 ? m->cond_threshold : 1.0e3;
+  for (int t = 0; t < nt * nt; t++) w->etc_host[t] = m->err_theta_cov[t];
   for (int t = 0; t < 9; t++) { w->sigma0[t] = m->sigma0[t]; w->sigma0f[t] = (float)m->sigma0[t]; }
   long nb = 0;
   for (int k = 0; k < nzp; k++) nb += m->band[k] ? 1 : 0;
@@ -747,9 +624,7 @@ extern "C" int cg_invert_bins_plain(cg_workspace w, float *const *data, float *c
   for (int t = 0; t < 6; t++) { if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; } a.cov[t] = (float2 *)cov[t]; }
   a.errcorr = (const float2 *)errcorr;
   a.K = w->K; a.em1 = w->em1; a.em2 = w->em2; a.em3 = w->em3; a.band = w->band;
-  std::vector<double> etc(nt * nt);
-  // errThetaCov is needed on the host for the per-launch constants
-  CG_CUDA(cudaMemcpy(etc.data(), w->etc, sizeof(double) * nt * nt, cudaMemcpyDeviceToHost));
+  const double *etc = w->etc_host;
   for (int l = 0; l < nt; l++) {
     for (int m = 0; m < nt; m++) a.c0[l * nt + m] = (float)(0.5 * (1.0 - w->wnc) * etc[l * nt + m]);
     a.cw[l] = (float)(w->wnc * etc[l * nt + l]);

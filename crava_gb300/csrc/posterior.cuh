@@ -76,6 +76,7 @@ struct Workspace {
   int is4d;
   double sigma0[9];
   float sigma0f[9];
+  double etc_host[kMaxTheta * kMaxTheta];  // errThetaCov, host copy (per-launch constants)
   double cond_threshold;
   // per-model tables (device)
   KTab<float> *ktab_f;

@@ -345,8 +345,23 @@ class TimeLapse:
             ws.reset_stats()
         self.nfail_split = []
 
-    def run_vintage(self, v, stream=None):
+    def run_vintage(self, v, stream=None, form="plain"):
+        """One vintage.  form "plain": the reference's three passes (merge, the 4D bin loop, split) as
+        separate kernels; "fp32" / "mixed": one pass per bin (cg_vintage4d), bit for bit the plain form in
+        FP32, or with the FP64 redo of guarded bins."""
         nxp = self.tl.nxp
+        if form in ("fp32", "mixed"):
+            for l, d in enumerate(self.data):
+                d.copy_(self.data_in[v][l])
+            api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
+            prec = api.PREC_MIXED if form == "mixed" else api.PREC_FP32
+            self.nfail_split.append(api.vintage4d(self.ws[v], self.mu_s, self.mu_d, self.ss, self.sd, self.dd,
+                                                  self.data, self.errcorr, self.post_mean, nxp, precision=prec,
+                                                  stream=stream))
+            api.fft_in_place_batch(self.post_mean, nxp, api.PARAMETER, inverse=True, stream=stream)
+            return
+        if form != "plain":
+            raise ValueError(form)
         api.state4d_merge(self.mu_s, self.mu_d, self.ss, self.sd, self.dd, self.mu_cur, self.cov_cur, nxp,
                           stream=stream)
         for l, d in enumerate(self.data):
@@ -360,9 +375,9 @@ class TimeLapse:
             self.post_mean[p].copy_(self.mu_cur[p])
         api.fft_in_place_batch(self.post_mean, nxp, api.PARAMETER, inverse=True, stream=stream)
 
-    def run(self, stream=None):
+    def run(self, stream=None, form="plain"):
         for v in range(len(self.tl.vintages)):
-            self.run_vintage(v, stream=stream)
+            self.run_vintage(v, stream=stream, form=form)
 
     def state(self):
         """(mu_s, mu_d, ss, sd, dd) spectra as numpy complex arrays."""

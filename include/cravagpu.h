@@ -483,6 +483,24 @@ int cg_condition_histogram(cg_workspace ws, unsigned long long *hist_chol, unsig
 int cg_invert_bins_fused_f64(cg_workspace ws, double *const *data, double *const *mean, double *const *cov,
                              void *stream);
 
+/* One vintage of the 4D time-lapse inversion (src/doinversion.cpp:96-135,
+ * src/crava.cpp:1028-1040) in one pass over the bins: State4D::merge,
+ * the bin loop with the 4D branch of findParameterVariances
+ * (src/seismicparametersholder.cpp:366-373) and State4D::split
+ * (src/state4d.cpp:140-580) for each bin, replacing cg_state4d_merge,
+ * cg_invert_bins_plain and cg_state4d_split.  The workspace's model must have
+ * is4d = 1.  State spectra (mu_s[3], mu_d[3], ss[6], sd[9], dd[6], the
+ * cg_state4d_* orders) are updated in place; data[ntheta]: data spectra in,
+ * residual spectra out; post_mean[3]: the current state's posterior mean
+ * out (the vintage's output before its inverse transform).  CG_PREC_FP32 is
+ * bit for bit the three separate passes; CG_PREC_MIXED redoes the bins whose
+ * data-covariance Cholesky fails or whose pivot-ratio estimate exceeds the
+ * model's cond_threshold in FP64 (merge, solve and split).  *nsplit_dev
+ * (device int, may be NULL) counts bins whose split kept the prior. */
+int cg_vintage4d(cg_workspace ws, float *const *mu_s, float *const *mu_d, float *const *ss, float *const *sd,
+                 float *const *dd, float *const *data, const float *errcorr, float *const *post_mean, int precision,
+                 int *nsplit_dev, void *stream);
+
 /* ========================================================================
  * Whole inversion from host buffers: the entry point a replacement of
  * Crava::computePostMeanResidAndFFTCov (src/crava.cpp:975-1285) calls with

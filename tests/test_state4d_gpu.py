@@ -134,3 +134,66 @@ def test_plain_4d_bin_loop_matches_reference_lib_matr(cuda):
     print("4D plain vs reference: update", e_upd, "resid", e_res, "cov", e_cov)
     assert e_upd < 1e-4 and e_res < 1e-5 and e_cov < 1e-5
     assert ws.stats()["failed"] == int(g["nfail"])
+
+
+def test_fused_vintage_fp32_bit_identical_to_three_passes(cuda):
+    """cg_vintage4d in FP32 (merge, 4D bin solve and split per bin in one pass) gives bit for bit the
+    state, residuals, posterior means and split-failure counts of the separate merge / bin-loop / split
+    kernels, over two vintages."""
+    from crava_gb300 import api, synthetic as S
+    from crava_gb300.pipeline import TimeLapse
+    tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=7)
+    out = {}
+    for form in ("plain", "fp32"):
+        run = TimeLapse(tl)
+        run.restore()
+        for v in range(len(tl.vintages)):
+            run.run_vintage(v, form=form)
+        torch.cuda.synchronize()
+        out[form] = (run.state(), [from_cube(x) for x in run.data], [x.cpu().numpy() for x in run.post_mean],
+                     [int(x.item()) for x in run.nfail_split])
+    (s_p, d_p, m_p, f_p), (s_f, d_f, m_f, f_f) = out["plain"], out["fp32"]
+    for a, b in zip(s_p, s_f):
+        for x, y in zip(a, b):
+            np.testing.assert_array_equal(x, y)
+    for x, y in zip(d_p, d_f):
+        np.testing.assert_array_equal(x, y)
+    for x, y in zip(m_p, m_f):
+        np.testing.assert_array_equal(x, y)
+    assert f_p == f_f
+
+
+@pytest.mark.parametrize("cond", [0.0, 1.0001])
+def test_fused_vintage_mixed_matches_fp64_oracle_chain(cuda, oracle, cond):
+    """cg_vintage4d in the MIXED form against the FP64 oracle chain; cond = 1.0001 sends (nearly) every
+    in-band bin through the FP64 redo of merge, solve and split."""
+    from crava_gb300 import api, synthetic as S
+    from crava_gb300.pipeline import TimeLapse
+    tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=7)
+    run = TimeLapse(tl)
+    if cond > 0:
+        for v, ws in enumerate(run.ws):
+            ws.set_model(run.tables, tl.vintages[v]["err_theta_cov"], tl.sigma_current(), tl.wnc, is4d=True,
+                         cond_threshold=cond)
+    run.restore()
+    state0 = run.state()
+    errc = api.as_spectrum(run.errcorr).cpu().numpy()
+    flagged = []
+    for v in range(len(tl.vintages)):
+        run.ws[v].reset_stats()
+        run.run_vintage(v, form="mixed")
+        flagged.append(run.ws[v].stats()["flagged"])
+    torch.cuda.synchronize()
+    got = run.state()
+    ref, ref_fails = _oracle_timelapse_chain(oracle, tl, state0, errc, run.tables)
+    names = ["mu_s", "mu_d", "ss", "sd", "dd"]
+    errs = {nm: rel(np.stack(a), np.stack(b)) for nm, a, b in zip(names, got, ref)}
+    upd = rel(np.stack(got[1]) - np.stack(state0[1]), np.stack(ref[1]) - np.stack(state0[1]))
+    print("fused mixed vintage (cond", cond, ") vs FP64 oracle chain:", errs, "dynamic update", upd, "flagged",
+          flagged, "split fails", [int(x.item()) for x in run.nfail_split], ref_fails)
+    assert [int(x.item()) for x in run.nfail_split] == ref_fails
+    assert errs["mu_s"] < 1e-6 and errs["mu_d"] < 1e-4 and upd < 1e-4
+    assert errs["ss"] < 1e-5 and errs["sd"] < 1e-5 and errs["dd"] < 1e-5
+    if cond > 0:
+        assert min(flagged) > 0
+        assert upd < 2e-6  # the FP64 redo brings the dynamic update to FP64-level agreement
