@@ -336,6 +336,146 @@ def conditioning_case(args, stream, flush, rank, sn, wnc):
     return out
 
 
+def cpu_simulation_sample(sc, cov_spec, post_mean, nreal, threads):
+    """Seconds per realisation of the oracle's posterior simulation (src/crava.cpp:1551-1734): seeded noise
+    (fillInComplexNoise), the per-bin factor applied in the reference's lib_matr order, three inverse
+    transforms and the posterior-mean add, over ``nreal`` realisations."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    for r in range(nreal):
+        seeds = O.fill_complex_noise(sc.nxp, sc.nyp, sc.nzp, 1000 + r, ncubes=3)
+        sim = O.simulate_bins(cov_spec, seeds, "f", threads)
+        for p in range(3):
+            f = O.fft3d_c2r(sim[p], sc.nxp, O.PARAMETER, "f", threads)
+            f[:, :, :sc.nxp] += post_mean[p]
+    return (time.perf_counter() - t0) / nreal
+
+
+def cpu_timelapse_vintage(tl, state, errc, threads):
+    """Seconds for one vintage of the oracle's 4D chain (State4D::merge, the data transforms, the 4D
+    branch of the bin loop, State4D::split, the posterior-mean inverse transforms), reference order, FP32."""
+    from oracle import oracle as O
+    from crava_gb300.pipeline import MERGE_TO_BIN
+    mu_s, mu_d, ss, sd, dd = state
+    tab = O.k_tables(tl.nxp, tl.wavelets, tl.A, tl.nz, tl.nzp, tl.dt_ms, tl.low_cut, tl.high_cut,
+                     tl.min_rel_thick, prec="f")
+    tab = dict(tab, nxp=tl.nxp)
+    v = tl.vintages[0]
+    t0 = time.perf_counter()
+    mu_cur, cov_cur = O.state4d_merge(mu_s, mu_d, ss, sd, dd, "f", threads)
+    data = [O.fft3d_r2c(d, tl.nxp, O.DATA, "f", threads) for d in v["data"]]
+    _, mu_post, cov_bin, _ = O.invert_bins(data, mu_cur, [cov_cur[t] for t in MERGE_TO_BIN], errc, tab,
+                                           v["err_theta_cov"], tl.sigma_current(), tl.wnc, is4d=True, prec="f",
+                                           nthreads=threads)
+    cov_post = [None] * 6
+    for k, t in enumerate(MERGE_TO_BIN):
+        cov_post[t] = cov_bin[k]
+    O.state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, "f", threads)
+    for m in mu_post:
+        O.fft3d_c2r(m, tl.nxp, O.PARAMETER, "f", threads)
+    return time.perf_counter() - t0
+
+
+def other_workloads(args, stream, flush, rank, peak, cpu_ok):
+    """The other workloads the metric's configuration list names, each timed with CUDA events after
+    warm-up, with the dominant kernel's roofline fraction and (rank 0, one GPU) the CPU oracle port timed
+    on the host cores beside it:
+      * the small CPU-sized inversion (80x80x160, 3 stacks), L2 flushed between steps;
+      * 64 uneven cubes in one graph-replayed batch;
+      * posterior simulation, 200^3, 128 realisations;
+      * 4D time-lapse, 256x256x192, two vintages x 4 stacks (three-pass plain form and one-pass fused form)."""
+    import numpy as np
+    import torch
+    from crava_gb300 import api, microbench as MB
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    threads = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 5))
+    out = {}
+
+    # small inversion (the reference's own CPU-sized case)
+    sc0 = S.config0(seed=20261203 + rank)
+    inv0 = Inversion(sc0, forms=("plain", "mixed"))
+    small = {"workload": "80x80x160 padded (64x64x128 cells), 3 stacks 10-30 deg, 30 Hz Ricker, S/N 4",
+             "bins": sc0.nbins, "ms": {}}
+    for form in ("plain", "mixed"):
+        for _ in range(max(args.warmup, 1)):
+            inv0.restore(form)
+            inv0.run(form)
+
+        def before(form=form):
+            inv0.restore(form)
+            flush.fill_(1.0)
+        small["ms"][form] = round(statistics.mean(MB._events_ms(lambda: inv0.run(form), steps, before)), 4)
+    small["Mbins_per_s_mixed"] = round(sc0.nbins / (small["ms"]["mixed"] * 1e-3) / 1e6, 1)
+    inv0.restore("mixed")
+    tr = MB._traced(lambda: inv0.run("mixed"))
+    small["roofline"] = MB.roofline_of(tr, peak)
+    if cpu_ok:
+        t = cpu_inversion(sc0, oracle_tables(sc0), "f", threads)[0]
+        small["cpu_baseline"] = {"value": round(sc0.nbins / t["total_s"] / 1e6, 3), "unit": "Mbins/s",
+                                 "cores": threads, "kind": "port", "sample": "one complete inversion"}
+    del inv0
+    out["small_80x80x160_3stacks"] = small
+
+    # batch of uneven cubes
+    t0 = time.perf_counter()
+    scs = S.config2(64)
+    t_gen = time.perf_counter() - t0
+    batch = MB.measure_batch(scs, "mixed", reps=steps, warmup=args.warmup, peak=peak, flush=flush)
+    batch["workload"] = ("64 cubes, nx, ny ~ U{32..192}, nz ~ U{64..160}, padded 25 % to 2/3/5/7-smooth sizes, "
+                         "2-8 stacks, Ricker 15-45 Hz, S/N 2-6, prior stds x U(0.5, 1.5)")
+    batch["generation_s"] = round(t_gen, 1)
+    if cpu_ok:
+        done, secs, ncubes = 0, 0.0, 0
+        for sc in scs:
+            secs += cpu_inversion(sc, oracle_tables(sc), "f", threads)[0]["total_s"]
+            done += sc.nbins
+            ncubes += 1
+            if secs > 8.0:
+                break
+        batch["cpu_baseline"] = {"value": round(done / secs / 1e6, 3), "unit": "Mbins/s", "cores": threads,
+                                 "kind": "port", "sample": f"complete inversions of the first {ncubes} cubes"}
+    del scs
+    out["batch_64_uneven_cubes"] = batch
+
+    # posterior simulation
+    sim, sc3 = MB.measure_simulate(nreal=128, reps=steps, warmup=1, peak=peak)
+    if cpu_ok:
+        inv3 = Inversion(sc3, forms=("mixed",))
+        inv3.restore("mixed")
+        inv3.run("mixed")
+        torch.cuda.synchronize()
+        pm, _, cov = inv3.results("mixed")
+        del inv3
+        spr = cpu_simulation_sample(sc3, list(cov), list(pm), 2, threads)
+        sim["cpu_baseline"] = {"value": round(1.0 / spr, 3), "unit": "realisations/s", "cores": threads,
+                               "kind": "port", "sample": "2 realisations (noise, factor, 3 inverse transforms, mean add)"}
+    out["simulation_200cube_128_realisations"] = sim
+
+    # 4D time-lapse
+    tl = S.config4()
+    from crava_gb300.pipeline import TimeLapse
+    run = TimeLapse(tl)
+    four = {"workload": "256x256x192 padded, 6-parameter state, 2 vintages x 4 stacks, S/N 4"}
+    for form in ("plain", "mixed"):
+        four[form], run = MB.measure_timelapse(tl, form, reps=steps, warmup=1, peak=peak, run=run)
+    four["speedup_mixed_vs_plain"] = round(four["plain"]["ms"] / four["mixed"]["ms"], 3)
+    if cpu_ok:
+        run.restore()
+        torch.cuda.synchronize()
+        state = run.state()
+        errc = api.as_spectrum(run.errcorr).cpu().numpy()
+        tv = cpu_timelapse_vintage(tl, state, errc, threads)
+        four["cpu_baseline"] = {"value": round(tl.nbins / (tv * len(tl.vintages)) / 1e6, 3), "unit": "Mbins/s",
+                                "cores": threads, "kind": "port",
+                                "sample": "one vintage of the 4D chain (merge, 4 data transforms, 4D bin loop, "
+                                          "split, 3 inverse transforms), scaled to two vintages"}
+    del run
+    out["timelapse_4d_256x256x192"] = four
+    return out
+
+
 def run_ours(args, world, rank, local):
     import numpy as np
     import torch
@@ -562,6 +702,11 @@ def run_ours(args, world, rank, local):
     cond_case = {"sn_10_reference_max": conditioning_case(args, stream, flush, rank, 10.0, 0.1),
                  "sn_1e5_outside_reference_range": conditioning_case(args, stream, flush, rank, 1.0e5, 1.0e-4)}
 
+    others = None
+    if not args.no_other_workloads:
+        others = other_workloads(args, stream, flush, rank, peak,
+                                 rank == 0 and world == 1 and not args.no_cpu_baseline)
+
     cpu = None
     vs_cpu64 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -620,6 +765,7 @@ def run_ours(args, world, rank, local):
             "gpu_launches": launches_per_step * args.steps,
             "clocks": clk,
             "cpu_baseline": cpu,
+            "other_workloads": others,
             "setup_s": {"synthetic_generation": round(t_gen, 1)},
         }
         print(json.dumps(line), flush=True)
@@ -635,6 +781,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-other-workloads", action="store_true",
+                    help="skip the small, batch, simulation and 4D workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 0)
     world, rank, local = dist_setup()

@@ -121,91 +121,153 @@ def copy_case(a):
     print(json.dumps({"case": {"what": "copy", "mb": a.mb, "reps": a.reps}, "rates": out}))
 
 
+def kernel_table(tr):
+    """Launch-tracer totals as {kernel: {launches, ms, GBps}}, longest first."""
+    return {k: {"launches": v[0], "ms": round(v[1], 4), "GBps": round(v[2] / max(v[1], 1e-12) / 1e6, 1)}
+            for k, v in sorted(tr.items(), key=lambda kv: -kv[1][1])}
+
+
+def roofline_of(tr, peak):
+    """The kernel with the largest share of a traced run against the HBM peak (GB/s): algorithmic bytes
+    over the launches' CUDA-event time."""
+    name, (nl, ms, by) = max(tr.items(), key=lambda kv: kv[1][1])
+    ach = by / max(ms * 1e-3, 1e-12) / 1e9
+    total = sum(v[1] for v in tr.values())
+    return {"bound": "hbm", "kernel": name, "launches": nl, "ms": round(ms, 4), "share": round(ms / total, 3),
+            "achieved": round(ach, 1), "peak": peak, "unit": "GB/s", "frac": round(ach / peak, 4)}
+
+
+def _events_ms(fn, reps, before=None):
+    """CUDA-event time of fn() on the current stream, ``before()`` (untimed) ahead of each repetition."""
+    st = torch.cuda.current_stream()
+    ev = []
+    for _ in range(reps):
+        if before is not None:
+            before()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        fn()
+        e1.record(st)
+        ev.append((e0, e1))
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def _traced(fn):
+    torch.cuda.synchronize()
+    _native.trace_enable(True)
+    fn()
+    torch.cuda.synchronize()
+    tr = _native.trace_collect()
+    _native.trace_enable(False)
+    return tr
+
+
+def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=8, peak=None, flush=None):
+    """The uneven-cube batch (cg_batch_run, graph replay) timed with CUDA events; the batch's own inputs
+    are restored (cg_batch_reset) before each repetition, outside the timed region.  Per-kernel shares
+    from one eager (not graph-replayed) run under the launch tracer."""
+    b = api.Batch(scs, nstreams=streams)
+    bins = b.bins
+
+    def before():
+        b.reset()
+        if flush is not None:
+            flush.fill_(1.0)
+    for _ in range(max(warmup, 1)):
+        before()
+        b.run(form, use_graph=True)
+    ms = _events_ms(lambda: b.run(form, use_graph=True), reps, before)
+    b.reset()
+    tr = _traced(lambda: b.run(form, use_graph=False))
+    b.close()
+    mean = sum(ms) / len(ms)
+    out = {"form": form, "cubes": len(scs), "bins": int(bins), "ms": round(mean, 4),
+           "Mbins_per_s": round(bins / (mean * 1e-3) / 1e6, 1), "ms_per_rep": [round(x, 4) for x in ms],
+           "eager_kernels": kernel_table(tr), "launches": int(sum(v[0] for v in tr.values()))}
+    if peak:
+        out["roofline"] = roofline_of(tr, peak)
+    return out
+
+
 def simulate_case(a):
-    """Posterior simulation on the 200^3 three-stack workload: one mixed inversion, the per-bin posterior
-    factor, then nreal realisations (noise, factor, inverse transform, mean add), timed with CUDA events."""
+    print(json.dumps(measure_simulate(nreal=a.nreal, reps=a.reps)[0]))
+
+
+def measure_simulate(sc=None, nreal=128, reps=3, warmup=1, peak=None):
+    """Posterior simulation on the 200^3 three-stack workload: one mixed inversion, then per call the
+    per-bin posterior factor and nreal realisations (seeded noise, factor, inverse transform, mean add),
+    timed with CUDA events (the fields, 3*nreal cubes, are far larger than L2)."""
     from . import synthetic as S
     from .pipeline import Inversion
-    sc = S.config3()
+    sc = sc or S.config3()
     inv = Inversion(sc, forms=("mixed",))
     inv.restore("mixed")
     inv.run("mixed")
     torch.cuda.synchronize()
     _, rnxp = api.dims(sc.nxp)
-    fields = [torch.empty((sc.nzp, sc.nyp, rnxp), device="cuda") for _ in range(3 * a.nreal)]
-    chol, nfail = api.posterior_cholesky(inv.cov, sc.nxp)
+    fields = [torch.empty((sc.nzp, sc.nyp, rnxp), device="cuda") for _ in range(3 * nreal)]
+    rep = [0]
 
-    def step(rep):
+    def step():
+        rep[0] += 1
         c, _ = api.posterior_cholesky(inv.cov, sc.nxp)
-        api.simulate_fields(c, fields, sc.nxp, seed=1000 + rep, post_mean=inv.mean)
-    step(0)
-    torch.cuda.synchronize()
-    ms = []
-    for r in range(a.reps):
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        step(r + 1)
-        e1.record()
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1))
-    _native.trace_enable(True)
-    step(99)
-    tr = _native.trace_collect()
-    _native.trace_enable(False)
-    best = min(ms)
+        api.simulate_fields(c, fields, sc.nxp, seed=1000 + rep[0], post_mean=inv.mean)
+    for _ in range(max(warmup, 1)):
+        step()
+    ms = _events_ms(step, reps)
+    tr = _traced(step)
+    _, nfail = api.posterior_cholesky(inv.cov, sc.nxp)
+    best = sum(ms) / len(ms)
     bins = sc.nbins
     # algorithmic bytes per realisation: 3 C2R (8 B/bin + 4 B/cell each) + mean read and field write
     # (2 x 3 x 4 B/cell); the factor (36 B/bin) is read once per call
     cells = sc.nxp * sc.nyp * sc.nzp
-    alg = a.nreal * (3 * (8 * bins + 4 * cells) + 24 * cells) + 36 * bins
-    print(json.dumps({"case": {"what": "simulate", "workload": "200^3 padded cube, 3 stacks, config-0 prior",
-                               "nreal": a.nreal, "bins": bins, "chol_fail": int(nfail.item())},
-                      "ms_per_call": ms, "realisations_per_s": a.nreal / (best * 1e-3),
-                      "Mbins_per_s": a.nreal * bins / (best * 1e-3) / 1e6,
-                      "algorithmic_GBps": alg / (best * 1e-3) / 1e9,
-                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
-                                  for k, v in tr.items()}}))
+    alg = nreal * (3 * (8 * bins + 4 * cells) + 24 * cells) + 36 * bins
+    out = {"workload": "200^3 padded cube, 3 stacks 10-30 deg, config-0 prior, 30 Hz Ricker, S/N 4",
+           "nreal": nreal, "bins": bins, "chol_fail": int(nfail.item()), "ms": round(best, 4),
+           "ms_per_call": [round(x, 4) for x in ms], "realisations_per_s": round(nreal / (best * 1e-3), 1),
+           "Mbins_per_s": round(nreal * bins / (best * 1e-3) / 1e6, 1),
+           "algorithmic_GBps": round(alg / (best * 1e-3) / 1e9, 1), "kernels": kernel_table(tr),
+           "launches": int(sum(v[0] for v in tr.values()))}
+    if peak:
+        out["roofline"] = roofline_of(tr, peak)
+    del fields, inv
+    return out, sc
 
 
 def timelapse_case(a):
-    """4D time-lapse on the 256x256x192 workload: two vintages x 4 stacks, each merge -> data transforms
-    -> plain bin loop (4D branch) -> split -> posterior-mean inverse transforms; timed with CUDA events,
-    the state restored between repetitions outside the timed region."""
+    print(json.dumps(measure_timelapse(form=a.form, reps=a.reps)[0]))
+
+
+def measure_timelapse(tl=None, form="mixed", reps=3, warmup=1, peak=None, run=None):
+    """4D time-lapse on the 256x256x192 workload: two vintages x 4 stacks, per vintage the data
+    transforms, merge -> 4D bin solve -> split (form "plain": three kernels as the reference's three
+    passes; "fp32" / "mixed": one pass per bin, cg_vintage4d) and the posterior-mean inverse transforms;
+    CUDA events, the state restored before each repetition outside the timed region."""
     from . import synthetic as S
     from .pipeline import TimeLapse
-    tl = S.config4()
-    run = TimeLapse(tl)
-    run.restore()
-    run.run()
-    torch.cuda.synchronize()
-    ms = []
-    for _ in range(a.reps):
+    tl = tl or S.config4()
+    run = run or TimeLapse(tl)
+    for _ in range(max(warmup, 1)):
         run.restore()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record()
-        run.run()
-        e1.record()
-        torch.cuda.synchronize()
-        ms.append(e0.elapsed_time(e1))
+        run.run(form=form)
+    ms = _events_ms(lambda: run.run(form=form), reps, run.restore)
     run.restore()
-    _native.trace_enable(True)
-    run.run()
-    tr = _native.trace_collect()
-    _native.trace_enable(False)
-    best = min(ms)
-    bins = tl.nbins
+    tr = _traced(lambda: run.run(form=form))
     fails = [int(x.item()) for x in run.nfail_split]
     st = [w.stats() for w in run.ws]
-    print(json.dumps({"case": {"what": "timelapse", "workload": "256x256x192 padded cube, 2 vintages x 4 stacks, "
-                                                            "6-parameter state", "bins": bins},
-                      "ms_per_run": ms, "Mbins_per_s": bins / (best * 1e-3) / 1e6,
-                      "joint_algorithmic_GBps": run.algorithmic_bytes() / (best * 1e-3) / 1e9,
-                      "split_fails": fails, "chol_fail": [x["failed"] for x in st],
-                      "kernels": {k: {"launches": v[0], "ms": v[1], "GBps": v[2] / max(v[1], 1e-12) / 1e6}
-                                  for k, v in tr.items()}}))
+    best = sum(ms) / len(ms)
+    bins = tl.nbins
+    out = {"form": form, "bins": bins, "ms": round(best, 4), "ms_per_run": [round(x, 4) for x in ms],
+           "Mbins_per_s": round(bins / (best * 1e-3) / 1e6, 1),
+           "joint_algorithmic_GBps": round(run.algorithmic_bytes() / (best * 1e-3) / 1e9, 1),
+           "split_fails": fails, "chol_fail": [x["failed"] for x in st], "fp64_bins": [x["flagged"] for x in st],
+           "kernels": kernel_table(tr), "launches": int(sum(v[0] for v in tr.values()))}
+    if peak:
+        out["roofline"] = roofline_of(tr, peak)
+    return out, run
 
 
 def ingest_case(a):

@@ -37,14 +37,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
+_FFT_WORKERS = os.cpu_count() or 1
+
 try:  # multi-threaded transforms for the input generator when scipy is present
     import scipy.fft as _sfft
 
     def _fftn(a):
-        return _sfft.fftn(a, norm="ortho", workers=os.cpu_count() or 1)
+        return _sfft.fftn(a, norm="ortho", workers=_FFT_WORKERS)
 
     def _ifftn(a):
-        return _sfft.ifftn(a, norm="ortho", workers=os.cpu_count() or 1)
+        return _sfft.ifftn(a, norm="ortho", workers=_FFT_WORKERS)
 except ImportError:  # pragma: no cover
     def _fftn(a):
         return np.fft.fftn(a, norm="ortho")
@@ -373,20 +375,42 @@ def config3(seed=20261206, **kw) -> Scenario:
                          seed=seed, **kw)
 
 
-def config2(ncubes=64, seed=20261205, **kw):
+def config2(ncubes=64, seed=20261205, workers=None, **kw):
     """64 independent cubes of uneven size: nx, ny ~ U{32..192}, nz ~ U{64..160},
     each padded (25 %) to the next 2/3/5/7-smooth size; 2-8 stacks at 0-40 deg,
-    Ricker peak U(15, 45) Hz, S/N U(2, 6), prior stds scaled by U(0.5, 1.5)."""
+    Ricker peak U(15, 45) Hz, S/N U(2, 6), prior stds scaled by U(0.5, 1.5).  ``workers`` > 1 builds
+    the cubes in that many spawned processes (default: one per core)."""
     rng = np.random.default_rng(seed)
-    out = []
+    jobs = []
     for c in range(ncubes):
         nx, ny = int(rng.integers(32, 193)), int(rng.integers(32, 193))
         nz = int(rng.integers(64, 161))
         nt = int(rng.integers(2, 9))
         theta = list(np.linspace(0.0, 40.0, nt)) if nt > 1 else [20.0]
-        out.append(make_scenario(nx, ny, nz, theta, float(rng.uniform(15, 45)), sn=float(rng.uniform(2, 6)),
-                                 std_scale=float(rng.uniform(0.5, 1.5)), seed=seed + 1 + c, **kw))
-    return out
+        jobs.append(((nx, ny, nz, theta, float(rng.uniform(15, 45))),
+                     dict(kw, sn=float(rng.uniform(2, 6)), std_scale=float(rng.uniform(0.5, 1.5)),
+                          seed=seed + 1 + c)))
+    if workers is None:
+        workers = min(ncubes, os.cpu_count() or 1)
+    if workers <= 1:
+        return [make_scenario(*a, **k) for a, k in jobs]
+    # every cube has its own seed, so a pool of single-threaded generators gives the same cubes; spawned
+    # workers share no state (CUDA included) with the caller
+    import concurrent.futures as cf
+    import multiprocessing as mp
+    with cf.ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn"),
+                                initializer=_single_threaded) as ex:
+        return list(ex.map(_make_scenario_job, jobs))
+
+
+def _single_threaded():
+    global _FFT_WORKERS
+    _FFT_WORKERS = 1
+
+
+def _make_scenario_job(job):
+    args, kw = job
+    return make_scenario(*args, **kw)
 
 
 # ----------------------------------------------------------------------------
