@@ -440,14 +440,28 @@ int fft3d_add(void *const *bufs, const void *const *addends, int count, int nxp,
     }
     if (forward) {
       T pre = covlike ? (T)1 : (T)(1.0 / sqrt(N));
-      if ((rc = launch_rows<T>(true, cs, ad, nb, nxp, nyp, nzp, pre, st))) return rc;
-      if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, -1, st))) return rc;
+      int xy = 0;
+      if constexpr (sizeof(T) == 4) {
+        xy = xy_planes(true, cs, ad, nb, nxp, nyp, nzp, (float)pre, st, kEpiNone);
+        if (xy < 0) return xy;
+      }
+      if (!xy) {
+        if ((rc = launch_rows<T>(true, cs, ad, nb, nxp, nyp, nzp, pre, st))) return rc;
+        if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, -1, st))) return rc;
+      }
       if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, -1, st))) return rc;
     } else {
       T post = covlike ? (T)(1.0 / N) : (T)(1.0 / sqrt(N));
       if ((rc = launch_cols<T>(cs, nb, nzp, cnxp, (long)cnxp * nyp, cnxp, nyp, +1, st))) return rc;
-      if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, +1, st))) return rc;
-      if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st, epi))) return rc;
+      int xy = 0;
+      if constexpr (sizeof(T) == 4) {
+        xy = xy_planes(false, cs, ad, nb, nxp, nyp, nzp, (float)post, st, epi);
+        if (xy < 0) return xy;
+      }
+      if (!xy) {
+        if ((rc = launch_cols<T>(cs, nb, nyp, cnxp, cnxp, (long)nyp * cnxp, nzp, +1, st))) return rc;
+        if ((rc = launch_rows<T>(false, cs, ad, nb, nxp, nyp, nzp, post, st, epi))) return rc;
+      }
     }
   }
   return CG_OK;

@@ -618,6 +618,10 @@ int fast_cols(const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride,
               int sign, const float2 *tw, cudaStream_t st, int *done_cols, bool no_alloc = false);
 int fast_rows(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows, float scale,
               const float2 *tw, cudaStream_t st, int epi = kEpiNone);
+// x and y passes of one z-plane per cluster (fft_xy.cu): 1 if they ran, 0 when (nxp, nyp) has no plane
+// kernel or the tuning table (CG_TUNE_XY_PLANE) selects the separate passes
+int xy_planes(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nyp, int nzp,
+              float scale, cudaStream_t st, int epi);
 // four-step kernels (fft_4step_*.cu); chosen by the tuning table
 int four_step_cols(int minb, const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride,
                    int nbatch, int sign, const float2 *tw, cudaStream_t st);

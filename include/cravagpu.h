@@ -94,7 +94,10 @@ int cg_device_faults(int *flag);
  * stack count n: 0 Cholesky of the n x n data covariance, 1 information form:
  * a 3 x 3 Cholesky per bin from per-k eigen-decompositions of the error
  * covariance, for models whose every in-band error diagonal is positive;
- * the default).  n = 0 sets the value for every n.  Built-in defaults were
+ * the default), CG_TUNE_XY_PLANE (x and y passes of a 3D transform per x
+ * length n = nxp: 0 two launches, 1 one launch of plane kernels, one z-plane
+ * per two-CTA cluster with the plane's intermediate spectrum in distributed
+ * shared memory; nxp = nyp = 256).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0
@@ -103,6 +106,7 @@ int cg_device_faults(int *flag);
 #define CG_TUNE_ROWS_KERNEL 3
 #define CG_TUNE_FUSED_Y 4
 #define CG_TUNE_BIN_FORM 5
+#define CG_TUNE_XY_PLANE 6
 int cg_tune_set(int key, int n, int value);
 int cg_tune_get(int key, int n);
 int cg_tune_clear(void);

@@ -228,3 +228,59 @@ def test_extended_lengths_match_oracle(cuda, oracle, dims):
     assert rel(from_cube(t), ref) < FFT_TOL
     api.inv_fft_in_place(t, nxp, api.DATA)
     assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL
+
+
+# x + y plane kernels (one z-plane per two-CTA cluster, intermediate spectrum in distributed shared memory):
+# against the FP64 oracle, bit for bit against the separate four-step x-row and column passes they restate,
+# several cubes in one launch, and the inverse's addend and exp epilogue
+XY_SIZES = [(256, 256, 3), (256, 256, 40)]
+
+
+@pytest.mark.parametrize("dims", XY_SIZES)
+def test_xy_plane_kernels_match_oracle_and_separate_passes(cuda, oracle, native, dims):
+    from crava_gb300 import _native, api
+    nxp, nyp, nzp = dims
+    x, ref = _variant_case(oracle, nxp, nyp, nzp)
+    native.cg_tune_clear()
+    try:
+        # separate passes with the four-step column kernel (the arithmetic the plane kernels restate)
+        assert native.cg_tune_set(6, 0, 0) == 0 and native.cg_tune_set(1, 0, 3) == 0
+        sep = [torch.from_numpy(x.copy()).cuda() for _ in range(3)]
+        api.fft_in_place_batch(sep, nxp, api.DATA)
+        sep_spec = [s.clone() for s in sep]
+        api.fft_in_place_batch(sep, nxp, api.DATA, inverse=True)
+        assert native.cg_tune_set(6, 0, 1) == 0
+        cubes = [torch.from_numpy(x.copy()).cuda() for _ in range(3)]
+        _native.trace_enable(True)
+        api.fft_in_place_batch(cubes, nxp, api.DATA)
+        spec = [c.clone() for c in cubes]
+        api.fft_in_place_batch(cubes, nxp, api.DATA, inverse=True)
+        tr = _native.trace_collect()
+        _native.trace_enable(False)
+        assert "k_xy_r2c" in tr and "k_yx_c2r" in tr, tr.keys()
+        for s, t, a, b in zip(spec, cubes, sep_spec, sep):
+            assert rel(from_cube(s), ref) < FFT_TOL
+            assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL
+            assert torch.equal(s, a), "forward plane kernel differs from the separate passes"
+            assert torch.equal(t, b), "inverse plane kernel differs from the separate passes"
+        # inverse with an addend (the posterior-mean add of simulation) and with the exp epilogue: identical to
+        # the separate passes
+        cnxp, rnxp = oracle.dims(nxp)
+        g = torch.Generator(device="cuda").manual_seed(7)
+        chol = torch.randn((9, nzp, nyp, cnxp), device="cuda", generator=g)
+        pm = [torch.randn((nzp, nyp, rnxp), device="cuda", generator=g) for _ in range(3)]
+        spec = [torch.randn((nzp, nyp, rnxp), device="cuda", generator=g) * 0.01 for _ in range(2)]
+        out = {}
+        for xy in (0, 1):
+            assert native.cg_tune_set(6, 0, xy) == 0
+            fields = [torch.empty((nzp, nyp, rnxp), device="cuda") for _ in range(3)]
+            api.simulate_fields(chol, fields, nxp, seed=5, post_mean=pm)
+            ex = [s.clone() for s in spec]
+            api.inv_fft_exp_batch(ex, nxp, api.PARAMETER)
+            out[xy] = (fields, ex)
+        for a, b in zip(out[0][0] + out[0][1], out[1][0] + out[1][1]):
+            assert torch.equal(a, b), "inverse plane kernel with addend / epilogue differs from the separate passes"
+    finally:
+        _native.trace_enable(False)
+        native.cg_tune_clear()
+        _native._apply_tuning(native)
