@@ -124,28 +124,71 @@ __device__ __forceinline__ void dft8(C2<T> *v, int sign)
   v[7] = csub<T>(e[3], t3);
 }
 
-// odd prime radix: direct DFT with the R-th roots taken from the twiddle
-// table (W_R^e = W_n^{e n / R})
-template <typename T, int R>
-__device__ __forceinline__ void dft_odd(C2<T> *v, int sign, const C2<T> *tw, int rstride)
+// cos(2 pi m / R) and sin(2 pi m / R) for the odd prime radices, m = 1 .. (R-1)/2 (the values of the
+// roots of unity to 22 digits; other m fold onto these by symmetry)
+__host__ __device__ constexpr double root_cos(int r, int m)
 {
-  C2<T> w[R];
+  return r == 3 ? -0.5
+       : r == 5 ? (m == 1 ? 0.3090169943749474241023 : -0.8090169943749474241023)
+       : (m == 1 ? 0.623489801858733530525 : m == 2 ? -0.2225209339563144042889 : -0.9009688679024191262361);
+}
+__host__ __device__ constexpr double root_sin(int r, int m)
+{
+  return r == 3 ? 0.8660254037844386467637
+       : r == 5 ? (m == 1 ? 0.9510565162951535721164 : 0.5877852522924731291687)
+       : (m == 1 ? 0.7818314824680298087084 : m == 2 ? 0.9749279121818236070181 : 0.4338837391175581204758);
+}
+// cos / sin of 2 pi m / R for any m
+__host__ __device__ constexpr double rc(int r, int m)
+{
+  return m % r == 0 ? 1.0 : m % r <= r / 2 ? root_cos(r, m % r) : root_cos(r, r - m % r);
+}
+__host__ __device__ constexpr double rs(int r, int m)
+{
+  return m % r == 0 ? 0.0 : m % r <= r / 2 ? root_sin(r, m % r) : -root_sin(r, r - m % r);
+}
+
+// odd prime radix R (3, 5, 7): the DFT X[u] = sum_q v[q] W^(qu), W = exp(sign 2 pi i / R), folded over the
+// conjugate-symmetric pairs: with t_q = v[q] + v[R-q], d_q = v[q] - v[R-q] (q = 1 .. (R-1)/2),
+//   X[0] = v[0] + sum t_q,   X[u], X[R-u] = A_u +- i sign B_u,
+//   A_u = v[0] + sum_q t_q cos(2 pi qu/R),   B_u = sum_q d_q sin(2 pi qu/R),
+// real constants in place of the (R-1)^2 complex products of the direct sum.  (tw and rstride are unused:
+// the roots are compile-time constants.)
+template <typename T, int R>
+__device__ __forceinline__ void dft_odd(C2<T> *v, int sign, const C2<T> *, int)
+{
+  constexpr int H = (R - 1) / 2;
+  C2<T> t[H], d[H];
 #pragma unroll
-  for (int e = 1; e < R; e++) w[e] = tw_at<T>(tw, e * rstride, sign);
-  C2<T> out[R];
-#pragma unroll
-  for (int u = 0; u < R; u++) {
-    C2<T> acc = v[0];
-#pragma unroll
-    for (int q = 1; q < R; q++) {
-      int e = (q * u) % R;
-      if (e == 0) acc = cadd<T>(acc, v[q]);
-      else acc = cadd<T>(acc, cmul<T>(v[q], w[e]));
-    }
-    out[u] = acc;
+  for (int q = 1; q <= H; q++) {
+    t[q - 1] = cadd<T>(v[q], v[R - q]);
+    d[q - 1] = csub<T>(v[q], v[R - q]);
   }
+  const C2<T> v0 = v[0];
+  C2<T> x0 = v0;
 #pragma unroll
-  for (int u = 0; u < R; u++) v[u] = out[u];
+  for (int q = 0; q < H; q++) x0 = cadd<T>(x0, t[q]);
+#pragma unroll
+  for (int u = 1; u <= H; u++) {
+    T ax = v0.x, ay = v0.y, bx = 0, by = 0;
+#pragma unroll
+    for (int q = 1; q <= H; q++) {
+      const T c = (T)rc(R, q * u), sn = (T)rs(R, q * u);
+      ax += t[q - 1].x * c;
+      ay += t[q - 1].y * c;
+      bx += d[q - 1].x * sn;
+      by += d[q - 1].y * sn;
+    }
+    // i sign B = sign (-by, bx)
+    if (sign > 0) {
+      v[u] = mk<T>(ax - by, ay + bx);
+      v[R - u] = mk<T>(ax + by, ay - bx);
+    } else {
+      v[u] = mk<T>(ax + by, ay - bx);
+      v[R - u] = mk<T>(ax - by, ay + bx);
+    }
+  }
+  v[0] = x0;
 }
 
 // One Stockham stage for the butterfly j of column c:
@@ -163,9 +206,9 @@ __device__ __forceinline__ void stockham_bfly(const C2<T> *src, C2<T> *dst, int 
 #pragma unroll
     for (int r = 1; r < R; r++) v[r] = cmul<T>(v[r], tw_at<T>(tw, jm * r * span * twstride, sign));
   }
-  if (R == 2) dft2<T>(v);
-  else if (R == 4) dft4<T>(v, sign);
-  else if (R == 8) dft8<T>(v, sign);
+  if constexpr (R == 2) dft2<T>(v);
+  else if constexpr (R == 4) dft4<T>(v, sign);
+  else if constexpr (R == 8) dft8<T>(v, sign);
   else dft_odd<T, R>(v, sign, tw, nb * twstride);
   const int d = (j - jm) * R + jm;
 #pragma unroll

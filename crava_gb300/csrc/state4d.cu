@@ -36,12 +36,10 @@ __global__ void k_state4d_merge(const __grid_constant__ S4Args a)
   for (int t = 0; t < 6; t++) a.cov_cur[t][b] = c6[t];
 }
 
-__global__ void __launch_bounds__(128, 3) k_state4d_split(const __grid_constant__ S4Args a)
+__global__ void __launch_bounds__(128, 4) k_state4d_split(const __grid_constant__ S4Args a)
 {
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.csize) return;
-  float2 F[6][6];
-  load_full6<float>(a.ss, a.sd, a.dd, b, F);
   float2 muF[6], muCpost[3];
 #pragma unroll
   for (int l = 0; l < 3; l++) { muF[l] = a.mu_s[l][b]; muF[l + 3] = a.mu_d[l][b]; muCpost[l] = a.mu_cur[l][b]; }
@@ -51,9 +49,7 @@ __global__ void __launch_bounds__(128, 3) k_state4d_split(const __grid_constant_
   Cpost[1][0] = make_float2(Cpost[0][1].x, -Cpost[0][1].y);
   Cpost[2][0] = make_float2(Cpost[0][2].x, -Cpost[0][2].y);
   Cpost[2][1] = make_float2(Cpost[1][2].x, -Cpost[1][2].y);
-  float2 out[6][6], muFpost[6];
-  if (!split_bin<float>(F, muF, muCpost, Cpost, out, muFpost) && a.nfail) atomicAdd(a.nfail, 1);
-  store_state<float>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, out, muFpost);
+  if (!split_bin<float>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, muF, muCpost, Cpost) && a.nfail) atomicAdd(a.nfail, 1);
 }
 
 static int fill_args(S4Args &a, float *const *mu_s, float *const *mu_d, float *const *ss, float *const *sd,

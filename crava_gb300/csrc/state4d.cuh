@@ -61,13 +61,28 @@ __device__ __forceinline__ void merge_cov(const C2<T> (*F)[6], C2<T> *cov6)
   }
 }
 
-// State4D::split of one bin: F, muF the full prior; muCpost, Cpost (Hermitian, all nine entries) the
-// current state's posterior (both consumed).  Writes the full posterior (upper triangle of out) and
-// muFpost; false when the Cholesky of the current prior fails (out = F, muFpost = muF, as the reference
-// keeps the prior).
+// entry (i, j) of the full Hermitian 6x6 prior of bin b, read from the stored upper triangle (i, j
+// compile-time after unrolling)
+__host__ __device__ constexpr int tri_t(int i, int j) { return i * (5 - i) / 2 + j; }  // 00 01 02 11 12 22
 template <typename T>
-__device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF, C2<T> *muCpost, C2<T> (*Cpost)[3],
-                                          C2<T> (*out)[6], C2<T> *muFpost)
+__device__ __forceinline__ C2<T> state_entry(float2 *const *ss, float2 *const *sd, float2 *const *dd, long b, int i,
+                                             int j)
+{
+  const int r = i < j ? i : j, c = i < j ? j : i;
+  const float2 v = c < 3 ? ss[tri_t(r, c)][b] : (r < 3 ? sd[r * 3 + c - 3][b] : dd[tri_t(r - 3, c - 3)][b]);
+  return i <= j ? mk<T>((T)v.x, (T)v.y) : mk<T>((T)v.x, -(T)v.y);
+}
+
+// State4D::split of bin b, in place on the 27 stored spectra.  muF is the bin's full prior mean; muCpost,
+// Cpost (Hermitian, all nine entries) the current state's posterior (both consumed).  The prior covariance
+// F is read from the grids twice (for the sums F(:, m) + F(:, m+3) at the start and for the final
+// F + sand^H * helper), so it is never held in registers as a whole; every posterior entry is stored as
+// soon as it is formed.  Returns false when the Cholesky of the current prior fails: the grids then keep
+// the prior, as the reference keeps it.
+template <typename T>
+__device__ __forceinline__ bool split_bin(float2 *const *mu_s, float2 *const *mu_d, float2 *const *ss,
+                                          float2 *const *sd, float2 *const *dd, long b, const C2<T> *muF,
+                                          C2<T> *muCpost, C2<T> (*Cpost)[3])
 {
   C2<T> muC[3];
 #pragma unroll
@@ -76,7 +91,10 @@ __device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF,
 #pragma unroll
   for (int l = 0; l < 6; l++)
 #pragma unroll
-    for (int m = 0; m < 3; m++) FvC[l][m] = mk<T>(F[l][m].x + F[l][m + 3].x, F[l][m].y + F[l][m + 3].y);
+    for (int m = 0; m < 3; m++) {
+      const C2<T> a = state_entry<T>(ss, sd, dd, b, l, m), c = state_entry<T>(ss, sd, dd, b, l, m + 3);
+      FvC[l][m] = mk<T>(a.x + c.x, a.y + c.y);
+    }
   C2<T> Cp[3][3];
 #pragma unroll
   for (int l = 0; l < 3; l++)
@@ -92,15 +110,7 @@ __device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF,
   for (int i = 0; i < 6; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) sand[j][i] = mk<T>(FvC[i][j].x, -FvC[i][j].y);
-  if (!chol_ref<T, 3>(L)) {
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-      for (int j = i; j < 6; j++) out[i][j] = F[i][j];
-#pragma unroll
-    for (int i = 0; i < 6; i++) muFpost[i] = muF[i];
-    return false;
-  }
+  if (!chol_ref<T, 3>(L)) return false;
   axeqb_ref<T, 3, 6>(L, sand);
 #pragma unroll
   for (int l = 0; l < 3; l++)
@@ -119,7 +129,7 @@ __device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF,
       }
       helper[i][j] = mk<T>(xr, xi);
     }
-  // out = adjoint(sand) * helper + F (only the upper triangle is stored)
+  // F + adjoint(sand) * helper, upper triangle, each entry stored as it is formed
 #pragma unroll
   for (int i = 0; i < 6; i++)
 #pragma unroll
@@ -131,7 +141,11 @@ __device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF,
         xr += ad.x * helper[k][j].x - ad.y * helper[k][j].y;
         xi += ad.y * helper[k][j].x + ad.x * helper[k][j].y;
       }
-      out[i][j] = mk<T>(xr + F[i][j].x, xi + F[i][j].y);
+      const C2<T> f = state_entry<T>(ss, sd, dd, b, i, j);
+      const float2 o = make_float2((float)(xr + f.x), (float)(xi + f.y));
+      if (j < 3) ss[tri_t(i, j)][b] = o;
+      else if (i < 3) sd[i * 3 + j - 3][b] = o;
+      else dd[tri_t(i - 3, j - 3)][b] = o;
     }
 #pragma unroll
   for (int l = 0; l < 3; l++) { muCpost[l].x -= muC[l].x; muCpost[l].y -= muC[l].y; }
@@ -144,29 +158,11 @@ __device__ __forceinline__ bool split_bin(const C2<T> (*F)[6], const C2<T> *muF,
       xr += ad.x * muCpost[j].x - ad.y * muCpost[j].y;
       xi += ad.y * muCpost[j].x + ad.x * muCpost[j].y;
     }
-    muFpost[i] = mk<T>(xr + muF[i].x, xi + muF[i].y);
+    const float2 o = make_float2((float)(xr + muF[i].x), (float)(xi + muF[i].y));
+    if (i < 3) mu_s[i][b] = o;
+    else mu_d[i - 3][b] = o;
   }
   return true;
-}
-
-// the full posterior back into the 27 stored spectra of bin b
-template <typename T>
-__device__ __forceinline__ void store_state(float2 *const *mu_s, float2 *const *mu_d, float2 *const *ss,
-                                            float2 *const *sd, float2 *const *dd, long b, const C2<T> (*out)[6],
-                                            const C2<T> *muFpost)
-{
-#pragma unroll
-  for (int t = 0; t < 6; t++) ss[t][b] = make_float2((float)out[tri_r(t)][tri_c(t)].x, (float)out[tri_r(t)][tri_c(t)].y);
-#pragma unroll
-  for (int t = 0; t < 9; t++) sd[t][b] = make_float2((float)out[sd_r(t)][sd_c(t)].x, (float)out[sd_r(t)][sd_c(t)].y);
-#pragma unroll
-  for (int t = 0; t < 6; t++)
-    dd[t][b] = make_float2((float)out[3 + tri_r(t)][3 + tri_c(t)].x, (float)out[3 + tri_r(t)][3 + tri_c(t)].y);
-#pragma unroll
-  for (int l = 0; l < 3; l++) {
-    mu_s[l][b] = make_float2((float)muFpost[l].x, (float)muFpost[l].y);
-    mu_d[l][b] = make_float2((float)muFpost[l + 3].x, (float)muFpost[l + 3].y);
-  }
 }
 
 }  // namespace cg

@@ -117,21 +117,19 @@ __device__ __forceinline__ bool vintage_bin(const V4Args &a, long b)
   Cpost[1][0] = mk<T>(S[0][1].x, -S[0][1].y);
   Cpost[2][0] = mk<T>(S[0][2].x, -S[0][2].y);
   Cpost[2][1] = mk<T>(S[1][2].x, -S[1][2].y);
-  C2<T> F[6][6], muF[6], out[6][6], muFpost[6];
-  load_full6<T>(a.ss, a.sd, a.dd, b, F);
+  C2<T> muF[6];
 #pragma unroll
   for (int l = 0; l < 3; l++) {
     const float2 s = a.mu_s[l][b], d = a.mu_d[l][b];
     muF[l] = mk<T>((T)s.x, (T)s.y);
     muF[l + 3] = mk<T>((T)d.x, (T)d.y);
   }
-  if (!split_bin<T>(F, muF, mu, Cpost, out, muFpost) && a.nsplit) atomicAdd(a.nsplit, 1);
-  store_state<T>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, out, muFpost);
+  if (!split_bin<T>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, muF, mu, Cpost) && a.nsplit) atomicAdd(a.nsplit, 1);
   return true;
 }
 
 template <int NT, int MODE>
-__global__ void __launch_bounds__(128) k_vintage4d(const __grid_constant__ V4Args a)
+__global__ void __launch_bounds__(128, 4) k_vintage4d(const __grid_constant__ V4Args a)
 {
   const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.csize) return;
