@@ -20,6 +20,7 @@
 // the reference; with the in-place buffers only the covariance is written.
 #include <cmath>
 #include <cstdlib>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -825,8 +826,11 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       memcpy(&af, &a, sizeof(af));
       int nsm = 0;
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
+      // grid-stride over the queue: one CTA per 8192 bins of the launch, at most four per SM, so that a small
+      // cube's (usually empty) fix-up does not hold hundreds of CTA slots beside other cubes' kernels
+      const int fix_ctas = (int)std::min<long>((long)nsm * 4, std::max<long>(1, (long)a.plane * nk / 8192));
       TraceScope ts("k_invert_fixup64", st, 0.0);
-      k_invert_fixup64<NT><<<nsm * 4, 128, 0, st>>>(af, w->ktab_d, sd);
+      k_invert_fixup64<NT><<<fix_ctas, 128, 0, st>>>(af, w->ktab_d, sd);
     } else if (use_info(w, NT)) {
       TraceScope ts("k_invert_info_fp32", st, fbytes);
       launch_info<NT, 0>(a, w, grid, threads, st);

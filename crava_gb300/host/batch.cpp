@@ -11,6 +11,7 @@
 // graph launch for the whole batch instead of ~20 launches per cube.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -199,13 +200,40 @@ extern "C" int cg_batch_reset(cg_batch b, void *stream)
   })
 }
 
+// Cubes to streams, longest first onto the least-loaded stream (LPT): the
+// streams finish close together instead of one stream ending on a run of
+// large cubes.  Work is estimated as bins x (stacks + 9 output spectra).
+static std::vector<int> stream_of_cubes(const cg_batch_s *b)
+{
+  const size_t n = b->cubes.size(), ns = b->streams.size();
+  std::vector<int> order(n), sid(n);
+  for (size_t i = 0; i < n; i++) order[i] = (int)i;
+  auto work = [&](int i) { return (double)b->cubes[i].bins() * (b->cubes[i].ntheta + 9); };
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
+  std::vector<double> load(ns, 0.0);
+  for (int i : order) {
+    size_t best = 0;
+    for (size_t s = 1; s < ns; s++)
+      if (load[s] < load[best]) best = s;
+    sid[i] = (int)best;
+    load[best] += work(i);
+  }
+  return sid;
+}
+
 static void queue_batch(cg_batch b, Crava::Form form, cudaStream_t st)
 {
   cuda_check(cudaEventRecord(b->fork, st), "fork");
   for (auto s : b->streams) cuda_check(cudaStreamWaitEvent(s, b->fork, 0), "fork wait");
-  for (size_t i = 0; i < b->cubes.size(); i++) {
+  const std::vector<int> sid = stream_of_cubes(b);
+  // largest cubes first, so each stream starts on its biggest piece of work
+  std::vector<int> order(b->cubes.size());
+  for (size_t i = 0; i < order.size(); i++) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int x, int y) { return b->cubes[x].bins() > b->cubes[y].bins(); });
+  for (int i : order) {
     BatchCube &c = b->cubes[i];
-    cudaStream_t cs = b->streams[i % b->streams.size()];
+    cudaStream_t cs = b->streams[sid[i]];
     for (auto *g : c.data) g->setTransformedStatus(false);
     for (auto *g : c.mean) g->setTransformedStatus(false);
     FFTGrid *a = c.mean[0], *bb = c.mean[1], *cc = c.mean[2];
