@@ -120,8 +120,10 @@ def _apply_tuning(L):
         for n, v in t.get("cols", {}).items():
             L.cg_tune_set(1, int(n), int(v["pipe"]))
             L.cg_tune_set(0, int(n), int(v["minb"]))
+            L.cg_tune_set(7, int(n), int(v.get("shape", 0)))
         for n, v in t.get("bin", {}).items():
             L.cg_tune_set(2, int(n), int(v["minb"]))
+            L.cg_tune_set(8, int(n), int(v.get("runs", 0)))
         for n, v in t.get("rows", {}).items():
             L.cg_tune_set(3, int(n), int(v["kernel"]))
         for n, v in t.get("fused_y", {}).items():

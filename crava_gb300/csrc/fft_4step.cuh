@@ -84,6 +84,15 @@ __host__ __device__ constexpr int fs_cols_w(int n)
   return (fs_n1(n) >= 16 && n / fs_n1(n) >= 16) ? 16 : 32;
 }
 
+// the tile shapes the tuning table chooses among per length (CG_TUNE_COLS_SHAPE):
+// bit 0 swaps the factors (N1 = N / fs_n1(N), the largest divisor not above
+// sqrt(N)), bit 1 takes the other tile width (16 <-> 32 columns)
+__host__ __device__ constexpr int fs_shape_n1(int n, int shape) { return (shape & 1) ? n / fs_n1(n) : fs_n1(n); }
+__host__ __device__ constexpr int fs_shape_w(int n, int shape)
+{
+  return (shape & 2) ? (fs_cols_w(n) == 16 ? 32 : 16) : fs_cols_w(n);
+}
+
 // ---------------------------------------------------------------------------
 // strided column pass.  Full tiles are W adjacent columns of one batch row.
 // The ntail columns left over in each batch row, taken row after row, form a
@@ -92,11 +101,12 @@ __host__ __device__ constexpr int fs_cols_w(int n)
 // Grid columns x >= nfull hold the tail tiles, numbered (x - nfull)*nbatch + y.
 // Shared layout: buf[(k1*N2 + n2)*W + c] (conflict-free for both passes).
 // ---------------------------------------------------------------------------
-template <int N, int W, int MINB>
+template <int N, int W, int N1_, int MINB>
 __global__ void __launch_bounds__(kFFTThreads, MINB) k_fft_cols_4s(const __grid_constant__ CubeSet cs, const float2 *__restrict__ twg,
                                                                    ColsGeom g, int sign)
 {
-  constexpr int N1 = fs_n1(N), N2 = N / N1;
+  constexpr int N1 = N1_, N2 = N / N1;
+  static_assert(N % N1 == 0, "N1 must divide N");
   constexpr int P1 = W * N2, P2 = W * N1;
   constexpr int B1 = (P1 + kFFTThreads - 1) / kFFTThreads, B2 = (P2 + kFFTThreads - 1) / kFFTThreads;
   extern __shared__ __align__(16) unsigned char smem_raw[];

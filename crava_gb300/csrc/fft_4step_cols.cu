@@ -4,18 +4,6 @@
 
 namespace cg {
 
-namespace {
-template <int N>
-int launch_minb(int minb, const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch,
-                int sign, const float2 *tw, cudaStream_t st)
-{
-  if constexpr (N <= 256)
-    if (minb == 4) return launch_cols_4s<N, 4>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
-  if (minb == 3) return launch_cols_4s<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
-  return launch_cols_4s<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
-}
-}  // namespace
-
 // the whole column pass with the four-step kernel, or 0 when n has no specialisation
 int four_step_cols(int minb, const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride, long batch_stride,
                    int nbatch, int sign, const float2 *tw, cudaStream_t st)
@@ -24,11 +12,11 @@ int four_step_cols(int minb, const CubeSet &cs, int ncubes, int n, int ncols, lo
 #define CG_COLS(NN) \
   case NN: return launch_minb<NN>(minb, cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
     CG_COLS(64) CG_COLS(80) CG_COLS(96) CG_COLS(100) CG_COLS(120) CG_COLS(128) CG_COLS(160) CG_COLS(192)
-    CG_COLS(200) CG_COLS(240) CG_COLS(256) CG_COLS(320) CG_COLS(384) CG_COLS(400) CG_COLS(480) CG_COLS(512)
 #undef CG_COLS
     default: break;
   }
   int rc;
+  if ((rc = four_step_cols_main2(minb, cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, tw, st))) return rc;
   if ((rc = four_step_cols_ext0(cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, tw, st))) return rc;
   if ((rc = four_step_cols_ext1(cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, tw, st))) return rc;
   if ((rc = four_step_cols_ext2(cs, ncubes, n, ncols, axis_stride, batch_stride, nbatch, sign, tw, st))) return rc;

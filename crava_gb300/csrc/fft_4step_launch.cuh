@@ -4,17 +4,18 @@
 
 #include "fft_4step.cuh"
 #include "trace.cuh"
+#include "tuning.cuh"
 
 namespace cg {
 
-template <int N, int MINB>
-int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
-                   const float2 *tw, cudaStream_t st)
+template <int N, int MINB, int SHAPE>
+int launch_cols_4s_shape(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch,
+                         int sign, const float2 *tw, cudaStream_t st)
 {
-  constexpr int W = fs_cols_w(N);
+  constexpr int W = fs_shape_w(N, SHAPE), N1 = fs_shape_n1(N, SHAPE);
   const size_t smem = ((size_t)N * W + N) * sizeof(float2);
   static bool attr_set[64] = {};
-  cudaError_t e = smem_limit_once(k_fft_cols_4s<N, W, MINB>, smem, attr_set);
+  cudaError_t e = smem_limit_once(k_fft_cols_4s<N, W, N1, MINB>, smem, attr_set);
   if (e != cudaSuccess) return cuda_status(e, "k_fft_cols_4s attribute");
   ColsGeom g;
   g.axis_stride = axis_stride;
@@ -27,9 +28,24 @@ int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, l
   const int tail_cols = (int)ceil_div(tail_tiles, (long)nbatch);
   dim3 grid(g.nfull + tail_cols, nbatch, ncubes);
   TraceScope ts("k_fft_cols_4s", st, 2.0 * ncubes * nbatch * (double)ncols * N * sizeof(float2));
-  k_fft_cols_4s<N, W, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
+  k_fft_cols_4s<N, W, N1, MINB><<<grid, kFFTThreads, smem, st>>>(cs, tw, g, sign);
   CG_CHECK_LAUNCH("k_fft_cols_4s");
   return 1;
+}
+
+// the tile shape the tuning table names for this length (0 when unset); a swap of equal factors is the default
+template <int N, int MINB>
+int launch_cols_4s(const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch, int sign,
+                   const float2 *tw, cudaStream_t st)
+{
+  int shape = cg_tune_get(CG_TUNE_COLS_SHAPE, N);
+  if (fs_n1(N) * fs_n1(N) == N) shape &= 2;
+  switch (shape) {
+    case 1: return launch_cols_4s_shape<N, MINB, 1>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    case 2: return launch_cols_4s_shape<N, MINB, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    case 3: return launch_cols_4s_shape<N, MINB, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+    default: return launch_cols_4s_shape<N, MINB, 0>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  }
 }
 
 template <int M>
@@ -81,6 +97,21 @@ int launch_rows_odd(bool forward, const CubeSet &cs, const CubeSet &addend, int 
   CG_CHECK_LAUNCH(forward ? "k_r2c_rows_odd" : "k_c2r_rows_odd");
   return 1;
 }
+
+// the four-step column pass of a tuned length with the resident-CTA target minb
+template <int N>
+int launch_minb(int minb, const CubeSet &cs, int ncubes, int ncols, long axis_stride, long batch_stride, int nbatch,
+                int sign, const float2 *tw, cudaStream_t st)
+{
+  if constexpr (N <= 256)
+    if (minb == 4) return launch_cols_4s<N, 4>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  if (minb == 3) return launch_cols_4s<N, 3>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+  return launch_cols_4s<N, 2>(cs, ncubes, ncols, axis_stride, batch_stride, nbatch, sign, tw, st);
+}
+
+// tuned lengths 200..512 (fft_4step_cols_main2.cu): 0 when not handled
+int four_step_cols_main2(int minb, const CubeSet &cs, int ncubes, int n, int ncols, long axis_stride,
+                         long batch_stride, int nbatch, int sign, const float2 *tw, cudaStream_t st);
 
 // odd x lengths (fft_4step_rows_odd.cu): 0 when not handled
 int four_step_rows_odd(bool forward, const CubeSet &cs, const CubeSet &addend, int ncubes, int nxp, int nrows,

@@ -754,6 +754,8 @@ template int fill_fused_args<double>(Workspace *, void *const *, void *const *, 
 // over nk planes keeps about four waves of 768 threads per SM
 static int bin_runs(const Workspace *w, long plane, int threads, int nk)
 {
+  const int forced = cg_tune_get(CG_TUNE_BIN_RUNS, w->ntheta);
+  if (forced > 0) return forced < kInfoBlocks ? forced : kInfoBlocks;
   int nsm = 0;
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, w->device);
   const long runs = (long)ceil_div(plane, threads) * nk;

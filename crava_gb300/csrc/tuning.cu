@@ -1,7 +1,7 @@
 // Tuning table: launch variants chosen per transform length or stack count.
 // Defaults are built in (measured on GB300); cg_tune_set overrides them, and
 // the environment variables CRAVA_COLS_MINB, CRAVA_COLS_PIPE, CRAVA_BIN_MINB,
-// CRAVA_ROWS_KERNEL, CRAVA_FUSED_Y, CRAVA_BIN_FORM and CRAVA_XY_PLANE override both (used by
+// CRAVA_ROWS_KERNEL, CRAVA_FUSED_Y, CRAVA_BIN_FORM, CRAVA_XY_PLANE, CRAVA_COLS_SHAPE and CRAVA_BIN_RUNS override both (used by
 // ad-hoc sweeps).
 #include <cstdlib>
 #include <map>
@@ -25,6 +25,8 @@ const char *env_name(int key)
     case CG_TUNE_FUSED_Y: return "CRAVA_FUSED_Y";
     case CG_TUNE_BIN_FORM: return "CRAVA_BIN_FORM";
     case CG_TUNE_XY_PLANE: return "CRAVA_XY_PLANE";
+    case CG_TUNE_COLS_SHAPE: return "CRAVA_COLS_SHAPE";
+    case CG_TUNE_BIN_RUNS: return "CRAVA_BIN_RUNS";
     default: return nullptr;
   }
 }
@@ -36,7 +38,9 @@ bool valid_value(int key, int value)
          (key == CG_TUNE_ROWS_KERNEL && (value == 0 || value == 1)) ||
          (key == CG_TUNE_FUSED_Y && (value >= 0 && value <= 2 || (value >= 4 && value <= 4096 && value % 2 == 0))) ||
          (key == CG_TUNE_BIN_FORM && (value == 0 || value == 1)) ||
-         (key == CG_TUNE_XY_PLANE && (value == 0 || value == 1));
+         (key == CG_TUNE_XY_PLANE && (value == 0 || value == 1)) ||
+         (key == CG_TUNE_COLS_SHAPE && (value >= 0 && value <= 3)) ||
+         (key == CG_TUNE_BIN_RUNS && (value >= 0 && value <= 8));
 }
 }  // namespace
 
@@ -61,7 +65,7 @@ using namespace cg;
 
 extern "C" int cg_tune_set(int key, int n, int value)
 {
-  if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_XY_PLANE || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
+  if (key < CG_TUNE_COLS_MINB || key > CG_TUNE_BIN_RUNS || n < 0) { set_error("cg_tune_set: bad key or n"); return CG_ERR_ARG; }
   if (!valid_value(key, value)) { set_error("cg_tune_set: value %d not valid for key %d", value, key); return CG_ERR_ARG; }
   std::lock_guard<std::mutex> lk(g_mu);
   g_table[((long)key << 32) | (unsigned)n] = value;
@@ -85,6 +89,8 @@ extern "C" int cg_tune_get(int key, int n)
     case CG_TUNE_FUSED_Y: return tune_get(key, n, 0);
     case CG_TUNE_BIN_FORM: return tune_get(key, n, 1);  // information form
     case CG_TUNE_XY_PLANE: return tune_get(key, n, 0);
+    case CG_TUNE_COLS_SHAPE: return tune_get(key, n, 0);
+    case CG_TUNE_BIN_RUNS: return tune_get(key, n, 0);
     default: set_error("cg_tune_get: bad key"); return CG_ERR_ARG;
   }
 }

@@ -97,7 +97,13 @@ int cg_device_faults(int *flag);
  * the default), CG_TUNE_XY_PLANE (x and y passes of a 3D transform per x
  * length n = nxp: 0 two launches, 1 one launch of plane kernels, one z-plane
  * per two-CTA cluster with the plane's intermediate spectrum in distributed
- * shared memory; nxp = nyp = 256).  n = 0 sets the value for every n.  Built-in defaults were
+ * shared memory; nxp = nyp = 256), CG_TUNE_COLS_SHAPE (four-step column
+ * tile per axis length n: bit 0 swaps the two factors N1 x N2 of n (N1 the
+ * largest divisor not above sqrt(n) instead of the smallest not below it),
+ * bit 1 takes the other tile width (16 <-> 32 columns); 0 = default),
+ * CG_TUNE_BIN_RUNS (fused bin kernels per stack count n: 256-bin runs each
+ * CTA solves with one staged per-k table, 1..8, or 0 = about four waves of
+ * CTAs, the default).  n = 0 sets the value for every n.  Built-in defaults were
  * measured on GB300; crava_gb300.autotune measures the candidates and stores
  * its choices. */
 #define CG_TUNE_COLS_MINB 0
@@ -107,6 +113,8 @@ int cg_device_faults(int *flag);
 #define CG_TUNE_FUSED_Y 4
 #define CG_TUNE_BIN_FORM 5
 #define CG_TUNE_XY_PLANE 6
+#define CG_TUNE_COLS_SHAPE 7
+#define CG_TUNE_BIN_RUNS 8
 int cg_tune_set(int key, int n, int value);
 int cg_tune_get(int key, int n);
 int cg_tune_clear(void);

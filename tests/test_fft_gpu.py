@@ -284,3 +284,26 @@ def test_xy_plane_kernels_match_oracle_and_separate_passes(cuda, oracle, native,
         _native.trace_enable(False)
         native.cg_tune_clear()
         _native._apply_tuning(native)
+
+
+# the four-step column tile shapes the autotuner chooses among (CG_TUNE_COLS_SHAPE: swapped factors, other
+# tile width), on tuned and further lengths, every axis
+SHAPE_SIZES = [(200, 120, 90), (42, 150, 189), (64, 96, 45), (40, 216, 147)]
+
+
+@pytest.mark.parametrize("shape", [1, 2, 3])
+def test_column_tile_shapes_match_oracle(cuda, oracle, native, shape):
+    from crava_gb300 import _native, api
+    native.cg_tune_clear()
+    try:
+        assert native.cg_tune_set(1, 0, 3) == 0 and native.cg_tune_set(7, 0, shape) == 0
+        for nxp, nyp, nzp in SHAPE_SIZES:
+            x, ref = _variant_case(oracle, nxp, nyp, nzp)
+            t = torch.from_numpy(x.copy()).cuda()
+            api.fft_in_place(t, nxp, api.DATA)
+            assert rel(from_cube(t), ref) < FFT_TOL, (shape, nxp, nyp, nzp)
+            api.inv_fft_in_place(t, nxp, api.DATA)
+            assert rel(t.cpu().numpy()[..., :nxp], x[..., :nxp]) < FFT_TOL, (shape, nxp, nyp, nzp)
+    finally:
+        native.cg_tune_clear()
+        _native._apply_tuning(native)

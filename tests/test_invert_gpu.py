@@ -247,6 +247,37 @@ def test_information_form_matches_fp64_oracle(cuda, oracle, dims, cond, form, nt
         assert st["flagged"] > 0
 
 
+@pytest.mark.parametrize("bin_form,cond", [(0, 0.0), (1, 0.0), (0, 1.0001), (1, 1.0001)])
+def test_bin_runs_per_cta_give_identical_results(cuda, bin_form, cond):
+    """The runs one CTA solves per staged per-k table (CG_TUNE_BIN_RUNS) change only how bins are grouped into
+    CTAs: every setting gives the same posterior bit for bit, in both bin forms, with and without the FP64 guard
+    forced on every in-band bin (the cube's bins fit the fix-up queue, so no bin falls back on overflow, which
+    would depend on the queue order)."""
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    from crava_gb300 import _native
+    sc = S.make_scenario(38, 51, 32, list(np.linspace(0.0, 40.0, 5)), 25.0, nxp=48, nyp=64, nzp=40, sn=3.0,
+                         notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=77)
+    assert sc.nbins <= 65536
+    L = _native.lib()
+    out = []
+    try:
+        assert L.cg_tune_set(5, 0, bin_form) == 0
+        inv = Inversion(sc, forms=("mixed",), cond_threshold=cond)
+        for runs in (0, 1, 3, 8):
+            assert L.cg_tune_set(8, 0, runs) == 0
+            inv.restore("mixed")
+            inv.run("mixed")
+            torch.cuda.synchronize()
+            out.append(inv.results("mixed"))
+    finally:
+        L.cg_tune_clear()
+        _native._apply_tuning(L)
+    for o in out[1:]:
+        for a, b in zip(o, out[0]):
+            np.testing.assert_array_equal(a, b)
+
+
 @pytest.mark.parametrize("nt", [1, 2, 3, 5, 8])
 def test_cold_inversion_matches_repeated_model_and_fp64_oracle(cuda, oracle, nt):
     """run_cold (operator tables, cg_workspace_set_model_async and the per-k table kernel inside the call)
