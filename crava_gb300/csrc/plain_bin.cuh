@@ -18,7 +18,8 @@ namespace cg {
 // false when the Cholesky of the data covariance fails (S, mu and res are
 // then left as they came in, as the reference keeps the prior); *cond
 // receives the squared ratio of the largest to the smallest Cholesky pivot.
-template <typename T, int NT>
+// FAST: reciprocal-multiply divisions (chol_ref); false keeps the reference's operations.
+template <typename T, int NT, bool FAST = false>
 __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const float2 *__restrict__ e1k,
                                             const float2 *__restrict__ e2k, const float2 *__restrict__ e3k,
                                             const float *c0t, const float *cwt, T lam, C2<T> (*S)[3], C2<T> *mu,
@@ -77,7 +78,7 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
       Sd[tri(l, m)] = mk<T>(xr + er, xi + ei);
     }
   }
-  if (!chol_ref<T, NT>(Sd)) return false;
+  if (!chol_ref<T, NT, FAST>(Sd)) return false;
   {
     T dmax = Sd[0].x, dmin = Sd[0].x;
 #pragma unroll
@@ -92,6 +93,8 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
 #pragma unroll
     for (int p = 0; p < 3; p++) KScc[p][l] = mk<T>(KS[l][p].x, -KS[l][p].y);
   // lib_matrAXeqBMatCpx: KS <- Sd^-1 KS
+  T rh[NT];
+  if constexpr (FAST) diag_rcp<T, NT>(Sd, rh);
 #pragma unroll
   for (int c = 0; c < 3; c++) {
 #pragma unroll
@@ -103,8 +106,12 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
         xi -= (KS[j][c].y * Sd[tri(i, j)].x + KS[j][c].x * Sd[tri(i, j)].y);
       }
       const C2<T> lii = Sd[tri(i, i)];
-      const T help = lii.x * lii.x + lii.y * lii.y;
-      KS[i][c] = mk<T>((xr * lii.x + xi * lii.y) / help, (xi * lii.x - xr * lii.y) / help);
+      if constexpr (FAST) {
+        KS[i][c] = mk<T>((xr * lii.x + xi * lii.y) * rh[i], (xi * lii.x - xr * lii.y) * rh[i]);
+      } else {
+        const T help = lii.x * lii.x + lii.y * lii.y;
+        KS[i][c] = mk<T>((xr * lii.x + xi * lii.y) / help, (xi * lii.x - xr * lii.y) / help);
+      }
     }
 #pragma unroll
     for (int i = NT - 1; i >= 0; i--) {
@@ -115,8 +122,12 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
         xi = xi - (-KS[j][c].x * Sd[tri(j, i)].y + KS[j][c].y * Sd[tri(j, i)].x);
       }
       const C2<T> lii = Sd[tri(i, i)];
-      const T help = lii.x * lii.x + lii.y * lii.y;
-      KS[i][c] = mk<T>((xr * lii.x - xi * lii.y) / help, (xi * lii.x + xr * lii.y) / help);
+      if constexpr (FAST) {
+        KS[i][c] = mk<T>((xr * lii.x - xi * lii.y) * rh[i], (xi * lii.x + xr * lii.y) * rh[i]);
+      } else {
+        const T help = lii.x * lii.x + lii.y * lii.y;
+        KS[i][c] = mk<T>((xr * lii.x - xi * lii.y) / help, (xi * lii.x + xr * lii.y) / help);
+      }
     }
   }
   // S -= KScc KS
@@ -133,14 +144,20 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
       S[p][q].x -= xr;
       S[p][q].y -= xi;
     }
-  // d -= K mu; ans = KS^H d; mu += ans; res -= K mu
+  // d -= K mu; ans = KS^H d; mu += ans; res -= K mu (K read again from the table, an L1 hit, so that it need
+  // not stay in registers through the solve)
+  auto kat = [&](int l, int p) -> C2<T> {
+    const float2 v = __ldg(&Kk[l * 3 + p]);
+    return mk<T>((T)v.x, (T)v.y);
+  };
 #pragma unroll
   for (int l = 0; l < NT; l++) {
     T xr = 0, xi = 0;
 #pragma unroll
     for (int p = 0; p < 3; p++) {
-      xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
-      xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
+      const C2<T> k = kat(l, p);
+      xr += k.x * mu[p].x - k.y * mu[p].y;
+      xi += k.y * mu[p].x + k.x * mu[p].y;
     }
     d[l].x -= xr;
     d[l].y -= xi;
@@ -161,8 +178,9 @@ __device__ __forceinline__ bool plain_solve(const float2 *__restrict__ Kk, const
     T xr = 0, xi = 0;
 #pragma unroll
     for (int p = 0; p < 3; p++) {
-      xr += K[l][p].x * mu[p].x - K[l][p].y * mu[p].y;
-      xi += K[l][p].y * mu[p].x + K[l][p].x * mu[p].y;
+      const C2<T> k = kat(l, p);
+      xr += k.x * mu[p].x - k.y * mu[p].y;
+      xi += k.y * mu[p].x + k.x * mu[p].y;
     }
     res[l].x -= xr;
     res[l].y -= xi;

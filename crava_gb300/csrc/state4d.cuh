@@ -79,7 +79,7 @@ __device__ __forceinline__ C2<T> state_entry(float2 *const *ss, float2 *const *s
 // F + sand^H * helper), so it is never held in registers as a whole; every posterior entry is stored as
 // soon as it is formed.  Returns false when the Cholesky of the current prior fails: the grids then keep
 // the prior, as the reference keeps it.
-template <typename T>
+template <typename T, bool FAST = false>
 __device__ __forceinline__ bool split_bin(float2 *const *mu_s, float2 *const *mu_d, float2 *const *ss,
                                           float2 *const *sd, float2 *const *dd, long b, const C2<T> *muF,
                                           C2<T> *muCpost, C2<T> (*Cpost)[3])
@@ -110,36 +110,35 @@ __device__ __forceinline__ bool split_bin(float2 *const *mu_s, float2 *const *mu
   for (int i = 0; i < 6; i++)
 #pragma unroll
     for (int j = 0; j < 3; j++) sand[j][i] = mk<T>(FvC[i][j].x, -FvC[i][j].y);
-  if (!chol_ref<T, 3>(L)) return false;
-  axeqb_ref<T, 3, 6>(L, sand);
+  if (!chol_ref<T, 3, FAST>(L)) return false;
+  axeqb_ref<T, 3, 6, FAST>(L, sand);
 #pragma unroll
   for (int l = 0; l < 3; l++)
 #pragma unroll
     for (int m = 0; m < 3; m++) { Cpost[l][m].x -= Cp[l][m].x; Cpost[l][m].y -= Cp[l][m].y; }
-  C2<T> helper[3][6];
+  // F + adjoint(sand) * helper, helper = Cpost * sand, upper triangle; one column of helper at a time (the
+  // sums keep their order), each entry stored as it is formed
 #pragma unroll
-  for (int i = 0; i < 3; i++)
+  for (int j = 0; j < 6; j++) {
+    C2<T> hj[3];
 #pragma unroll
-    for (int j = 0; j < 6; j++) {
+    for (int i = 0; i < 3; i++) {
       T xr = 0, xi = 0;
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         xr += Cpost[i][k].x * sand[k][j].x - Cpost[i][k].y * sand[k][j].y;
         xi += Cpost[i][k].y * sand[k][j].x + Cpost[i][k].x * sand[k][j].y;
       }
-      helper[i][j] = mk<T>(xr, xi);
+      hj[i] = mk<T>(xr, xi);
     }
-  // F + adjoint(sand) * helper, upper triangle, each entry stored as it is formed
 #pragma unroll
-  for (int i = 0; i < 6; i++)
-#pragma unroll
-    for (int j = i; j < 6; j++) {
+    for (int i = 0; i <= j; i++) {
       T xr = 0, xi = 0;
 #pragma unroll
       for (int k = 0; k < 3; k++) {
         const C2<T> ad = mk<T>(sand[k][i].x, -sand[k][i].y);
-        xr += ad.x * helper[k][j].x - ad.y * helper[k][j].y;
-        xi += ad.y * helper[k][j].x + ad.x * helper[k][j].y;
+        xr += ad.x * hj[k].x - ad.y * hj[k].y;
+        xi += ad.y * hj[k].x + ad.x * hj[k].y;
       }
       const C2<T> f = state_entry<T>(ss, sd, dd, b, i, j);
       const float2 o = make_float2((float)(xr + f.x), (float)(xi + f.y));
@@ -147,6 +146,7 @@ __device__ __forceinline__ bool split_bin(float2 *const *mu_s, float2 *const *mu
       else if (i < 3) sd[i * 3 + j - 3][b] = o;
       else dd[tri_t(i - 3, j - 3)][b] = o;
     }
+  }
 #pragma unroll
   for (int l = 0; l < 3; l++) { muCpost[l].x -= muC[l].x; muCpost[l].y -= muC[l].y; }
 #pragma unroll

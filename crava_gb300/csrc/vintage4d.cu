@@ -17,7 +17,11 @@
 // CG_PREC_MIXED flags a bin whose data-covariance Cholesky fails or whose
 // pivot-ratio condition estimate exceeds the workspace threshold: the FP32
 // pass leaves it untouched and queues it, and k_vintage4d_fix64 redoes its
-// merge, solve and split in FP64 from the untouched inputs.
+// merge, solve and split in FP64 from the untouched inputs.  The MIXED FP32
+// pass divides by reciprocal multiplication (one division per pivot instead
+// of one per element: the reference-order IEEE divisions were about a third
+// of the kernel's instructions), so unlike the FP32 form it is not bit for bit
+// the three passes; the FP64 redo keeps the reference's operations.
 #include <cstring>
 
 #include "common.cuh"
@@ -94,7 +98,7 @@ __device__ __forceinline__ bool vintage_bin(const V4Args &a, long b)
     if constexpr (sizeof(T) == 4) lam = sqrtf(ec.x * ec.x);
     else lam = sqrt((T)ec.x * (T)ec.x);
     T cond = (T)0;
-    const bool ok = plain_solve<T, NT>(a.K + (long)k * NT * 3, a.em1 + (long)k * NT, a.em2 + (long)k * NT,
+    const bool ok = plain_solve<T, NT, MODE == 1>(a.K + (long)k * NT * 3, a.em1 + (long)k * NT, a.em2 + (long)k * NT,
                                        a.em3 + (long)k * NT, a.c0, a.cw, lam, S, mu, res, &cond);
     if (MODE == 1 && (!ok || cond > (T)a.cond_thr)) {
       const int pos = atomicAdd(&a.counters[0], 1);
@@ -124,7 +128,7 @@ __device__ __forceinline__ bool vintage_bin(const V4Args &a, long b)
     muF[l] = mk<T>((T)s.x, (T)s.y);
     muF[l + 3] = mk<T>((T)d.x, (T)d.y);
   }
-  if (!split_bin<T>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, muF, mu, Cpost) && a.nsplit) atomicAdd(a.nsplit, 1);
+  if (!split_bin<T, MODE == 1>(a.mu_s, a.mu_d, a.ss, a.sd, a.dd, b, muF, mu, Cpost) && a.nsplit) atomicAdd(a.nsplit, 1);
   return true;
 }
 
