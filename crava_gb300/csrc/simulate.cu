@@ -54,16 +54,22 @@ __device__ __forceinline__ U4 philox4x32_10(U4 c, uint32_t k0, uint32_t k1)
   return c;
 }
 
-// four standard normals from one Philox block (Box-Muller on (0,1] uniforms)
+// four standard normals from one Philox block (Box-Muller on (0,1) uniforms).  The
+// radius and angle use the hardware approximations (__logf, rsqrtf, __sincosf:
+// errors near 1e-6, immaterial to the distribution); the accurate library
+// functions made this kernel issue-bound on their range reductions.
 __device__ __forceinline__ void normals4(U4 r, float *g)
 {
   const float s = 2.3283064365386963e-10f;  // 2^-32
   const float u0 = ((float)r.x + 0.5f) * s, u1 = ((float)r.y + 0.5f) * s;
   const float u2 = ((float)r.z + 0.5f) * s, u3 = ((float)r.w + 0.5f) * s;
-  const float r0 = sqrtf(-2.0f * logf(u0)), r1 = sqrtf(-2.0f * logf(u2));
+  // u rounds to 1.0f for draws within 128 of 2^32 (t = -0): radius 0 there, as sqrt would give
+  const float t0 = -2.0f * __logf(u0), t1 = -2.0f * __logf(u2);
+  const float r0 = t0 > 0.0f ? t0 * rsqrtf(t0) : 0.0f, r1 = t1 > 0.0f ? t1 * rsqrtf(t1) : 0.0f;
+  const float two_pi = 6.283185307179586f;
   float s0, c0, s1, c1;
-  sincospif(2.0f * u1, &s0, &c0);
-  sincospif(2.0f * u3, &s1, &c1);
+  __sincosf(two_pi * u1, &s0, &c0);
+  __sincosf(two_pi * u3, &s1, &c1);
   g[0] = r0 * c0;
   g[1] = r0 * s0;
   g[2] = r1 * c1;
