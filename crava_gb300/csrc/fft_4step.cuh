@@ -306,7 +306,10 @@ __global__ void __launch_bounds__(kFFTThreads) k_r2c_rows_4s(const __grid_consta
 // global memory (the second read of a row hits L1), so no shared memory is
 // used before the exchange; pass 2 stores z[n] = (x[2n], x[2n+1]).
 // ---------------------------------------------------------------------------
-template <int M>
+// ADD: the launch has addends (the posterior-mean add of simulation); they are
+// loaded before pass 2's DFT so their latency overlaps it (a load after each
+// store could not be hoisted over the stores, which may alias)
+template <int M, bool ADD>
 __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_constant__ CubeSet cs, const __grid_constant__ CubeSet addend,
                                                              const float2 *__restrict__ twg, int nrows,
                                                              float postscale, int epi)
@@ -382,7 +385,7 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
     }
   }
   __syncthreads();
-  const float2 *add = addend.ptr[blockIdx.z] ? (const float2 *)addend.ptr[blockIdx.z] + (long)r0 * CN : nullptr;
+  const float2 *add = ADD && addend.ptr[blockIdx.z] ? (const float2 *)addend.ptr[blockIdx.z] + (long)r0 * CN : nullptr;
 #pragma unroll
   for (int q = 0; q < B2; q++) {
     const int t = q * kFFTThreads + threadIdx.x;
@@ -391,28 +394,38 @@ __global__ void __launch_bounds__(kFFTThreads) k_c2r_rows_4s(const __grid_consta
       float2 u[N2];
 #pragma unroll
       for (int n2 = 0; n2 < N2; n2++) u[n2] = buf[row * P + n2 * Q + k1];
+      const float2 *ap = (ADD && add && row < nr) ? add + (long)row * CN : nullptr;
+      float2 av[ADD ? N2 + 1 : 1];
+      if constexpr (ADD) {
+        if (ap) {
+#pragma unroll
+          for (int k2 = 0; k2 < N2; k2++) av[k2] = __ldg(ap + k1 + N1 * k2);
+          av[N2] = k1 == 0 ? __ldg(ap + M) : make_float2(0.f, 0.f);
+        }
+      }
       reg_fft<float, N2, 2 * N1>(u, +1, tw);
       if (row < nr) {
         float2 *op = base + (long)row * CN;
-        const float2 *ap = add ? add + (long)row * CN : nullptr;
 #pragma unroll
         for (int k2 = 0; k2 < N2; k2++) {
           const int e = k1 + N1 * k2;
           float2 z = make_float2(u[k2].x * postscale, u[k2].y * postscale);
-          if (ap) {
-            const float2 s = ap[e];
-            z.x += s.x;
-            z.y += s.y;
+          if constexpr (ADD) {
+            if (ap) {
+              z.x += av[k2].x;
+              z.y += av[k2].y;
+            }
           }
           op[e] = make_float2(epilogue<float>(z.x, epi), epilogue<float>(z.y, epi));
         }
         if (k1 == 0) {
           // the row's padding pair: zero, plus the addend's padding
           float2 z = make_float2(0.f, 0.f);
-          if (ap) {
-            const float2 s = ap[M];
-            z.x += s.x;
-            z.y += s.y;
+          if constexpr (ADD) {
+            if (ap) {
+              z.x += av[N2].x;
+              z.y += av[N2].y;
+            }
           }
           op[M] = make_float2(epilogue<float>(z.x, epi), epilogue<float>(z.y, epi));
         }

@@ -64,10 +64,21 @@ int launch_rows_4s(bool forward, const CubeSet &cs, const CubeSet &addend, int n
     TraceScope ts("k_r2c_rows_4s", st, bytes);
     k_r2c_rows_4s<M><<<grid, kFFTThreads, smem, st>>>(cs, tw, nrows, scale);
   } else {
-    e = smem_limit_once(k_c2r_rows_4s<M>, smem, attr_inv);
-    if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_4s attribute");
-    TraceScope ts("k_c2r_rows_4s", st, bytes);
-    k_c2r_rows_4s<M><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale, epi);
+    bool any_add = false;
+    for (int i = 0; i < ncubes; i++) any_add = any_add || addend.ptr[i] != nullptr;
+    if (any_add) {
+      static bool attr_add[64] = {};
+      e = smem_limit_once(k_c2r_rows_4s<M, true>, smem, attr_add);
+      if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_4s attribute");
+      // the addend is one more read of a row's 2(M+1) floats
+      TraceScope ts("k_c2r_rows_4s", st, bytes + (double)ncubes * nrows * (M + 1.0) * sizeof(float2));
+      k_c2r_rows_4s<M, true><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale, epi);
+    } else {
+      e = smem_limit_once(k_c2r_rows_4s<M, false>, smem, attr_inv);
+      if (e != cudaSuccess) return cuda_status(e, "k_c2r_rows_4s attribute");
+      TraceScope ts("k_c2r_rows_4s", st, bytes);
+      k_c2r_rows_4s<M, false><<<grid, kFFTThreads, smem, st>>>(cs, addend, tw, nrows, scale, epi);
+    }
   }
   CG_CHECK_LAUNCH(forward ? "k_r2c_rows_4s" : "k_c2r_rows_4s");
   return 1;
