@@ -397,7 +397,7 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok):
     sc0 = S.config0(seed=20261203 + rank)
     inv0 = Inversion(sc0, forms=("plain", "mixed"))
     small = {"workload": "80x80x160 padded (64x64x128 cells), 3 stacks 10-30 deg, 30 Hz Ricker, S/N 4",
-             "bins": sc0.nbins, "ms": {}}
+             "bins": sc0.nbins, "ms": {}, "ms_stat": "median"}
     for form in ("plain", "mixed"):
         for _ in range(max(args.warmup, 1)):
             inv0.restore(form)
@@ -406,7 +406,7 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok):
         def before(form=form):
             inv0.restore(form)
             flush.fill_(1.0)
-        small["ms"][form] = round(statistics.mean(MB._events_ms(lambda: inv0.run(form), steps, before)), 4)
+        small["ms"][form] = round(statistics.median(MB._events_ms(lambda: inv0.run(form), steps, before)), 4)
     small["Mbins_per_s_mixed"] = round(sc0.nbins / (small["ms"]["mixed"] * 1e-3) / 1e6, 1)
     inv0.restore("mixed")
     tr = MB._traced(lambda: inv0.run("mixed"))

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import statistics
 
 import numpy as np
 import torch
@@ -167,7 +168,7 @@ def _traced(fn):
 def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=8, peak=None, flush=None):
     """The uneven-cube batch (cg_batch_run, graph replay) timed with CUDA events; the batch's own inputs
     are restored (cg_batch_reset) before each repetition, outside the timed region.  Per-kernel shares
-    from one eager (not graph-replayed) run under the launch tracer."""
+    from one eager (not graph-replayed) single-stream run under the launch tracer."""
     b = api.Batch(scs, nstreams=streams)
     bins = b.bins
 
@@ -179,11 +180,17 @@ def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=8, peak=None, flu
         before()
         b.run(form, use_graph=True)
     ms = _events_ms(lambda: b.run(form, use_graph=True), reps, before)
+    b.close()
+    # per-kernel shares from one eager run on a single stream (kernels of concurrent streams would overlap
+    # inside each other's event pairs)
+    b = api.Batch(scs, nstreams=1)
+    b.reset()
+    b.run(form, use_graph=False)
     b.reset()
     tr = _traced(lambda: b.run(form, use_graph=False))
     b.close()
-    mean = sum(ms) / len(ms)
-    out = {"form": form, "cubes": len(scs), "bins": int(bins), "ms": round(mean, 4),
+    mean = statistics.median(ms)
+    out = {"form": form, "cubes": len(scs), "bins": int(bins), "ms": round(mean, 4), "ms_stat": "median",
            "Mbins_per_s": round(bins / (mean * 1e-3) / 1e6, 1), "ms_per_rep": [round(x, 4) for x in ms],
            "eager_kernels": kernel_table(tr), "launches": int(sum(v[0] for v in tr.values()))}
     if peak:
@@ -219,14 +226,14 @@ def measure_simulate(sc=None, nreal=128, reps=3, warmup=1, peak=None):
     ms = _events_ms(step, reps)
     tr = _traced(step)
     _, nfail = api.posterior_cholesky(inv.cov, sc.nxp)
-    best = sum(ms) / len(ms)
+    best = statistics.median(ms)
     bins = sc.nbins
     # algorithmic bytes per realisation: 3 C2R (8 B/bin + 4 B/cell each) + mean read and field write
     # (2 x 3 x 4 B/cell); the factor (36 B/bin) is read once per call
     cells = sc.nxp * sc.nyp * sc.nzp
     alg = nreal * (3 * (8 * bins + 4 * cells) + 24 * cells) + 36 * bins
     out = {"workload": "200^3 padded cube, 3 stacks 10-30 deg, config-0 prior, 30 Hz Ricker, S/N 4",
-           "nreal": nreal, "bins": bins, "chol_fail": int(nfail.item()), "ms": round(best, 4),
+           "nreal": nreal, "bins": bins, "chol_fail": int(nfail.item()), "ms": round(best, 4), "ms_stat": "median",
            "ms_per_call": [round(x, 4) for x in ms], "realisations_per_s": round(nreal / (best * 1e-3), 1),
            "Mbins_per_s": round(nreal * bins / (best * 1e-3) / 1e6, 1),
            "algorithmic_GBps": round(alg / (best * 1e-3) / 1e9, 1), "kernels": kernel_table(tr),
@@ -258,9 +265,9 @@ def measure_timelapse(tl=None, form="mixed", reps=3, warmup=1, peak=None, run=No
     tr = _traced(lambda: run.run(form=form))
     fails = [int(x.item()) for x in run.nfail_split]
     st = [w.stats() for w in run.ws]
-    best = sum(ms) / len(ms)
+    best = statistics.median(ms)
     bins = tl.nbins
-    out = {"form": form, "bins": bins, "ms": round(best, 4), "ms_per_run": [round(x, 4) for x in ms],
+    out = {"form": form, "bins": bins, "ms": round(best, 4), "ms_stat": "median", "ms_per_run": [round(x, 4) for x in ms],
            "Mbins_per_s": round(bins / (best * 1e-3) / 1e6, 1),
            "joint_algorithmic_GBps": round(run.algorithmic_bytes() / (best * 1e-3) / 1e9, 1),
            "split_fails": fails, "chol_fail": [x["failed"] for x in st], "fp64_bins": [x["flagged"] for x in st],
