@@ -135,6 +135,25 @@ def adjustment(sc, l, corr_t, min_int_fq, f_peak, cases, error_var):
     return wav, ct_f, adj
 
 
+def local_noise(post, mean, nx, ny, nz, nxp, err_theta_cov, prior_var0, post_var0, scale):
+    """Crava::computeG and Crava::correctAlphaBetaRho: post, mean 3 real padded cubes (nzp, nyp, rnxp) each,
+    scale (ntheta, ny, nx) local noise scales.  Returns (G (ntheta, 3), the 3 corrected posterior cubes)."""
+    n = len(err_theta_cov)
+    nzp, nyp, rnxp = post[0].shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, ntheta=n)
+        _w(d, "etc.f64", err_theta_cov, np.float64)
+        _w(d, "priorvar0.f64", prior_var0, np.float64)
+        _w(d, "postvar0.f64", post_var0, np.float64)
+        _w(d, "scale.f64", scale, np.float64)
+        _w(d, "post.f32", np.stack(post), np.float32)
+        _w(d, "mean.f32", np.stack(mean), np.float32)
+        _run("localnoise", d)
+        G = _r(d, "G.f64", np.float64, (n, 3))
+        out = [_r(d, f"post_{q}.f32", np.float32, (nzp, nyp, rnxp)) for q in ("alpha", "beta", "rho")]
+    return G, out
+
+
 CRAVA_GEOM = ("x0", "y0", "dx", "dy", "il0", "xl0", "ilstepx", "ilstepy", "xlstepx", "xlstepy", "angle")
 
 

@@ -17,6 +17,8 @@
 //                               (src/state4d.cpp:140-580) on given spectra.
 //   crava_o2 adjust     <dir>   Crava::computeAdjustmentFactor (src/crava.cpp:807-903)
 //                               for given local shifts, gains and stretches.
+//   crava_o2 localnoise <dir>   Crava::computeG and Crava::correctAlphaBetaRho
+//                               (src/crava.cpp:2261-2569) on given cubes and scales.
 //   crava_o2 crava_write / crava_read <dir>
 //                               FFTGrid::writeCravaFile / readCravaFile.
 //   crava_o2 storm_write / storm_read <dir>
@@ -55,6 +57,7 @@
 #include "src/crava.h"
 #include "src/definitions.h"
 #include "src/fftgrid.h"
+#include "src/modelavodynamic.h"
 #include "src/modelgeneral.h"
 #include "src/modelsettings.h"
 #include "src/seismicparametersholder.h"
@@ -407,6 +410,76 @@ int cmd_adjust()
   return 0;
 }
 
+// Crava::computeG and Crava::correctAlphaBetaRho (src/crava.cpp:2261-2343, :2471-2569) on the posterior and
+// prior-mean cubes post.f32 / mean.f32 (real domain, 3 cubes each), the local noise scales scale.f64 (ntheta x
+// ny x nx, the ModelAVODynamic grids), errThetaCov and the prior / posterior variances at the origin.  Writes G
+// (ntheta x 3) and the corrected posterior cubes.
+int cmd_localnoise()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"], n = (int)p["ntheta"];
+  const size_t rsize = (size_t)2 * (nxp / 2 + 1) * nyp * nzp;
+  std::vector<double> etc = read_arr<double>("etc.f64", (size_t)n * n);
+  std::vector<double> pv0 = read_arr<double>("priorvar0.f64", 9);
+  std::vector<double> qv0 = read_arr<double>("postvar0.f64", 9);
+  std::vector<double> scale = read_arr<double>("scale.f64", (size_t)n * nx * ny);
+  std::vector<float> post = read_arr<float>("post.f32", rsize * 3);
+  std::vector<float> mean = read_arr<float>("mean.f32", rsize * 3);
+
+  Crava *crava = static_cast<Crava *>(operator new(sizeof(Crava)));
+  memset((void *)crava, 0, sizeof(Crava));
+  crava->nx_ = nx;
+  crava->ny_ = ny;
+  crava->nz_ = nz;
+  crava->ntheta_ = n;
+  crava->errThetaCov_ = new double *[n];
+  for (int l = 0; l < n; l++) {
+    crava->errThetaCov_[l] = new double[n];
+    for (int m = 0; m < n; m++) crava->errThetaCov_[l][m] = etc[(size_t)l * n + m];
+  }
+  new (&crava->priorVar0_) NRLib::Matrix(3, 3);
+  new (&crava->postVar0_) NRLib::Matrix(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      crava->priorVar0_(a, b) = pv0[3 * a + b];
+      crava->postVar0_(a, b) = qv0[3 * a + b];
+    }
+  FFTGrid **pg[3] = {&crava->postAlpha_, &crava->postBeta_, &crava->postRho_};
+  FFTGrid **mg[3] = {&crava->meanAlpha_, &crava->meanBeta_, &crava->meanRho_};
+  for (int q = 0; q < 3; q++) {
+    *pg[q] = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::PARAMETER, &post[rsize * q], false);
+    *mg[q] = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::PARAMETER, &mean[rsize * q], false);
+  }
+  // the ModelAVODynamic members correctAlphaBetaRho reads: the angles (their count) and the noise-scale grids
+  ModelAVODynamic *mad = static_cast<ModelAVODynamic *>(operator new(sizeof(ModelAVODynamic)));
+  memset((void *)mad, 0, sizeof(ModelAVODynamic));
+  new (&mad->angle_) std::vector<float>(n, 0.0f);
+  new (&mad->localNoiseScale_) std::vector<Grid2D *>(n, (Grid2D *)NULL);
+  for (int l = 0; l < n; l++) {
+    Grid2D *g = new Grid2D(nx, ny, 0.0);
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) (*g)(i, j) = scale[((size_t)l * ny + j) * nx + i];
+    mad->localNoiseScale_[l] = g;
+  }
+  crava->modelAVOdynamic_ = mad;
+
+  NRLib::Matrix G(n, 3);
+  crava->computeG(G);
+  std::vector<double> gout((size_t)n * 3);
+  for (int l = 0; l < n; l++)
+    for (int q = 0; q < 3; q++) gout[(size_t)l * 3 + q] = G(l, q);
+  write_raw("G.f64", &gout[0], sizeof(double) * gout.size());
+
+  ModelSettings ms;
+  ms.nSimulations_ = 0;
+  crava->correctAlphaBetaRho(&ms);
+  dump_grid("post_alpha.f32", crava->postAlpha_);
+  dump_grid("post_beta.f32", crava->postBeta_);
+  dump_grid("post_rho.f32", crava->postRho_);
+  return 0;
+}
+
 // FFTGrid::writeCravaFile (src/fftgrid.cpp:2410-2441) of the cube cube.f32 with the geometry of params.txt
 int cmd_crava_write()
 {
@@ -513,7 +586,7 @@ int main(int argc, char **argv)
   signal(SIGSEGV, on_fault);
   signal(SIGABRT, on_fault);
   if (argc != 3) {
-    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|crava_write|crava_read|storm_write|storm_read|"
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|crava_write|crava_read|storm_write|storm_read|"
                     "factorable} <dir>\n");
     return 1;
   }
@@ -523,6 +596,7 @@ int main(int argc, char **argv)
   if (c == "state4d") return cmd_state4d();
   if (c == "factorable") return cmd_factorable();
   if (c == "adjust") return cmd_adjust();
+  if (c == "localnoise") return cmd_localnoise();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();
   if (c == "storm_write") return cmd_storm_write();

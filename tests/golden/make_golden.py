@@ -212,6 +212,29 @@ def inversion_4d_case(name, tl, vintage=0):
                         merged=merged, split=split)
 
 
+def local_noise_case(name, n, dims, seed):
+    """Crava::computeG + Crava::correctAlphaBetaRho by the reference's own code (crava_o2) on a posterior that
+    differs from the prior mean by noise, local noise scales that vary over the traces (one RMISSING cell),
+    and posterior variances at the origin between 30 and 70 % of the prior."""
+    nx, ny, nz, nxp, nyp, nzp = dims
+    sc = S.make_scenario(nx, ny, nz, list(np.linspace(5, 40, n)), 28.0, nxp=nxp, nyp=nyp, nzp=nzp, seed=seed)
+    Sm = sc.sigma0.astype(np.float64)
+    rng = np.random.default_rng(seed)
+    Q = np.linalg.cholesky(Sm)
+    B = rng.standard_normal((3, 3)) * 0.1
+    F = np.eye(3) * 0.55 + (B + B.T) * 0.1
+    Smd = Q @ F @ F.T @ Q.T
+    Smd = 0.5 * (Smd + Smd.T)
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    scale = np.stack([1.0 + 0.8 * (0.5 + 0.5 * np.sin(xx / 3.0 + l) * np.cos(yy / 4.0)) for l in range(n)])
+    scale[0, 1, 1] = -99999.0
+    post = [m + 0.02 * rng.standard_normal(m.shape).astype(np.float32) for m in sc.mean]
+    G, out = o2.local_noise(post, sc.mean, nx, ny, nz, nxp, sc.err_theta_cov, Sm, Smd, scale)
+    np.savez_compressed(os.path.join(HERE, name), nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp,
+                        err_theta_cov=sc.err_theta_cov, prior_var0=Sm, post_var0=Smd, scale=scale,
+                        post=np.stack(post), mean=np.stack(sc.mean), G=G, out=np.stack(out))
+
+
 def simulation_case(name, inv, seed):
     nxp, nyp, nzp = int(inv["nxp"]), int(inv["nyp"]), int(inv["nzp"])
     noise = O.ref_fill_complex_noise(nxp, nyp, nzp, seed, 3)
@@ -227,6 +250,12 @@ def main():
         raise SystemExit("set CRAVA_REFERENCE_SRC to the reference checkout")
     O.build_ref()
     o2.build(src)
+    only = set(sys.argv[1:])  # fixture names to (re)write; all when none are given
+    if only:
+        if "reference_localnoise.npz" in only:
+            local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
+        print("fixtures written to", HERE)
+        return
     fft_case("fft_even.npz", 16, 12, 20, 11)
     fft_case("fft_odd.npz", 15, 9, 7, 12)
     fft_case("fft_mixed.npz", 40, 21, 25, 13)
@@ -244,6 +273,7 @@ def main():
     simulation_case("simulation_c0small.npz", inv, 231171)
     tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=8)
     inversion_4d_case("inversion_4d_n4.npz", tl)
+    local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

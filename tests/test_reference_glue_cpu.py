@@ -227,3 +227,24 @@ def test_storm_file_bytes_and_reader_match_reference(native, tmp_path):
     assert (rh["ni"], rh["nj"], rh["nk"]) == (5, 4, 3)
     assert rh["x_min"] == hv["x_min"] and rh["lx"] == hv["lx"] and rh["z_top"] == hv["z_top"]
     assert abs(rh["angle"] - np.pi * hv["angle_deg"] / 180.0) < 1e-15 and rh["lz"] == hv["z_bot"] - hv["z_top"]
+
+
+def test_local_noise_correction_matches_reference(oracle):
+    """Crava::computeG and Crava::correctAlphaBetaRho run by the reference's own code (crava_o2): computeG
+    restated with LAPACK's geev reproduces the reference's G, and the oracle's correction with that G is bit for
+    bit the reference's on every trace but the one whose scale is RMISSING, where the reference takes the square
+    root of a negative ratio and writes NaN (here that trace counts at the minimum scale)."""
+    from crava_gb300 import api
+    g = golden("reference_localnoise.npz")
+    nx, ny, nz, nxp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp"))
+    G = api.local_noise_g(g["err_theta_cov"], g["prior_var0"], g["post_var0"])
+    assert np.abs(G - g["G"]).max() <= 1e-12 * np.abs(g["G"]).max()
+    out, _ = oracle.correct_alpha_beta_rho(list(g["post"]), list(g["mean"]), nx, ny, nz, nxp, g["G"],
+                                           g["err_theta_cov"], g["prior_var0"], g["post_var0"], g["scale"])
+    miss = np.zeros(g["out"][0].shape, bool)
+    jj, ii = np.nonzero((g["scale"] == -99999.0).any(axis=0))
+    miss[:nz, jj, ii] = True
+    for p in range(3):
+        ref = g["out"][p]
+        np.testing.assert_array_equal(out[p][~miss], ref[~miss])
+        assert np.isnan(ref[miss]).all() and np.isfinite(out[p][miss]).all()

@@ -78,3 +78,26 @@ def test_gpu_state4d_merge_and_split_match_reference(cuda):
     print("GPU State4D vs reference: merge", e_merge, "split", e_split, "kept prior", int(nfail.item()))
     assert e_merge < 1e-7
     assert e_split < 2e-5
+
+
+def test_gpu_local_noise_correction_matches_reference(cuda):
+    """cg_correct_alpha_beta_rho with the reference's G against Crava::correctAlphaBetaRho run by the reference's
+    own code: every trace but the RMISSING one (NaN in the reference, the minimum scale here)."""
+    from crava_gb300 import api
+    g = golden("reference_localnoise.npz")
+    nx, ny, nz, nxp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp"))
+    P = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in g["post"]]
+    M = [torch.from_numpy(np.ascontiguousarray(m)).cuda() for m in g["mean"]]
+    ns = torch.from_numpy(np.ascontiguousarray(g["scale"])).cuda()
+    api.correct_alpha_beta_rho(P, M, nx, ny, nz, nxp, g["G"], g["err_theta_cov"], g["prior_var0"], g["post_var0"], ns)
+    torch.cuda.synchronize()
+    miss = np.zeros(g["out"][0].shape, bool)
+    jj, ii = np.nonzero((g["scale"] == -99999.0).any(axis=0))
+    miss[:nz, jj, ii] = True
+    for p in range(3):
+        got, ref, mean = P[p].cpu().numpy(), g["out"][p], g["mean"][p]
+        e = rel(got[~miss] - mean[~miss], ref[~miss] - mean[~miss])
+        print("local-noise correction vs reference, parameter", p, ": update rel", e,
+              "max abs", np.abs(got[~miss] - ref[~miss]).max())
+        assert e < 1e-6
+        assert np.isfinite(got[miss]).all()
