@@ -154,6 +154,31 @@ def local_noise(post, mean, nx, ny, nz, nxp, err_theta_cov, prior_var0, post_var
     return G, out
 
 
+def fill_in_data(values, gbox, nx, ny, nz, nxp, nyp, nzp, sbox, cubetype, smooth_length):
+    """FFTGrid::fillInData from a STORM grid: values (gnk, gny, gnx) on the box gbox = (gx0, gy0, gz0, glx, gly,
+    glz), a constant-thickness simbox sbox = (x0, y0, z0, lx, ly, lz, rot, dx, dy, dz).  Returns (the filled cube
+    (nzp, nyp, rnxp), per-column traces (ncol, gnk), state (ncol,), z0_data, dz_data, z0_grid, dz_grid (ncol,),
+    the three missing/dead counts)."""
+    gnk, gny, gnx = values.shape
+    rnxp = 2 * (nxp // 2 + 1)
+    ncol = rnxp * nyp
+    gx0, gy0, gz0, glx, gly, glz = gbox
+    x0, y0, z0, lx, ly, lz, rot, dx, dy, dz = sbox
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, gnx=gnx, gny=gny, gnk=gnk, cubetype=int(cubetype),
+                smooth_length=float(smooth_length), gx0=float(gx0), gy0=float(gy0), gz0=float(gz0), glx=float(glx),
+                gly=float(gly), glz=float(glz), x0=float(x0), y0=float(y0), z0=float(z0), lx=float(lx),
+                ly=float(ly), lz=float(lz), rot=float(rot), dx=float(dx), dy=float(dy), dz=float(dz))
+        _w(d, "grid.f32", values, np.float32)
+        _run("fillindata", d)
+        cube = _r(d, "cube.f32", np.float32, (nzp, nyp, rnxp))
+        traces = _r(d, "traces.f32", np.float32, (ncol, gnk))
+        state = _r(d, "state.i32", np.int32)
+        cols = [_r(d, f, np.float32) for f in ("z0_data.f32", "dz_data.f32", "z0_grid.f32", "dz_grid.f32")]
+        counts = _r(d, "counts.i32", np.int32)
+    return (cube, traces, state, *cols, counts)
+
+
 CRAVA_GEOM = ("x0", "y0", "dx", "dy", "il0", "xl0", "ilstepx", "ilstepy", "xlstepx", "xlstepy", "angle")
 
 

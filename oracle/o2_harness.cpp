@@ -19,6 +19,7 @@
 //                               for given local shifts, gains and stretches.
 //   crava_o2 localnoise <dir>   Crava::computeG and Crava::correctAlphaBetaRho
 //                               (src/crava.cpp:2261-2569) on given cubes and scales.
+//   crava_o2 fillindata <dir>   FFTGrid::fillInData from a STORM grid onto a simbox.
 //   crava_o2 crava_write / crava_read <dir>
 //                               FFTGrid::writeCravaFile / readCravaFile.
 //   crava_o2 storm_write / storm_read <dir>
@@ -480,6 +481,68 @@ int cmd_localnoise()
   return 0;
 }
 
+// FFTGrid::fillInData (src/fftgrid.cpp:138-370) from a STORM grid (grid.f32, gnk x gny x gnx, a box from
+// (gx0, gy0, gz0) of size glx x gly x glz) into a cube on a constant-thickness simbox (x0, y0, top z0, lx x ly x lz,
+// rotation rot, cells dx x dy x dz).  Writes the filled cube and, per column c = i + rnxp*j, what the reference's
+// own geometry code hands the per-trace core: the trace (makeTraceFromStormGrid), its first-sample time and
+// interval, the column's simbox top and cell thickness (getFillNumber, Simbox::getCoord, getdz) and whether the
+// column is outside the grid or its trace missing.
+int cmd_fillindata()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"];
+  const int gnx = (int)p["gnx"], gny = (int)p["gny"], gnk = (int)p["gnk"], cubetype = (int)p["cubetype"];
+  const float smooth = (float)p["smooth_length"];
+  std::vector<float> vals = read_arr<float>("grid.f32", (size_t)gnx * gny * gnk);
+  Surface top(p["x0"], p["y0"], p["lx"], p["ly"], 2, 2, p["z0"]);
+  Simbox sb(p["x0"], p["y0"], top, p["lx"], p["ly"], p["lz"], p["rot"], p["dx"], p["dy"], p["dz"]);
+  NRLib::Volume vol(p["gx0"], p["gy0"], p["gz0"], p["glx"], p["gly"], p["glz"], p["rot"]);
+  StormContGrid grid(vol, gnx, gny, gnk);
+  for (int k = 0; k < gnk; k++)
+    for (int j = 0; j < gny; j++)
+      for (int i = 0; i < gnx; i++) grid(i, j, k) = vals[((size_t)k * gny + j) * gnx + i];
+
+  FFTGrid *fg = new FFTGrid(nx, ny, nz, nxp, nyp, nzp);
+  fg->setType(cubetype);
+  const int rnxp = 2 * (nxp / 2 + 1), ncol = rnxp * nyp;
+  std::vector<float> traces((size_t)ncol * gnk, 0.0f), z0d(ncol, 0.0f), dzd(ncol, 0.0f), z0g(ncol), dzg(ncol);
+  std::vector<int> state(ncol, 1);
+  for (int j = 0; j < nyp; j++)
+    for (int i = 0; i < rnxp; i++) {
+      const int c = i + rnxp * j;
+      const int refi = fg->getFillNumber(i, nx, nxp), refj = fg->getFillNumber(j, ny, nyp);
+      double x, y, z0;
+      sb.getCoord(refi, refj, 0, x, y, z0);
+      z0g[c] = static_cast<float>(z0);
+      dzg[c] = static_cast<float>(sb.getdz(refi, refj));
+      const float xf = static_cast<float>(x), yf = static_cast<float>(y);
+      if (!grid.IsInside(xf, yf)) continue;
+      std::vector<float> tr;
+      bool missing = true;
+      float z0_data = RMISSING, dz_data = RMISSING, dz_min = RMISSING;
+      fg->makeTraceFromStormGrid(&grid, tr, missing, z0_data, dz_data, dz_min, xf, yf);
+      if (missing) continue;
+      state[c] = 0;
+      z0d[c] = z0_data;
+      dzd[c] = dz_data;
+      for (int k = 0; k < gnk && k < (int)tr.size(); k++) traces[(size_t)c * gnk + k] = tr[k];
+    }
+  int m1 = 0, m2 = 0, m3 = 0;
+  std::string err;
+  fg->fillInData(&sb, &grid, NULL, smooth, 1, m1, m2, m3, std::string("data"), err, false, false);
+  dump_grid("cube.f32", fg);
+  write_raw("traces.f32", &traces[0], sizeof(float) * traces.size());
+  write_raw("state.i32", &state[0], sizeof(int) * state.size());
+  write_raw("z0_data.f32", &z0d[0], sizeof(float) * ncol);
+  write_raw("dz_data.f32", &dzd[0], sizeof(float) * ncol);
+  write_raw("z0_grid.f32", &z0g[0], sizeof(float) * ncol);
+  write_raw("dz_grid.f32", &dzg[0], sizeof(float) * ncol);
+  const int counts[3] = {m1, m2, m3};
+  write_raw("counts.i32", counts, sizeof(counts));
+  return 0;
+}
+
 // FFTGrid::writeCravaFile (src/fftgrid.cpp:2410-2441) of the cube cube.f32 with the geometry of params.txt
 int cmd_crava_write()
 {
@@ -586,7 +649,7 @@ int main(int argc, char **argv)
   signal(SIGSEGV, on_fault);
   signal(SIGABRT, on_fault);
   if (argc != 3) {
-    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|crava_write|crava_read|storm_write|storm_read|"
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|fillindata|crava_write|crava_read|storm_write|storm_read|"
                     "factorable} <dir>\n");
     return 1;
   }
@@ -597,6 +660,7 @@ int main(int argc, char **argv)
   if (c == "factorable") return cmd_factorable();
   if (c == "adjust") return cmd_adjust();
   if (c == "localnoise") return cmd_localnoise();
+  if (c == "fillindata") return cmd_fillindata();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();
   if (c == "storm_write") return cmd_storm_write();

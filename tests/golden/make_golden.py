@@ -235,6 +235,41 @@ def local_noise_case(name, n, dims, seed):
                         post=np.stack(post), mean=np.stack(sc.mean), G=G, out=np.stack(out))
 
 
+def fill_in_data_case(name, seed):
+    """FFTGrid::fillInData by the reference's own code (crava_o2) from a STORM grid onto a constant-thickness
+    simbox, for a DATA cube (guard-zone taper) and a PARAMETER cube (end extrapolation and trend): the grid starts
+    80 ms above the simbox and ends 48 ms below it, and covers 80 % of it along x, so the columns beyond are
+    outside; the parameter traces have leading and trailing zeros."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz, nxp, nyp, nzp = 18, 14, 40, 24, 20, 50
+    dx = dy = 25.0
+    dz = 4.0
+    sbox = (0.0, 0.0, 1000.0, nx * dx, ny * dy, nz * dz, 0.0, dx, dy, dz)
+    gnx, gny, gnk = 15, ny, nz + 32
+    gbox = (0.0, 0.0, 1000.0 - 80.0, gnx * dx, gny * dy, gnk * dz)
+    t = np.arange(gnk)
+    out = {}
+    for kind, ctype in (("data", O.DATA), ("param", O.PARAMETER)):
+        v = np.zeros((gnk, gny, gnx), np.float32)
+        for j in range(gny):
+            for i in range(gnx):
+                if kind == "data":
+                    tr = sum(rng.uniform(0.3, 1.0) * np.sin(2 * np.pi * rng.uniform(0.02, 0.12) * t + rng.uniform(0, 6))
+                             for _ in range(3))
+                else:
+                    tr = 8.0 + 0.002 * t + 0.05 * np.sin(2 * np.pi * 0.03 * t + 0.1 * i + 0.2 * j)
+                    tr[:int(rng.integers(0, 6))] = 0.0
+                    tr[gnk - int(rng.integers(0, 5)):] = 0.0
+                v[:, j, i] = tr
+        cube, traces, state, z0d, dzd, z0g, dzg, counts = o2.fill_in_data(v, gbox, nx, ny, nz, nxp, nyp, nzp, sbox,
+                                                                         ctype, 20.0)
+        out.update({f"{kind}_values": v, f"{kind}_cube": cube, f"{kind}_traces": traces, f"{kind}_state": state,
+                    f"{kind}_z0_data": z0d, f"{kind}_dz_data": dzd, f"{kind}_z0_grid": z0g,
+                    f"{kind}_dz_grid": dzg, f"{kind}_counts": counts})
+    np.savez_compressed(os.path.join(HERE, name), nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp,
+                        smooth_length=20.0, **out)
+
+
 def simulation_case(name, inv, seed):
     nxp, nyp, nzp = int(inv["nxp"]), int(inv["nyp"]), int(inv["nzp"])
     noise = O.ref_fill_complex_noise(nxp, nyp, nzp, seed, 3)
@@ -254,6 +289,8 @@ def main():
     if only:
         if "reference_localnoise.npz" in only:
             local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
+        if "reference_fillindata.npz" in only:
+            fill_in_data_case("reference_fillindata.npz", 16)
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -274,6 +311,7 @@ def main():
     tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=8)
     inversion_4d_case("inversion_4d_n4.npz", tl)
     local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
+    fill_in_data_case("reference_fillindata.npz", 16)
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

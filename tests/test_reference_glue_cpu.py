@@ -248,3 +248,22 @@ def test_local_noise_correction_matches_reference(oracle):
         ref = g["out"][p]
         np.testing.assert_array_equal(out[p][~miss], ref[~miss])
         assert np.isnan(ref[miss]).all() and np.isfinite(out[p][miss]).all()
+
+
+@pytest.mark.parametrize("kind", ["data", "param"])
+def test_fill_in_data_matches_reference(oracle, kind):
+    """FFTGrid::fillInData run by the reference's own code (crava_o2) from a STORM grid onto a simbox: fed the
+    per-column traces and geometry the reference's lookups produced, the oracle's per-trace core (taper or
+    extrapolation and trend, FFT resampling, interpolation onto the cells) gives the reference's cube."""
+    g = golden("reference_fillindata.npz")
+    nx, ny, nz, nxp, nyp, nzp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp", "nyp", "nzp"))
+    st = g[f"{kind}_state"]
+    dz_data = np.unique(g[f"{kind}_dz_data"][st == 0])
+    assert len(dz_data) == 1
+    cube, ext = oracle.fill_in_data(nxp, nyp, nzp, nz, kind == "data", g[f"{kind}_traces"], st.astype(np.uint8),
+                                    g[f"{kind}_z0_data"], g[f"{kind}_z0_grid"], g[f"{kind}_dz_grid"], float(dz_data[0]),
+                                    float(g["smooth_length"]))
+    ref = g[f"{kind}_cube"]
+    assert rel(cube, ref) < 1e-6
+    dead = np.nonzero(st)[0]
+    assert np.all(cube.reshape(nzp, -1)[:, dead] == 0) and np.all(ref.reshape(nzp, -1)[:, dead] == 0)

@@ -101,3 +101,24 @@ def test_gpu_local_noise_correction_matches_reference(cuda):
               "max abs", np.abs(got[~miss] - ref[~miss]).max())
         assert e < 1e-6
         assert np.isfinite(got[miss]).all()
+
+
+@pytest.mark.parametrize("kind", ["data", "param"])
+def test_gpu_fill_in_data_matches_reference(cuda, kind):
+    """cg_fill_in_data fed the per-column traces and geometry of the reference's own fillInData run (crava_o2)
+    against the cube that run produced."""
+    from crava_gb300 import api
+    g = golden("reference_fillindata.npz")
+    nx, ny, nz, nxp, nyp, nzp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp", "nyp", "nzp"))
+    st = g[f"{kind}_state"]
+    dz_data = float(np.unique(g[f"{kind}_dz_data"][st == 0])[0])
+    _, rnxp = api.dims(nxp)
+    buf = torch.full((nzp, nyp, rnxp), 7.0, device="cuda")
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    api.fill_in_data(buf, nxp, nz, api.DATA if kind == "data" else api.PARAMETER, dev(g[f"{kind}_traces"]),
+                     dev(st.astype(np.uint8)), dev(g[f"{kind}_z0_data"]), dev(g[f"{kind}_z0_grid"]),
+                     dev(g[f"{kind}_dz_grid"]), dz_data, float(g["smooth_length"]))
+    got = buf.cpu().numpy()
+    e = rel(got, g[f"{kind}_cube"])
+    print("fillInData", kind, "GPU vs reference:", e)
+    assert e < 2e-6
