@@ -179,6 +179,16 @@ def fill_in_data(values, gbox, nx, ny, nz, nxp, nyp, nzp, sbox, cubetype, smooth
     return (cube, traces, state, *cols, counts)
 
 
+def interpolate_seismic(cube, nx, ny, nz, nxp, threshold):
+    """FFTGrid::interpolateSeismic on a real padded DATA cube (nzp, nyp, rnxp); returns the result."""
+    nzp, nyp, rnxp = cube.shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, threshold=float(threshold))
+        _w(d, "cube.f32", cube, np.float32)
+        _run("interpolate", d)
+        return _r(d, "out.f32", np.float32, (nzp, nyp, rnxp))
+
+
 CRAVA_GEOM = ("x0", "y0", "dx", "dy", "il0", "xl0", "ilstepx", "ilstepy", "xlstepx", "xlstepy", "angle")
 
 

@@ -20,6 +20,7 @@
 //   crava_o2 localnoise <dir>   Crava::computeG and Crava::correctAlphaBetaRho
 //                               (src/crava.cpp:2261-2569) on given cubes and scales.
 //   crava_o2 fillindata <dir>   FFTGrid::fillInData from a STORM grid onto a simbox.
+//   crava_o2 interpolate <dir>  FFTGrid::interpolateSeismic on a DATA cube.
 //   crava_o2 crava_write / crava_read <dir>
 //                               FFTGrid::writeCravaFile / readCravaFile.
 //   crava_o2 storm_write / storm_read <dir>
@@ -543,6 +544,21 @@ int cmd_fillindata()
   return 0;
 }
 
+// FFTGrid::interpolateSeismic (src/fftgrid.cpp:2576-2738) on the DATA cube cube.f32 (real domain) with the
+// energy threshold of params.txt; writes the result
+int cmd_interpolate()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"];
+  const size_t rsize = (size_t)2 * (nxp / 2 + 1) * nyp * nzp;
+  std::vector<float> cube = read_arr<float>("cube.f32", rsize);
+  FFTGrid *g = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::DATA, &cube[0], false);
+  g->interpolateSeismic((float)p["threshold"]);
+  dump_grid("out.f32", g);
+  return 0;
+}
+
 // FFTGrid::writeCravaFile (src/fftgrid.cpp:2410-2441) of the cube cube.f32 with the geometry of params.txt
 int cmd_crava_write()
 {
@@ -649,7 +665,7 @@ int main(int argc, char **argv)
   signal(SIGSEGV, on_fault);
   signal(SIGABRT, on_fault);
   if (argc != 3) {
-    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|fillindata|crava_write|crava_read|storm_write|storm_read|"
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|fillindata|interpolate|crava_write|crava_read|storm_write|storm_read|"
                     "factorable} <dir>\n");
     return 1;
   }
@@ -661,6 +677,7 @@ int main(int argc, char **argv)
   if (c == "adjust") return cmd_adjust();
   if (c == "localnoise") return cmd_localnoise();
   if (c == "fillindata") return cmd_fillindata();
+  if (c == "interpolate") return cmd_interpolate();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();
   if (c == "storm_write") return cmd_storm_write();

@@ -270,6 +270,22 @@ def fill_in_data_case(name, seed):
                         smooth_length=20.0, **out)
 
 
+def interpolate_case(name, seed):
+    """FFTGrid::interpolateSeismic by the reference's own code (crava_o2): dead traces alone, in pairs, on the
+    simbox edge and at a corner, and traces of low energy, with energy thresholds 0 and 0.3."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz, nxp, nyp, nzp = 14, 11, 20, 18, 15, 25
+    rnxp = 2 * (nxp // 2 + 1)
+    cube = rng.uniform(-1.5, 1.5, (nzp, nyp, rnxp)).astype(np.float32)
+    for (j, i) in ((2, 3), (5, 5), (5, 6), (0, 0), (0, 1), (1, 0), (10, 13), (7, 0), (4, 13)):
+        cube[:, j, i] = 0.0
+    for (j, i) in ((8, 8), (3, 10)):
+        cube[:, j, i] *= 0.2
+    outs = {f"out_{t:g}": o2.interpolate_seismic(cube, nx, ny, nz, nxp, t) for t in (0.0, 0.3)}
+    np.savez_compressed(os.path.join(HERE, name), nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, cube=cube,
+                        thresholds=np.array([0.0, 0.3]), **outs)
+
+
 def simulation_case(name, inv, seed):
     nxp, nyp, nzp = int(inv["nxp"]), int(inv["nyp"]), int(inv["nzp"])
     noise = O.ref_fill_complex_noise(nxp, nyp, nzp, seed, 3)
@@ -291,6 +307,8 @@ def main():
             local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
         if "reference_fillindata.npz" in only:
             fill_in_data_case("reference_fillindata.npz", 16)
+        if "reference_interpolate.npz" in only:
+            interpolate_case("reference_interpolate.npz", 17)
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -312,6 +330,7 @@ def main():
     inversion_4d_case("inversion_4d_n4.npz", tl)
     local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
     fill_in_data_case("reference_fillindata.npz", 16)
+    interpolate_case("reference_interpolate.npz", 17)
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

@@ -122,3 +122,15 @@ def test_gpu_fill_in_data_matches_reference(cuda, kind):
     e = rel(got, g[f"{kind}_cube"])
     print("fillInData", kind, "GPU vs reference:", e)
     assert e < 2e-6
+
+
+@pytest.mark.parametrize("threshold", [0.0, 0.3])
+def test_gpu_interpolate_seismic_bit_exact_vs_reference(cuda, threshold):
+    """cg_interpolate_seismic against FFTGrid::interpolateSeismic run by the reference's own code: bit for bit."""
+    from crava_gb300 import api
+    g = golden("reference_interpolate.npz")
+    nx, ny, nz, nxp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp"))
+    t = torch.from_numpy(np.ascontiguousarray(g["cube"])).cuda()
+    api.interpolate_seismic(t, nx, ny, nz, nxp, threshold)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(t.cpu().numpy(), g[f"out_{threshold:g}"])
