@@ -242,7 +242,10 @@ def variable_thickness(sc: Scenario, amp=0.3, surfaces=True, dead_traces=0, seed
     shift = gain = None
     if surfaces:
         shift = rng.uniform(-4.0, 4.0, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
-        gain = rng.uniform(0.85, 1.2, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
+        gain = rng.uniform(0.85, 1.2, (sc.ntheta, sc.ny, sc.nx))
+        # as Wavelet::setGainGrid leaves a gain grid (src/wavelet.cpp:704-737): divided by its geometric mean,
+        # which then multiplies the wavelet; at mean 1 the wavelet is unchanged
+        gain = (gain / np.exp(np.log(gain).mean(axis=(1, 2), keepdims=True))).astype(np.float32)
     data = [d.copy() for d in sc.data]
     if dead_traces:
         idx = rng.choice(sc.nx * sc.ny, dead_traces, replace=False)

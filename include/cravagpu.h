@@ -259,7 +259,9 @@ int cg_scale_wavelet_tables(int ntheta, int nz, int nzp, const float *wavelets, 
  * tables: device copy of cg_scale_wavelet_tables; rel_thick: [nyp][nxp]
  * (device) Simbox::getRelThick at every padded trace (must be positive);
  * shift, gain: [ntheta][ny][nx] (device) local wavelet time shift (ms) and
- * gain surfaces, or NULL for none.  n_bad (host, ntheta ints, may be NULL):
+ * gain surfaces, or NULL for none; gain as Wavelet::setGainGrid leaves it
+ * (src/wavelet.cpp:704-737: divided by its geometric mean, which multiplies
+ * the wavelet the tables are built from).  n_bad (host, ntheta ints, may be NULL):
  * traces at or below the energy limit.  The slack floats of each row (x >=
  * nxp) are overwritten.  Waits for the stream when interpolating. */
 int cg_divide_by_scale_wavelet(float *const *data, int ntheta, int nx, int ny, int nz, int nxp, int nyp, int nzp,

@@ -179,6 +179,41 @@ def fill_in_data(values, gbox, nx, ny, nz, nxp, nyp, nzp, sbox, cubetype, smooth
     return (cube, traces, state, *cols, counts)
 
 
+def divide_scale_wavelet(sc, corr_t, min_int_fq, f_peak, thick_nodes, shift, gain, energy_threshold, dx=25.0, dy=25.0,
+                         z0=1000.0):
+    """Crava::divideDataByScaleWavelet on the scenario's DATA cubes over a simbox whose bottom is
+    z0 + lz * thick_nodes (nj, ni nodes over the simbox area); shift, gain (ntheta, ny, nx).  Returns (the divided
+    cubes, the relative thickness at every padded trace (nyp, nxp), the simbox lz, the reference's resampled
+    wavelets (ntheta, nzp) and gain grids (ntheta, ny, nx) after Wavelet::setGainGrid, the filtered temporal
+    correlation)."""
+    n, nzp = sc.ntheta, sc.nzp
+    nj, ni = thick_nodes.shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=sc.nxp, nyp=sc.nyp, nzp=nzp, ntheta=n, ncorrt=len(corr_t),
+                min_int_fq=int(min_int_fq), dt=float(sc.dt_ms), fpeak=float(f_peak), low_cut=float(sc.low_cut),
+                high_cut=float(sc.high_cut), wnc=float(sc.wnc), energy_threshold=float(energy_threshold), ni=ni,
+                nj=nj, dx=float(dx), dy=float(dy), z0=float(z0))
+        _w(d, "theta.f32", sc.theta_deg, np.float32)
+        _w(d, "A.f32", sc.A, np.float32)
+        _w(d, "etc.f64", sc.err_theta_cov, np.float64)
+        _w(d, "sigma0.f32", np.asarray(sc.sigma0, dtype=np.float64).astype(np.float32), np.float32)
+        _w(d, "corrxy.f64", np.asarray(sc.corr_xy, dtype=np.float32).astype(np.float64), np.float64)
+        _w(d, "corrt.f32", corr_t, np.float32)
+        _w(d, "data.f32", np.stack(sc.data), np.float32)
+        _w(d, "thick.f64", thick_nodes, np.float64)
+        _w(d, "shift.f32", shift, np.float32)
+        _w(d, "gain.f32", gain, np.float32)
+        _run("divide", d)
+        shp = sc.data[0].shape
+        out = [_r(d, f"out{l}.f32", np.float32, shp) for l in range(n)]
+        rel = _r(d, "relthick.f64", np.float64, (sc.nyp, sc.nxp))
+        lz = float(_r(d, "lz.f64", np.float64)[0])
+        wav = _r(d, "wavelets.f32", np.float32, (n, nzp))
+        gn = _r(d, "gain_normalised.f32", np.float32, (n, sc.ny, sc.nx))
+        ctf = _r(d, "corrt_filtered.f32", np.float32)
+    return out, rel, lz, wav, gn, ctf
+
+
 def interpolate_seismic(cube, nx, ny, nz, nxp, threshold):
     """FFTGrid::interpolateSeismic on a real padded DATA cube (nzp, nyp, rnxp); returns the result."""
     nzp, nyp, rnxp = cube.shape

@@ -21,6 +21,7 @@
 //                               (src/crava.cpp:2261-2569) on given cubes and scales.
 //   crava_o2 fillindata <dir>   FFTGrid::fillInData from a STORM grid onto a simbox.
 //   crava_o2 interpolate <dir>  FFTGrid::interpolateSeismic on a DATA cube.
+//   crava_o2 divide     <dir>   Crava::divideDataByScaleWavelet on a simbox of non-constant thickness.
 //   crava_o2 crava_write / crava_read <dir>
 //                               FFTGrid::writeCravaFile / readCravaFile.
 //   crava_o2 storm_write / storm_read <dir>
@@ -544,6 +545,118 @@ int cmd_fillindata()
   return 0;
 }
 
+// Crava::divideDataByScaleWavelet (src/crava.cpp:678-804) on ntheta DATA cubes (data.f32, real domain) over a
+// simbox of non-constant thickness: a flat top at z0 and a bottom z0 + lz r(x, y), r given at ni x nj nodes over
+// the simbox area (thick.f64, max 1), local wavelet shift and gain grids (shift.f32, gain.f32, ntheta x ny x nx),
+// Ricker wavelets built and resampled by the reference (Wavelet1D), the prior temporal correlation of corrt.f32.
+// Writes the divided cubes, the simbox's relative thickness at every padded trace, its lz, the wavelets and gain
+// grids as Wavelet::setGainGrid leaves them (grid divided by its geometric mean, wavelet multiplied by it) and the
+// filtered temporal correlation the adjustment factor used.
+int cmd_divide()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"], n = (int)p["ntheta"];
+  const int ncorrt = (int)p["ncorrt"], min_int_fq = (int)p["min_int_fq"], ni = (int)p["ni"], nj = (int)p["nj"];
+  const float dt = (float)p["dt"], fpeak = (float)p["fpeak"];
+  const double dx = p["dx"], dy = p["dy"], z0 = p["z0"];
+  const size_t rsize = (size_t)2 * (nxp / 2 + 1) * nyp * nzp;
+  std::vector<float> theta = read_arr<float>("theta.f32", n);
+  std::vector<float> A = read_arr<float>("A.f32", (size_t)n * 3);
+  std::vector<double> etc = read_arr<double>("etc.f64", (size_t)n * n);
+  std::vector<float> s0 = read_arr<float>("sigma0.f32", 9);
+  std::vector<double> cxy = read_arr<double>("corrxy.f64", (size_t)nxp * nyp);
+  std::vector<float> corrT = read_arr<float>("corrt.f32", ncorrt);
+  std::vector<float> data = read_arr<float>("data.f32", rsize * n);
+  std::vector<double> thick = read_arr<double>("thick.f64", (size_t)ni * nj);
+  std::vector<float> shift = read_arr<float>("shift.f32", (size_t)n * nx * ny);
+  std::vector<float> gain = read_arr<float>("gain.f32", (size_t)n * nx * ny);
+
+  ModelSettings ms;
+  Surface corr_xy(0.0, 0.0, 25.0 * nxp, 25.0 * nyp, nxp, nyp, 0.0);
+  for (int j = 0; j < nyp; j++)
+    for (int i = 0; i < nxp; i++) corr_xy(i + nxp * j) = cxy[(size_t)j * nxp + i];
+  SeismicParametersHolder sp;
+  sp.priorVar0_.resize(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) sp.priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
+  sp.createCorrGrids(nx, ny, nz, nxp, nyp, nzp, false);
+  sp.initializeCorrelations(&corr_xy, corrT, 0.0f, 0.0f, min_int_fq, nzp);
+  float *filtered = sp.getPriorCorrTFiltered(nz, nzp);
+  write_raw("corrt_filtered.f32", filtered, sizeof(float) * nzp);
+  delete[] filtered;
+
+  const double lx = dx * nx, ly = dy * ny, lz = (double)nz * dt;
+  Surface top(0.0, 0.0, lx, ly, ni, nj, z0);
+  Surface bot(0.0, 0.0, lx, ly, ni, nj, z0);
+  for (int j = 0; j < nj; j++)
+    for (int i = 0; i < ni; i++) bot(i + ni * j) = z0 + lz * thick[(size_t)j * ni + i];
+  Simbox sb(0.0, 0.0, top, lx, ly, lz, 0.0, dx, dy, (double)dt);
+  sb.setDepth(top, bot, nz);
+  std::vector<double> rel((size_t)nxp * nyp);
+  for (int j = 0; j < nyp; j++)
+    for (int i = 0; i < nxp; i++) rel[(size_t)j * nxp + i] = sb.getRelThick(i, j);
+  write_raw("relthick.f64", &rel[0], sizeof(double) * rel.size());
+  const double lz_box = sb.getlz();
+  write_raw("lz.f64", &lz_box, sizeof(double));
+
+  Crava *crava = static_cast<Crava *>(operator new(sizeof(Crava)));
+  memset((void *)crava, 0, sizeof(Crava));
+  crava->nx_ = nx;
+  crava->ny_ = ny;
+  crava->nz_ = nz;
+  crava->nxp_ = nxp;
+  crava->nyp_ = nyp;
+  crava->nzp_ = nzp;
+  crava->ntheta_ = n;
+  crava->lowCut_ = (float)p["low_cut"];
+  crava->highCut_ = (float)p["high_cut"];
+  crava->wnc_ = (float)p["wnc"];
+  crava->energyTreshold_ = (float)p["energy_threshold"];
+  crava->simbox_ = &sb;
+  new (&crava->priorVar0_) NRLib::Matrix(3, 3);
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) crava->priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
+  crava->thetaDeg_ = new float[n];
+  crava->A_ = new float *[n];
+  crava->errThetaCov_ = new double *[n];
+  crava->seisWavelet_ = new Wavelet *[n];
+  crava->seisData_ = new FFTGrid *[n];
+  std::vector<float> wavs((size_t)n * nzp);
+  for (int l = 0; l < n; l++) {
+    crava->thetaDeg_[l] = theta[l];
+    crava->A_[l] = new float[3];
+    for (int q = 0; q < 3; q++) crava->A_[l][q] = A[(size_t)l * 3 + q];
+    crava->errThetaCov_[l] = new double[n];
+    for (int m = 0; m < n; m++) crava->errThetaCov_[l][m] = etc[(size_t)l * n + m];
+    int err = 0;
+    Wavelet1D *w = new Wavelet1D(&ms, crava->A_[l], theta[l], fpeak, err);
+    if (err) { fprintf(stderr, "wavelet: error %d\n", err); return 3; }
+    w->resample(dt, nz, nzp);
+    Grid2D *gs = new Grid2D(nx, ny, 0.0), *gg = new Grid2D(nx, ny, 1.0);
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) {
+        (*gs)(i, j) = shift[((size_t)l * ny + j) * nx + i];
+        (*gg)(i, j) = gain[((size_t)l * ny + j) * nx + i];
+      }
+    w->setShiftGrid(gs);
+    w->setGainGrid(gg);  // divides the grid by its geometric mean and multiplies the wavelet by it
+    // the wavelet (time domain) and the gain grid as the division sees them
+    Wavelet1D wt(w);
+    if (!wt.isReal_) wt.invFFT1DInPlace();
+    for (int k = 0; k < nzp; k++) wavs[(size_t)l * nzp + k] = wt.rAmp_[k];
+    for (int j = 0; j < ny; j++)
+      for (int i = 0; i < nx; i++) gain[((size_t)l * ny + j) * nx + i] = (float)(*gg)(i, j);
+    crava->seisWavelet_[l] = w;
+    crava->seisData_[l] = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::DATA, &data[rsize * l], false);
+  }
+  write_raw("wavelets.f32", &wavs[0], sizeof(float) * wavs.size());
+  write_raw("gain_normalised.f32", &gain[0], sizeof(float) * gain.size());
+  crava->divideDataByScaleWavelet(sp);
+  for (int l = 0; l < n; l++) dump_grid("out" + NRLib::ToString(l) + ".f32", crava->seisData_[l]);
+  return 0;
+}
+
 // FFTGrid::interpolateSeismic (src/fftgrid.cpp:2576-2738) on the DATA cube cube.f32 (real domain) with the
 // energy threshold of params.txt; writes the result
 int cmd_interpolate()
@@ -665,7 +778,7 @@ int main(int argc, char **argv)
   signal(SIGSEGV, on_fault);
   signal(SIGABRT, on_fault);
   if (argc != 3) {
-    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|fillindata|interpolate|crava_write|crava_read|storm_write|storm_read|"
+    fprintf(stderr, "usage: crava_o2 {inversion|state4d|adjust|localnoise|fillindata|interpolate|divide|crava_write|crava_read|storm_write|storm_read|"
                     "factorable} <dir>\n");
     return 1;
   }
@@ -678,6 +791,7 @@ int main(int argc, char **argv)
   if (c == "localnoise") return cmd_localnoise();
   if (c == "fillindata") return cmd_fillindata();
   if (c == "interpolate") return cmd_interpolate();
+  if (c == "divide") return cmd_divide();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();
   if (c == "storm_write") return cmd_storm_write();

@@ -286,6 +286,29 @@ def interpolate_case(name, seed):
                         thresholds=np.array([0.0, 0.3]), **outs)
 
 
+def divide_case(name, seed):
+    """Crava::divideDataByScaleWavelet by the reference's own code (crava_o2): 3 stacks over a simbox whose
+    relative thickness varies from 0.7 to 1 (a bottom surface on 4 x 3 nodes), local wavelet shifts of up to 4 ms
+    and gains 0.85-1.2, two dead traces, energy threshold 0 (interpolateSeismic after the division)."""
+    sc = S.make_scenario(14, 10, 30, [10.0, 20.0, 30.0], 30.0, nxp=18, nyp=14, nzp=40, seed=seed)
+    rng = np.random.default_rng(seed)
+    data = [d.copy() for d in sc.data]
+    for (j, i) in ((3, 4), (7, 11)):
+        for dd in data:
+            dd[:, j, i] = 0.0
+    from dataclasses import replace
+    sc = replace(sc, data=data)
+    thick = np.array([[1.0, 0.9, 0.8, 0.85], [0.95, 0.75, 0.7, 0.8], [0.9, 0.85, 0.9, 1.0]])
+    shift = rng.uniform(-4.0, 4.0, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
+    gain = rng.uniform(0.85, 1.2, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
+    out, rel, lz, wav, gn, ctf = o2.divide_scale_wavelet(sc, sc.corr_t, sc.min_int_fq, 30.0, thick, shift, gain, 0.0)
+    np.savez_compressed(os.path.join(HERE, name), nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=sc.nxp, nyp=sc.nyp, nzp=sc.nzp,
+                        dt_ms=sc.dt_ms, low_cut=sc.low_cut, high_cut=sc.high_cut, wnc=sc.wnc, A=sc.A,
+                        sigma0=sc.sigma0, err_theta_cov=sc.err_theta_cov, data=np.stack(data), shift=shift,
+                        gain=gain, gain_normalised=gn, rel_thick=rel, lz=lz, wavelets=wav, corr_t_filtered=ctf,
+                        out=np.stack(out))
+
+
 def simulation_case(name, inv, seed):
     nxp, nyp, nzp = int(inv["nxp"]), int(inv["nyp"]), int(inv["nzp"])
     noise = O.ref_fill_complex_noise(nxp, nyp, nzp, seed, 3)
@@ -309,6 +332,8 @@ def main():
             fill_in_data_case("reference_fillindata.npz", 16)
         if "reference_interpolate.npz" in only:
             interpolate_case("reference_interpolate.npz", 17)
+        if "reference_divide.npz" in only:
+            divide_case("reference_divide.npz", 18)
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -331,6 +356,7 @@ def main():
     local_noise_case("reference_localnoise.npz", 5, (21, 17, 24, 24, 20, 30), 15)
     fill_in_data_case("reference_fillindata.npz", 16)
     interpolate_case("reference_interpolate.npz", 17)
+    divide_case("reference_divide.npz", 18)
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

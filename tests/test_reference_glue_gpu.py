@@ -134,3 +134,26 @@ def test_gpu_interpolate_seismic_bit_exact_vs_reference(cuda, threshold):
     api.interpolate_seismic(t, nx, ny, nz, nxp, threshold)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(t.cpu().numpy(), g[f"out_{threshold:g}"])
+
+
+def test_gpu_scale_wavelet_division_matches_reference(cuda):
+    """cg_scale_wavelet_tables + cg_divide_by_scale_wavelet (with interpolateSeismic) against
+    Crava::divideDataByScaleWavelet run by the reference's own code on a simbox of non-constant thickness, with the
+    wavelets and gain grids as the reference's Wavelet::setGainGrid leaves them."""
+    from crava_gb300 import api
+    g = golden("reference_divide.npz")
+    nx, ny, nz, nxp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp"))
+    dt, lz = float(g["dt_ms"]), float(g["lz"])
+    s0 = np.asarray(g["sigma0"]).astype(np.float32).astype(np.float64)
+    tab = api.scale_wavelet_tables(g["wavelets"], g["A"], s0, g["corr_t_filtered"], g["err_theta_cov"], nz, dt, lz,
+                                   float(g["low_cut"]), float(g["high_cut"]), float(g["wnc"]))
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()  # noqa: E731
+    cubes = [dev(x) for x in g["data"]]
+    nbad = api.divide_by_scale_wavelet(cubes, nx, ny, nz, nxp, dev(tab), dev(g["rel_thick"]), dt, lz,
+                                       float(g["low_cut"]), float(g["high_cut"]), 0.0, shift=dev(g["shift"]),
+                                       gain=dev(g["gain_normalised"]))
+    assert nbad == [2, 2, 2]
+    for l, c in enumerate(cubes):
+        e = rel(c.cpu().numpy()[..., :nxp], g["out"][l][..., :nxp])
+        print("scale-wavelet division, angle", l, "GPU vs reference:", e)
+        assert e < 2e-5
