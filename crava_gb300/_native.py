@@ -207,6 +207,8 @@ def _declare(L):
         "cg_batch_reset": ([V, V], I),
         "cg_batch_run": ([V, I, I, V], I),
         "cg_batch_read": ([V, I, PP, PP, PP], I),
+        "cg_batch_set_simulation": ([V, I, I, ct.c_ulonglong], I),
+        "cg_batch_read_fields": ([V, I, I, PP], I),
         "cg_batch_bins": ([V], ct.c_long),
         "cg_tune_set": ([I, I, I], I),
         "cg_tune_get": ([I, I], I),

@@ -618,6 +618,19 @@ class Batch:
         return (np.stack([m[:, :, :sc.nxp] for m in mean]), np.stack([r.view(np.complex64) for r in res]),
                 np.stack([c.view(np.complex64) for c in cov]))
 
+    def set_simulation(self, i, nreal, seed=0):
+        """Draw nreal posterior realisations of cube i after its inversion in every later run
+        (cg_batch_set_simulation); nreal = 0 removes them."""
+        check(lib().cg_batch_set_simulation(self.h, i, nreal, ct.c_ulonglong(seed)), "cg_batch_set_simulation")
+
+    def read_fields(self, i, r):
+        """Realisation r of cube i: 3 real padded cubes (alpha, beta, rho) as numpy float32."""
+        sc = self.scs[i]
+        out = [np.empty_like(sc.mean[0]) for _ in range(3)]
+        pf, k = _pp_np(out)
+        check(lib().cg_batch_read_fields(self.h, i, r, pf), "cg_batch_read_fields")
+        return out
+
     def close(self):
         if getattr(self, "h", None):
             lib().cg_batch_destroy(self.h)

@@ -1,9 +1,10 @@
-// Batched inversions of many independent cubes of uneven size, angle count
-// and model, as one unit of GPU work.
+// Batched inversions of many independent cubes of uneven size, angle count,
+// model and realisation count, as one unit of GPU work.
 //
 // Every cube has its own model (operator tables, workspace) and device cubes.
 // A batch run queues each cube's whole inversion (prior spectra, forward
-// transforms, fused bin kernel, inverse transforms) on one of several streams
+// transforms, fused bin kernel, inverse transforms) and, where set, its
+// posterior simulation (factor, noise, inverse transforms, mean add) on one of several streams
 // forked from the caller's stream and joins them back, so small cubes run
 // side by side on the GPU.  With use_graph, the first run is captured into a
 // CUDA graph (after a warm-up run that creates every twiddle table and kernel
@@ -41,6 +42,11 @@ struct BatchCube {
   Crava *crava = nullptr;
   std::vector<FFTGrid *> data, mean, cov;
   std::vector<float *> data_in, mean_in;  // pristine real-domain inputs (device)
+  // posterior simulation after the inversion (cg_batch_set_simulation): factor planes, 3*nreal fields
+  int nreal = 0;
+  unsigned long long seed = 0;
+  float *chol = nullptr;
+  std::vector<float *> fields;
   long rsize() const { return 2L * (nxp / 2 + 1) * nyp * nzp; }
   long bins() const { return (long)(nxp / 2 + 1) * nyp * nzp; }
 };
@@ -85,6 +91,8 @@ extern "C" void cg_batch_destroy(cg_batch b)
     for (auto *g : c.cov) delete g;
     for (auto *p : c.data_in) cudaFree(p);
     for (auto *p : c.mean_in) cudaFree(p);
+    if (c.chol) cudaFree(c.chol);
+    for (auto *p : c.fields) cudaFree(p);
     delete c.crava;
   }
   for (auto s : b->streams) cudaStreamDestroy(s);
@@ -202,13 +210,14 @@ extern "C" int cg_batch_reset(cg_batch b, void *stream)
 
 // Cubes to streams, longest first onto the least-loaded stream (LPT): the
 // streams finish close together instead of one stream ending on a run of
-// large cubes.  Work is estimated as bins x (stacks + 9 output spectra).
+// large cubes.  Work is estimated as bins x (stacks + 9 output spectra + 9 per
+// realisation: three fields through three inverse passes).
 static std::vector<int> stream_of_cubes(const cg_batch_s *b)
 {
   const size_t n = b->cubes.size(), ns = b->streams.size();
   std::vector<int> order(n), sid(n);
   for (size_t i = 0; i < n; i++) order[i] = (int)i;
-  auto work = [&](int i) { return (double)b->cubes[i].bins() * (b->cubes[i].ntheta + 9); };
+  auto work = [&](int i) { return (double)b->cubes[i].bins() * (b->cubes[i].ntheta + 9 + 9 * b->cubes[i].nreal); };
   std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return work(x) > work(y); });
   std::vector<double> load(ns, 0.0);
   for (int i : order) {
@@ -238,6 +247,15 @@ static void queue_batch(cg_batch b, Crava::Form form, cudaStream_t st)
     for (auto *g : c.mean) g->setTransformedStatus(false);
     FFTGrid *a = c.mean[0], *bb = c.mean[1], *cc = c.mean[2];
     c.crava->computePostMeanResidAndFFTCov(c.data.data(), a, bb, cc, c.cov.data(), nullptr, form, cs);
+    if (c.nreal > 0) {
+      float *cov[6], *pm[3];
+      for (int t = 0; t < 6; t++) cov[t] = c.cov[t]->devicePtr();
+      for (int q = 0; q < 3; q++) pm[q] = c.mean[q]->devicePtr();
+      int rc = cg_posterior_cholesky(cov, c.chol, c.nxp, c.nyp, c.nzp, nullptr, cs);
+      if (rc == CG_OK)
+        rc = cg_simulate_fields(c.chol, nullptr, c.fields.data(), c.nreal, 0, c.seed, c.nxp, c.nyp, c.nzp, pm, cs);
+      if (rc != CG_OK) throw Error(rc, "batch simulation: " + std::string(cg_last_error()));
+    }
   }
   for (size_t s = 0; s < b->streams.size(); s++) {
     cuda_check(cudaEventRecord(b->join[s], b->streams[s]), "join");
@@ -304,6 +322,49 @@ extern "C" int cg_batch_read(cg_batch b, int i, float *const *post_mean, float *
       for (int l = 0; l < c.ntheta; l++) cuda_check(cudaMemcpy(resid[l], c.data[l]->devicePtr(), bytes, cudaMemcpyDeviceToHost), "read");
     if (post_cov)
       for (int t = 0; t < 6; t++) cuda_check(cudaMemcpy(post_cov[t], c.cov[t]->devicePtr(), bytes, cudaMemcpyDeviceToHost), "read");
+    return CG_OK;
+  })
+}
+
+extern "C" int cg_batch_set_simulation(cg_batch b, int i, int nreal, unsigned long long seed)
+{
+  if (!b || i < 0 || i >= (int)b->cubes.size() || nreal < 0) { cg::set_error("cg_batch_set_simulation: bad argument"); return CG_ERR_ARG; }
+  CG_TRY({
+    BatchCube &c = b->cubes[i];
+    cuda_check(cudaDeviceSynchronize(), "batch simulation set-up");
+    if (c.chol) { cudaFree(c.chol); c.chol = nullptr; }
+    for (auto *p : c.fields) cudaFree(p);
+    c.fields.clear();
+    c.nreal = 0;
+    c.seed = seed;
+    if (nreal > 0) {
+      cuda_check(cg::dev_malloc((void **)&c.chol, sizeof(float) * 9 * (size_t)c.bins()), "batch factor");
+      for (int t = 0; t < 3 * nreal; t++) {
+        float *f = nullptr;
+        cuda_check(cg::dev_malloc((void **)&f, sizeof(float) * c.rsize()), "batch field");
+        c.fields.push_back(f);
+      }
+      c.nreal = nreal;
+    }
+    // the captured graph no longer matches the work: recapture on the next graph run
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    b->graph_form = -1;
+    b->warm = false;
+    return CG_OK;
+  })
+}
+
+extern "C" int cg_batch_read_fields(cg_batch b, int i, int r, float *const *fields)
+{
+  if (!b || i < 0 || i >= (int)b->cubes.size() || !fields) { cg::set_error("cg_batch_read_fields: bad argument"); return CG_ERR_ARG; }
+  CG_TRY({
+    BatchCube &c = b->cubes[i];
+    if (r < 0 || r >= c.nreal) throw Error(CG_ERR_ARG, "cube " + std::to_string(i) + " has no realisation " + std::to_string(r));
+    const size_t bytes = sizeof(float) * c.rsize();
+    cuda_check(cudaDeviceSynchronize(), "batch read");
+    for (int q = 0; q < 3; q++)
+      if (fields[q]) cuda_check(cudaMemcpy(fields[q], c.fields[3 * r + q], bytes, cudaMemcpyDeviceToHost), "read field");
     return CG_OK;
   })
 }

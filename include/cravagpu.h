@@ -595,6 +595,15 @@ int cg_batch_run(cg_batch batch, int form, int use_graph, void *stream);
 int cg_batch_read(cg_batch batch, int i, float *const *post_mean, float *const *resid, float *const *post_cov);
 /* Total frequency bins of the batch (sum of cnxp*nyp*nzp). */
 long cg_batch_bins(cg_batch batch);
+/* Posterior simulation inside the batch (Crava::simulate, src/crava.cpp:1551-1734, per cube): every later
+ * cg_batch_run draws nreal realisations of cube i right after its inversion, on the cube's stream -- the
+ * per-bin posterior factor (cg_posterior_cholesky), seeded counter-based noise keyed by (seed, realisation),
+ * three inverse transforms and the posterior-mean add (cg_simulate_fields).  Allocates the cube's factor and
+ * 3*nreal field cubes now, never during a run; nreal = 0 removes the simulation.  A captured graph is
+ * recaptured on the next graph run.  Cubes may have different realisation counts. */
+int cg_batch_set_simulation(cg_batch batch, int i, int nreal, unsigned long long seed);
+/* Realisation r of cube i: 3 real padded cubes (host, rnxp*nyp*nzp floats each: alpha, beta, rho); synchronises. */
+int cg_batch_read_fields(cg_batch batch, int i, int r, float *const *fields);
 
 /* ========================================================================
  * Posterior simulation (Crava::simulate, src/crava.cpp:1551-1734).

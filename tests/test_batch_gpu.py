@@ -61,3 +61,49 @@ def test_batch_cube_matches_fp64_oracle(cuda, oracle):
         e = (rel(pm, post64), rel(pm - prior, post64 - prior), rel(res, res64), rel(cov, cov64))
         print("batch cube", i, (sc.nxp, sc.nyp, sc.nzp, sc.ntheta), "vs FP64 oracle:", e)
         assert e[0] < 1e-6 and e[1] < 1e-4 and e[2] < 1e-4 and e[3] < 1e-4
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_batch_simulation_matches_single_cube(cuda, use_graph):
+    """Realisations drawn inside the batch equal the single-cube chain on the same posterior and seed."""
+    import torch
+    from crava_gb300 import api
+    scs = _scenarios()
+    b = api.Batch(scs, nstreams=3)
+    nreal = {0: 2, 2: 3, 3: 1}
+    for i, n in nreal.items():
+        b.set_simulation(i, n, seed=100 + i)
+    for rep in range(2):
+        b.reset()
+        b.run("mixed", use_graph=use_graph)
+        got = {i: [b.read_fields(i, r) for r in range(n)] for i, n in nreal.items()}
+        for i, n in nreal.items():
+            sc = scs[i]
+            inv = api.HostInversion(sc)
+            data = [d.copy() for d in sc.data]
+            mean = [m.copy() for m in sc.mean]
+            cov = [np.zeros_like(sc.data[0]) for _ in range(6)]
+            inv.run(data, mean, cov, form="mixed")
+            chol, nfail = api.posterior_cholesky([torch.from_numpy(c).cuda() for c in cov], sc.nxp)
+            fields = [torch.empty_like(torch.from_numpy(sc.mean[0])).cuda() for _ in range(3 * n)]
+            api.simulate_fields(chol, fields, sc.nxp, seed=100 + i,
+                                post_mean=[torch.from_numpy(m).cuda() for m in mean])
+            torch.cuda.synchronize()
+            for r in range(n):
+                for p in range(3):
+                    want = fields[3 * r + p].cpu().numpy()[:, :, :sc.nxp]
+                    assert np.array_equal(got[i][r][p][:, :, :sc.nxp], want), (rep, i, r, p)
+                # a realisation is not the posterior mean
+                assert not np.array_equal(got[i][r][0][:, :, :sc.nxp], mean[0][:, :, :sc.nxp])
+    # realisations are per-seed: two different seeds give different fields
+    assert not np.array_equal(got[2][0][0], got[2][1][0])
+    with pytest.raises(Exception):
+        b.read_fields(1, 0)
+    with pytest.raises(Exception):
+        b.read_fields(0, 2)
+    # removing the simulation keeps the inversion results
+    b.set_simulation(0, 0)
+    b.reset()
+    b.run("mixed", use_graph=use_graph)
+    with pytest.raises(Exception):
+        b.read_fields(0, 0)
