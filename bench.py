@@ -376,14 +376,16 @@ def cpu_timelapse_vintage(tl, state, errc, threads):
     return time.perf_counter() - t0
 
 
-def other_workloads(args, stream, flush, rank, peak, cpu_ok):
+def other_workloads(args, stream, flush, rank, peak, cpu_ok, sc1=None):
     """The other workloads the metric's configuration list names, each timed with CUDA events after
     warm-up, with the dominant kernel's roofline fraction and (rank 0, one GPU) the CPU oracle port timed
     on the host cores beside it:
       * the small CPU-sized inversion (80x80x160, 3 stacks), L2 flushed between steps;
       * 64 uneven cubes in one graph-replayed batch;
       * posterior simulation, 200^3, 128 realisations;
-      * 4D time-lapse, 256x256x192, two vintages x 4 stacks (three-pass plain form and one-pass fused form)."""
+      * 4D time-lapse, 256x256x192, two vintages x 4 stacks (three-pass plain form and one-pass fused form);
+      * the headline model with nonzero correlation gradients (non-separable prior: plain form against the
+        fused form reading the per-bin prior table)."""
     import numpy as np
     import torch
     from crava_gb300 import api, microbench as MB
@@ -417,6 +419,40 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok):
                                  "cores": threads, "kind": "port", "sample": "one complete inversion"}
     del inv0
     out["small_80x80x160_3stacks"] = small
+
+    # the headline model with correlation gradients
+    if sc1 is not None:
+        import dataclasses
+        gsc = dataclasses.replace(sc1, corr_grad=(0.37, -0.21))
+        invg = Inversion(gsc, forms=("plain", "mixed"))
+        grad = {"workload": "the 256^3 5-stack model with correlation gradients (corrGradI, corrGradJ) = "
+                            "(0.37, -0.21): a prior that is not separable",
+                "bins": gsc.nbins, "ms": {}, "ms_stat": "median"}
+        outs = {}
+        for form in ("plain", "mixed"):
+            for _ in range(max(args.warmup, 1)):
+                invg.restore(form)
+                invg.run(form)
+
+            def before(form=form):
+                invg.restore(form)
+                flush.fill_(1.0)
+            grad["ms"][form] = round(statistics.median(MB._events_ms(lambda: invg.run(form), steps, before)), 4)
+            invg.restore(form)
+            invg.run(form)
+            torch.cuda.synchronize()
+            outs[form] = invg.results(form)
+        grad["Mbins_per_s_mixed"] = round(gsc.nbins / (grad["ms"]["mixed"] * 1e-3) / 1e6, 1)
+        grad["speedup_mixed_vs_plain"] = round(grad["ms"]["plain"] / grad["ms"]["mixed"], 3)
+        prior = np.stack([m[:, :, :gsc.nxp] for m in gsc.mean]).astype(np.float64)
+        pm_p, _, cov_p = outs["plain"]
+        pm_m, _, cov_m = outs["mixed"]
+        grad["mixed_vs_plain"] = {"update_rel_diff": float(f"{rel(pm_m - prior, pm_p - prior):.3e}"),
+                                  "cov_rel_diff": float(f"{rel(cov_m, cov_p):.3e}")}
+        invg.restore("mixed")
+        grad["roofline"] = MB.roofline_of(MB._traced(lambda: invg.run("mixed")), peak)
+        del invg, outs
+        out["gradients_256_5stacks"] = grad
 
     # batch of uneven cubes
     t0 = time.perf_counter()
@@ -705,7 +741,7 @@ def run_ours(args, world, rank, local):
     others = None
     if not args.no_other_workloads:
         others = other_workloads(args, stream, flush, rank, peak,
-                                 rank == 0 and world == 1 and not args.no_cpu_baseline)
+                                 rank == 0 and world == 1 and not args.no_cpu_baseline, sc1=sc)
 
     cpu = None
     vs_cpu64 = None

@@ -160,6 +160,7 @@ def _declare(L):
         "cg_workspace_reset_stats": ([V, V], I),
         "cg_invert_bins_plain": ([V, PP, PP, PP, V, V], I),
         "cg_prior_spectra": ([V, V, V, I, V], I),
+        "cg_prior_spectra_grad": ([V, V, V, F, F, I, V], I),
         "cg_invert_bins_fused": ([V, PP, PP, PP, I, V], I),
         "cg_invert_cubes_fused": ([V, PP, PP, PP, I, V], I),
         "cg_invert_bins_fused_f64": ([V, PP, PP, PP, V], I),

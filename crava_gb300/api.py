@@ -330,9 +330,16 @@ class Workspace:
         pc, k3 = _pp(cov)
         check(lib().cg_invert_bins_plain(self.h, pd, pm, pc, _vp(errcorr), _stream(stream)), "cg_invert_bins_plain")
 
-    def prior_spectra(self, corr_xy, circ_corr_t, precision=PREC_MIXED, stream=None):
-        check(lib().cg_prior_spectra(self.h, _vp(corr_xy), _vp(circ_corr_t), precision, _stream(stream)),
-              "cg_prior_spectra")
+    def prior_spectra(self, corr_xy, circ_corr_t, precision=PREC_MIXED, stream=None, grad=(0.0, 0.0)):
+        """Prior of the fused forms (cg_prior_spectra; cg_prior_spectra_grad for nonzero correlation
+        gradients grad = (corrGradI, corrGradJ))."""
+        gi, gj = float(grad[0]), float(grad[1])
+        if gi == 0.0 and gj == 0.0:
+            check(lib().cg_prior_spectra(self.h, _vp(corr_xy), _vp(circ_corr_t), precision, _stream(stream)),
+                  "cg_prior_spectra")
+        else:
+            check(lib().cg_prior_spectra_grad(self.h, _vp(corr_xy), _vp(circ_corr_t), gi, gj, precision,
+                                              _stream(stream)), "cg_prior_spectra_grad")
 
     def invert_cubes(self, data, mean, cov, precision=PREC_MIXED, stream=None):
         """Whole fused inversion from real-domain cubes (cg_invert_cubes_fused)."""
@@ -492,11 +499,18 @@ def vintage4d(ws, mu_s, mu_d, ss, sd, dd, data, errcorr, post_mean, nxp, precisi
     return nsplit
 
 
+def corr_grad(sc):
+    """(corrGradI, corrGradJ) of a scenario as float32 values; (0, 0) when it has none."""
+    g = getattr(sc, "corr_grad", (0.0, 0.0))
+    return float(np.float32(g[0])), float(np.float32(g[1]))
+
+
 class _InvModel(ct.Structure):
     _fields_ = [("ntheta", ct.c_int), ("wavelets", ct.c_void_p), ("A", ct.c_void_p), ("err_theta_cov", ct.c_void_p),
                 ("sigma0", ct.c_void_p), ("corr_xy", ct.c_void_p), ("circ_corr_t", ct.c_void_p),
                 ("wnc", ct.c_float), ("low_cut", ct.c_float), ("high_cut", ct.c_float), ("dt_ms", ct.c_float),
-                ("min_rel_thick", ct.c_float), ("cond_threshold", ct.c_double)]
+                ("min_rel_thick", ct.c_float), ("cond_threshold", ct.c_double), ("corr_grad_i", ct.c_float),
+                ("corr_grad_j", ct.c_float)]
 
 
 class HostInversion:
@@ -511,7 +525,7 @@ class HostInversion:
                       np.ascontiguousarray(sc.sigma0, np.float64).reshape(9),
                       np.ascontiguousarray(sc.corr_xy, np.float32), np.ascontiguousarray(sc.circ_corr_t, np.float32)]
         m = _InvModel(sc.ntheta, *[a.ctypes.data for a in self._arrs], sc.wnc, sc.low_cut, sc.high_cut, sc.dt_ms,
-                      sc.min_rel_thick, cond_threshold)
+                      sc.min_rel_thick, cond_threshold, *corr_grad(sc))
         h = ct.c_void_p()
         check(lib().cg_inversion_create(ct.byref(h), sc.nx, sc.ny, sc.nz, sc.nxp, sc.nyp, sc.nzp, ct.byref(m)),
               "cg_inversion_create")
@@ -584,7 +598,7 @@ class Batch:
                     np.ascontiguousarray(sc.corr_xy, np.float32), np.ascontiguousarray(sc.circ_corr_t, np.float32)]
             self._keep.append(arrs)
             m = _InvModel(sc.ntheta, *[a.ctypes.data for a in arrs], sc.wnc, sc.low_cut, sc.high_cut, sc.dt_ms,
-                          sc.min_rel_thick, cond_threshold)
+                          sc.min_rel_thick, cond_threshold, *corr_grad(sc))
             cubes[i] = _BatchCube(sc.nx, sc.ny, sc.nz, sc.nxp, sc.nyp, sc.nzp, m)
         h = ct.c_void_p()
         check(lib().cg_batch_create(ct.byref(h), ct.cast(cubes, ct.c_void_p), len(self.scs), nstreams),

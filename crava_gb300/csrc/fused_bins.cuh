@@ -44,6 +44,10 @@ struct FusedArgs {
   const float2 *ct;       // nzp/2+1
   const double2 *cxy_d;   // FP64 tables (FP64 mode)
   const double2 *ct_d;
+  // per-bin (s, lam) table of a prior with nonzero correlation gradients
+  // (cg_prior_spectra_grad), bin order; null for the separable prior
+  const float2 *sl;
+  const double2 *sl_d;
   const KTab<T> *ktab;
   T sig0[6];
   int cnxp, nyp, nzp, plane;
@@ -56,9 +60,25 @@ struct FusedArgs {
 };
 
 // prior scale s = |Re(Cxy Ct)| and error eigenvalue lam = |Re Cxy| of one bin
-template <typename T>
+// (separable prior); TAB: s = |Re P|, lam = |Re E| read from the per-bin
+// table of a prior made non-separable by correlation gradients (a separate
+// instantiation, so the separable kernels carry no table code)
+template <typename T, bool TAB = false>
 __device__ __forceinline__ void bin_scales(const FusedArgs<T> &a, int ij, int k, T &s, T &lam)
 {
+  if constexpr (TAB) {
+    const long b = (long)k * a.plane + ij;
+    if (sizeof(T) == 8 && a.sl_d) {
+      const double2 v = a.sl_d[b];
+      s = (T)v.x;
+      lam = (T)v.y;
+    } else {
+      const float2 v = __ldg(&a.sl[b]);
+      s = (T)v.x;
+      lam = (T)v.y;
+    }
+    return;
+  }
   const int cnzp = a.nzp / 2 + 1;
   if (sizeof(T) == 8) {
     const double2 cx = a.cxy_d[ij];

@@ -69,9 +69,11 @@ int cg::invert_cubes_fused(cg_workspace w, float *const *data, float *const *mea
   for (int p = 0; p < 3; p++) { if (!mean[p]) { set_error("null mean[%d]", p); return CG_ERR_ARG; } fwd[nt + p] = mean[p]; }
   for (int t = 0; t < 6; t++) if (!cov[t]) { set_error("null cov[%d]", t); return CG_ERR_ARG; }
   const int zc = cg_tune_get(CG_TUNE_FUSED_Y, nyp);
-  if (zc == 2 && ysplit_fits(w)) return invert_cubes_ysplit(w, data, mean, cov, precision, st, bins_done);
+  // the y-fused and y-split kernels take the separable prior only; a per-bin prior table (correlation
+  // gradients) goes through the stand-alone bin kernels
+  if (zc == 2 && ysplit_fits(w) && !w->sl_on) return invert_cubes_ysplit(w, data, mean, cov, precision, st, bins_done);
   if (zc >= 4 && nt + 3 <= kMaxBatch) return chunked_y(w, data, mean, cov, precision, zc, st, bins_done);
-  if (!ybin_length(nyp)) {
+  if (!ybin_length(nyp) || w->sl_on) {
     // no fused kernel for this y length: three-pass transforms around the bin kernel
     if ((rc = fft3d<float>(fwd, nt + 3, nxp, nyp, nzp, CG_DATA, true, st))) return rc;
     if ((rc = cg_invert_bins_fused(w, data, mean, cov, precision, stream))) return rc;

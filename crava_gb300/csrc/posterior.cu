@@ -26,6 +26,7 @@
 
 #include "common.cuh"
 #include "fft.cuh"
+#include "fill.cuh"
 #include "posterior.cuh"
 #include "fused_bins.cuh"
 #include "linalg.cuh"
@@ -113,12 +114,12 @@ __global__ void __launch_bounds__(128) k_invert_plain(const __grid_constant__ Pl
 }
 
 // one bin of k_invert_fused (plane k, bin ij of the plane)
-template <typename T, int NT, int MODE>
+template <typename T, int NT, int MODE, bool TAB>
 __device__ __forceinline__ void fused_bin(const FusedArgs<T> &a, const KTab<T> &kt, int k, int ij)
 {
   const long b = (long)k * a.plane + ij;
   T s, lam;
-  bin_scales<T>(a, ij, k, s, lam);
+  bin_scales<T, TAB>(a, ij, k, s, lam);
   if (!kt.band) {
     write_prior_cov<T>(a, b, s);
     return;
@@ -166,7 +167,7 @@ __device__ __forceinline__ void fused_bin(const FusedArgs<T> &a, const KTab<T> &
 // resident-CTA target handed to the register allocator (1 = unconstrained,
 // 6 = at most 85 registers).  A CTA solves nruns runs of blockDim.x bins of
 // one plane, so the per-k table is staged once for all of them.
-template <typename T, int NT, int MODE, int MINB = 1>
+template <typename T, int NT, int MODE, int MINB = 1, bool TAB = false>
 __global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a, int nruns)
 {
   __shared__ KTab<T> kt;
@@ -181,7 +182,7 @@ __global__ void __launch_bounds__(128, MINB) k_invert_fused(FusedArgs<T> a, int 
   for (int r = 0; r < nruns; r++) {
     const int ij = (blockIdx.x * nruns + r) * blockDim.x + threadIdx.x;
     if (ij >= a.plane) return;
-    fused_bin<T, NT, MODE>(a, kt, k, ij);
+    fused_bin<T, NT, MODE, TAB>(a, kt, k, ij);
   }
 }
 
@@ -196,12 +197,12 @@ struct InfoArgs {
 };
 
 // one bin of k_invert_info (plane k, bin ij of the plane)
-template <int NT, int MODE>
+template <int NT, int MODE, bool TAB>
 __device__ __forceinline__ void info_bin(const FusedArgs<float> &a, const ITab &it, const InfoArgs &ia, int k, int ij)
 {
   const long b = (long)k * a.plane + ij;
   float s, lam;
-  bin_scales<float>(a, ij, k, s, lam);
+  bin_scales<float, TAB>(a, ij, k, s, lam);
   if (!it.band) {
     write_prior_cov<float>(a, b, s);
     return;
@@ -336,7 +337,7 @@ __device__ __forceinline__ void info_bin(const FusedArgs<float> &a, const ITab &
 __host__ __device__ constexpr int info_threads(int minb) { return minb == 6 ? 256 : 128; }
 constexpr int kInfoBlocks = 8;
 
-template <int NT, int MODE, int MINB>
+template <int NT, int MODE, int MINB, bool TAB = false>
 __global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(MINB))
     k_invert_info(FusedArgs<float> a, const ITab *__restrict__ itab, InfoArgs ia, int nruns)
 {
@@ -352,7 +353,7 @@ __global__ void __launch_bounds__(info_threads(MINB), MINB * 128 / info_threads(
   for (int r = 0; r < nruns; r++) {
     const int ij = (blockIdx.x * nruns + r) * blockDim.x + threadIdx.x;
     if (ij >= a.plane) return;
-    info_bin<NT, MODE>(a, it, ia, k, ij);
+    info_bin<NT, MODE, TAB>(a, it, ia, k, ij);
   }
 }
 
@@ -361,7 +362,7 @@ struct S0Args {
 };
 
 // FP64 redo of the bins the MIXED pass queued.
-template <int NT>
+template <int NT, bool TAB = false>
 __global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, const KTab<double> *__restrict__ ktd,
                                                         S0Args s0)
 {
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(128) k_invert_fixup64(FusedArgs<float> a, cons
     const int ij = (int)(b - (long)k * a.plane);
     const KTab<double> &kt = ktd[k];
     float sf, lamf;
-    bin_scales<float>(a, ij, k, sf, lamf);
+    bin_scales<float, TAB>(a, ij, k, sf, lamf);
     const double s = sf, lam = lamf;
     double2 d[NT], mu[3], cov[6], L[NT * (NT + 1) / 2];
 #pragma unroll
@@ -479,7 +480,7 @@ extern "C" void cg_workspace_destroy(cg_workspace w)
 {
   if (!w) return;
   void *ptrs[] = {w->ktab_f, w->ktab_d, w->model_dev, w->cxy_f, w->ct_f, w->cxy_d, w->ct_d, w->queue, w->counters,
-                  w->itab};
+                  w->itab, w->sl_f, w->sl_d};
   if (w->model_copied) {
     cudaEventSynchronize(w->model_copied);
     cudaEventDestroy(w->model_copied);
@@ -704,11 +705,85 @@ extern "C" int cg_prior_spectra(cg_workspace w, const float *corr_xy, const floa
   if (rc) return rc;
   if (!corr_xy || !circ_corr_t) { set_error("null correlation input"); return CG_ERR_ARG; }
   cudaStream_t st = (cudaStream_t)stream;
+  w->sl_on = w->sl_d_on = false;
   if (precision == CG_PREC_FP64) {
     rc = prior_tables<double>(w, corr_xy, circ_corr_t, w->cxy_d, w->ct_d, st);
     if (rc) return rc;
   }
   return prior_tables<float>(w, corr_xy, circ_corr_t, w->cxy_f, w->ct_f, st);
+}
+
+namespace cg {
+// (|Re P|, |Re E|) of every bin: the prior scale and error eigenvalue the bin
+// solve takes from the covariance and error-correlation spectra
+// (SeismicParametersHolder::getParameterCovariance keeps |Re| of the
+// covariance, src/seismicparametersholder.cpp:407-425); out may alias P
+template <typename T>
+__global__ void k_scale_table(const C2<T> *P, const C2<T> *E, C2<T> *out, long n)
+{
+  const long b = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= n) return;
+  const T re_p = P[b].x, re_e = E[b].x;
+  if constexpr (sizeof(T) == 4) out[b] = mk<T>(fabsf(re_p), fabsf(re_e));
+  else out[b] = mk<T>(fabs(re_p), fabs(re_e));
+}
+}  // namespace cg
+
+extern "C" int cg_prior_spectra_grad(cg_workspace w, const float *corr_xy, const float *circ_corr_t, float grad_i,
+                                     float grad_j, int precision, void *stream)
+{
+  int rc = check_ws(w);
+  if (rc) return rc;
+  if (grad_i == 0.0f && grad_j == 0.0f) return cg_prior_spectra(w, corr_xy, circ_corr_t, precision, stream);
+  if (!corr_xy || !circ_corr_t) { set_error("null correlation input"); return CG_ERR_ARG; }
+  if (!(std::isfinite(grad_i) && std::isfinite(grad_j))) { set_error("correlation gradients must be finite"); return CG_ERR_ARG; }
+  cudaStream_t st = (cudaStream_t)stream;
+  const int nxp = w->nxp, nyp = w->nyp, nzp = w->nzp;
+  const long csize = (long)(nxp / 2 + 1) * nyp * nzp;  // bins; a real cube is the same bytes as csize float2
+  w->sl_on = w->sl_d_on = false;
+  if (!w->sl_f) CG_CUDA(dev_malloc((void **)&w->sl_f, sizeof(float2) * csize));
+  if (precision == CG_PREC_FP64 && !w->sl_d) CG_CUDA(dev_malloc((void **)&w->sl_d, sizeof(double2) * csize));
+  float *P = (float *)w->sl_f, *E = nullptr;
+  CG_CUDA(scratch_alloc((void **)&E, sizeof(float2) * csize, st));
+  // the parameter-correlation cube (fillInParamCorr, unit scalar) in the table's own memory and the
+  // error-correlation cube (fillInErrCorr) beside it, both transformed as FFTCovGrids transforms covariances
+  rc = fill_param_corr<float>(P, nxp, nyp, nzp, corr_xy, circ_corr_t, grad_i, grad_j, 1.0f, st);
+  if (!rc) rc = fill_err_corr<float>(E, nxp, nyp, nzp, corr_xy, grad_i, grad_j, st);
+  if (!rc) {
+    void *b[2] = {P, E};
+    rc = fft3d<float>(b, 2, nxp, nyp, nzp, CG_COVARIANCE, true, st);
+  }
+  if (!rc) {
+    TraceScope ts("k_scale_table", st, 24.0 * csize);
+    k_scale_table<float><<<(unsigned)ceil_div(csize, 256), 256, 0, st>>>((const float2 *)P, (const float2 *)E,
+                                                                         (float2 *)P, csize);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = cuda_status(e, "k_scale_table");
+  }
+  if (!rc && precision == CG_PREC_FP64) {
+    // the same cubes filled and transformed in FP64
+    double *Pd = (double *)w->sl_d, *Ed = nullptr;
+    cudaError_t e = scratch_alloc((void **)&Ed, sizeof(double2) * csize, st);
+    if (e == cudaSuccess) {
+      rc = fill_param_corr<double>(Pd, nxp, nyp, nzp, corr_xy, circ_corr_t, grad_i, grad_j, 1.0, st);
+      if (!rc) rc = fill_err_corr<double>(Ed, nxp, nyp, nzp, corr_xy, grad_i, grad_j, st);
+      if (!rc) {
+        void *b[2] = {Pd, Ed};
+        rc = fft3d<double>(b, 2, nxp, nyp, nzp, CG_COVARIANCE, true, st);
+      }
+      if (!rc) k_scale_table<double><<<(unsigned)ceil_div(csize, 256), 256, 0, st>>>((const double2 *)Pd,
+                                                                                     (const double2 *)Ed,
+                                                                                     (double2 *)Pd, csize);
+      e = cudaGetLastError();
+      cudaFreeAsync(Ed, st);
+    }
+    if (!rc && e != cudaSuccess) rc = cuda_status(e, "FP64 scale table");
+  }
+  cudaFreeAsync(E, st);
+  if (rc) return rc;
+  w->sl_on = true;
+  w->sl_d_on = precision == CG_PREC_FP64;
+  return CG_OK;
 }
 
 // Occupancy variant of the FP32 fused kernels (tuning key CG_TUNE_BIN_MINB).
@@ -731,6 +806,8 @@ int fill_fused_args(Workspace *w, void *const *data, void *const *mean, void *co
   a.ct = (const float2 *)w->ct_f;
   a.cxy_d = (const double2 *)w->cxy_d;
   a.ct_d = (const double2 *)w->ct_d;
+  a.sl = w->sl_on ? (const float2 *)w->sl_f : nullptr;
+  a.sl_d = w->sl_on && w->sl_d_on ? (const double2 *)w->sl_d : nullptr;
   a.ktab = (const KTab<T> *)(sizeof(T) == 8 ? (const void *)w->ktab_d : (const void *)w->ktab_f);
   const int pq[6][2] = {{0, 0}, {1, 1}, {2, 2}, {0, 1}, {0, 2}, {1, 2}};
   for (int t = 0; t < 6; t++) a.sig0[t] = (T)w->sigma0f[pq[t][0] * 3 + pq[t][1]];
@@ -773,9 +850,11 @@ static void launch_info(const FusedArgs<float> &a, const Workspace *w, dim3 grid
   for (int q = 0; q < 6; q++) ia.s0i[q] = w->sig0inv[q];
   const int mb = cg_tune_get(CG_TUNE_BIN_MINB, NT);
   threads = info_threads(mb == 6 || mb == 5 ? mb : 4);
+  if (a.sl) threads = info_threads(4);  // the per-bin prior table has one build
   const int nruns = bin_runs(w, a.plane, threads, (int)grid.y);
   grid.x = ceil_div(a.plane, (long)threads * nruns);
-  if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
+  if (a.sl) k_invert_info<NT, MODE, 4, true><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
+  else if (mb == 6) k_invert_info<NT, MODE, 6><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
   else if (mb == 5) k_invert_info<NT, MODE, 5><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
   else k_invert_info<NT, MODE, 4><<<grid, threads, 0, st>>>(a, w->itab, ia, nruns);
 }
@@ -804,7 +883,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
     constexpr int NT = decltype(NTc)::value;
     if constexpr (sizeof(T) == 8) {
       TraceScope ts("k_invert_fused_fp64", st, fbytes);
-      k_invert_fused<T, NT, 2><<<fgrid, threads, 0, st>>>(a, fruns);
+      if (a.sl) k_invert_fused<T, NT, 2, 1, true><<<fgrid, threads, 0, st>>>(a, fruns);
+      else k_invert_fused<T, NT, 2><<<fgrid, threads, 0, st>>>(a, fruns);
     } else if (precision == CG_PREC_MIXED) {
       // the queue position counter starts at zero for every inversion (stream ordered); a z-chunk of a
       // chunked inversion appends to the queue and its fix-up starts where the chunk's entries start
@@ -816,7 +896,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
         launch_info<NT, 1>(a, w, grid, threads, st);
       } else {
         TraceScope ts("k_invert_fused_mixed", st, fbytes);
-        if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<fgrid, threads, 0, st>>>(a, fruns);
+        if (a.sl) k_invert_fused<T, NT, 1, 1, true><<<fgrid, threads, 0, st>>>(a, fruns);
+        else if (bin_minb(NT) == 6) k_invert_fused<T, NT, 1, 6><<<fgrid, threads, 0, st>>>(a, fruns);
         else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 1, 5><<<fgrid, threads, 0, st>>>(a, fruns);
         else if (bin_minb(NT) == 4) k_invert_fused<T, NT, 1, 4><<<fgrid, threads, 0, st>>>(a, fruns);
         else k_invert_fused<T, NT, 1, 1><<<fgrid, threads, 0, st>>>(a, fruns);
@@ -832,7 +913,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       // cube's (usually empty) fix-up does not hold hundreds of CTA slots beside other cubes' kernels
       const int fix_ctas = (int)std::min<long>((long)nsm * 4, std::max<long>(1, (long)a.plane * nk / 8192));
       TraceScope ts("k_invert_fixup64", st, 0.0);
-      k_invert_fixup64<NT><<<fix_ctas, 128, 0, st>>>(af, w->ktab_d, sd);
+      if (af.sl) k_invert_fixup64<NT, true><<<fix_ctas, 128, 0, st>>>(af, w->ktab_d, sd);
+      else k_invert_fixup64<NT><<<fix_ctas, 128, 0, st>>>(af, w->ktab_d, sd);
     } else if (use_info(w, NT)) {
       TraceScope ts("k_invert_info_fp32", st, fbytes);
       launch_info<NT, 0>(a, w, grid, threads, st);
@@ -840,7 +922,8 @@ static int fused_launch(Workspace *w, void *const *data, void *const *mean, void
       TraceScope ts("k_invert_fused_fp32", st, fbytes);
       // the FP32 mode spills more than MIXED under the 85-register cap (228 B against 128 B at five
       // stacks; 0.47 against 0.39 ms at 256^3): its tight setting is the 128-register build
-      if (bin_minb(NT) == 6 || bin_minb(NT) == 4) k_invert_fused<T, NT, 0, 4><<<fgrid, threads, 0, st>>>(a, fruns);
+      if (a.sl) k_invert_fused<T, NT, 0, 1, true><<<fgrid, threads, 0, st>>>(a, fruns);
+      else if (bin_minb(NT) == 6 || bin_minb(NT) == 4) k_invert_fused<T, NT, 0, 4><<<fgrid, threads, 0, st>>>(a, fruns);
       else if (bin_minb(NT) == 5) k_invert_fused<T, NT, 0, 5><<<fgrid, threads, 0, st>>>(a, fruns);
       else k_invert_fused<T, NT, 0, 1><<<fgrid, threads, 0, st>>>(a, fruns);
     }
@@ -891,6 +974,7 @@ namespace cg {
 // failed factorisations.
 template <int NT>
 __global__ void __launch_bounds__(128) k_cond_hist(const float2 *__restrict__ cxy, const float2 *__restrict__ ct,
+                                                   const float2 *__restrict__ sl,
                                                    const KTab<double> *__restrict__ ktd, const ITab *__restrict__ itab,
                                                    InfoArgs ia, int plane, int nzp, bool info,
                                                    unsigned long long *hist, int nb)
@@ -903,9 +987,17 @@ __global__ void __launch_bounds__(128) k_cond_hist(const float2 *__restrict__ cx
   const KTab<double> &kt = ktd[k];
   if (ij < plane && kt.band) {
     const int cnzp = nzp / 2 + 1;
-    const float2 cx = cxy[ij];
-    const float2 t = k < cnzp ? ct[k] : make_float2(ct[nzp - k].x, -ct[nzp - k].y);
-    const float sf = fabsf(cx.x * t.x - cx.y * t.y), lamf = fabsf(cx.x);
+    float sf, lamf;
+    if (sl) {
+      const float2 v = sl[(long)k * plane + ij];
+      sf = v.x;
+      lamf = v.y;
+    } else {
+      const float2 cx = cxy[ij];
+      const float2 t = k < cnzp ? ct[k] : make_float2(ct[nzp - k].x, -ct[nzp - k].y);
+      sf = fabsf(cx.x * t.x - cx.y * t.y);
+      lamf = fabsf(cx.x);
+    }
     {
       double2 L[NT * (NT + 1) / 2];
       double inv[NT], cond = 0.0;
@@ -972,7 +1064,8 @@ extern "C" int cg_condition_histogram(cg_workspace w, unsigned long long *hist_c
   if (e == cudaSuccess) {
     rc = dispatch_nt(w->ntheta, [&](auto NTc) -> int {
       constexpr int NT = decltype(NTc)::value;
-      k_cond_hist<NT><<<grid, 128, 0, st>>>((const float2 *)w->cxy_f, (const float2 *)w->ct_f, w->ktab_d, w->itab,
+      k_cond_hist<NT><<<grid, 128, 0, st>>>((const float2 *)w->cxy_f, (const float2 *)w->ct_f,
+                                            w->sl_on ? (const float2 *)w->sl_f : nullptr, w->ktab_d, w->itab,
                                             ia, plane, w->nzp, w->info_ok, d, nbuckets);
       return CG_OK;
     });

@@ -97,6 +97,11 @@ struct Workspace {
   float *ct_f;      // real staging 2*(nzp/2+1) -> complex nzp/2+1
   double *cxy_d;
   double *ct_d;
+  // per-bin (|Re P|, |Re E|) table of a prior with correlation gradients
+  // (cg_prior_spectra_grad), allocated on first use; used while sl_on
+  float2 *sl_f;
+  double2 *sl_d;
+  bool sl_on, sl_d_on;
   // mixed-precision fix-up queue and counters (device)
   int *queue;
   int queue_cap;

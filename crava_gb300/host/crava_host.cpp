@@ -221,9 +221,9 @@ int Crava::computePostMeanResidAndFFTCov(FFTGrid **seisData, FFTGrid *&postAlpha
     errCorr->setTransformedStatus(true);
     check(cg_invert_bins_plain(ws_, d, mu, cv, errCorr->devicePtr(), stream), "bin loop (plain)");
   } else {
-    if (m_.corrGradI != 0.0f || m_.corrGradJ != 0.0f)
-      throw Error(CG_ERR_UNSUPPORTED, "the fused form needs zero correlation gradients; use the plain form");
-    check(cg_prior_spectra(ws_, d_corr_xy_, d_circ_t_, CG_PREC_FP32, stream), "prior spectra");
+    // separable prior tables, or the per-bin table when the correlation gradients are nonzero
+    check(cg_prior_spectra_grad(ws_, d_corr_xy_, d_circ_t_, m_.corrGradI, m_.corrGradJ, CG_PREC_FP32, stream),
+          "prior spectra");
     // transforms, bin loop and inverse transforms of the means in one call (the y passes fused with the bins)
     check(cg::invert_cubes_fused(ws_, d, mu, cv, form == FUSED_MIXED ? CG_PREC_MIXED : CG_PREC_FP32, stream,
                                  (cudaEvent_t)binsDone),
@@ -309,6 +309,8 @@ extern "C" int cg_inversion_create(cg_inversion *out, int nx, int ny, int nz, in
     im.dt_ms = m->dt_ms;
     im.minRelThick = m->min_rel_thick > 0 ? m->min_rel_thick : 1.0f;
     im.condThreshold = m->cond_threshold;
+    im.corrGradI = m->corr_grad_i;
+    im.corrGradJ = m->corr_grad_j;
     cg_inversion_s *h = new cg_inversion_s();
     h->nx = nx; h->ny = ny; h->nz = nz; h->nxp = nxp; h->nyp = nyp; h->nzp = nzp; h->ntheta = m->ntheta;
     try {

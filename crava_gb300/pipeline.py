@@ -71,6 +71,7 @@ class Inversion:
         self.mean_in = torch.from_numpy(np.stack(sc.mean)).to(**f32)
         self.corr_xy = torch.from_numpy(np.ascontiguousarray(sc.corr_xy, dtype=np.float32)).to(**f32)
         self.circ_t = torch.from_numpy(np.ascontiguousarray(sc.circ_corr_t, dtype=np.float32)).to(**f32)
+        self.grad = api.corr_grad(sc)
         shape = tuple(self.data_in.shape[1:])
         self.data = [torch.empty(shape, **f32) for _ in range(n)]
         self.mean = [torch.empty(shape, **f32) for _ in range(3)]
@@ -80,10 +81,11 @@ class Inversion:
             self.err_in = torch.empty(shape, **f32)
             self.errcorr = torch.empty(shape, **f32)
             s = torch.cuda.current_stream()
+            gi, gj = self.grad
             for t, (p, q) in enumerate(COV_PAIRS):
-                api.check_call("cg_fill_param_corr", self.cov_in[t], nxp, nyp, nzp, self.corr_xy, self.circ_t, 0.0,
-                               0.0, float(np.float32(sc.sigma0[p, q])), s)
-            api.check_call("cg_fill_err_corr", self.err_in, nxp, nyp, nzp, self.corr_xy, 0.0, 0.0, s)
+                api.check_call("cg_fill_param_corr", self.cov_in[t], nxp, nyp, nzp, self.corr_xy, self.circ_t, gi,
+                               gj, float(np.float32(sc.sigma0[p, q])), s)
+            api.check_call("cg_fill_err_corr", self.err_in, nxp, nyp, nzp, self.corr_xy, gi, gj, s)
         if "fp64" in self.forms:
             f64 = dict(dtype=torch.float64, device=self.dev)
             self.data64 = [torch.empty(shape, **f64) for _ in range(n)]
@@ -137,17 +139,17 @@ class Inversion:
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
         elif form in ("fp32", "mixed"):
             prec = api.PREC_MIXED if form == "mixed" else api.PREC_FP32
-            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
+            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
             self.ws.invert_cubes(self.data, self.mean, self.cov, prec, stream=stream)
         elif form in ("fp32_3pass", "mixed_3pass"):
             prec = api.PREC_MIXED if form == "mixed_3pass" else api.PREC_FP32
-            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
+            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
             api.fft_in_place_batch(self.data, nxp, api.DATA, stream=stream)
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, stream=stream)
             self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=stream)
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
         elif form == "fp64":
-            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP64, stream=stream)
+            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP64, stream=stream, grad=self.grad)
             for d in self.data64:
                 api.fft_in_place(d, nxp, api.DATA, stream=stream)
             for m in self.mean64:
@@ -176,7 +178,7 @@ class Inversion:
                                      sc.min_rel_thick)
         self.ws.set_model(tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=self.cond_threshold,
                           stream=stream, asynchronous=True)
-        self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream)
+        self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
         self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=stream)
         api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
 

@@ -212,6 +212,7 @@ class Scenario:
     energy_threshold: float = 0.0             # FFTGrid::interpolateSeismic
     corr_t: np.ndarray | None = None          # the temporal correlation lags circ_corr_t was made from
     min_int_fq: int = 0                       # the lowest inverted frequency index of computeCircCorrT
+    corr_grad: tuple = (0.0, 0.0)             # (corrGradI, corrGradJ), ModelGeneral::getCorrGradIJ
 
     @property
     def ntheta(self):
@@ -304,7 +305,7 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
                   dx=25.0, dy=25.0, sn=4.0, stds=(0.10, 0.07, 0.05), corr=(0.7, 0.3, 0.3),
                   lateral_range=1000.0, temporal_range_ms=20.0, temporal_power=1.5, low_cut=5.0,
                   high_cut=55.0, wnc=0.1, notches_hz=(), std_scale=1.0, seed=20261203,
-                  keep_truth=False, pd_corr_xy=False) -> Scenario:
+                  keep_truth=False, pd_corr_xy=False, corr_grad=(0.0, 0.0)) -> Scenario:
     """Build one seeded scenario.  Sizes are log-domain (ln Vp, ln Vs, ln rho)."""
     rng = np.random.default_rng(seed)
     nxp = nxp or padded_size(nx, pad)
@@ -344,7 +345,8 @@ def make_scenario(nx, ny, nz, theta_deg, f_peak, *, nxp=None, nyp=None, nzp=None
     return Scenario(nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp, dt_ms=dt_ms, theta_deg=list(theta_deg),
                     A=A, wavelets=wav, corr_xy=cxy, circ_corr_t=cct, sigma0=sig0, err_theta_cov=etc,
                     data=data, mean=mean, wnc=wnc, low_cut=low_cut, high_cut=high_cut, sn=list(snr),
-                    truth=[t for t in truth] if keep_truth else None, corr_t=corr_t, min_int_fq=min_int_fq)
+                    truth=[t for t in truth] if keep_truth else None, corr_t=corr_t, min_int_fq=min_int_fq,
+                    corr_grad=(float(np.float32(corr_grad[0])), float(np.float32(corr_grad[1]))))
 
 
 # ----------------------------------------------------------------------------

@@ -462,6 +462,20 @@ int cg_invert_bins_plain(cg_workspace ws, float *const *data, float *const *mean
 int cg_prior_spectra(cg_workspace ws, const float *corr_xy, const float *circ_corr_t, int precision,
                      void *stream);
 
+/* The prior of the fused forms for any correlation gradients (corrGradI/J,
+ * ModelGeneral::getCorrGradIJ, src/modelgeneral.cpp:2400-2414).  Zero
+ * gradients: cg_prior_spectra.  Otherwise the correlation is no longer
+ * separable, so the parameter-correlation cube (FFTGrid::fillInParamCorr,
+ * src/fftgrid.cpp:1072-1119) and the error-correlation cube
+ * (FFTGrid::fillInErrCorr, src/fftgrid.cpp:1018-1070) are filled and
+ * transformed as FFTCovGrids transforms them, and every bin's prior scale
+ * |Re P| and error eigenvalue |Re E| are kept in a per-bin table (8 bytes per
+ * bin, 16 more for CG_PREC_FP64) that the fused bin kernels read in place of
+ * the separable factors.  The table stays in use until the next
+ * cg_prior_spectra / cg_prior_spectra_grad call. */
+int cg_prior_spectra_grad(cg_workspace ws, const float *corr_xy, const float *circ_corr_t, float grad_i,
+                          float grad_j, int precision, void *stream);
+
 /* Fused posterior: same data/mean in-out convention as the plain form; cov[6]
  * is output only.  precision CG_PREC_FP32 or CG_PREC_MIXED.  Needs
  * cg_prior_spectra first. */
@@ -533,6 +547,7 @@ typedef struct cg_inversion_model {
   const float *circ_corr_t;     /* [nzp] cyclic temporal correlation (computeCircCorrT) */
   float wnc, low_cut, high_cut, dt_ms, min_rel_thick;
   double cond_threshold;        /* CG_PREC_MIXED guard, <= 0 for the default */
+  float corr_grad_i, corr_grad_j; /* correlation gradients (ModelGeneral::getCorrGradIJ), 0 for none */
 } cg_inversion_model;
 
 int cg_inversion_create(cg_inversion *inv, int nx, int ny, int nz, int nxp, int nyp, int nzp,

@@ -59,7 +59,9 @@ def inversion(sc, corr_t, min_int_fq, f_peak, wavelets=None):
     with tempfile.TemporaryDirectory() as d:
         _params(d, nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=nxp, nyp=nyp, nzp=nzp, ntheta=n, ncorrt=len(corr_t),
                 min_int_fq=int(min_int_fq), dt=float(sc.dt_ms), fpeak=float(f_peak), low_cut=float(sc.low_cut),
-                high_cut=float(sc.high_cut), wnc=float(sc.wnc), given_wavelets=int(wavelets is not None))
+                high_cut=float(sc.high_cut), wnc=float(sc.wnc), given_wavelets=int(wavelets is not None),
+                grad_i=float(np.float32(getattr(sc, "corr_grad", (0.0, 0.0))[0])),
+                grad_j=float(np.float32(getattr(sc, "corr_grad", (0.0, 0.0))[1])))
         if wavelets is not None:
             _w(d, "wavelets_in.f32", wavelets, np.float32)
         _w(d, "theta.f32", sc.theta_deg, np.float32)

@@ -7,7 +7,8 @@
 //                               prior covariance cubes (SeismicParametersHolder::
 //                               initializeCorrelations: computeCircCorrT +
 //                               FFTGrid::fillInParamCorr), error correlation
-//                               (FFTGrid::fillInErrCorr), the data and prior-mean
+//                               (FFTGrid::fillInErrCorr; both with the correlation
+//                               gradients grad_i / grad_j, 0 when absent), the data and prior-mean
 //                               transforms (FFTGrid::fftInPlace), then
 //                               Crava::computePostMeanResidAndFFTCov itself
 //                               (src/crava.cpp:975-1285); afterwards the per-k
@@ -133,6 +134,7 @@ int cmd_inversion()
   const int ncorrt = (int)p["ncorrt"], min_int_fq = (int)p["min_int_fq"];
   const float dt = (float)p["dt"], fpeak = (float)p["fpeak"], low_cut = (float)p["low_cut"];
   const float high_cut = (float)p["high_cut"], wnc = (float)p["wnc"];
+  const float grad_i = (float)p["grad_i"], grad_j = (float)p["grad_j"];  // correlation gradients (0 if absent)
   const int cnxp = nxp / 2 + 1, rnxp = 2 * cnxp;
   const size_t rsize = (size_t)rnxp * nyp * nzp;
 
@@ -189,7 +191,7 @@ int cmd_inversion()
   for (int a = 0; a < 3; a++)
     for (int b = 0; b < 3; b++) sp.priorVar0_(a, b) = static_cast<double>(s0[3 * a + b]);
   sp.createCorrGrids(nx, ny, nz, nxp, nyp, nzp, false);
-  sp.initializeCorrelations(&corr_xy, corrT, 0.0f, 0.0f, min_int_fq, nzp);
+  sp.initializeCorrelations(&corr_xy, corrT, grad_i, grad_j, min_int_fq, nzp);
   fftw_real *circ = sp.computeCircCorrT(corrT, min_int_fq, nzp);
   write_raw("circcorrt.f32", circ, sizeof(float) * nzp);
   fftw_free(circ);
@@ -201,7 +203,7 @@ int cmd_inversion()
   }
 
   FFTGrid *errcorr = make_grid(nx, ny, nz, nxp, nyp, nzp, FFTGrid::COVARIANCE, NULL, false);
-  errcorr->fillInErrCorr(&corr_xy, 0.0f, 0.0f);
+  errcorr->fillInErrCorr(&corr_xy, grad_i, grad_j);
   dump_grid("errcorr_real.f32", errcorr);
 
   // data and prior means, transformed by the reference's own fftInPlace (src/crava.cpp:177-184)

@@ -82,11 +82,13 @@ def oracle_pipeline(O, sc, prec="d", nthreads=None, tables=None):
     data = [O.fft3d_r2c(d, sc.nxp, O.DATA, prec, nt) for d in sc.data]
     mean = [O.fft3d_r2c(m, sc.nxp, O.PARAMETER, prec, nt) for m in sc.mean]
     covs = []
+    gi, gj = getattr(sc, "corr_grad", (0.0, 0.0))
     for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]:
-        c = O.fill_param_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, sc.circ_corr_t, 0, 0,
+        c = O.fill_param_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, sc.circ_corr_t, gi, gj,
                               float(np.float32(sc.sigma0[p, q])), prec=prec)
         covs.append(O.fft3d_r2c(c, sc.nxp, O.COVARIANCE, prec, nt))
-    ec = O.fft3d_r2c(O.fill_err_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, prec=prec), sc.nxp, O.COVARIANCE, prec, nt)
+    ec = O.fft3d_r2c(O.fill_err_corr(sc.nxp, sc.nyp, sc.nzp, sc.corr_xy, gi, gj, prec=prec), sc.nxp, O.COVARIANCE,
+                     prec, nt)
     s0 = np.asarray(sc.sigma0, dtype=np.float64).astype(np.float32).astype(np.float64)
     res, mu, cov, nf = O.invert_bins(data, mean, covs, ec, tables, sc.err_theta_cov, s0, sc.wnc, prec=prec,
                                      nthreads=nt)

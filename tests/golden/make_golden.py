@@ -84,11 +84,20 @@ def inversion_case(name, sc, f_peak):
                wavelet_norms=r["wavelet_norms"],
                data_spec=np.stack(data), mean_spec=np.stack(mean), cov_spec=np.stack(covs), errcorr_spec=ec,
                out_resid=np.stack(res), out_mean=np.stack(mu), out_cov=np.stack(cov), out_mean_real=np.stack(post_real),
-               nfail=nfail, is4d=0,
+               nfail=nfail, is4d=0, corr_grad=np.array(getattr(sc, "corr_grad", (0.0, 0.0)), np.float32),
                crava_mean_real=r["out_mean_real"], crava_resid=r["out_resid"], crava_cov=r["out_cov"],
                **tab, **{k + "_nct": r[k + "_nct"] for k in NCT})
     np.savez_compressed(os.path.join(HERE, name), **out)
     return out
+
+
+def gradient_case(name):
+    """An inversion whose prior and error correlation carry nonzero correlation gradients (corrGradI/J): the
+    reference's fillInParamCorr / fillInErrCorr with the gradients and its bin loop on the resulting
+    non-separable spectra."""
+    sc = S.make_scenario(18, 14, 22, [0.0, 15.0, 30.0, 40.0], 25.0, nxp=24, nyp=18, nzp=28, sn=3.0,
+                         notches_hz=(2.0, 80.0), low_cut=1.0, high_cut=100.0, seed=6, corr_grad=(0.37, -0.21))
+    return inversion_case(name, sc, 25.0)
 
 
 def wavelet_case(name):
@@ -334,6 +343,8 @@ def main():
             interpolate_case("reference_interpolate.npz", 17)
         if "reference_divide.npz" in only:
             divide_case("reference_divide.npz", 18)
+        if "inversion_grad.npz" in only:
+            gradient_case("inversion_grad.npz")
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -357,6 +368,7 @@ def main():
     fill_in_data_case("reference_fillindata.npz", 16)
     interpolate_case("reference_interpolate.npz", 17)
     divide_case("reference_divide.npz", 18)
+    gradient_case("inversion_grad.npz")
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

@@ -17,7 +17,8 @@ def _ws_from_golden(g, cond_threshold=0.0):
     return ws
 
 
-@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz",
+                                  "inversion_grad.npz"])
 def test_plain_matches_reference_lib_matr(cuda, case):
     """Same input spectra as the reference run -> same posterior (FP32 vs FP32)."""
     g = golden(case)
@@ -39,17 +40,20 @@ def test_plain_matches_reference_lib_matr(cuda, case):
     assert ws.stats()["failed"] == int(g["nfail"])
 
 
-@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"])
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz",
+                                  "inversion_grad.npz"])
 @pytest.mark.parametrize("form", ["fp32", "mixed"])
 def test_fused_matches_fp64_oracle_on_reference_inputs(cuda, oracle, case, form):
-    """Fused kernel (prior regenerated from the separable spectra) vs the FP64 restatement."""
+    """Fused kernel (prior regenerated from the separable spectra, or from the per-bin table when the
+    correlation gradients are nonzero) vs the FP64 restatement."""
     from crava_gb300 import api
     g = golden(case)
     ws = _ws_from_golden(g)
     nxp, nyp, nzp = int(g["nxp"]), int(g["nyp"]), int(g["nzp"])
+    gi, gj = (float(x) for x in g["corr_grad"]) if "corr_grad" in g else (0.0, 0.0)
     corr_xy = torch.from_numpy(g["corr_xy"].astype(np.float32)).cuda()
     circ = torch.from_numpy(g["circ_corr_t"].astype(np.float32)).cuda()
-    ws.prior_spectra(corr_xy, circ, api.PREC_FP32)
+    ws.prior_spectra(corr_xy, circ, api.PREC_FP32, grad=(gi, gj))
     data = [to_cube(x) for x in g["data_spec"]]
     mean = [to_cube(x) for x in g["mean_spec"]]
     cov = [to_cube(np.zeros_like(x)) for x in g["cov_spec"]]
@@ -60,9 +64,11 @@ def test_fused_matches_fp64_oracle_on_reference_inputs(cuda, oracle, case, form)
     covs = []
     s0f = g["sigma0"].astype(np.float32).astype(np.float64)
     for (p, q) in [(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]:
-        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], 0, 0, float(s0f[p, q]), prec="d")
+        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], gi, gj, float(s0f[p, q]),
+                                   prec="d")
         covs.append(oracle.fft3d_r2c(c, nxp, oracle.COVARIANCE, "d"))
-    ec = oracle.fft3d_r2c(oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"], prec="d"), nxp, oracle.COVARIANCE, "d")
+    ec = oracle.fft3d_r2c(oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"], gi, gj, prec="d"), nxp,
+                          oracle.COVARIANCE, "d")
     tab = {k: g[k].astype(np.complex128) if g[k].dtype == np.complex64 else g[k] for k in ("K", "em1", "em2", "em3", "band")}
     tab["nxp"] = nxp
     r64, m64, c64, _ = oracle.invert_bins(list(g["data_spec"].astype(np.complex128)),
@@ -337,3 +343,73 @@ def test_condition_histogram_counts_every_inband_bin(cuda):
     assert hi2 == hi
     fl = inv2.ws.stats()["flagged"]
     assert sum(hi[2:]) <= fl <= sum(hi[1:])  # above the threshold of 10 (decade 1 holds 10 itself)
+
+
+# nonzero correlation gradients: the prior is no longer separable (fillInParamCorr's shifted temporal
+# correlation); the fused forms read the per-bin table of cg_prior_spectra_grad
+@pytest.mark.parametrize("dims", [(40, 36, 48), (36, 128, 40)])
+@pytest.mark.parametrize("form", ["plain", "fp32", "mixed", "fp64", "mixed_3pass"])
+def test_correlation_gradients_match_fp64_oracle(cuda, oracle, dims, form):
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    grad = (0.37, -0.21)
+    sc = S.scaled_config1(*dims, seed=23, corr_grad=grad)
+    inv = Inversion(sc, forms=(form,))
+    inv.restore(form)
+    inv.run(form)
+    torch.cuda.synchronize()
+    pm, res, cov = inv.results(form)
+    post64, res64, cov64, _ = oracle_pipeline(oracle, sc, "d", tables=inv.tables)
+    prior = np.stack([m[:, :, :sc.nxp] for m in sc.mean]).astype(np.float64)
+    e = (rel(pm, post64), rel(pm - prior, post64 - prior), rel(res, res64), rel(cov, cov64))
+    print(dims, form, "gradients", grad, "vs FP64 oracle (mean, update, resid, cov):", e)
+    tol = 1e-10 if form == "fp64" else 1e-4
+    assert e[0] < (1e-12 if form == "fp64" else 1e-6)
+    assert e[1] < tol and e[2] < tol and e[3] < tol
+    # the gradients change the answer: the separable (zero-gradient) prior is far from the oracle's
+    sc0 = S.scaled_config1(*dims, seed=23)
+    post0, _, cov0, _ = oracle_pipeline(oracle, sc0, "d", tables=inv.tables)
+    assert rel(post0 - prior, post64 - prior) > 1e-2 and rel(cov0, cov64) > 1e-2
+
+
+def test_correlation_gradients_through_host_context(cuda):
+    """The C++ host layer (cg_inversion_*) takes the gradients from its model struct and gives the
+    pipeline's fused mixed answer bit for bit."""
+    from crava_gb300 import api, synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.scaled_config1(40, 128, 48, seed=24, corr_grad=(-0.3, 0.45))
+    inv = Inversion(sc, forms=("mixed",))
+    inv.restore("mixed")
+    inv.run("mixed")
+    torch.cuda.synchronize()
+    pm, res, cov = inv.results("mixed")
+    h = api.HostInversion(sc)
+    data = [d.copy() for d in sc.data]
+    mean = [m.copy() for m in sc.mean]
+    cv = [np.zeros_like(sc.data[0]) for _ in range(6)]
+    h.run(data, mean, cv, form="mixed")
+    assert np.array_equal(np.stack([m[:, :, :sc.nxp] for m in mean]), pm)
+    assert np.array_equal(np.stack([d.view(np.complex64) for d in data]), res)
+    assert np.array_equal(np.stack([c.view(np.complex64) for c in cv]), cov)
+
+
+@pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_grad.npz"])
+def test_correlation_fills_bit_exact_vs_reference(cuda, case):
+    """cg_fill_param_corr / cg_fill_err_corr against the cubes the reference's fillInParamCorr (times
+    priorVar0) and fillInErrCorr wrote, with zero and nonzero correlation gradients."""
+    from crava_gb300 import api
+    g = golden(case)
+    nxp, nyp, nzp = int(g["nxp"]), int(g["nyp"]), int(g["nzp"])
+    gi, gj = (float(x) for x in g["corr_grad"]) if "corr_grad" in g else (0.0, 0.0)
+    corr_xy = torch.from_numpy(g["corr_xy"].astype(np.float32)).cuda()
+    circ = torch.from_numpy(g["circ_corr_t"].astype(np.float32)).cuda()
+    s0f = g["sigma0"].astype(np.float32)
+    buf = torch.empty(g["errcorr_real"].shape, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+    for t, (p, q) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
+        api.check_call("cg_fill_param_corr", buf, nxp, nyp, nzp, corr_xy, circ, gi, gj, float(s0f[p, q]), st)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(buf.cpu().numpy(), g["prior_cov_real"][t])
+    api.check_call("cg_fill_err_corr", buf, nxp, nyp, nzp, corr_xy, gi, gj, st)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(buf.cpu().numpy(), g["errcorr_real"])

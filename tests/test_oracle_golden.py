@@ -36,7 +36,7 @@ def test_fft_matches_reference_fftw(oracle, case):
 
 
 @pytest.mark.parametrize("case", ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz",
-                                  "inversion_4d_n4.npz"])
+                                  "inversion_4d_n4.npz", "inversion_grad.npz"])
 def test_bin_loop_bit_exact_vs_reference(oracle, case):
     """Same spectra in -> the FP32 restatement reproduces lib_matr bit for bit (3D and 4D branches)."""
     g = golden(case)

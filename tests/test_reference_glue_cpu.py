@@ -15,7 +15,7 @@ import pytest
 
 from conftest import golden, oracle_pipeline, rel
 
-CASES = ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"]
+CASES = ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz", "inversion_grad.npz"]
 TABLES = ("K", "em1", "em2", "em3")
 
 
@@ -27,7 +27,8 @@ def _scenario(g):
                       wavelets=g["wavelets"], corr_xy=g["corr_xy"], circ_corr_t=g["circ_corr_t"],
                       sigma0=g["sigma0"], err_theta_cov=g["err_theta_cov"], data=list(g["data_real"]),
                       mean=list(g["mean_real"]), wnc=float(g["wnc"]), low_cut=float(g["low_cut"]),
-                      high_cut=float(g["high_cut"]))
+                      high_cut=float(g["high_cut"]),
+                      corr_grad=tuple(float(x) for x in g["corr_grad"]) if "corr_grad" in g else (0.0, 0.0))
 
 
 def test_ricker_wavelets_match_reference():
@@ -59,15 +60,21 @@ def test_circ_corr_t_matches_reference(oracle):
 
 @pytest.mark.parametrize("case", CASES)
 def test_prior_and_error_correlation_fills_bit_exact(oracle, case):
-    """FFTGrid::fillInParamCorr x priorVar0 (initializeCorrelations) and fillInErrCorr."""
+    """FFTGrid::fillInParamCorr x priorVar0 (initializeCorrelations) and fillInErrCorr, with the fixture's
+    correlation gradients (nonzero in inversion_grad.npz, where the error correlation's |lag| < 1 window
+    depends on the last bit of the float lag)."""
     g = golden(case)
     nxp, nyp, nzp = int(g["nxp"]), int(g["nyp"]), int(g["nzp"])
+    gi, gj = (float(x) for x in g["corr_grad"]) if "corr_grad" in g else (0.0, 0.0)
     s0 = np.asarray(g["sigma0"]).astype(np.float32)
     for t, (p, q) in enumerate([(0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2)]):
-        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], 0, 0, float(s0[p, q]))
+        c = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], gi, gj, float(s0[p, q]))
         np.testing.assert_array_equal(c[..., :nxp], g["prior_cov_real"][t][..., :nxp])
-    e = oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"])
+    e = oracle.fill_err_corr(nxp, nyp, nzp, g["corr_xy"], gi, gj)
     np.testing.assert_array_equal(e[..., :nxp], g["errcorr_real"][..., :nxp])
+    if gi or gj:  # the gradients matter: the separable fill differs
+        c0 = oracle.fill_param_corr(nxp, nyp, nzp, g["corr_xy"], g["circ_corr_t"], 0, 0, float(s0[0, 0]))
+        assert not np.array_equal(c0[..., :nxp], g["prior_cov_real"][0][..., :nxp])
 
 
 @pytest.mark.parametrize("case", CASES)

@@ -15,7 +15,7 @@ from conftest import from_cube, golden, rel, to_cube
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz"]
+CASES = ["inversion_c0small.npz", "inversion_c1small.npz", "inversion_n8odd.npz", "inversion_grad.npz"]
 
 
 def _scenario(g):
@@ -25,7 +25,8 @@ def _scenario(g):
                       wavelets=g["wavelets"], corr_xy=g["corr_xy"], circ_corr_t=g["circ_corr_t"],
                       sigma0=g["sigma0"], err_theta_cov=g["err_theta_cov"], data=list(g["data_real"]),
                       mean=list(g["mean_real"]), wnc=float(g["wnc"]), low_cut=float(g["low_cut"]),
-                      high_cut=float(g["high_cut"]))
+                      high_cut=float(g["high_cut"]),
+                      corr_grad=tuple(float(x) for x in g["corr_grad"]) if "corr_grad" in g else (0.0, 0.0))
 
 
 @pytest.mark.parametrize("case", CASES)
