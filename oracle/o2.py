@@ -213,7 +213,8 @@ def divide_scale_wavelet(sc, corr_t, min_int_fq, f_peak, thick_nodes, shift, gai
         wav = _r(d, "wavelets.f32", np.float32, (n, nzp))
         gn = _r(d, "gain_normalised.f32", np.float32, (n, sc.ny, sc.nx))
         ctf = _r(d, "corrt_filtered.f32", np.float32)
-    return out, rel, lz, wav, gn, ctf
+        mult = [_r(d, f"mult{l}.f32", np.float32, shp) for l in range(n)]
+    return out, rel, lz, wav, gn, ctf, mult
 
 
 def interpolate_seismic(cube, nx, ny, nz, nxp, threshold):

@@ -22,7 +22,8 @@
 //                               (src/crava.cpp:2261-2569) on given cubes and scales.
 //   crava_o2 fillindata <dir>   FFTGrid::fillInData from a STORM grid onto a simbox.
 //   crava_o2 interpolate <dir>  FFTGrid::interpolateSeismic on a DATA cube.
-//   crava_o2 divide     <dir>   Crava::divideDataByScaleWavelet on a simbox of non-constant thickness.
+//   crava_o2 divide     <dir>   Crava::divideDataByScaleWavelet on a simbox of non-constant thickness,
+//                               then Crava::multiplyDataByScaleWaveletAndWriteToFile on the result.
 //   crava_o2 crava_write / crava_read <dir>
 //                               FFTGrid::writeCravaFile / readCravaFile.
 //   crava_o2 storm_write / storm_read <dir>
@@ -656,6 +657,18 @@ int cmd_divide()
   write_raw("gain_normalised.f32", &gain[0], sizeof(float) * gain.size());
   crava->divideDataByScaleWavelet(sp);
   for (int l = 0; l < n; l++) dump_grid("out" + NRLib::ToString(l) + ".f32", crava->seisData_[l]);
+  // the inverse step, as it runs on the residuals before they are written: the divided cubes are
+  // transformed (the state the bin loop leaves them in) and handed to
+  // Crava::multiplyDataByScaleWaveletAndWriteToFile (src/crava.cpp:906-968); with no output format set
+  // (FFTGrid::formatFlag_ = 0) its writeFile writes nothing
+  for (int l = 0; l < n; l++) {
+    crava->seisData_[l]->setAccessMode(FFTGrid::RANDOMACCESS);
+    crava->seisData_[l]->fftInPlace();
+    crava->seisData_[l]->endAccess();
+  }
+  FFTGrid::formatFlag_ = 0;
+  crava->multiplyDataByScaleWaveletAndWriteToFile("residuals");
+  for (int l = 0; l < n; l++) dump_grid("mult" + NRLib::ToString(l) + ".f32", crava->seisData_[l]);
   return 0;
 }
 

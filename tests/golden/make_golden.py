@@ -298,7 +298,8 @@ def interpolate_case(name, seed):
 def divide_case(name, seed):
     """Crava::divideDataByScaleWavelet by the reference's own code (crava_o2): 3 stacks over a simbox whose
     relative thickness varies from 0.7 to 1 (a bottom surface on 4 x 3 nodes), local wavelet shifts of up to 4 ms
-    and gains 0.85-1.2, two dead traces, energy threshold 0 (interpolateSeismic after the division)."""
+    and gains 0.85-1.2, two dead traces, energy threshold 0 (interpolateSeismic after the division); then the
+    reference's multiplyDataByScaleWaveletAndWriteToFile on the divided cubes (mult)."""
     sc = S.make_scenario(14, 10, 30, [10.0, 20.0, 30.0], 30.0, nxp=18, nyp=14, nzp=40, seed=seed)
     rng = np.random.default_rng(seed)
     data = [d.copy() for d in sc.data]
@@ -310,12 +311,13 @@ def divide_case(name, seed):
     thick = np.array([[1.0, 0.9, 0.8, 0.85], [0.95, 0.75, 0.7, 0.8], [0.9, 0.85, 0.9, 1.0]])
     shift = rng.uniform(-4.0, 4.0, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
     gain = rng.uniform(0.85, 1.2, (sc.ntheta, sc.ny, sc.nx)).astype(np.float32)
-    out, rel, lz, wav, gn, ctf = o2.divide_scale_wavelet(sc, sc.corr_t, sc.min_int_fq, 30.0, thick, shift, gain, 0.0)
+    out, rel, lz, wav, gn, ctf, mult = o2.divide_scale_wavelet(sc, sc.corr_t, sc.min_int_fq, 30.0, thick, shift, gain,
+                                                               0.0)
     np.savez_compressed(os.path.join(HERE, name), nx=sc.nx, ny=sc.ny, nz=sc.nz, nxp=sc.nxp, nyp=sc.nyp, nzp=sc.nzp,
                         dt_ms=sc.dt_ms, low_cut=sc.low_cut, high_cut=sc.high_cut, wnc=sc.wnc, A=sc.A,
                         sigma0=sc.sigma0, err_theta_cov=sc.err_theta_cov, data=np.stack(data), shift=shift,
                         gain=gain, gain_normalised=gn, rel_thick=rel, lz=lz, wavelets=wav, corr_t_filtered=ctf,
-                        out=np.stack(out))
+                        out=np.stack(out), mult=np.stack(mult))
 
 
 def simulation_case(name, inv, seed):

@@ -303,3 +303,19 @@ def test_scale_wavelet_division_matches_reference(oracle):
         assert nbad == 2
         ref = g["out"][l]
         assert rel(d[..., :nxp], ref[..., :nxp]) < 1e-6, l
+
+
+def test_scale_wavelet_multiply_matches_reference(oracle):
+    """Crava::multiplyDataByScaleWaveletAndWriteToFile (src/crava.cpp:906-968) run by the reference's own code
+    (crava_o2) on its divided cubes after their forward transform (the state the bin loop leaves the residuals
+    in): the oracle's per-trace product on the divided cubes against the reference's result.  The reference
+    round-trips each cube through its 3D transforms first and transforms its global wavelet back and forth
+    once per trace (createLocalWavelet1D, getCAmp), so the two agree to FP32 rounding of those steps."""
+    g = golden("reference_divide.npz")
+    nx, ny, nxp = (int(g[k]) for k in ("nx", "ny", "nxp"))
+    for l in range(len(g["A"])):
+        m = oracle.multiply_scale_wavelet(g["out"][l], nx, ny, g["wavelets"][l], float(g["dt_ms"]), g["rel_thick"],
+                                          g["shift"][l], g["gain_normalised"][l], prec="f")
+        e = rel(m[..., :nxp], g["mult"][l][..., :nxp])
+        print("multiply, angle", l, "oracle vs reference:", e)
+        assert e < 2e-6, l

@@ -158,3 +158,24 @@ def test_gpu_scale_wavelet_division_matches_reference(cuda):
         e = rel(c.cpu().numpy()[..., :nxp], g["out"][l][..., :nxp])
         print("scale-wavelet division, angle", l, "GPU vs reference:", e)
         assert e < 2e-5
+
+
+def test_gpu_scale_wavelet_multiply_matches_reference(cuda):
+    """cg_multiply_by_scale_wavelet on the reference's divided cubes against the reference's own
+    multiplyDataByScaleWaveletAndWriteToFile product (crava_o2, the same cubes after their forward transform)."""
+    from crava_gb300 import api
+    g = golden("reference_divide.npz")
+    nx, ny, nz, nxp = (int(g[k]) for k in ("nx", "ny", "nz", "nxp"))
+    dt, lz = float(g["dt_ms"]), float(g["lz"])
+    s0 = np.asarray(g["sigma0"]).astype(np.float32).astype(np.float64)
+    tab = api.scale_wavelet_tables(g["wavelets"], g["A"], s0, g["corr_t_filtered"], g["err_theta_cov"], nz, dt, lz,
+                                   float(g["low_cut"]), float(g["high_cut"]), float(g["wnc"]))
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).cuda()  # noqa: E731
+    cubes = [dev(x) for x in g["out"]]
+    api.multiply_by_scale_wavelet(cubes, nx, ny, nxp, dev(tab), dev(g["rel_thick"]), dt, shift=dev(g["shift"]),
+                                  gain=dev(g["gain_normalised"]))
+    torch.cuda.synchronize()
+    for l, c in enumerate(cubes):
+        e = rel(c.cpu().numpy()[..., :nxp], g["mult"][l][..., :nxp])
+        print("scale-wavelet multiply, angle", l, "GPU vs reference:", e)
+        assert e < 2e-5
