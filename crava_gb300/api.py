@@ -587,7 +587,7 @@ class _BatchCube(ct.Structure):
 class Batch:
     """Many independent inversions of uneven cubes as one unit of GPU work (cg_batch_*)."""
 
-    def __init__(self, scenarios, nstreams=8, cond_threshold=0.0):
+    def __init__(self, scenarios, nstreams=3, cond_threshold=0.0):
         self.scs = list(scenarios)
         self._keep = []
         cubes = (_BatchCube * len(self.scs))()

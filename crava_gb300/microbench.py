@@ -165,7 +165,7 @@ def _traced(fn):
     return tr
 
 
-def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=8, peak=None, flush=None):
+def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=3, peak=None, flush=None):
     """The uneven-cube batch (cg_batch_run, graph replay) timed with CUDA events; the batch's own inputs
     are restored (cg_batch_reset) before each repetition, outside the timed region.  Per-kernel shares
     from one eager (not graph-replayed) single-stream run under the launch tracer."""
@@ -421,7 +421,7 @@ def main():
     ap.add_argument("--nreal", type=int, default=128)
     ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
-    ap.add_argument("--streams", type=int, default=8)
+    ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--nxp", type=int, default=256)
     ap.add_argument("--nyp", type=int, default=256)
     ap.add_argument("--nzp", type=int, default=64)

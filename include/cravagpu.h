@@ -594,7 +594,9 @@ typedef struct cg_batch_cube {
   cg_inversion_model model;     /* host arrays, read during cg_batch_create only */
 } cg_batch_cube;
 
-/* Allocates every cube's device grids, pristine input copies and model. */
+/* Allocates every cube's device grids, pristine input copies and model.
+ * nstreams: concurrent cube streams; on GB300 two or three were fastest for
+ * 64 uneven cubes (13.3 ms against 14.9 ms with eight and 14.8 ms with one). */
 int cg_batch_create(cg_batch *batch, const cg_batch_cube *cubes, int ncubes, int nstreams);
 void cg_batch_destroy(cg_batch batch);
 /* Upload cube i's real-domain inputs (host, rsize floats each) as its pristine copy. */
