@@ -191,6 +191,9 @@ def _declare(L):
         "cg_storm_write": ([ct.c_char_p, V, I, I, I, V], I),
         "cg_storm_read_header": ([ct.c_char_p, V, V, V, V], I),
         "cg_storm_read": ([ct.c_char_p, V, ct.c_long], I),
+        "cg_storm_surface_write": ([ct.c_char_p, V, I, I, ct.c_double, ct.c_double, ct.c_double, ct.c_double], I),
+        "cg_storm_surface_read_header": ([ct.c_char_p, V, V, V, V, V, V], I),
+        "cg_storm_surface_read": ([ct.c_char_p, V, ct.c_long], I),
         "cg_log_transform": ([V, ct.c_long, V], I),
         "cg_fft3d_c2r_exp_batch": ([PP, I, I, I, I, I, V], I),
         "cg_cov_origin": ([PP, I, I, I, I, V, V, V], I),

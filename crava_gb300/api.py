@@ -15,6 +15,7 @@ solve runs in libcravagpu.so.  Names follow the reference:
 from __future__ import annotations
 
 import ctypes as ct
+import os
 
 import numpy as np
 import torch
@@ -399,7 +400,41 @@ class StormHeader(ct.Structure):
     _fields_ = [("zone_number", ct.c_int), ("model_file", ct.c_char * 256), ("missing_code", ct.c_float),
                 ("variable", ct.c_char * 256), ("x_min", ct.c_double), ("lx", ct.c_double), ("y_min", ct.c_double),
                 ("ly", ct.c_double), ("z_top", ct.c_double), ("z_bot", ct.c_double), ("erosion_top", ct.c_double),
-                ("erosion_bot", ct.c_double), ("lz", ct.c_double), ("angle_deg", ct.c_double)]
+                ("erosion_bot", ct.c_double), ("lz", ct.c_double), ("angle_deg", ct.c_double),
+                ("z_top_file", ct.c_char * 256), ("z_bot_file", ct.c_char * 256),
+                ("erosion_top_file", ct.c_char * 256), ("erosion_bot_file", ct.c_char * 256)]
+
+
+# the four surfaces of a STORM grid: header field of the file name, suffix the reference gives the file
+STORM_SURFACES = (("z_top_file", "_top"), ("z_bot_file", "_bot"), ("erosion_top_file", "_erosion_top"),
+                  ("erosion_bot_file", "_erosion_bot"))
+
+
+class StormSurface:
+    """A regular surface (NRLib RegularSurface): z (nj, ni) float64, nodes over [x_min, x_min + lx] x
+    [y_min, y_min + ly]; -999 marks a missing node."""
+
+    def __init__(self, z, x_min, y_min, lx, ly):
+        self.z = np.ascontiguousarray(z, dtype=np.float64)
+        self.x_min, self.y_min, self.lx, self.ly = float(x_min), float(y_min), float(lx), float(ly)
+
+
+def write_storm_surface(path, surf: StormSurface):
+    """STORM binary surface file (cg_storm_surface_write)."""
+    nj, ni = surf.z.shape
+    check(lib().cg_storm_surface_write(str(path).encode(), surf.z.ctypes.data, ni, nj, surf.x_min, surf.y_min,
+                                       surf.lx, surf.ly), "cg_storm_surface_write")
+
+
+def read_storm_surface(path) -> StormSurface:
+    """STORM binary surface file (cg_storm_surface_read_header / cg_storm_surface_read)."""
+    ni, nj = ct.c_int(), ct.c_int()
+    g = [ct.c_double() for _ in range(4)]
+    check(lib().cg_storm_surface_read_header(str(path).encode(), ct.byref(ni), ct.byref(nj),
+                                             *[ct.byref(x) for x in g]), "cg_storm_surface_read_header")
+    z = np.empty((nj.value, ni.value), dtype=np.float64)
+    check(lib().cg_storm_surface_read(str(path).encode(), z.ctypes.data, z.size), "cg_storm_surface_read")
+    return StormSurface(z, *[x.value for x in g])
 
 
 def write_crava_file(path, cube: np.ndarray, geom, nx: int, ny: int):
@@ -424,15 +459,23 @@ def read_crava_file(path, nxp: int, nyp: int, nzp: int):
     return c, g, (int(n[0]), int(n[1]))
 
 
-def write_storm(path, values: np.ndarray, header: StormHeader):
-    """STORM binary grid; values (nk, nj, ni) float32 (i fastest)."""
+def write_storm(path, values: np.ndarray, header: StormHeader, surfaces=None):
+    """STORM binary grid; values (nk, nj, ni) float32 (i fastest).  surfaces: optional dict of StormSurface by
+    header field ("z_top_file", "z_bot_file", "erosion_top_file", "erosion_bot_file"); each is written beside
+    the grid as <path>_top, <path>_bot, ... and named in the header without its directory, as
+    StormContGrid::WriteToFile does by default (remove_path)."""
     v = np.ascontiguousarray(values, dtype=np.float32)
     nk, nj, ni = v.shape
+    for field, suffix in STORM_SURFACES:
+        if surfaces and field in surfaces:
+            write_storm_surface(str(path) + suffix, surfaces[field])
+            setattr(header, field, os.path.basename(str(path) + suffix).encode())
     check(lib().cg_storm_write(str(path).encode(), v.ctypes.data, ni, nj, nk, ct.byref(header)), "cg_storm_write")
 
 
 def read_storm(path):
-    """STORM binary grid with constant surfaces: (values (nk, nj, ni), StormHeader)."""
+    """STORM binary grid: (values (nk, nj, ni), StormHeader).  Surfaces given as files keep their names in the
+    header's *_file fields (read_storm_surfaces loads them)."""
     h = StormHeader()
     ni, nj, nk = ct.c_int(), ct.c_int(), ct.c_int()
     check(lib().cg_storm_read_header(str(path).encode(), ct.byref(h), ct.byref(ni), ct.byref(nj), ct.byref(nk)),
@@ -440,6 +483,17 @@ def read_storm(path):
     v = np.empty((nk.value, nj.value, ni.value), dtype=np.float32)
     check(lib().cg_storm_read(str(path).encode(), v.ctypes.data, v.size), "cg_storm_read")
     return v, h
+
+
+def read_storm_surfaces(path, header: StormHeader):
+    """The surface files a STORM grid's header names, resolved against the grid file's directory as
+    StormContGrid::ReadFromFile does (commonPath): dict of StormSurface by header field."""
+    out = {}
+    for field, _ in STORM_SURFACES:
+        name = getattr(header, field).decode()
+        if name:
+            out[field] = read_storm_surface(os.path.join(os.path.dirname(str(path)), name))
+    return out
 
 
 def exp_transform(t: torch.Tensor, stream=None):

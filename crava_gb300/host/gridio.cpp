@@ -184,6 +184,13 @@ extern "C" int cg_crava_file_read(const char *path, float *rvalue, int rnxp, int
   return CG_OK;
 }
 
+// a surface in the grid header: its file name when it has one, else the constant
+static std::string surf_token(const char *file, double z)
+{
+  const size_t n = strnlen(file, 256);
+  return n ? std::string(file, n) : g14(z);
+}
+
 extern "C" int cg_storm_write(const char *path, const float *values, int ni, int nj, int nk,
                               const cg_storm_header *hd)
 {
@@ -195,7 +202,8 @@ extern "C" int cg_storm_write(const char *path, const float *values, int ni, int
     << hd->zone_number << " " << hd->model_file << " " << g14((double)hd->missing_code) << "\n\n"
     << hd->variable << "\n\n"
     << g14(hd->x_min) << " " << g14(hd->lx) << " " << g14(hd->y_min) << " " << g14(hd->ly) << " "
-    << g14(hd->z_top) << " " << g14(hd->z_bot) << " " << g14(hd->erosion_top) << " " << g14(hd->erosion_bot)
+    << surf_token(hd->z_top_file, hd->z_top) << " " << surf_token(hd->z_bot_file, hd->z_bot) << " "
+    << surf_token(hd->erosion_top_file, hd->erosion_top) << " " << surf_token(hd->erosion_bot_file, hd->erosion_bot)
     << "\n" << g14(hd->lz) << " " << g14(hd->angle_deg) << "\n"
     << "\n" << ni << " " << nj << " " << nk << "\n";
   const std::string head = s.str();
@@ -226,12 +234,15 @@ static int storm_header(std::ifstream &f, const char *path, cg_storm_header *hd,
   {
     double *dst[10] = {&h.x_min, &h.lx, &h.y_min, &h.ly, &h.z_top, &h.z_bot, &h.erosion_top, &h.erosion_bot, &h.lz,
                        &h.angle_deg};
+    char *files[4] = {h.z_top_file, h.z_bot_file, h.erosion_top_file, h.erosion_bot_file};
     for (int q = 0; q < 10; q++) {
       if (!next_token(f, t)) goto bad;
       if (!parse_double(t, *dst[q])) {
-        if (q >= 4 && q < 8) {
-          cg::set_error("%s: surface %s given as a file; only constant surfaces are supported", path, t.c_str());
-          return CG_ERR_UNSUPPORTED;
+        // a surface given as a file (Volume::ReadVolumeFromFile): keep its name
+        if (q >= 4 && q < 8 && t.size() < 256) {
+          std::snprintf(files[q - 4], 256, "%s", t.c_str());
+          *dst[q] = 0.0;
+          continue;
         }
         goto bad;
       }
@@ -281,5 +292,84 @@ extern "C" int cg_storm_read(const char *path, float *values, long n)
     cg::set_error("%s: %s barriers found; only grids without barriers are supported", path, t.c_str());
     return CG_ERR_UNSUPPORTED;
   }
+  return CG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// STORM binary surfaces
+// ---------------------------------------------------------------------------
+extern "C" int cg_storm_surface_write(const char *path, const double *z, int ni, int nj, double x_min, double y_min,
+                                      double lx, double ly)
+{
+  if (!path || !z || ni < 2 || nj < 2) { cg::set_error("cg_storm_surface_write: bad argument (ni, nj >= 2)"); return CG_ERR_ARG; }
+  std::ofstream f(path, std::ios::out | std::ios::binary | std::ios::trunc);
+  if (!f) { cg::set_error("cannot open %s for writing", path); return CG_ERR_ARG; }
+  std::ostringstream s;
+  s << "STORMGRID_BINARY\n\n"
+    << ni << " " << nj << " " << g14(lx / (ni - 1)) << " " << g14(ly / (nj - 1)) << "\n"
+    << g14(x_min) << " " << g14(x_min + lx) << " " << g14(y_min) << " " << g14(y_min + ly) << "\n";
+  const std::string head = s.str();
+  f.write(head.data(), (std::streamsize)head.size());
+  const size_t n = (size_t)ni * nj;
+  std::vector<unsigned char> buf;
+  buf.reserve(8 * n);
+  for (size_t i = 0; i < n; i++) put_be64(buf, d2u(z[i]));
+  f.write((const char *)buf.data(), (std::streamsize)buf.size());
+  if (!f) { cg::set_error("write error on %s", path); return CG_ERR_STATE; }
+  return CG_OK;
+}
+
+// parses a surface header; leaves the stream at the first data byte
+static int surface_header(std::ifstream &f, const char *path, int *ni, int *nj, double *x_min, double *y_min,
+                          double *lx, double *ly)
+{
+  std::string t;
+  double v[8];
+  if (!next_token(f, t) || t != "STORMGRID_BINARY") { cg::set_error("%s is not a STORM binary surface", path); return CG_ERR_ARG; }
+  for (int q = 0; q < 8; q++)
+    if (!next_token(f, t) || !parse_double(t, v[q])) { cg::set_error("%s: malformed STORM surface header", path); return CG_ERR_ARG; }
+  const int n_i = (int)v[0], n_j = (int)v[1];
+  const double dx = v[2], dy = v[3], lxv = v[5] - v[4], lyv = v[7] - v[6];
+  if (n_i < 2 || n_j < 2) { cg::set_error("%s: %d x %d nodes", path, n_i, n_j); return CG_ERR_ARG; }
+  // NRLib's consistency test (|a - b| <= 1e-4 a)
+  if (!(std::fabs(lxv / (n_i - 1) - dx) <= 1e-4 * (lxv / (n_i - 1)))) { cg::set_error("%s: dx != lx/(nx-1)", path); return CG_ERR_ARG; }
+  if (!(std::fabs(lyv / (n_j - 1) - dy) <= 1e-4 * (lyv / (n_j - 1)))) { cg::set_error("%s: dy != ly/(ny-1)", path); return CG_ERR_ARG; }
+  int c;
+  while ((c = f.get()) != EOF && c != '\n') {}
+  if (c == EOF) { cg::set_error("%s: truncated", path); return CG_ERR_ARG; }
+  *ni = n_i;
+  *nj = n_j;
+  if (x_min) *x_min = v[4];
+  if (y_min) *y_min = v[6];
+  if (lx) *lx = lxv;
+  if (ly) *ly = lyv;
+  return CG_OK;
+}
+
+extern "C" int cg_storm_surface_read_header(const char *path, int *ni, int *nj, double *x_min, double *y_min,
+                                            double *lx, double *ly)
+{
+  if (!path || !ni || !nj) { cg::set_error("cg_storm_surface_read_header: bad argument"); return CG_ERR_ARG; }
+  std::ifstream f(path, std::ios::in | std::ios::binary);
+  if (!f) { cg::set_error("cannot open %s", path); return CG_ERR_ARG; }
+  return surface_header(f, path, ni, nj, x_min, y_min, lx, ly);
+}
+
+extern "C" int cg_storm_surface_read(const char *path, double *z, long n)
+{
+  if (!path || !z) { cg::set_error("cg_storm_surface_read: bad argument"); return CG_ERR_ARG; }
+  std::ifstream f(path, std::ios::in | std::ios::binary);
+  if (!f) { cg::set_error("cannot open %s", path); return CG_ERR_ARG; }
+  int ni = 0, nj = 0;
+  int rc = surface_header(f, path, &ni, &nj, nullptr, nullptr, nullptr, nullptr);
+  if (rc) return rc;
+  if ((long)ni * nj != n) { cg::set_error("%s holds %d x %d nodes, not %ld", path, ni, nj, n); return CG_ERR_ARG; }
+  std::vector<unsigned char> buf(8 * (size_t)n);
+  f.read((char *)buf.data(), (std::streamsize)buf.size());
+  if ((size_t)f.gcount() != buf.size()) { cg::set_error("%s: truncated data", path); return CG_ERR_STATE; }
+  for (long i = 0; i < n; i++) z[i] = u2d(get_be64(buf.data() + 8 * i));
+  // CheckEndOfFile: nothing but whitespace may follow
+  std::string t;
+  if (next_token(f, t)) { cg::set_error("%s: file too long", path); return CG_ERR_ARG; }
   return CG_OK;
 }

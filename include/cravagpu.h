@@ -329,9 +329,14 @@ int cg_crava_file_write(const char *path, const float *rvalue, int rnxp, int nyp
 int cg_crava_file_read(const char *path, float *rvalue, int rnxp, int nyp, int nzp, double *geom, int *nxny);
 
 /* STORM binary grids (NRLib StormContGrid, libs/nrlib/stormgrid/
- * stormcontgrid.cpp:72-200) with constant surfaces: values are ni*nj*nk
- * floats, i fastest.  Grids whose surfaces are files, ASCII grids and grids
- * with barriers give CG_ERR_UNSUPPORTED. */
+ * stormcontgrid.cpp:72-200): values are ni*nj*nk floats, i fastest.  Each of
+ * the four surfaces (top, bottom, erosion top, erosion bottom) is a constant
+ * or a STORM binary surface file (NRLib Volume::WriteVolumeToFile /
+ * ReadVolumeFromFile, libs/nrlib/volume/volume.cpp:338-440): a non-empty
+ * *_file field is written into the header in place of the constant, and a
+ * header token that is not a number is returned there (the file name as the
+ * header holds it; the reference resolves it against the grid file's
+ * directory).  ASCII grids and grids with barriers give CG_ERR_UNSUPPORTED. */
 typedef struct {
   int zone_number;
   char model_file[256];
@@ -340,11 +345,27 @@ typedef struct {
   double x_min, lx, y_min, ly;
   double z_top, z_bot, erosion_top, erosion_bot;  /* constant surfaces */
   double lz, angle_deg;
+  char z_top_file[256], z_bot_file[256], erosion_top_file[256], erosion_bot_file[256];
 } cg_storm_header;
 
 int cg_storm_write(const char *path, const float *values, int ni, int nj, int nk, const cg_storm_header *header);
 int cg_storm_read_header(const char *path, cg_storm_header *header, int *ni, int *nj, int *nk);
 int cg_storm_read(const char *path, float *values, long n);
+
+/* STORM binary surfaces (NRLib WriteStormBinarySurf / ReadStormBinarySurf,
+ * libs/nrlib/surface/surfaceio.hpp:101-147,439-464): an ni x nj regular grid
+ * of big-endian doubles (i fastest) over [x_min, x_min + lx] x [y_min,
+ * y_min + ly], nodes at spacing lx/(ni-1), ly/(nj-1); -999 marks a missing
+ * node.  ni, nj >= 2.  read_header checks dx = lx/(ni-1) and dy = ly/(nj-1)
+ * as the reference does.  The reference's other surface formats (Irap
+ * classic ASCII, SGRI) are refused with CG_ERR_ARG.  The grid header's lz is
+ * written as given (the reference samples max(bottom - top) on a 100 x 100
+ * grid over the volume, Volume::RecalculateLZ, volume.cpp:494-515). */
+int cg_storm_surface_write(const char *path, const double *z, int ni, int nj, double x_min, double y_min,
+                           double lx, double ly);
+int cg_storm_surface_read_header(const char *path, int *ni, int *nj, double *x_min, double *y_min, double *lx,
+                                 double *ly);
+int cg_storm_surface_read(const char *path, double *z, long n);
 
 /* ========================================================================
  * Output grids after the bin loop

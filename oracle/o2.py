@@ -288,6 +288,43 @@ def storm_read(raw):
         return v.reshape(int(hdr["nk"]), int(hdr["nj"]), int(hdr["ni"])), hdr
 
 
+def storm_write_surf(values, top, bot, surf_geom, **hdr):
+    """StormContGrid::WriteToFile with regular top / bottom surfaces top, bot (nj, ni) float64 over surf_geom
+    (x_min, y_min, lx, ly): returns {file name: bytes} for the grid and the surface files beside it."""
+    nk, nj, ni = values.shape
+    snj, sni = top.shape
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, ni=ni, nj=nj, nk=nk, surf_ni=sni, surf_nj=snj, sx_min=float(surf_geom[0]),
+                sy_min=float(surf_geom[1]), slx=float(surf_geom[2]), sly=float(surf_geom[3]),
+                **{k: float(hdr[k]) for k in STORM_PARAMS if k not in ("z_top", "z_bot")})
+        _w(d, "values.f32", values, np.float32)
+        _w(d, "top.f64", top, np.float64)
+        _w(d, "bot.f64", bot, np.float64)
+        _run("storm_write_surf", d)
+        out = {}
+        for name in sorted(os.listdir(d)):
+            if name.startswith("out.storm"):
+                with open(os.path.join(d, name), "rb") as f:
+                    out[name] = f.read()
+        return out
+
+
+def storm_read_surf(files):
+    """StormContGrid::ReadFromFile of files["in.storm"] with its surface files beside it (files: {name: bytes}):
+    (values (nk, nj, ni), {"top"/"bot": (z (nj, ni), geometry (ni, nj, x_min, y_min, lx, ly))})."""
+    with tempfile.TemporaryDirectory() as d:
+        for name, raw in files.items():
+            with open(os.path.join(d, name), "wb") as f:
+                f.write(raw)
+        _run("storm_read_surf", d)
+        surf = {}
+        for q in ("top", "bot"):
+            g = _r(d, f"{q}_geom.f64", np.float64)
+            surf[q] = (_r(d, f"{q}_read.f64", np.float64).reshape(int(g[1]), int(g[0])), g)
+        v = _r(d, "values_read.f32", np.float32)
+    return v, surf
+
+
 def closest_factorable(ns):
     ns = np.asarray(ns, dtype=np.int32)
     with tempfile.TemporaryDirectory() as d:

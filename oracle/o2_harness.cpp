@@ -29,6 +29,9 @@
 //   crava_o2 storm_write / storm_read <dir>
 //                               NRLib::StormContGrid::WriteToFile / ReadFromFile
 //                               (constant surfaces).
+//   crava_o2 storm_write_surf / storm_read_surf <dir>
+//                               the same with regular top and bottom surfaces
+//                               written to / read from files beside the grid.
 //   crava_o2 factorable <dir>   FFTGrid::findClosestFactorableNumber.
 //
 // <dir> holds params.txt ("key value" lines) and raw little-endian arrays
@@ -71,6 +74,7 @@
 #include "src/wavelet1D.h"
 #include "nrlib/stormgrid/stormcontgrid.hpp"
 #include "nrlib/surface/surface.hpp"
+#include "nrlib/surface/regularsurface.hpp"
 #undef private
 #undef protected
 
@@ -766,6 +770,57 @@ int cmd_storm_read()
   return 0;
 }
 
+// StormContGrid::WriteToFile of values.f32 whose top and bottom surfaces are regular surfaces (top.f64,
+// bot.f64: surf_ni x surf_nj nodes over [sx_min, sx_min + slx] x [sy_min, sy_min + sly]) and whose erosion
+// surfaces are constants: out.storm plus the surface files the writer puts beside it (out.storm_top,
+// out.storm_bot, WriteStormBinarySurf)
+int cmd_storm_write_surf()
+{
+  std::map<std::string, double> p = read_params();
+  const size_t ni = (size_t)p["ni"], nj = (size_t)p["nj"], nk = (size_t)p["nk"];
+  const size_t sni = (size_t)p["surf_ni"], snj = (size_t)p["surf_nj"];
+  std::vector<float> v = read_arr<float>("values.f32", ni * nj * nk);
+  std::vector<double> top = read_arr<double>("top.f64", sni * snj), bot = read_arr<double>("bot.f64", sni * snj);
+  NRLib::RegularSurface<double> st(p["sx_min"], p["sy_min"], p["slx"], p["sly"], sni, snj, 0.0);
+  NRLib::RegularSurface<double> sb(p["sx_min"], p["sy_min"], p["slx"], p["sly"], sni, snj, 0.0);
+  std::copy(top.begin(), top.end(), st.begin());
+  std::copy(bot.begin(), bot.end(), sb.begin());
+  NRLib::StormContGrid g(ni, nj, nk);
+  g.SetDimensions(p["x_min"], p["y_min"], p["lx"], p["ly"]);
+  g.SetAngle(p["angle_deg"] * NRLib::Pi / 180.0);
+  g.SetSurfaces(st, sb, NRLib::ConstantSurface<double>(p["erosion_top"]),
+                NRLib::ConstantSurface<double>(p["erosion_bot"]));
+  g.SetZoneNumber((int)p["zone"]);
+  g.SetModelFileName("ModelFile");
+  g.SetMissingCode((float)p["missing"]);
+  g.SetVariableName("Vp");
+  std::copy(v.begin(), v.end(), g.begin());
+  g.WriteToFile(g_dir + "/out.storm");
+  return 0;
+}
+
+// StormContGrid::ReadFromFile of in.storm, whose top and bottom surfaces are files beside it: the values,
+// and the two surfaces as the reader loaded them (nodes and geometry)
+int cmd_storm_read_surf()
+{
+  NRLib::StormContGrid g;
+  g.ReadFromFile(g_dir + "/in.storm");
+  std::vector<float> v(g.begin(), g.end());
+  write_raw("values_read.f32", &v[0], sizeof(float) * v.size());
+  const NRLib::Surface<double> *surf[2] = {&g.GetTopSurface(), &g.GetBotSurface()};
+  const char *name[2] = {"top", "bot"};
+  for (int q = 0; q < 2; q++) {
+    const NRLib::RegularSurface<double> *rs = dynamic_cast<const NRLib::RegularSurface<double> *>(surf[q]);
+    if (!rs) { fprintf(stderr, "%s surface is not a regular surface\n", name[q]); return 3; }
+    std::vector<double> z(rs->begin(), rs->end());
+    write_raw(std::string(name[q]) + "_read.f64", &z[0], sizeof(double) * z.size());
+    const double geom[6] = {(double)rs->GetNI(), (double)rs->GetNJ(), rs->GetXMin(), rs->GetYMin(),
+                            rs->GetXMax() - rs->GetXMin(), rs->GetYMax() - rs->GetYMin()};
+    write_raw(std::string(name[q]) + "_geom.f64", geom, sizeof(geom));
+  }
+  return 0;
+}
+
 int cmd_factorable()
 {
   std::map<std::string, double> p = read_params();
@@ -807,6 +862,8 @@ int main(int argc, char **argv)
   if (c == "fillindata") return cmd_fillindata();
   if (c == "interpolate") return cmd_interpolate();
   if (c == "divide") return cmd_divide();
+  if (c == "storm_write_surf") return cmd_storm_write_surf();
+  if (c == "storm_read_surf") return cmd_storm_read_surf();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();
   if (c == "storm_write") return cmd_storm_write();

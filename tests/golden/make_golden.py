@@ -172,6 +172,47 @@ def file_format_case(name):
                         read_storm_keys=np.array(sorted(read_hdr)))
 
 
+def storm_surface_case(name):
+    """A STORM grid whose top and bottom surfaces are regular surfaces written to files beside it: the
+    reference's StormContGrid::WriteToFile output (grid and surface files) and its ReadFromFile view of the
+    library's files."""
+    from crava_gb300 import api
+    rng = np.random.default_rng(19)
+    hdr = dict(zone=2, missing=-999.25, x_min=456000.0, lx=1600.0, y_min=6780000.0, ly=1200.0, z_top=0.0,
+               z_bot=0.0, erosion_top=1750.0, erosion_bot=2450.5, angle_deg=12.5)
+    values = rng.standard_normal((3, 4, 5)).astype(np.float32)
+    surf_geom = np.array([455700.0, 6779950.0, 1900.0, 1600.0])  # covers the rotated volume
+    yy, xx = np.mgrid[0:4, 0:6]
+    top = 1800.0 + 3.25 * xx - 1.5 * yy + rng.uniform(-2, 2, (4, 6))
+    bot = top + 600.0 + 0.125 * xx * yy
+    top[2, 3] = -999.0  # a missing node
+    ref = o2.storm_write_surf(values, top, bot, surf_geom, **hdr)
+    tmpdir = os.path.join(HERE, "_tmp_surf")
+    os.makedirs(tmpdir, exist_ok=True)
+    h = api.StormHeader()
+    h.zone_number, h.model_file, h.missing_code, h.variable = 2, b"ModelFile", -999.25, b"Vp"
+    h.x_min, h.lx, h.y_min, h.ly = hdr["x_min"], hdr["lx"], hdr["y_min"], hdr["ly"]
+    h.erosion_top, h.erosion_bot = hdr["erosion_top"], hdr["erosion_bot"]
+    h.lz, h.angle_deg = float(np.max(bot) - np.min(top[top > -999])), hdr["angle_deg"]
+    surfs = {"z_top_file": api.StormSurface(top, *surf_geom), "z_bot_file": api.StormSurface(bot, *surf_geom)}
+    api.write_storm(os.path.join(tmpdir, "out.storm"), values, h, surfaces=surfs)
+    ours = {}
+    for n in sorted(os.listdir(tmpdir)):
+        with open(os.path.join(tmpdir, n), "rb") as f:
+            ours[n] = f.read()
+        os.remove(os.path.join(tmpdir, n))
+    os.rmdir(tmpdir)
+    files = dict(ours)
+    files["in.storm"] = files.pop("out.storm")
+    read_values, read_surf = o2.storm_read_surf(files)
+    out = dict(values=values, top=top, bot=bot, surf_geom=surf_geom, header=np.array([hdr[k] for k in o2.STORM_PARAMS]),
+               ref_names=np.array(sorted(ref)), read_values=read_values, read_top=read_surf["top"][0],
+               read_top_geom=read_surf["top"][1], read_bot=read_surf["bot"][0], read_bot_geom=read_surf["bot"][1])
+    for i, n in enumerate(sorted(ref)):
+        out[f"ref_file{i}"] = np.frombuffer(ref[n], np.uint8)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
 def factorable_case(name):
     ns = np.array(list(range(1, 260)) + [341, 343, 500, 511, 625, 1000, 1023, 1025, 2047, 4097, 10000], np.int32)
     np.savez_compressed(os.path.join(HERE, name), n=ns, closest=o2.closest_factorable(ns))
@@ -347,6 +388,8 @@ def main():
             divide_case("reference_divide.npz", 18)
         if "inversion_grad.npz" in only:
             gradient_case("inversion_grad.npz")
+        if "reference_storm_surfaces.npz" in only:
+            storm_surface_case("reference_storm_surfaces.npz")
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -371,6 +414,7 @@ def main():
     interpolate_case("reference_interpolate.npz", 17)
     divide_case("reference_divide.npz", 18)
     gradient_case("inversion_grad.npz")
+    storm_surface_case("reference_storm_surfaces.npz")
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

@@ -65,12 +65,41 @@ def test_storm_round_trip_and_header_text(native, tmp_path):
 
 def test_storm_unsupported_forms(native, tmp_path):
     from crava_gb300 import api
+    # a surface given as a file keeps its name; a surface file that is not STORM binary is refused
     p = tmp_path / "surf.storm"
     p.write_bytes(b"storm_petro_binary\n\n0 ModelFile -999\n\nVp\n\n0 100 0 100 top.irap 2400 1800 2400\n600 0\n\n1 1 1\n"
                   + struct.pack(">f", 1.0) + b"0")
-    with pytest.raises(RuntimeError, match="constant surfaces"):
-        api.read_storm(p)
+    v, h = api.read_storm(p)
+    assert h.z_top_file == b"top.irap" and h.z_bot == 2400.0 and v.shape == (1, 1, 1)
+    (tmp_path / "top.irap").write_bytes(b"-996 2 50 50\n0 100 0 100\n")
+    with pytest.raises(RuntimeError, match="not a STORM binary surface"):
+        api.read_storm_surfaces(p, h)
     q = tmp_path / "ascii.storm"
     q.write_bytes(b"storm_petro_ascii\n\n0 ModelFile -999\n")
     with pytest.raises(RuntimeError, match="ASCII"):
         api.read_storm(q)
+
+
+def test_storm_surface_round_trip_and_checks(native, tmp_path):
+    from crava_gb300 import api
+    rng = np.random.default_rng(3)
+    z = rng.uniform(1000, 2000, (5, 7))
+    p = tmp_path / "s.storm_top"
+    api.write_storm_surface(p, api.StormSurface(z, 100.0, 200.0, 60.0, 40.0))
+    raw = p.read_bytes()
+    assert raw.startswith(b"STORMGRID_BINARY\n\n7 5 10 10\n100 160 200 240\n")
+    assert len(raw) == len(b"STORMGRID_BINARY\n\n7 5 10 10\n100 160 200 240\n") + 8 * z.size
+    s = api.read_storm_surface(p)
+    np.testing.assert_array_equal(s.z, z)
+    assert (s.x_min, s.y_min, s.lx, s.ly) == (100.0, 200.0, 60.0, 40.0)
+    # inconsistent spacing, trailing bytes and a truncated body are refused as the reference refuses them
+    bad = raw.replace(b"7 5 10 10", b"7 5 11 10")
+    (tmp_path / "b1").write_bytes(bad)
+    with pytest.raises(RuntimeError, match="dx"):
+        api.read_storm_surface(tmp_path / "b1")
+    (tmp_path / "b2").write_bytes(raw + b"x")
+    with pytest.raises(RuntimeError, match="too long"):
+        api.read_storm_surface(tmp_path / "b2")
+    (tmp_path / "b3").write_bytes(raw[:-8])
+    with pytest.raises(RuntimeError, match="truncated"):
+        api.read_storm_surface(tmp_path / "b3")

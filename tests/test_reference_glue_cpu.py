@@ -319,3 +319,46 @@ def test_scale_wavelet_multiply_matches_reference(oracle):
         e = rel(m[..., :nxp], g["mult"][l][..., :nxp])
         print("multiply, angle", l, "oracle vs reference:", e)
         assert e < 2e-6, l
+
+
+def test_storm_surface_files_match_reference(native, tmp_path):
+    """A STORM grid whose top and bottom surfaces are regular surfaces in files beside it
+    (Volume::WriteVolumeToFile / ReadVolumeFromFile, WriteStormBinarySurf / ReadStormBinarySurf): the
+    library writes the reference's bytes for the grid and both surface files (lz given as the reference
+    computed it), reads the reference's files back, and the reference read the library's files."""
+    from crava_gb300 import api
+    g = golden("reference_storm_surfaces.npz")
+    hv = dict(zip(("zone", "missing", "x_min", "lx", "y_min", "ly", "z_top", "z_bot", "erosion_top", "erosion_bot",
+                   "angle_deg"), g["header"]))
+    ref = {str(n): bytes(g[f"ref_file{i}"]) for i, n in enumerate(g["ref_names"])}
+    head = ref["out.storm"].split(b"\n")
+    lz = float(head[7].split()[0])  # Volume::RecalculateLZ's sampled maximum thickness
+    h = api.StormHeader()
+    h.zone_number, h.model_file, h.missing_code, h.variable = int(hv["zone"]), b"ModelFile", hv["missing"], b"Vp"
+    h.x_min, h.lx, h.y_min, h.ly = hv["x_min"], hv["lx"], hv["y_min"], hv["ly"]
+    h.erosion_top, h.erosion_bot, h.lz, h.angle_deg = hv["erosion_top"], hv["erosion_bot"], lz, hv["angle_deg"]
+    sg = g["surf_geom"]
+    surfs = {"z_top_file": api.StormSurface(g["top"], *sg), "z_bot_file": api.StormSurface(g["bot"], *sg)}
+    p = tmp_path / "out.storm"
+    api.write_storm(p, g["values"], h, surfaces=surfs)
+    for name, raw in ref.items():
+        assert (tmp_path / name).read_bytes() == raw, name
+    # the library reads the reference's files
+    d = tmp_path / "ref"
+    d.mkdir()
+    for name, raw in ref.items():
+        (d / name).write_bytes(raw)
+    v, rh = api.read_storm(d / "out.storm")
+    np.testing.assert_array_equal(v, g["values"])
+    assert rh.z_top_file == b"out.storm_top" and rh.z_bot_file == b"out.storm_bot" and rh.lz == lz
+    assert rh.erosion_top == hv["erosion_top"] and rh.erosion_bot == hv["erosion_bot"]
+    s = api.read_storm_surfaces(d / "out.storm", rh)
+    assert set(s) == {"z_top_file", "z_bot_file"}
+    np.testing.assert_array_equal(s["z_top_file"].z, g["top"])
+    np.testing.assert_array_equal(s["z_bot_file"].z, g["bot"])
+    assert (s["z_top_file"].x_min, s["z_top_file"].y_min) == (sg[0], sg[1])
+    assert abs(s["z_top_file"].lx - sg[2]) < 1e-9 and abs(s["z_top_file"].ly - sg[3]) < 1e-9
+    # the reference read the library's files (written with its own lz) back exactly
+    np.testing.assert_array_equal(g["read_values"].reshape(g["values"].shape), g["values"])
+    np.testing.assert_array_equal(g["read_top"], g["top"])
+    np.testing.assert_array_equal(g["read_bot"], g["bot"])
