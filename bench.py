@@ -497,6 +497,8 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok, sc1=None):
     for form in ("plain", "mixed"):
         four[form], run = MB.measure_timelapse(tl, form, reps=steps, warmup=1, peak=peak, run=run)
     four["speedup_mixed_vs_plain"] = round(four["plain"]["ms"] / four["mixed"]["ms"], 3)
+    # the step between vintages when the state evolves (State4D::evolve): not part of the workload above
+    four["evolve_step"] = MB.measure_evolve(run, reps=max(steps, 3), peak=peak)
     if cpu_ok:
         run.restore()
         torch.cuda.synchronize()

@@ -172,6 +172,8 @@ def _declare(L):
         "cg_simulate_fields": ([V, PP, PP, I, I, ct.c_uint64, I, I, I, PP, V], I),
         "cg_state4d_merge": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V], I),
         "cg_state4d_split": ([PP, PP, PP, PP, PP, PP, PP, I, I, I, V, V], I),
+        "cg_state4d_evolve": ([PP, PP, PP, PP, PP, V, V, V, V, I, I, I, V], I),
+        "cg_fill_genexp_corr": ([V, I, I, I, ct.c_double, ct.c_double, ct.c_double, F, F, V], I),
         "cg_scale": ([V, ct.c_long, F, V], I),
         "cg_add": ([V, V, ct.c_long, V], I),
         "cg_host_register": ([V, ct.c_size_t], I),

@@ -532,6 +532,24 @@ def state4d_merge(mu_s, mu_d, ss, sd, dd, mu_cur, cov_cur, nxp, stream=None):
     check(lib().cg_state4d_merge(*[k[0] for k in keep], nxp, nyp, nzp, _stream(stream)), "cg_state4d_merge")
 
 
+def state4d_evolve(mu_s, mu_d, ss, sd, dd, nxp, E, c, C, lam=None, stream=None):
+    """State4D::evolve on the state spectra in place (cg_state4d_evolve): E, C (6, 6), c (6,) float64;
+    lam the transformed increment correlation cube (fill_genexp_corr + COVARIANCE transform) or None."""
+    nzp, nyp, _ = mu_s[0].shape
+    Ed, cd, Cd = (np.ascontiguousarray(x, dtype=np.float64) for x in (E, c, C))
+    ps = [_pp(g) for g in (mu_s, mu_d, ss, sd, dd)]
+    check(lib().cg_state4d_evolve(*[p for p, _ in ps], _vp(lam) if lam is not None else None, Ed.ctypes.data,
+                                  cd.ctypes.data, Cd.ctypes.data, nxp, nyp, nzp, _stream(stream)),
+          "cg_state4d_evolve")
+
+
+def fill_genexp_corr(buf: torch.Tensor, nxp, range_x, range_y, range_z, grad_i=0.0, grad_j=0.0, stream=None):
+    """FFTGrid::fillInGenExpCorr into a real padded cube (cg_fill_genexp_corr)."""
+    nzp, nyp, _ = buf.shape
+    check(lib().cg_fill_genexp_corr(_vp(buf), nxp, nyp, nzp, float(range_x), float(range_y), float(range_z),
+                                    float(grad_i), float(grad_j), _stream(stream)), "cg_fill_genexp_corr")
+
+
 def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, nxp, stream=None):
     """State4D::split in place; returns a device counter of bins that kept the prior."""
     nzp, nyp, _ = mu_s[0].shape

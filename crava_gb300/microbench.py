@@ -277,6 +277,39 @@ def measure_timelapse(tl=None, form="mixed", reps=3, warmup=1, peak=None, run=No
     return out, run
 
 
+def measure_evolve(run, reps=5, peak=None):
+    """State4D::evolve (cg_state4d_evolve) on a TimeLapse run's state with an evolution that decays and couples
+    the dynamic part and adds a covariance increment (transformed GenExp correlation), timed with CUDA
+    events; algorithmic bytes per bin: read and write the 27 state spectra, read the increment's."""
+    import numpy as np
+    tl = run.tl
+    nxp, nyp, nzp = tl.nxp, tl.nyp, tl.nzp
+    E = np.block([[np.eye(3), np.zeros((3, 3))],
+                  [0.1 * np.eye(3), 0.9 * np.eye(3) + 0.05 * (np.ones((3, 3)) - np.eye(3))]])
+    c = np.array([0.0, 0.0, 0.0, 0.01, -0.02, 0.005])
+    C = np.zeros((6, 6))
+    C[3:, 3:] = 4e-4 * np.array([[1.0, 0.3, 0.2], [0.3, 1.0, 0.25], [0.2, 0.25, 1.0]])
+    _, rnxp = api.dims(nxp)
+    lam = torch.empty((nzp, nyp, rnxp), device="cuda")
+    api.fill_genexp_corr(lam, nxp, tl.nx / 3.0, tl.ny / 3.0, 20.0)
+    api.fft_in_place(lam, nxp, api.COVARIANCE)
+
+    def step():
+        api.state4d_evolve(run.mu_s, run.mu_d, run.ss, run.sd, run.dd, nxp, E, c, C, lam=lam)
+    run.restore()
+    step()
+    ms = _events_ms(step, reps, run.restore)
+    run.restore()
+    tr = _traced(step)
+    best = statistics.median(ms)
+    byt = 8.0 * tl.nbins * (27 + 27 + 1)
+    out = {"bins": tl.nbins, "ms": round(best, 4), "ms_stat": "median", "GBps": round(byt / (best * 1e-3) / 1e9, 1),
+           "algorithmic_bytes": byt, "kernels": kernel_table(tr)}
+    if peak:
+        out["roofline"] = roofline_of(tr, peak)
+    return out
+
+
 def ingest_case(a):
     """Data ingest of one 256^3 DATA cube: 258 x 256 column traces of 205 samples (4 ms) resampled onto the
     grid (transforms of length 210 and 840), timed with CUDA events."""

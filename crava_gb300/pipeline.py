@@ -278,7 +278,11 @@ class TimeLapse:
 
     The state is held as spectra (27 cubes: 3 + 3 means, 6 + 9 + 6 covariance blocks), built from the
     separable prior exactly as the reference builds its 4D grids (fillInParamCorr x Sigma entry, then a
-    COVARIANCE transform).  Between vintages nothing evolves (E = I, c = 0, C = 0).  The reference's
+    COVARIANCE transform).  Between vintages v and v + 1 the state evolves when the scenario gives a time
+    evolution (State4D::evolve, src/state4d.cpp:800-996, called by ModelGeneral::advanceTime before the next
+    merge, src/modelgeneral.cpp:4852-4870): mu <- E mu + c, Sig <- E Sig E^T + C Re(lambda), lambda the
+    transformed GenExp correlation evolve builds (ranges nx/3, ny/3, 20); with none, nothing evolves
+    (E = I, c = 0, C = 0).  The reference's
     inverse-then-forward transform of the posterior means between the bin loop and split
     (src/crava.cpp:1262-1264, :352-354) is an identity up to rounding and is not repeated here.
     """
@@ -326,6 +330,14 @@ class TimeLapse:
         self.errcorr = torch.empty(shape, **f32)
         api.check_call("cg_fill_err_corr", self.errcorr, nxp, nyp, nzp, corr_xy, 0.0, 0.0, s)
         api.fft_in_place(self.errcorr, nxp, api.COVARIANCE)
+        self.evolution = getattr(tl, "evolution", None)
+        self.lam = None
+        if self.evolution:
+            # the increment's spatial correlation State4D::evolve transforms (its fixed ranges)
+            self.lam = torch.empty(shape, **f32)
+            api.fill_genexp_corr(self.lam, nxp, float(np.float32(tl.nx)) / 3.0, float(np.float32(tl.ny)) / 3.0,
+                                 20.0)
+            api.fft_in_place(self.lam, nxp, api.COVARIANCE)
         self.tables = api.operator_tables(tl.wavelets, tl.A, tl.nz, nzp, tl.dt_ms, tl.low_cut, tl.high_cut,
                                           tl.min_rel_thick)
         self.data_in, self.ws = [], []
@@ -377,8 +389,17 @@ class TimeLapse:
             self.post_mean[p].copy_(self.mu_cur[p])
         api.fft_in_place_batch(self.post_mean, nxp, api.PARAMETER, inverse=True, stream=stream)
 
+    def evolve(self, step, stream=None):
+        """State4D::evolve with time step `step` of the scenario's evolution (between vintages step and
+        step + 1)."""
+        E, c, C = self.evolution[step]
+        api.state4d_evolve(self.mu_s, self.mu_d, self.ss, self.sd, self.dd, self.tl.nxp, E, c, C, lam=self.lam,
+                           stream=stream)
+
     def run(self, stream=None, form="plain"):
         for v in range(len(self.tl.vintages)):
+            if v > 0 and self.evolution:
+                self.evolve(v - 1, stream=stream)
             self.run_vintage(v, stream=stream, form=form)
 
     def state(self):

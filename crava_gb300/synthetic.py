@@ -448,6 +448,9 @@ class TimeLapseScenario:
     low_cut: float = 5.0
     high_cut: float = 55.0
     min_rel_thick: float = 1.0
+    # per step between vintages v and v+1: (E (6, 6), c (6,), C (6, 6)) of the time evolution
+    # (TimeEvolution::getEvolutionMatrix / getMeanCorrectionTerm / getCovarianceCorrectionTerm); None: none
+    evolution: list | None = None
 
     @property
     def ntheta(self):

@@ -690,6 +690,28 @@ int cg_state4d_split(float *const *mu_s, float *const *mu_d, float *const *ss, f
                      float *const *mu_post, float *const *cov_post, int nxp, int nyp, int nzp, int *nfail_dev,
                      void *stream);
 
+/* State4D::evolve (src/state4d.cpp:800-996), the step between two vintages
+ * (ModelGeneral::advanceTime, src/modelgeneral.cpp:4852-4870), on the state
+ * spectra in place: per bin mu <- E mu (+ c sqrt(nxp*nyp*nzp) at bin
+ * (0,0,0), a constant in the real domain) and Sig <- E Sig E^T +
+ * C Re(lambda), with E = evolution[36], c = mean_correction[6], C =
+ * cov_correction[36] (row-major 6x6, parameter order Vp, Vs, rho static then
+ * dynamic: TimeEvolution::getEvolutionMatrix / getMeanCorrectionTerm /
+ * getCovarianceCorrectionTerm) and lambda_spec the transformed correlation of
+ * the increment (cg_fill_genexp_corr + COVARIANCE transform; NULL for none).
+ * The reference forms the products in FP64 and stores FP32; they are formed
+ * in FP32 here (FP64 runs at a small fraction of the FP32 rate on GB300). */
+int cg_state4d_evolve(float *const *mu_s, float *const *mu_d, float *const *ss, float *const *sd, float *const *dd,
+                      const float *lambda_spec, const double *evolution, const double *mean_correction,
+                      const double *cov_correction, int nxp, int nyp, int nzp, void *stream);
+
+/* FFTGrid::fillInGenExpCorr (src/fftgrid.cpp:1144-1187): the real padded
+ * cube exp(-3 sqrt((i/Rx)^2 + (j/Ry)^2 + (k'/Rz)^2)) with cyclic lags and k'
+ * the k lag shifted by the gradients, RMISSING in the row padding.  State4D::
+ * evolve fills it with Rx = nx/3, Ry = ny/3, Rz = 20 and no gradients. */
+int cg_fill_genexp_corr(float *buf, int nxp, int nyp, int nzp, double range_x, double range_y, double range_z,
+                        float grad_i, float grad_j, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -114,6 +114,25 @@ def state4d(state27, post9, nxp):
     return merged, split
 
 
+def state4d_evolve(state27, nx, ny, nz, nxp, E, c, C):
+    """State4D::evolve with one time step (E, C (6, 6), c (6,)) on the 27 state spectra ((nzp, nyp, cnxp)
+    complex64; grids of logical size nx x ny x nz).  Returns (evolved 27 spectra, the increment correlation
+    cube (nzp, nyp, rnxp) as fillInGenExpCorr writes it, and its transform)."""
+    state27 = np.ascontiguousarray(state27, dtype=np.complex64)
+    nzp, nyp, cnxp = state27.shape[1:]
+    with tempfile.TemporaryDirectory() as d:
+        _params(d, nx=nx, ny=ny, nz=nz, nxp=nxp, nyp=nyp, nzp=nzp)
+        _w(d, "state.f32", state27.view(np.float32), np.float32)
+        _w(d, "E.f64", E, np.float64)
+        _w(d, "c.f64", c, np.float64)
+        _w(d, "C.f64", C, np.float64)
+        _run("state4d_evolve", d)
+        ev = _r(d, "evolved.f32", np.float32).view(np.complex64).reshape(27, nzp, nyp, cnxp)
+        gr = _r(d, "genexp_real.f32", np.float32).reshape(nzp, nyp, 2 * cnxp)
+        gs = _r(d, "genexp_spec.f32", np.float32).view(np.complex64).reshape(nzp, nyp, cnxp)
+    return ev, gr, gs
+
+
 def adjustment(sc, l, corr_t, min_int_fq, f_peak, cases, error_var):
     """Crava::computeAdjustmentFactor for angle l of the scenario: the reference's Ricker (f_peak) resampled
     on the grid is the global wavelet; cases: (n, 3) of (time shift ms, gain, stretch).  Returns (the

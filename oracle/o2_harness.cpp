@@ -16,6 +16,9 @@
 //                               thickness branches (src/crava.cpp:1337-1386).
 //   crava_o2 state4d    <dir>   State4D::merge and State4D::split
 //                               (src/state4d.cpp:140-580) on given spectra.
+//   crava_o2 state4d_evolve <dir>
+//                               State4D::evolve (src/state4d.cpp:800-996) for given
+//                               evolution and correction terms.
 //   crava_o2 adjust     <dir>   Crava::computeAdjustmentFactor (src/crava.cpp:807-903)
 //                               for given local shifts, gains and stretches.
 //   crava_o2 localnoise <dir>   Crava::computeG and Crava::correctAlphaBetaRho
@@ -71,6 +74,7 @@
 #include "src/seismicparametersholder.h"
 #include "src/simbox.h"
 #include "src/state4d.h"
+#include "src/timeevolution.h"
 #include "src/wavelet1D.h"
 #include "nrlib/stormgrid/stormcontgrid.hpp"
 #include "nrlib/surface/surface.hpp"
@@ -350,6 +354,53 @@ int cmd_state4d()
     for (int t = 0; t < 27; t++) memcpy(&out[rsize * t], g[t]->rvalue_, sizeof(float) * rsize);
     write_raw("split.f32", &out[0], sizeof(float) * out.size());
   }
+  return 0;
+}
+
+// State4D::evolve (src/state4d.cpp:800-996) with one time step of a TimeEvolution whose evolution matrix,
+// mean and covariance correction terms are E.f64, c.f64, C.f64, on the 27 state spectra of state.f32 (grids
+// of logical size nx x ny x nz, which set the increment's correlation ranges); also the increment's
+// correlation cube as evolve builds it (FFTGrid::fillInGenExpCorr) before and after its transform
+int cmd_state4d_evolve()
+{
+  std::map<std::string, double> p = read_params();
+  const int nx = (int)p["nx"], ny = (int)p["ny"], nz = (int)p["nz"];
+  const int nxp = (int)p["nxp"], nyp = (int)p["nyp"], nzp = (int)p["nzp"];
+  const size_t rsize = (size_t)2 * (nxp / 2 + 1) * nyp * nzp;
+  std::vector<float> st = read_arr<float>("state.f32", rsize * 27);
+  std::vector<double> E = read_arr<double>("E.f64", 36), c = read_arr<double>("c.f64", 6),
+                      C = read_arr<double>("C.f64", 36);
+  std::vector<FFTGrid *> g(27);
+  for (int t = 0; t < 27; t++)
+    g[t] = make_grid(nx, ny, nz, nxp, nyp, nzp, t < 6 ? FFTGrid::PARAMETER : FFTGrid::COVARIANCE, &st[rsize * t], true);
+  State4D s4;
+  s4.setStaticMu(g[0], g[1], g[2]);
+  s4.setDynamicMu(g[3], g[4], g[5]);
+  s4.setStaticSigma(g[6], g[7], g[8], g[9], g[10], g[11]);
+  s4.setStaticDynamicSigma(g[12], g[13], g[14], g[15], g[16], g[17], g[18], g[19], g[20]);
+  s4.setDynamicSigma(g[21], g[22], g[23], g[24], g[25], g[26]);
+  TimeEvolution te;
+  NRLib::Matrix Em(6, 6), Cm(6, 6);
+  NRLib::Vector cv(6);
+  for (int a = 0; a < 6; a++) {
+    cv(a) = c[a];
+    for (int b = 0; b < 6; b++) { Em(a, b) = E[6 * a + b]; Cm(a, b) = C[6 * a + b]; }
+  }
+  te.evolution_matrix_.push_back(Em);
+  te.mean_correction_term_.push_back(cv);
+  te.cov_correction_term_.push_back(Cm);
+  s4.evolve(0, te);
+  {
+    std::vector<float> out(rsize * 27);
+    for (int t = 0; t < 27; t++) memcpy(&out[rsize * t], g[t]->rvalue_, sizeof(float) * rsize);
+    write_raw("evolved.f32", &out[0], sizeof(float) * out.size());
+  }
+  FFTGrid lam(nx, ny, nz, nxp, nyp, nzp);
+  lam.createGrid();
+  lam.fillInGenExpCorr(float(nx) / 3.0, float(ny) / 3.0, 20.0, 0.0f, 0.0f);
+  dump_grid("genexp_real.f32", &lam);
+  lam.fftInPlace();
+  dump_grid("genexp_spec.f32", &lam);
   return 0;
 }
 
@@ -863,6 +914,7 @@ int main(int argc, char **argv)
   if (c == "interpolate") return cmd_interpolate();
   if (c == "divide") return cmd_divide();
   if (c == "storm_write_surf") return cmd_storm_write_surf();
+  if (c == "state4d_evolve") return cmd_state4d_evolve();
   if (c == "storm_read_surf") return cmd_storm_read_surf();
   if (c == "crava_write") return cmd_crava_write();
   if (c == "crava_read") return cmd_crava_read();

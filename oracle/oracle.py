@@ -99,6 +99,11 @@ def lib():
                                                              ct.POINTER(ct.c_int), ct.c_int]
             getattr(L, "or_fill_param_corr" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, PR, PR,
                                                                ct.c_float, ct.c_float, R]
+            getattr(L, "or_state4d_evolve" + sfx).argtypes = [ct.c_size_t, PPR, PPR, PPR, PPR, PPR, PR,
+                                                              ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                                              ct.c_int, ct.c_int, ct.c_int]
+            getattr(L, "or_fill_genexp" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, ct.c_double,
+                                                           ct.c_double, ct.c_double, ct.c_float, ct.c_float]
             getattr(L, "or_fill_err_corr" + sfx).argtypes = [PR, ct.c_int, ct.c_int, ct.c_int, PR,
                                                              ct.c_float, ct.c_float]
             getattr(L, "or_k_tables" + sfx).argtypes = [
@@ -329,6 +334,33 @@ def state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post6, prec="f", nthreads
     pp = [_pp([_real_view(x) for x in grp], R) for grp in st + post]
     getattr(lib(), "or_state4d_split_" + prec)(st[0][0].size, *pp, ct.byref(nf), nthreads)
     return st, nf.value
+
+
+def state4d_evolve(state27, nxp, nyp, nzp, E, c, C, lam=None, prec="f", nthreads=None):
+    """State4D::evolve on the 27 state spectra (mu_s 3, mu_d 3, ss 6, sd 9, dd 6; (nzp, nyp, cnxp) complex
+    each): returns the evolved copies.  E, C (6, 6), c (6,); lam the transformed increment correlation or None."""
+    cdt = np.complex64 if prec == "f" else np.complex128
+    R = ct.c_float if prec == "f" else ct.c_double
+    st = [np.ascontiguousarray(x, dtype=cdt).copy() for x in state27]
+    grp = [st[0:3], st[3:6], st[6:12], st[12:21], st[21:27]]
+    pp = [_pp([_real_view(x) for x in g], R) for g in grp]
+    lm = np.ascontiguousarray(lam, dtype=cdt) if lam is not None else None
+    Ed, cd, Cd = (np.ascontiguousarray(x, dtype=np.float64) for x in (E, c, C))
+    getattr(lib(), "or_state4d_evolve_" + prec)(st[0].size, pp[0], pp[1], pp[2], pp[3], pp[4],
+                                                _ptr(_real_view(lm), R) if lm is not None else None,
+                                                Ed.ctypes.data, cd.ctypes.data, Cd.ctypes.data, nxp, nyp, nzp,
+                                                nthreads or os.cpu_count())
+    return st
+
+
+def fill_genexp(nxp, nyp, nzp, rx, ry, rz, gradI=0.0, gradJ=0.0, prec="f"):
+    """FFTGrid::fillInGenExpCorr: real padded cube (nzp, nyp, rnxp)."""
+    R = ct.c_float if prec == "f" else ct.c_double
+    _, rnxp = dims(nxp)
+    buf = np.zeros((nzp, nyp, rnxp), dtype=_rdt(prec))
+    getattr(lib(), "or_fill_genexp_" + prec)(_ptr(buf, R), nxp, nyp, nzp, float(rx), float(ry), float(rz), gradI,
+                                             gradJ)
+    return buf
 
 
 def fill_param_corr(nxp, nyp, nzp, corrXY, circCorrT, gradI=0.0, gradJ=0.0, scalar=1.0, prec="f"):

@@ -262,6 +262,25 @@ def inversion_4d_case(name, tl, vintage=0):
                         merged=merged, split=split)
 
 
+EVOLVE_E = np.block([[np.eye(3), np.zeros((3, 3))],
+                     [0.1 * np.eye(3), 0.9 * np.eye(3) + 0.05 * (np.ones((3, 3)) - np.eye(3))]])
+EVOLVE_C_MEAN = np.array([0.0, 0.0, 0.0, 0.01, -0.02, 0.005])
+EVOLVE_C_COV = np.block([[np.zeros((3, 3)), np.zeros((3, 3))],
+                         [np.zeros((3, 3)), 4e-4 * np.array([[1.0, 0.3, 0.2], [0.3, 1.0, 0.25], [0.2, 0.25, 1.0]])]])
+
+
+def evolve_case(name):
+    """State4D::evolve by the reference's own code (crava_o2) with one time step of a time evolution (the
+    dynamic part decays, couples to the static part, gains a mean shift and a covariance increment) on the
+    split state of state4d_n4.npz, and the increment's correlation cube evolve builds (fillInGenExpCorr)."""
+    g = np.load(os.path.join(HERE, "state4d_n4.npz"))
+    state = g["split"]
+    nx, ny, nz, nxp = 16, 12, 11, int(g["nxp"])
+    ev, gr, gs = o2.state4d_evolve(state, nx, ny, nz, nxp, EVOLVE_E, EVOLVE_C_MEAN, EVOLVE_C_COV)
+    np.savez_compressed(os.path.join(HERE, name), nx=nx, ny=ny, nz=nz, nxp=nxp, state=state, E=EVOLVE_E,
+                        c=EVOLVE_C_MEAN, C=EVOLVE_C_COV, evolved=ev, genexp_real=gr, genexp_spec=gs)
+
+
 def local_noise_case(name, n, dims, seed):
     """Crava::computeG + Crava::correctAlphaBetaRho by the reference's own code (crava_o2) on a posterior that
     differs from the prior mean by noise, local noise scales that vary over the traces (one RMISSING cell),
@@ -390,6 +409,8 @@ def main():
             gradient_case("inversion_grad.npz")
         if "reference_storm_surfaces.npz" in only:
             storm_surface_case("reference_storm_surfaces.npz")
+        if "state4d_evolve.npz" in only:
+            evolve_case("state4d_evolve.npz")
         print("fixtures written to", HERE)
         return
     fft_case("fft_even.npz", 16, 12, 20, 11)
@@ -415,6 +436,7 @@ def main():
     divide_case("reference_divide.npz", 18)
     gradient_case("inversion_grad.npz")
     storm_surface_case("reference_storm_surfaces.npz")
+    evolve_case("state4d_evolve.npz")
     r = O.ref_rnorm01_seq(231171, 4096)
     np.savez_compressed(os.path.join(HERE, "rnorm01.npz"), seed=231171, draws=r)
     print("fixtures written to", HERE)

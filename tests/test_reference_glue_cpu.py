@@ -362,3 +362,24 @@ def test_storm_surface_files_match_reference(native, tmp_path):
     np.testing.assert_array_equal(g["read_values"].reshape(g["values"].shape), g["values"])
     np.testing.assert_array_equal(g["read_top"], g["top"])
     np.testing.assert_array_equal(g["read_bot"], g["bot"])
+
+
+def test_state4d_evolve_matches_reference(oracle):
+    """State4D::evolve (src/state4d.cpp:800-996) run by the reference's own code (crava_o2) with one time step
+    of a time evolution: the oracle's GenExp correlation fill is bit for bit the reference's
+    fillInGenExpCorr, and its evolved state (FP64 products, as the reference forms them) agrees to the
+    reference's FP32 storage."""
+    g = golden("state4d_evolve.npz")
+    nx, ny, nxp = int(g["nx"]), int(g["ny"]), int(g["nxp"])
+    st = g["state"]
+    nzp, nyp, _ = st.shape[1:]
+    gr = oracle.fill_genexp(nxp, nyp, nzp, nx / 3.0, ny / 3.0, 20.0)
+    np.testing.assert_array_equal(gr, g["genexp_real"])
+    ev = np.stack(oracle.state4d_evolve(list(st), nxp, nyp, nzp, g["E"], g["c"], g["C"], lam=g["genexp_spec"]))
+    assert rel(ev, g["evolved"]) < 1e-8
+    for t in range(27):
+        assert np.abs(ev[t] - g["evolved"][t]).max() <= 4e-7 * np.abs(g["evolved"][t]).max(), t
+    # the increment and the mean shift are both visible in the fixture
+    ev0 = np.stack(oracle.state4d_evolve(list(st), nxp, nyp, nzp, g["E"], g["c"], g["C"], lam=None))
+    assert rel(ev0, g["evolved"]) > 1e-5
+    assert g["evolved"][3][0, 0, 0] != st[3][0, 0, 0]

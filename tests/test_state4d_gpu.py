@@ -197,3 +197,77 @@ def test_fused_vintage_mixed_matches_fp64_oracle_chain(cuda, oracle, cond):
     if cond > 0:
         assert min(flagged) > 0
         assert upd < 1e-5  # the FP64 redo: only the FP32 storage of state and data remains
+
+
+def test_evolve_and_genexp_match_reference(cuda):
+    """cg_fill_genexp_corr and cg_state4d_evolve against the reference's fillInGenExpCorr and
+    State4D::evolve (crava_o2; products in FP32 here, FP64 there)."""
+    from conftest import golden
+    from crava_gb300 import api
+    g = golden("state4d_evolve.npz")
+    nx, ny, nxp = int(g["nx"]), int(g["ny"]), int(g["nxp"])
+    st = g["state"]
+    nzp, nyp, _ = st.shape[1:]
+    buf = torch.empty(g["genexp_real"].shape, dtype=torch.float32, device="cuda")
+    api.fill_genexp_corr(buf, nxp, nx / 3.0, ny / 3.0, 20.0)
+    torch.cuda.synchronize()
+    gr = buf.cpu().numpy()
+    # exp of the device against the host library: equal but for the odd last-bit case
+    assert np.abs(gr - g["genexp_real"]).max() <= 6e-8 * np.abs(g["genexp_real"][..., :nxp]).max()
+    api.fft_in_place(buf, nxp, api.COVARIANCE)
+    lam_gpu = from_cube(buf)
+    assert rel(lam_gpu, g["genexp_spec"]) < 1e-6
+    cubes = [to_cube(x) for x in st]
+    grp = [cubes[0:3], cubes[3:6], cubes[6:12], cubes[12:21], cubes[21:27]]
+    api.state4d_evolve(*grp, nxp, g["E"], g["c"], g["C"], lam=to_cube(g["genexp_spec"]))
+    torch.cuda.synchronize()
+    got = np.stack([from_cube(x) for x in cubes])
+    e = rel(got, g["evolved"])
+    worst = max(float(np.abs(got[t] - g["evolved"][t]).max() / np.abs(g["evolved"][t]).max()) for t in range(27))
+    print("evolve vs reference: rel", e, "worst cube max-abs / max", worst)
+    assert e < 1e-6 and worst < 1e-5
+
+
+def test_timelapse_with_evolution_matches_fp64_oracle_chain(cuda, oracle):
+    """Two vintages with State4D::evolve between them (as ModelGeneral::advanceTime calls it) on the GPU
+    against merge -> bin loop -> split -> evolve -> merge -> bin loop -> split in the FP64 oracle."""
+    from crava_gb300 import api, synthetic as S
+    from crava_gb300.pipeline import TimeLapse, MERGE_TO_BIN
+    E = np.block([[np.eye(3), np.zeros((3, 3))],
+                  [0.1 * np.eye(3), 0.9 * np.eye(3) + 0.05 * (np.ones((3, 3)) - np.eye(3))]])
+    c = np.array([0.0, 0.0, 0.0, 0.01, -0.02, 0.005])
+    C = np.zeros((6, 6))
+    C[3:, 3:] = 4e-4 * np.array([[1.0, 0.3, 0.2], [0.3, 1.0, 0.25], [0.2, 0.25, 1.0]])
+    tl = S.make_timelapse(16, 12, 11, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=20, nyp=15, nzp=14, seed=7)
+    tl.evolution = [(E, c, C)]
+    for form in ("plain", "mixed"):
+        run = TimeLapse(tl)
+        run.restore()
+        state0 = run.state()
+        errc = api.as_spectrum(run.errcorr).cpu().numpy()
+        lam = api.as_spectrum(run.lam).cpu().numpy()
+        run.run(form=form)
+        torch.cuda.synchronize()
+        got = run.state()
+        mu_s, mu_d, ss, sd, dd = [list(x) for x in state0]
+        tab = dict(run.tables, nxp=tl.nxp)
+        for v, vin in enumerate(tl.vintages):
+            if v > 0:
+                st = oracle.state4d_evolve(mu_s + mu_d + ss + sd + dd, tl.nxp, tl.nyp, tl.nzp, E, c, C, lam=lam,
+                                           prec="d")
+                mu_s, mu_d, ss, sd, dd = st[0:3], st[3:6], st[6:12], st[12:21], st[21:27]
+            mu_cur, cov_cur = oracle.state4d_merge(mu_s, mu_d, ss, sd, dd, prec="d")
+            data = [oracle.fft3d_r2c(d, tl.nxp, oracle.DATA, "d") for d in vin["data"]]
+            _, mu_post, cov_bin, _ = oracle.invert_bins(data, mu_cur, [cov_cur[t] for t in MERGE_TO_BIN], errc,
+                                                        tab, vin["err_theta_cov"], tl.sigma_current(), tl.wnc,
+                                                        is4d=True, prec="d")
+            cov_post = [None] * 6
+            for k, t in enumerate(MERGE_TO_BIN):
+                cov_post[t] = cov_bin[k]
+            (mu_s, mu_d, ss, sd, dd), _ = oracle.state4d_split(mu_s, mu_d, ss, sd, dd, mu_post, cov_post, prec="d")
+        ref = (mu_s, mu_d, ss, sd, dd)
+        names = ["mu_s", "mu_d", "ss", "sd", "dd"]
+        errs = {nm: rel(np.stack(a), np.stack(b)) for nm, a, b in zip(names, got, ref)}
+        print(form, "timelapse with evolution vs FP64 oracle chain:", errs)
+        assert errs["mu_s"] < 1e-6 and errs["mu_d"] < 1e-4
+        assert errs["ss"] < 1e-5 and errs["sd"] < 1e-5 and errs["dd"] < 1e-5
