@@ -450,7 +450,7 @@ def localnoise_case(a):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("what", choices=["fft", "invert", "batch", "copy", "simulate", "timelapse", "ingest",
-                                     "thickness", "localnoise"])
+                                     "thickness", "localnoise", "evolve"])
     ap.add_argument("--nreal", type=int, default=128)
     ap.add_argument("--mb", type=int, default=512)
     ap.add_argument("--ncubes", type=int, default=64)
@@ -480,6 +480,14 @@ def main():
         return
     if a.what == "localnoise":
         localnoise_case(a)
+        return
+    if a.what == "evolve":
+        # the 4D state of the 256x256x192 workload (one vintage's data is enough: evolve reads only the state)
+        from . import synthetic as S
+        from .pipeline import TimeLapse
+        tl = S.make_timelapse(205, 205, 154, [0.0, 40.0 / 3, 80.0 / 3, 40.0], 25.0, nxp=256, nyp=256, nzp=192,
+                              nvintages=1, seed=3)
+        print(json.dumps(measure_evolve(TimeLapse(tl), reps=a.reps)))
         return
     if a.what == "batch":
         # graph replays: time the whole batch with CUDA events
