@@ -780,7 +780,8 @@ def run_ours(args, world, rank, local):
                                           for k, v in sorted(tr_cold.items(), key=lambda kv: -kv[1][1])},
                               "what": "mixed form with the model's per-k set-up inside the step: host operator "
                                       "tables built while the forward transforms run, one upload, the per-k "
-                                      "table kernel (cg_workspace_set_model_async)"},
+                                      "table kernel (cg_workspace_set_model_async) and the prior spectra on a "
+                                      "high-priority side stream beside the transforms"},
             "accuracy_vs_cpu_fp64": vs_cpu64,
             "condition_histogram": {"buckets": "decades of the squared Cholesky pivot ratio, last = failed",
                                     "threshold": 1.0e3, "chol_form_fp64": hist_chol, "info_form_fp32": hist_info},

@@ -165,22 +165,30 @@ class Inversion:
         as the reference does it inside computePostMeanResidAndFFTCov (the per-k operator and error factors,
         fillErrMultVectors / getNextErrorVariance, src/crava.cpp:1108-1120).  The forward transforms of the
         data and prior means are queued first; the host builds the operator tables (from the wavelets) while
-        the GPU transforms, then queues their upload and the per-k table kernel
-        (cg_workspace_set_model_async), the prior spectra, the bin kernel and the inverse transforms."""
+        the GPU transforms, then queues their upload, the per-k table kernel (cg_workspace_set_model_async)
+        and the prior spectra on a high-priority side stream, so that they run beside the transforms (their
+        single-warp CTAs take the SM slots the transform CTAs free first); the bin kernel waits for both,
+        then the inverse transforms."""
         sc = self.sc
         if self.thick:
             raise ValueError("run_cold covers the constant-thickness model")
         prec = {"mixed": api.PREC_MIXED, "fp32": api.PREC_FP32}[form]
         nxp = sc.nxp
+        main = stream if stream is not None else torch.cuda.current_stream()
+        if getattr(self, "_side", None) is None:
+            self._side = torch.cuda.Stream(priority=-100)  # mapped to the device's highest priority
+        side = self._side
+        side.wait_stream(main)  # the workspace's earlier work is done before its tables change
         # DATA and PARAMETER cubes share the 1/sqrt(N) scaling: one batched launch per pass for all of them
-        api.fft_in_place_batch(self.data + self.mean, nxp, api.DATA, stream=stream)
+        api.fft_in_place_batch(self.data + self.mean, nxp, api.DATA, stream=main)
         tables = api.operator_tables(sc.wavelets, sc.A, sc.nz, sc.nzp, sc.dt_ms, sc.low_cut, sc.high_cut,
                                      sc.min_rel_thick)
         self.ws.set_model(tables, sc.err_theta_cov, sc.sigma0, sc.wnc, cond_threshold=self.cond_threshold,
-                          stream=stream, asynchronous=True)
-        self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
-        self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=stream)
-        api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
+                          stream=side, asynchronous=True)
+        self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=side, grad=self.grad)
+        main.wait_stream(side)
+        self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=main)
+        api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=main)
 
     # -- output grids (the steps after the bin loop) ------------------------
     def outputs(self, form, stream=None):
