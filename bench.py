@@ -417,6 +417,9 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok, sc1=None):
         t = cpu_inversion(sc0, oracle_tables(sc0), "f", threads)[0]
         small["cpu_baseline"] = {"value": round(sc0.nbins / t["total_s"] / 1e6, 3), "unit": "Mbins/s",
                                  "cores": threads, "kind": "port", "sample": "one complete inversion"}
+        t1 = cpu_inversion(sc0, oracle_tables(sc0), "f", 1)[0]
+        small["cpu_baseline_1core"] = {"value": round(sc0.nbins / t1["total_s"] / 1e6, 3), "unit": "Mbins/s",
+                                       "cores": 1, "kind": "port", "sample": "one complete inversion"}
     del inv0
     out["small_80x80x160_3stacks"] = small
 
