@@ -223,6 +223,35 @@ def cpu_inversion(sc, tables, prec="f", threads=None):
     return t, post, np.stack(res), np.stack(cov), nf
 
 
+def simulated_fields_vs_fp64(sc, inv, threads):
+    """One realisation of the posterior, GPU chain (mixed inversion, per-bin factor, inverse transforms, mean
+    add) against the FP64 oracle chain (FP64 inversion of the same inputs with the same operator tables, FP64
+    factor and transforms), both fed the same noise field: the reference's own fillInComplexNoise stream
+    (seed 231171) injected into cg_simulate_fields.  Relative L2 error of the three fields, and of the
+    fields' deviation from the posterior mean (the simulated part alone)."""
+    import numpy as np
+    import torch
+    from crava_gb300 import api
+    from oracle import oracle as O
+    nxp = sc.nxp
+    noise = O.fill_complex_noise(nxp, sc.nyp, sc.nzp, 231171, 3)
+    _, post64, _, cov64, _ = cpu_inversion(sc, inv.tables, "d", threads)
+    z64 = O.simulate_bins(list(cov64), list(noise), prec="d", nthreads=threads)
+    dev64 = np.stack([O.fft3d_c2r(z, nxp, O.PARAMETER, "d", threads)[:, :, :nxp] for z in z64])
+    f64 = dev64 + post64
+    chol, _ = api.posterior_cholesky(inv.cov, nxp)
+    _, rnxp = api.dims(nxp)
+    fields = [torch.empty((sc.nzp, sc.nyp, rnxp), device="cuda") for _ in range(3)]
+    nz = [torch.from_numpy(np.ascontiguousarray(x).view(np.float32)).cuda() for x in noise]
+    api.simulate_fields(chol, fields, nxp, noise=nz, post_mean=inv.mean)
+    torch.cuda.synchronize()
+    got = np.stack([f.cpu().numpy()[:, :, :nxp] for f in fields])
+    pm = np.stack([m.cpu().numpy()[:, :, :nxp] for m in inv.mean])
+    return {"fields_rel_err": float(f"{rel(got, f64):.3e}"),
+            "simulated_part_rel_err": float(f"{rel(got - pm, dev64):.3e}"),
+            "noise": "reference fillInComplexNoise stream (oracle restatement pinned to RandomGen), seed 231171"}
+
+
 def oracle_tables(sc):
     """The per-k operator tables from the oracle's own restatement (no product code on the CPU arm)."""
     from oracle import oracle as O
@@ -486,10 +515,14 @@ def other_workloads(args, stream, flush, rank, peak, cpu_ok, sc1=None):
         inv3.run("mixed")
         torch.cuda.synchronize()
         pm, _, cov = inv3.results("mixed")
-        del inv3
         spr = cpu_simulation_sample(sc3, list(cov), list(pm), 2, threads)
         sim["cpu_baseline"] = {"value": round(1.0 / spr, 3), "unit": "realisations/s", "cores": threads,
                                "kind": "port", "sample": "2 realisations (noise, factor, 3 inverse transforms, mean add)"}
+        try:
+            sim["fields_vs_cpu_fp64"] = simulated_fields_vs_fp64(sc3, inv3, threads)
+        except Exception as e:  # an accuracy side figure must not cost the bench line
+            sim["fields_vs_cpu_fp64"] = {"error": repr(e)[:300]}
+        del inv3
     out["simulation_200cube_128_realisations"] = sim
 
     # 4D time-lapse
