@@ -8,7 +8,9 @@
 //             (invertSeismicData, src/crava.cpp:1389-1438, lib_matr.c), FP32.
 //   fused  -- the prior and error covariances are regenerated per bin from the
 //             separable spectra c(i,j,k) = Cxy(i,j) Ct(k) (fillInParamCorr /
-//             fillInErrCorr with zero correlation gradients), the per-k
+//             fillInErrCorr with zero correlation gradients; with nonzero
+//             gradients each bin's two scales are read from a per-bin table
+//             built by cg_prior_spectra_grad), the per-k
 //             matrices K S0 K^H and the error-term matrix are precomputed once
 //             per model, and the posterior is formed from one Cholesky factor:
 //               Sd = s M + lam E + D,  Y = L^-1 K S0,  v = L^-1 (d - K mu)
