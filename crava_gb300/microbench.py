@@ -165,11 +165,18 @@ def _traced(fn):
     return tr
 
 
-def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=3, peak=None, flush=None):
+def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=3, peak=None, flush=None, nreal=None):
     """The uneven-cube batch (cg_batch_run, graph replay) timed with CUDA events; the batch's own inputs
     are restored (cg_batch_reset) before each repetition, outside the timed region.  Per-kernel shares
-    from one eager (not graph-replayed) single-stream run under the launch tracer."""
-    b = api.Batch(scs, nstreams=streams)
+    from one eager (not graph-replayed) single-stream run under the launch tracer.  nreal: optional
+    posterior realisations per cube (cg_batch_set_simulation), drawn inside the same graph."""
+    def with_sims(b):
+        if nreal is not None:
+            for i, n in enumerate(nreal):
+                if n > 0:
+                    b.set_simulation(i, int(n), seed=1000 + i)
+        return b
+    b = with_sims(api.Batch(scs, nstreams=streams))
     bins = b.bins
 
     def before():
@@ -183,7 +190,7 @@ def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=3, peak=None, flu
     b.close()
     # per-kernel shares from one eager run on a single stream (kernels of concurrent streams would overlap
     # inside each other's event pairs)
-    b = api.Batch(scs, nstreams=1)
+    b = with_sims(api.Batch(scs, nstreams=1))
     b.reset()
     b.run(form, use_graph=False)
     b.reset()
@@ -191,6 +198,7 @@ def measure_batch(scs, form="mixed", reps=3, warmup=3, streams=3, peak=None, flu
     b.close()
     mean = statistics.median(ms)
     out = {"form": form, "cubes": len(scs), "bins": int(bins), "ms": round(mean, 4), "ms_stat": "median",
+           "realisations": int(sum(nreal)) if nreal is not None else 0,
            "Mbins_per_s": round(bins / (mean * 1e-3) / 1e6, 1), "ms_per_rep": [round(x, 4) for x in ms],
            "eager_kernels": kernel_table(tr), "launches": int(sum(v[0] for v in tr.values()))}
     if peak:
