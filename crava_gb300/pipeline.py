@@ -160,6 +160,24 @@ class Inversion:
         else:
             raise ValueError(form)
 
+    def capture(self, form):
+        """The inversion of ``form`` on the working cubes captured once as a CUDA graph (after one warm run,
+        which creates the transform tables and kernel attributes outside the capture); replay() runs the
+        same launches on the same buffers with one host call, so a small cube's step is not bound by the
+        host's launch rate.  Restore the inputs before each replay, as before each run."""
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            self.restore(form)
+            self.run(form)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        with torch.cuda.graph(g):
+            self.run(form)
+        torch.cuda.synchronize()
+        return g
+
     def run_cold(self, form="mixed", stream=None):
         """One inversion of a model the workspace has not seen: the per-model work happens inside the call,
         as the reference does it inside computePostMeanResidAndFFTCov (the per-k operator and error factors,
