@@ -413,3 +413,24 @@ def test_correlation_fills_bit_exact_vs_reference(cuda, case):
     api.check_call("cg_fill_err_corr", buf, nxp, nyp, nzp, corr_xy, gi, gj, st)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(buf.cpu().numpy(), g["errcorr_real"])
+
+
+@pytest.mark.parametrize("form", ["plain", "fp32", "mixed"])
+def test_captured_step_replays_the_eager_inversion(cuda, form):
+    """Inversion.capture: the step captured once as a CUDA graph gives, on every replay, the eager step's
+    outputs bit for bit (the benchmark's headline step is this replay)."""
+    from crava_gb300 import synthetic as S
+    from crava_gb300.pipeline import Inversion
+    sc = S.scaled_config1(40, 36, 48, seed=27)
+    inv = Inversion(sc, forms=(form,))
+    inv.restore(form)
+    inv.run(form)
+    torch.cuda.synchronize()
+    eager = inv.results(form)
+    g = inv.capture(form)
+    for _ in range(2):
+        inv.restore(form)
+        g.replay()
+        torch.cuda.synchronize()
+        for a, b in zip(inv.results(form), eager):
+            assert np.array_equal(a, b)
