@@ -139,8 +139,19 @@ class Inversion:
             api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=stream)
         elif form in ("fp32", "mixed"):
             prec = api.PREC_MIXED if form == "mixed" else api.PREC_FP32
-            self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
-            self.ws.invert_cubes(self.data, self.mean, self.cov, prec, stream=stream)
+            main = stream if stream is not None else torch.cuda.current_stream()
+            if self.ws_fused_y():
+                self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=main, grad=self.grad)
+                self.ws.invert_cubes(self.data, self.mean, self.cov, prec, stream=main)
+            else:
+                # the prior spectra depend on the model only: a side branch beside the forward transforms
+                side = self._prior_stream()
+                side.wait_stream(main)
+                self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=side, grad=self.grad)
+                api.fft_in_place_batch(self.data + self.mean, nxp, api.DATA, stream=main)
+                main.wait_stream(side)
+                self.ws.invert_fused(self.data, self.mean, self.cov, prec, stream=main)
+                api.fft_in_place_batch(self.mean, nxp, api.PARAMETER, inverse=True, stream=main)
         elif form in ("fp32_3pass", "mixed_3pass"):
             prec = api.PREC_MIXED if form == "mixed_3pass" else api.PREC_FP32
             self.ws.prior_spectra(self.corr_xy, self.circ_t, api.PREC_FP32, stream=stream, grad=self.grad)
@@ -177,6 +188,21 @@ class Inversion:
             self.run(form)
         torch.cuda.synchronize()
         return g
+
+    def ws_fused_y(self):
+        """Whether cg_invert_cubes_fused takes a y-fused, y-split or z-chunked route for this cube (tuning
+        table CG_TUNE_FUSED_Y for its y length, separable prior): those interleave the y transforms with the
+        bins and run as one call."""
+        sc = self.sc
+        if any(self.grad):
+            return False
+        zc = api.lib().cg_tune_get(4, sc.nyp)  # CG_TUNE_FUSED_Y
+        return zc == 2 or zc >= 4 or (zc == 1 and sc.nyp in (128, 200, 256))
+
+    def _prior_stream(self):
+        if getattr(self, "_pstream", None) is None:
+            self._pstream = torch.cuda.Stream()
+        return self._pstream
 
     def run_cold(self, form="mixed", stream=None):
         """One inversion of a model the workspace has not seen: the per-model work happens inside the call,
