@@ -14,8 +14,9 @@
 // parallel Jacobi: in each step the lanes compute the rotations of up to four
 // disjoint index pairs at once (round-robin pairing), then apply them to the
 // columns, the eigenvectors and the rows with one matrix element per lane.
-// FP64 throughout; the FP64 rate of this GPU is low, so the work is spread
-// over one warp per plane on all SMs instead of one thread per plane, and the
+// The FP64 rate of this GPU is low, so the work is spread over one warp per
+// plane on all SMs instead of one thread per plane, the Jacobi sweeps run in
+// FP32 first and finish in FP64 from there (see below), and the FP64
 // rotation's square roots and reciprocal are hardware approximations refined
 // by Newton-Raphson steps.
 #include "posterior.cuh"
@@ -68,6 +69,91 @@ __device__ __forceinline__ void conj_all(C *v, int n, int lane)
   for (int i = lane; i < n; i += 32) v[i].y = -v[i].y;
 }
 
+// 1/sqrt(x) and 1/x per element type: FP64 as above, FP32 from the hardware's own instructions
+__device__ __forceinline__ double jrsqrt(double x) { return rsqrt_nr(x); }
+__device__ __forceinline__ double jrcp(double x) { return rcp_nr(x); }
+__device__ __forceinline__ float jrsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ float jrcp(float x) { return __frcp_rn(x); }
+
+template <typename T>
+struct JacobiScratch {
+  int rp[kMaxTheta / 2], rq[kMaxTheta / 2];
+  T rc[kMaxTheta / 2], rsn[kMaxTheta / 2];
+  C2<T> rph[kMaxTheta / 2];
+};
+
+// Parallel cyclic Jacobi sweeps on the Hermitian nt x nt matrix a (shared memory), accumulating the
+// rotations into v, until the squared off-diagonal Frobenius norm falls to tol times the squared diagonal
+// (or max_sweeps).  Over an even number of indices (index nt is a dummy when nt is odd: its pairs are
+// skipped); the lanes compute the rotations of up to four disjoint pairs at once (round-robin pairing), then
+// apply them to the columns of a and v and the rows of a with one matrix element per lane.
+template <typename T>
+__device__ void jacobi_sweeps(C2<T> (*a)[kMaxTheta], C2<T> (*v)[kMaxTheta], JacobiScratch<T> &js, int nt,
+                              int max_sweeps, T tol, T tiny, T small_rel, int lane)
+{
+  const int ne = nt + (nt & 1), np = ne / 2;
+  for (int sweep = 0; sweep < max_sweeps; sweep++) {
+    double off = 0.0, diag = 0.0;
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      if (l == m) diag += (double)a[l][l].x * a[l][l].x;
+      else if (m > l) off += (double)a[l][m].x * a[l][m].x + (double)a[l][m].y * a[l][m].y;
+    }
+    off = warp_sum(off);
+    diag = warp_sum(diag);
+    if (off <= (double)tol * diag || off == 0.0) break;
+    for (int r = 0; r < ne - 1; r++) {
+      if (lane < np) {
+        int i0, i1;
+        if (lane == 0) { i0 = ne - 1; i1 = r; }
+        else { i0 = (r + lane) % (ne - 1); i1 = (r - lane + ne - 1) % (ne - 1); }
+        const int pp = min(i0, i1), qq = max(i0, i1);
+        T c = 1, s = 0;
+        C2<T> e = mk<T>(1, 0);
+        if (qq < nt) {
+          const C2<T> apq = a[pp][qq];
+          const T mag2 = apq.x * apq.x + apq.y * apq.y;
+          // an element far under the stopping criterion is left (the approximations need normal operands)
+          if (mag2 > tiny && mag2 > small_rel * (a[pp][pp].x * a[pp][pp].x + a[qq][qq].x * a[qq][qq].x)) {
+            const T ri = jrsqrt(mag2);
+            e = mk<T>(apq.x * ri, -apq.y * ri);  // e^{-i arg a_pq}
+            const T th = (a[qq][qq].x - a[pp][pp].x) * ((T)0.5 * ri);
+            const T q = th * th + (T)1;
+            const T tt = (th >= (T)0 ? (T)1 : (T)-1) * jrcp(fabs(th) + q * jrsqrt(q));
+            c = jrsqrt(tt * tt + (T)1);
+            s = tt * c;
+          }
+        }
+        js.rp[lane] = pp; js.rq[lane] = qq; js.rc[lane] = c; js.rsn[lane] = s; js.rph[lane] = e;
+      }
+      __syncwarp();
+      // columns of a and v: a <- a J, v <- v J
+      for (int i = lane; i < 2 * np * nt; i += 32) {
+        const int which = i / (np * nt), j = (i / nt) % np, row = i % nt;
+        const int pp = js.rp[j], qq = js.rq[j];
+        if (qq >= nt) continue;
+        C2<T> (*x)[kMaxTheta] = which ? v : a;
+        const T c = js.rc[j], s = js.rsn[j];
+        const C2<T> xp = x[row][pp], xq = cmul<T>(js.rph[j], x[row][qq]);
+        x[row][pp] = mk<T>(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
+        x[row][qq] = mk<T>(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
+      }
+      __syncwarp();
+      // rows of a: a <- J^H a
+      for (int i = lane; i < np * nt; i += 32) {
+        const int j = i / nt, col = i % nt;
+        const int pp = js.rp[j], qq = js.rq[j];
+        if (qq >= nt) continue;
+        const T c = js.rc[j], s = js.rsn[j];
+        const C2<T> xp = a[pp][col], xq = cmul<T>(cconj<T>(js.rph[j]), a[qq][col]);
+        a[pp][col] = mk<T>(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
+        a[qq][col] = mk<T>(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 }  // namespace
 
 template <int NT>
@@ -82,10 +168,11 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
   __shared__ KTab<float> f;
   __shared__ ITab o;
   __shared__ double2 a[kMaxTheta][kMaxTheta], v[kMaxTheta][kMaxTheta], g[kMaxTheta][3];
+  __shared__ double2 a0[kMaxTheta][kMaxTheta];
+  __shared__ float2 af[kMaxTheta][kMaxTheta], vf[kMaxTheta][kMaxTheta];
   __shared__ double dm[kMaxTheta];
-  __shared__ double rc[kMaxTheta / 2], rsn[kMaxTheta / 2];
-  __shared__ double2 rph[kMaxTheta / 2];
-  __shared__ int rp[kMaxTheta / 2], rq[kMaxTheta / 2];
+  __shared__ JacobiScratch<double> jsd;
+  __shared__ JacobiScratch<float> jsf;
 
   for (int i = lane; i < (int)(sizeof(KTab<double>) / sizeof(double)); i += 32) ((double *)&t)[i] = 0.0;
   for (int i = lane; i < (int)(sizeof(KTab<float>) / sizeof(float)); i += 32) ((float *)&f)[i] = 0.0f;
@@ -196,70 +283,63 @@ __global__ void __launch_bounds__(32) k_prep_model(const __grid_constant__ PrepA
       v[l][m] = make_double2(l == m ? 1.0 : 0.0, 0.0);
     }
     __syncwarp();
-    // parallel cyclic Jacobi over an even number of indices (index nt is a
-    // dummy when nt is odd: its pairs are skipped)
-    const int ne = nt + (nt & 1), np = ne / 2;
-    for (int sweep = 0; sweep < kPrepSweeps; sweep++) {
-      double off = 0.0, diag = 0.0;
-      for (int i = lane; i < nt * nt; i += 32) {
-        const int l = i / nt, m = i % nt;
-        if (l == m) diag += a[l][l].x * a[l][l].x;
-        else if (m > l) off += a[l][m].x * a[l][m].x + a[l][m].y * a[l][m].y;
-      }
-      off = warp_sum(off);
-      diag = warp_sum(diag);
-      if (off <= 1e-30 * diag || off == 0.0) break;
-      for (int r = 0; r < ne - 1; r++) {
-        if (lane < np) {
-          int i0, i1;
-          if (lane == 0) { i0 = ne - 1; i1 = r; }
-          else { i0 = (r + lane) % (ne - 1); i1 = (r - lane + ne - 1) % (ne - 1); }
-          const int pp = min(i0, i1), qq = max(i0, i1);
-          double c = 1.0, s = 0.0;
-          double2 e = make_double2(1.0, 0.0);
-          if (qq < nt) {
-            const double2 apq = a[pp][qq];
-            const double mag2 = apq.x * apq.x + apq.y * apq.y;
-            // an element below 1e-150 (squared) against the diagonal is left: it is already far under
-            // the stopping criterion, and the refined approximations need normal operands
-            if (mag2 > 1e-300 && mag2 > 1e-40 * (a[pp][pp].x * a[pp][pp].x + a[qq][qq].x * a[qq][qq].x)) {
-              const double ri = rsqrt_nr(mag2);
-              e = make_double2(apq.x * ri, -apq.y * ri);  // e^{-i arg a_pq}
-              const double th = (a[qq][qq].x - a[pp][pp].x) * (0.5 * ri);
-              const double q = th * th + 1.0;
-              const double tt = (th >= 0.0 ? 1.0 : -1.0) * rcp_nr(fabs(th) + q * rsqrt_nr(q));
-              c = rsqrt_nr(tt * tt + 1.0);
-              s = tt * c;
-            }
-          }
-          rp[lane] = pp; rq[lane] = qq; rc[lane] = c; rsn[lane] = s; rph[lane] = e;
-        }
-        __syncwarp();
-        // columns of a and v: a <- a J, v <- v J
-        for (int i = lane; i < 2 * np * nt; i += 32) {
-          const int which = i / (np * nt), j = (i / nt) % np, row = i % nt;
-          const int pp = rp[j], qq = rq[j];
-          if (qq >= nt) continue;
-          double2 (*x)[kMaxTheta] = which ? v : a;
-          const double c = rc[j], s = rsn[j];
-          const double2 xp = x[row][pp], xq = cmul<double>(rph[j], x[row][qq]);
-          x[row][pp] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
-          x[row][qq] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
-        }
-        __syncwarp();
-        // rows of a: a <- J^H a
-        for (int i = lane; i < np * nt; i += 32) {
-          const int j = i / nt, col = i % nt;
-          const int pp = rp[j], qq = rq[j];
-          if (qq >= nt) continue;
-          const double c = rc[j], s = rsn[j];
-          const double2 xp = a[pp][col], xq = cmul<double>(cconj<double>(rph[j]), a[qq][col]);
-          a[pp][col] = make_double2(c * xp.x - s * xq.x, c * xp.y - s * xq.y);
-          a[qq][col] = make_double2(s * xp.x + c * xq.x, s * xp.y + c * xq.y);
-        }
-        __syncwarp();
-      }
+    // The eigen-decomposition in two precisions: cyclic Jacobi sweeps in FP32 down to FP32's resolution
+    // (a handful of sweeps at the FP32 rate), the accumulated rotations re-orthonormalised in FP64
+    // (modified Gram-Schmidt), the matrix brought to that basis in FP64 (a similarity transform, so the
+    // eigenvalues are the original's), and FP64 sweeps from there: from FP32 accuracy they converge in one
+    // or two sweeps (quadratic convergence) instead of the whole run in FP64, the slow unit of this GPU.
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      a0[l][m] = a[l][m];
+      af[l][m] = make_float2((float)a[l][m].x, (float)a[l][m].y);
+      vf[l][m] = make_float2(l == m ? 1.0f : 0.0f, 0.0f);
     }
+    __syncwarp();
+    jacobi_sweeps<float>(af, vf, jsf, nt, 10, 1e-12f, 1e-36f, 1e-14f, lane);
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      v[l][m] = make_double2((double)vf[l][m].x, (double)vf[l][m].y);
+    }
+    __syncwarp();
+    for (int j = 0; j < nt; j++) {
+      for (int q = 0; q < j; q++) {
+        // v_j -= (v_q^H v_j) v_q
+        double2 d = make_double2(0.0, 0.0);
+        if (lane < nt) d = cmulc<double>(v[lane][j], v[lane][q]);
+        d.x = warp_sum(d.x);
+        d.y = warp_sum(d.y);
+        if (lane < nt) v[lane][j] = csub<double>(v[lane][j], cmul<double>(d, v[lane][q]));
+        __syncwarp();
+      }
+      double n2 = lane < nt ? v[lane][j].x * v[lane][j].x + v[lane][j].y * v[lane][j].y : 0.0;
+      n2 = warp_sum(n2);
+      const double rn = rsqrt_nr(n2);
+      if (lane < nt) v[lane][j] = make_double2(v[lane][j].x * rn, v[lane][j].y * rn);
+      __syncwarp();
+    }
+    // a = v^H a0 v (through a: first a0 v, then v^H of it)
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int k2 = 0; k2 < nt; k2++) acc = cadd<double>(acc, cmul<double>(a0[l][k2], v[k2][m]));
+      a[l][m] = acc;
+    }
+    __syncwarp();
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      double2 acc = make_double2(0.0, 0.0);
+      for (int k2 = 0; k2 < nt; k2++) acc = cadd<double>(acc, cmul<double>(cconj<double>(v[k2][l]), a[k2][m]));
+      a0[l][m] = acc;
+    }
+    __syncwarp();
+    for (int i = lane; i < nt * nt; i += 32) {
+      const int l = i / nt, m = i % nt;
+      // Hermitian by construction: take the upper triangle's value for both
+      a[l][m] = l <= m ? a0[l][m] : cconj<double>(a0[m][l]);
+      if (l == m) a[l][m].y = 0.0;
+    }
+    __syncwarp();
+    jacobi_sweeps<double>(a, v, jsd, nt, kPrepSweeps, 1e-30, 1e-300, 1e-40, lane);
     for (int m = lane; m < nt; m += 32) o.mu[m] = (float)(a[m][m].x > 0.0 ? a[m][m].x : 0.0);
     for (int i = lane; i < nt * nt; i += 32) {
       const int l = i / nt, m = i % nt;
