@@ -806,10 +806,15 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     pm3, _, _ = inv3.results("mixed")
     pm3_64, _, _ = inv3.results("fp64")
+    from crava_gb300 import microbench as MB
+    inv3.restore("mixed")
+    tr3 = MB._traced(lambda: inv3.run("mixed"))
     three_stack = {"ms": {k: round(v, 4) for k, v in three.items()},
                    "speedup_mixed_vs_plain": round(three["plain"] / three["mixed"], 3),
                    "mean_rel_err_vs_fp64": float(f"{rel(pm3, pm3_64):.3e}"),
-                   "Mbins_per_s_mixed": round(sc3.nbins / (three["mixed"] * 1e-3) / 1e6, 1)}
+                   "Mbins_per_s_mixed": round(sc3.nbins / (three["mixed"] * 1e-3) / 1e6, 1),
+                   "roofline": MB.roofline_of(tr3, peak),
+                   "kernels": MB.kernel_table(tr3)}
     del inv3, pm3, pm3_64
     clk = clocks.stop()  # sampled from the first timed form step to the last end-to-end step
 
